@@ -1,0 +1,170 @@
+/*
+ * qxgpu.h -- C ABI of the GB300 (sm_103a) executor for QXTools' contraction programmes.
+ *
+ * The reference has no FFI: its contraction hot path is Julia code that walks a plan of
+ * pairwise contractions (`single_amplitude`, src/simulation.jl:86-91, which calls
+ * QXTns.contract_tn!) or a `.qx` DSL programme built by `build_compute_graph`
+ * (src/compute_graph/compute_graph.jl:15-98) and run by `QXContexts.execute`
+ * (bin/qxrun.jl:83-87).  This header is the boundary that replaces both: a programme is the
+ * `.qx` command list (docs/src/users_guide.md:93-165) with tensor symbols mapped to integer
+ * ids, leaf data is the TensorCache table (src/compute_graph/tensor_cache.jl:6-111), and an
+ * amplitude call takes an explicit list of output bitstrings (the `.yml` `List` method,
+ * src/outputs.jl:63-68) and a range of slice ids (qxrun's `--number-slices`,
+ * bin/qxrun.jl:36-39).
+ *
+ * Conventions
+ *   - Every entry point returns QXG_OK (0) or a negative qxg_status; no exception crosses
+ *     the ABI.  qxg_last_error() returns a thread-local message for the last failure.
+ *   - Arrays are column-major (first index fastest), like Julia arrays; complex numbers are
+ *     interleaved (re, im) doubles.
+ *   - The caller owns every host array; the library copies what it keeps.  Device buffers
+ *     belong to the programme handle.  One handle owns one CUDA stream and is not
+ *     thread-safe; separate handles may be used from separate threads.
+ */
+#ifndef QXGPU_H
+#define QXGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum qxg_status {
+    QXG_OK = 0,
+    QXG_ERR_INVALID = -1,      /* malformed programme, bad label, dimension mismatch, bad argument */
+    QXG_ERR_CUDA = -2,         /* a CUDA runtime or driver call failed */
+    QXG_ERR_OOM = -3,          /* the workspace does not fit in device memory or the set limit */
+    QXG_ERR_UNSUPPORTED = -4,  /* valid input outside what this build supports */
+    QXG_ERR_TIMEOUT = -5,      /* a bounded device-side wait gave up */
+    QXG_ERR_STATE = -6         /* call made in the wrong order (e.g. data not set) */
+} qxg_status;
+
+/* One instruction per `.qx` command (docs/src/users_guide.md:93-165; node types built at
+ * src/compute_graph/compute_graph.jl:25-35 (load/output), :39-58 (view), :61-90 (ncon),
+ * :94 (save)).  Tensor symbols are mapped to dense ids 0..ntensors-1 by the caller. */
+typedef enum qxg_opcode {
+    QXG_OP_LOAD = 1,    /* dst = leaf data[a]                         ("load t1 data_2 2,2")  */
+    QXG_OP_VIEW = 2,    /* dst = a[.., v_b, ..] at rank position pos  ("view t1_s t1 v1 1 2") */
+    QXG_OP_OUTPUT = 3,  /* dst = basis vector of output qubit a       ("output t6 1 2")       */
+    QXG_OP_NCON = 4,    /* dst = pairwise contraction of a and b      ("ncon I2 1 t1_s 1,2 t4 2") */
+    QXG_OP_SAVE = 5     /* the programme's result is tensor a         ("save output t11")     */
+} qxg_opcode;
+
+typedef struct qxg_instr {
+    int32_t op;        /* qxg_opcode */
+    int32_t dst;       /* tensor id written (LOAD, VIEW, OUTPUT, NCON); unused for SAVE */
+    int32_t a;         /* LOAD: data id; VIEW: source tensor; OUTPUT: qubit (0-based);
+                          NCON: first operand; SAVE: saved tensor */
+    int32_t b;         /* VIEW: slice variable id (0-based, `v1` -> 0); OUTPUT: dimension (2);
+                          NCON: second operand */
+    int32_t pos;       /* VIEW: rank position of the sliced index (0-based) */
+    int32_t dim;       /* VIEW: bond dimension of the sliced index */
+    int32_t nc;        /* NCON: number of labels of dst (0: scalar) */
+    int32_t na;        /* NCON: number of labels of a (0: scalar, the DSL's `0`) */
+    int32_t nb;        /* NCON: number of labels of b */
+    int32_t label_off; /* NCON: offset into the labels array: nc labels of dst, then na of a,
+                          then nb of b.  Labels are positive integers local to the command;
+                          a label in a and b but not dst is summed, in a, b and dst batched. */
+} qxg_instr;
+
+typedef enum qxg_precision {
+    QXG_PREC_FP64 = 0,        /* ComplexF64 storage and arithmetic (the plain executor) */
+    QXG_PREC_SPLIT_BF16 = 1,  /* Complex64 storage, FP32 accumulation, 3xBF16 tensor-core products */
+    QXG_PREC_SPLIT_TF32 = 2,  /* Complex64 storage, FP32 accumulation, 3xTF32 tensor-core products */
+    QXG_PREC_FP32 = 3         /* Complex64 storage, FP32 CUDA-core arithmetic only */
+} qxg_precision;
+
+typedef struct qxg_options {
+    int32_t precision;            /* qxg_precision */
+    int32_t device;               /* CUDA device ordinal */
+    int64_t workspace_limit;      /* max bytes of intermediate workspace; 0 = 3/4 of free memory */
+    int32_t max_bitstring_batch;  /* bitstrings per pass through the programme; 0 = automatic */
+    int32_t max_slice_batch;      /* slices per pass; 0 = automatic */
+    int32_t use_graphs;           /* capture each pass in a CUDA graph (1) or launch eagerly (0) */
+    int32_t reserved[7];
+} qxg_options;
+
+typedef struct qxg_program qxg_program;
+
+typedef struct qxg_program_info {
+    int64_t num_slices;           /* product of the slice variables' dimensions */
+    int64_t output_size;          /* elements of the saved tensor per bitstring (1 = amplitude) */
+    int32_t num_qubits;
+    int32_t num_steps;            /* ncon instructions */
+    int32_t bitstring_batch;      /* chosen bitstrings per pass */
+    int32_t slice_batch;          /* chosen slices per pass */
+    int64_t workspace_bytes;      /* device workspace in use */
+    double flops_per_amplitude;   /* algorithmic FLOPs (8 |C| K per ncon) for one bitstring,
+                                     summed over all slices */
+    double flops_executed_per_pass;  /* FLOPs one pass executes (shared sub-trees counted once) */
+    double bytes_executed_per_pass;  /* algorithmic bytes one pass moves: s(|A|+|B|+|C|) per ncon */
+    int32_t num_steps_invariant;  /* ncon steps computed once per call */
+    int32_t num_steps_slice;      /* ncon steps computed once per slice batch */
+    int32_t num_steps_bitstring;  /* ncon steps computed once per (slice batch, bitstring batch) */
+    int32_t reserved[5];
+} qxg_program_info;
+
+/* Build a programme from the `.qx` command list.  data_rank[i] and the concatenated
+ * data_dims give the shape of leaf data i (the `load` dims; TensorCache keys `data_N`,
+ * src/compute_graph/tensor_cache.jl:90-106).  Replaces parsing a `.qx` file into a
+ * QXContexts ComputeGraph (bin/qxrun.jl:83 -> QXContexts.execute). */
+int qxg_program_create(const qxg_instr* instrs, int32_t ninstr,
+                       const int32_t* labels, int64_t nlabels,
+                       const int32_t* data_rank, const int64_t* data_dims, int32_t ndata,
+                       int32_t nqubits, const qxg_options* opts, qxg_program** out);
+
+/* Copy leaf data `data_id` (column-major, interleaved complex, `nelem` complex values) to the
+ * device.  Replaces loading `data_N` from the `.jld2` file (src/compute_graph/tensor_cache.jl:90-106). */
+int qxg_program_set_data(qxg_program* prog, int32_t data_id, const double* re_im, int64_t nelem);
+
+/* Amplitudes of `nbitstrings` bitstrings, summed over slices [slice_begin, slice_end).
+ * bitstrings: nbitstrings * nqubits chars from {'0','1','+','-'}, character i is qubit i+1
+ * (docs/src/basics.md:55-64).  out_re_im: nbitstrings * output_size complex values, each
+ * bitstring's saved tensor in column-major order.  Host buffers; the call is synchronous.
+ * Replaces `single_amplitude` (src/simulation.jl:86-91) called once per bitstring, and the
+ * slice loop of QXContexts.execute (bin/qxrun.jl:83-87, `max_slices`). */
+int qxg_amplitudes(qxg_program* prog, const char* bitstrings, int32_t nbitstrings,
+                   int64_t slice_begin, int64_t slice_end, double* out_re_im);
+
+/* As qxg_amplitudes, with device-resident bitstrings and result (d_out_re_im: FP64 complex),
+ * enqueued on the programme's stream; returns without synchronising.  No counterpart in the
+ * reference (its executor is host-driven); used when inputs already live in HBM. */
+int qxg_amplitudes_device(qxg_program* prog, const char* d_bitstrings, int32_t nbitstrings,
+                          int64_t slice_begin, int64_t slice_end, double* d_out_re_im);
+
+/* Wait for work enqueued on the programme's stream. */
+int qxg_program_synchronize(qxg_program* prog);
+
+/* The programme's CUDA stream (a cudaStream_t), for callers that order their own work. */
+void* qxg_program_stream(qxg_program* prog);
+
+/* Sizes, chosen batches and FLOP counts of a created programme. */
+int qxg_program_info_get(const qxg_program* prog, qxg_program_info* info);
+
+/* Free the device buffers, graphs and stream of a programme.  Accepts NULL. */
+void qxg_program_destroy(qxg_program* prog);
+
+/* One pairwise contraction on device buffers: C = ncon(A, B) with the labels and dimensions
+ * of one `ncon` command (a ContractCommand, src/compute_graph/compute_graph.jl:61-74;
+ * QXTns.contract_pair! semantics).  A, B, C are column-major interleaved complex arrays of
+ * the given precision's storage type (QXG_PREC_FP64: double2 with FP64 arithmetic; the other
+ * modes: float2 with FP32 arithmetic); `stream` is a cudaStream_t or NULL for the default
+ * stream.  Dimensions must be powers of two.  Enqueues one kernel and allocates nothing. */
+int qxg_ncon(int32_t precision,
+             void* C, int32_t nc, const int32_t* c_labels,
+             const void* A, int32_t na, const int32_t* a_labels, const int64_t* a_dims,
+             const void* B, int32_t nb, const int32_t* b_labels, const int64_t* b_dims,
+             void* stream);
+
+/* Thread-local description of the last error ("" when none). */
+const char* qxg_last_error(void);
+
+/* Library version string, e.g. "qxgpu 0.1.0 sm_103a". */
+const char* qxg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QXGPU_H */

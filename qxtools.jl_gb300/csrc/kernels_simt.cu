@@ -1,0 +1,250 @@
+// CUDA-core kernels of the executor: the general pairwise contraction (one `ncon` command,
+// docs/src/users_guide.md:124-146), view materialisation for a batch of slices
+// (users_guide.md:104-122), output vectors for a batch of bitstrings (users_guide.md:149-158)
+// and the FP64 sum over slices (users_guide.md:11-17).
+//
+// The contraction kernel is the plain executor's hot loop (ComplexF64 on the FP64 pipe) and
+// the small-K path of the Complex64 executors (FP32 FMA).  A block owns tiles of 2^TB
+// consecutive result elements; because a bit permutation is additive over disjoint bits,
+// offset(tile | lo) = offset(tile) + offset(lo), so the low-bit offsets of the result and all
+// K offsets (up to 2^kKTableBits) are tabulated once per block in shared memory and each
+// element costs two table reads instead of a full bit deposit.
+#include "qxgpu_internal.h"
+
+namespace qxg {
+
+namespace {
+
+template <typename T> struct Real;
+template <> struct Real<double2> { using type = double; };
+template <> struct Real<float2> { using type = float; };
+
+constexpr int kThreads = 256;
+constexpr int kTileBits = 10;          // 1024 result elements per tile, 4 per thread
+
+// 2^n as a float for |n| <= 126 by building the IEEE bits directly (exact power of two).
+__device__ __forceinline__ float pow2f(int n) {
+    n = n < -126 ? -126 : (n > 127 ? 127 : n);
+    return __int_as_float((n + 127) << 23);
+}
+__device__ __forceinline__ double pow2d(int n) {
+    n = n < -1022 ? -1022 : (n > 1023 ? 1023 : n);
+    return __longlong_as_double((long long)(n + 1023) << 52);
+}
+// Binary exponent e of |x| with |x| in [2^(e-1), 2^e) for normal floats (frexp convention).
+__device__ __forceinline__ int exp_of(float x) {
+    return (int)((__float_as_uint(x) >> 23) & 0xffu) - 126;
+}
+
+__device__ __forceinline__ int read_m(const int* exps, int slot) {
+    int m = exps[2 * slot + 1];
+    return m < -400 ? 0 : m;            // all-zero tensor: no scaling
+}
+
+template <typename T, bool SCALED>
+__global__ void __launch_bounds__(kThreads)
+contract_kernel(const StepArgs a, int* exps) {
+    using R = typename Real<T>::type;
+    __shared__ int64_t tA[1 << kKTableBits], tB[1 << kKTableBits];
+    __shared__ int64_t lA[1 << kTileBits], lB[1 << kTileBits];
+    const int nkt = a.nk < kKTableBits ? a.nk : kKTableBits;
+    const int KT = 1 << nkt;
+    int ncb = 0;
+    while ((int64_t(1) << ncb) < a.nC) ncb++;
+    const int tb = ncb < kTileBits ? ncb : kTileBits;
+    const int TS = 1 << tb;
+    for (int k = threadIdx.x; k < KT; k += kThreads) { tA[k] = pdep(k, a.kA); tB[k] = pdep(k, a.kB); }
+    for (int i = threadIdx.x; i < TS; i += kThreads) { lA[i] = pdep(i, a.cA); lB[i] = pdep(i, a.cB); }
+    __syncthreads();
+
+    const T* __restrict__ A = static_cast<const T*>(a.A);
+    const T* __restrict__ B = static_cast<const T*>(a.B);
+    T* __restrict__ C = static_cast<T*>(a.C);
+    const int64_t KO = int64_t(1) << (a.nk - nkt);
+    R scale = R(1);
+    if (SCALED) {
+        const int mA = read_m(exps, a.expA), mB = read_m(exps, a.expB);
+        scale = (R)pow2f(-(mA + mB));
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            exps[2 * a.expC] = exps[2 * a.expA] + exps[2 * a.expB] + mA + mB;
+    }
+    int emax = kExpUnset;
+    const int64_t ntiles = a.nC >> tb;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t tbase = t << tb;
+        const int64_t ta = pdep(tbase, a.cA), tbb = pdep(tbase, a.cB);
+        for (int i = threadIdx.x; i < TS; i += kThreads) {
+            const int64_t a0 = ta + lA[i], b0 = tbb + lB[i];
+            R re = R(0), im = R(0);
+            for (int64_t ko = 0; ko < KO; ko++) {
+                const int64_t ah = a0 + (ko ? pdep(ko << nkt, a.kA) : 0);
+                const int64_t bh = b0 + (ko ? pdep(ko << nkt, a.kB) : 0);
+#pragma unroll 4
+                for (int k = 0; k < KT; k++) {
+                    const T x = A[ah + tA[k]];
+                    const T y = B[bh + tB[k]];
+                    re = fma(x.x, y.x, re);
+                    re = fma(-x.y, y.y, re);
+                    im = fma(x.x, y.y, im);
+                    im = fma(x.y, y.x, im);
+                }
+            }
+            if (SCALED) {
+                re *= scale; im *= scale;
+                const float mx = fmaxf(fabsf((float)re), fabsf((float)im));
+                if (mx > 0.f) emax = max(emax, exp_of(mx));
+            }
+            T out; out.x = re; out.y = im;
+            C[tbase + i] = out;
+        }
+    }
+    if (SCALED) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.expC + 1], emax);
+    }
+}
+
+template <typename T>
+__global__ void view_kernel(const ViewArgs a, int* exps) {
+    const T* __restrict__ S = static_cast<const T*>(a.src);
+    T* __restrict__ D = static_cast<T*>(a.dst);
+    if (exps && blockIdx.x == 0 && threadIdx.x == 0) {
+        exps[2 * a.exp_dst] = exps[2 * a.exp_src];
+        exps[2 * a.exp_dst + 1] = exps[2 * a.exp_src + 1];
+    }
+    const PassParams p = *a.params;
+    const int64_t lomask = (int64_t(1) << a.sigma_shift) - 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t sigma = i >> a.sigma_shift;
+        const int64_t s = p.slice_base + sigma;
+        T v; v.x = 0; v.y = 0;
+        if (sigma < p.slices_valid && s < p.num_slices) {
+            int64_t off = pdep(i & lomask, a.map);
+            for (int f = 0; f < a.nfix; f++) {
+                const int64_t val = (s / a.var_stride[f]) % a.var_dim[f];
+                off += val << a.fix_shift[f];
+            }
+            v = S[off];
+        }
+        D[i] = v;
+    }
+}
+
+template <typename T>
+__global__ void output_kernel(const OutputArgs a, int* exps) {
+    T* __restrict__ D = static_cast<T*>(a.dst);
+    if (exps && blockIdx.x == 0 && threadIdx.x == 0) { exps[2 * a.exp_dst] = 0; exps[2 * a.exp_dst + 1] = 1; }
+    const PassParams p = *a.params;
+    const double r = 0.70710678118654752440;
+    for (int beta = blockIdx.x * blockDim.x + threadIdx.x; beta < a.nbeta; beta += gridDim.x * blockDim.x) {
+        double v0 = 0.0, v1 = 0.0;
+        if (beta < p.bits_valid) {
+            const char ch = a.bitstrings[(int64_t)(p.bit_base + beta) * a.nqubits + a.qubit];
+            if (ch == '0') { v0 = 1.0; }
+            else if (ch == '1') { v1 = 1.0; }
+            else if (ch == '+') { v0 = r; v1 = r; }
+            else if (ch == '-') { v0 = r; v1 = -r; }
+        }
+        T x0, x1;
+        x0.x = v0; x0.y = 0; x1.x = v1; x1.y = 0;
+        D[2 * beta] = x0;
+        D[2 * beta + 1] = x1;
+    }
+}
+
+template <typename T>
+__global__ void reduce_kernel(const ReduceArgs a, const int* exps) {
+    const T* __restrict__ Rt = static_cast<const T*>(a.root);
+    const PassParams p = *a.params;
+    const int64_t total = a.out_size * a.nbeta;
+    const double scale = exps ? pow2d(exps[2 * a.exp_root]) : 1.0;
+    const int ns = a.nsigma > 1 ? min(a.nsigma, p.slices_valid) : 1;
+    const double mult = a.nsigma > 1 ? 1.0 : (double)p.slices_valid;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total; idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = idx % a.out_size;
+        const int beta = (int)(idx / a.out_size);
+        if (beta >= p.bits_valid && !a.broadcast) continue;
+        int64_t off = pdep(beta, a.beta_map);
+        int64_t rem = e;
+        for (int ax = 0; ax < a.naxes; ax++) {
+            const int64_t d = rem % a.axis_dim[ax];
+            rem /= a.axis_dim[ax];
+            for (int j = 0; j < a.axis_nbits[ax]; j++)
+                if ((d >> j) & 1) off += int64_t(1) << a.axis_bitpos[ax][j];
+        }
+        double re = 0.0, im = 0.0;
+        for (int s = 0; s < ns; s++) {
+            const T v = Rt[off + pdep(s, a.sigma_map)];
+            re += (double)v.x;
+            im += (double)v.y;
+        }
+        re *= scale * mult; im *= scale * mult;
+        if (a.broadcast) {
+            for (int b = 0; b < p.bits_valid; b++) {
+                double* o = a.out + 2 * ((int64_t)(p.bit_base + b) * a.out_size + e);
+                o[0] += re; o[1] += im;
+            }
+        } else {
+            double* o = a.out + 2 * ((int64_t)(p.bit_base + beta) * a.out_size + e);
+            o[0] += re; o[1] += im;
+        }
+    }
+}
+
+__global__ void reset_exps_kernel(int* exps, int begin, int end) {
+    for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+        exps[2 * i] = 0;
+        exps[2 * i + 1] = kExpUnset;
+    }
+}
+
+int grid_for(int64_t n, int threads, int cap) {
+    int64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+
+}  // namespace
+
+cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count) {
+    int ncb = 0;
+    while ((int64_t(1) << ncb) < a.nC) ncb++;
+    const int tb = ncb < kTileBits ? ncb : kTileBits;
+    const int64_t ntiles = a.nC >> tb;
+    const int64_t cap = (int64_t)sm_count * 8;
+    const int grid = (int)(ntiles < cap ? ntiles : cap);
+    if (fp64) contract_kernel<double2, false><<<grid, kThreads, 0, s>>>(a, exps);
+    else if (exps) contract_kernel<float2, true><<<grid, kThreads, 0, s>>>(a, exps);
+    else contract_kernel<float2, false><<<grid, kThreads, 0, s>>>(a, exps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_view(const ViewArgs& a, bool fp64, int* exps, cudaStream_t s) {
+    const int g = grid_for(a.n, 256, 4096);
+    if (fp64) view_kernel<double2><<<g, 256, 0, s>>>(a, exps);
+    else view_kernel<float2><<<g, 256, 0, s>>>(a, exps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_output(const OutputArgs& a, bool fp64, int* exps, cudaStream_t s) {
+    const int g = grid_for(a.nbeta, 256, 1024);
+    if (fp64) output_kernel<double2><<<g, 256, 0, s>>>(a, exps);
+    else output_kernel<float2><<<g, 256, 0, s>>>(a, exps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce(const ReduceArgs& a, bool fp64, const int* exps, cudaStream_t s) {
+    const int g = grid_for(a.out_size * a.nbeta, 256, 4096);
+    if (fp64) reduce_kernel<double2><<<g, 256, 0, s>>>(a, exps);
+    else reduce_kernel<float2><<<g, 256, 0, s>>>(a, exps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reset_exps(int* exps, int begin, int end, cudaStream_t s) {
+    if (end <= begin) return cudaSuccess;
+    reset_exps_kernel<<<grid_for(end - begin, 256, 64), 256, 0, s>>>(exps, begin, end);
+    return cudaGetLastError();
+}
+
+}  // namespace qxg

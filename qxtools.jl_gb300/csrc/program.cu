@@ -1,0 +1,1009 @@
+// Host side of the executor: compiles a `.qx` command list (include/qxgpu.h, qxg_instr) into
+// per-step bit maps, plans the device workspace, and runs the programme over batches of
+// slices and bitstrings.  This replaces QXContexts.execute's walk (bin/qxrun.jl:83-87) and
+// `single_amplitude`'s contract_tn! (src/simulation.jl:86-91).
+//
+// Execution model.  Tensors that depend on neither the output bitstring nor a slice variable
+// ("invariant") are computed once per call; tensors that depend on slice variables only are
+// computed once per slice batch; tensors that depend on output tensors are computed once per
+// (slice batch, bitstring batch).  Slice and bitstring batches are extra bit fields ("sigma",
+// "beta") of the tensors that depend on them, so a batch of slices or bitstrings is one
+// larger contraction instead of many small ones.  The saved tensor is summed over the slice
+// batch in FP64 and accumulated across slice batches (users_guide.md:11-17).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/qxgpu.h"
+#include "qxgpu_internal.h"
+#include "tc_gemm.h"
+
+using namespace qxg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define QXG_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t _e = (call);                                                             \
+        if (_e != cudaSuccess)                                                               \
+            return fail(QXG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));   \
+    } while (0)
+
+int ilog2(int64_t x) {
+    int b = 0;
+    while ((int64_t(1) << b) < x) b++;
+    return b;
+}
+int64_t pow2ceil(int64_t x) { return int64_t(1) << ilog2(x < 1 ? 1 : x); }
+
+// A physical bit of a tensor: logical axis `axis` bit `j`, or a batch bit.
+constexpr int16_t kBeta = -1, kSigma = -2;
+struct PBit {
+    int16_t axis;
+    int16_t j;
+    bool operator==(const PBit& o) const { return axis == o.axis && j == o.j; }
+};
+
+struct Tensor {
+    int kind = 0;                       // QXG_OP_*
+    int instr = -1;
+    std::vector<int64_t> dims;          // logical dims (views: sliced axis 1)
+    std::vector<int64_t> pdims;         // padded to powers of two
+    bool beta = false, sigma = false;
+    int group = 0;                      // 0 invariant, 1 slice, 2 bitstring
+    int data_id = -1;                   // LOAD
+    int qubit = -1;                     // OUTPUT
+    int view_root = -1;                 // VIEW: LOAD/OUTPUT tensor at the start of the chain
+    std::vector<std::pair<int, int>> fixes;   // VIEW: (axis, slice variable)
+    bool needed = false;                // read by an ncon or the save
+    // per batch plan
+    std::vector<PBit> layout;
+    int64_t arena_off = -1;
+    int slot = -1;                      // exponent slot
+};
+
+struct Step {                           // an executable item of a pass
+    int kind;                           // QXG_OP_NCON / VIEW / OUTPUT
+    int tensor;                         // tensor produced
+    StepArgs sargs;
+    ViewArgs vargs;
+    OutputArgs oargs;
+    bool use_tc = false;                // tensor-core path (split modes)
+    TcStep tc;                          // tensor-core step description
+    double flops = 0, bytes = 0;
+};
+
+struct Plan {
+    int bc = 0, sc = 0;                 // bitstring / slice batch sizes (powers of two)
+    std::vector<Tensor> T;              // tensors with layouts for this plan
+    std::vector<Step> steps[3];         // per group, in execution order
+    int slot_begin[3], slot_end[3];
+    size_t arena_bytes = 0;
+    size_t tc_scratch_bytes = 0;
+    ReduceArgs red;
+    double flops_pass[3] = {0, 0, 0}, bytes_pass[3] = {0, 0, 0};
+};
+
+}  // namespace
+
+struct qxg_program {
+    qxg_options opts;
+    bool fp64 = true;
+    int esize = 16;
+    int device = 0;
+    int sm_count = 148;
+    cudaStream_t stream = nullptr;
+    int nqubits = 0;
+    std::vector<qxg_instr> ins;
+    std::vector<int32_t> labels;
+    std::vector<std::vector<int64_t>> ddims, dpdims;
+    std::vector<void*> d_data;
+    std::vector<int> data_m;
+    std::vector<bool> data_set;
+    std::vector<Tensor> base;           // tensors without batch layouts
+    int root = -1;
+    std::vector<int64_t> var_dim;
+    int64_t nslices = 1;
+    double flops_per_amp = 0;
+    // batch plan and device buffers
+    std::unique_ptr<Plan> plan;
+    void* d_arena = nullptr;
+    size_t arena_cap = 0;
+    void* d_scratch = nullptr;
+    size_t scratch_cap = 0;
+    int* d_exps = nullptr;
+    int nslots = 0;
+    PassParams* d_params = nullptr;
+    PassParams* h_params = nullptr;     // pinned, one per pass
+    size_t h_params_cap = 0;
+    char* d_bits = nullptr;
+    size_t d_bits_cap = 0;
+    double* d_out = nullptr;
+    size_t d_out_cap = 0;
+    std::vector<int> h_exps_init;
+};
+
+namespace {
+
+// ------------------------------------------------------------------------------------------
+// structural compile
+// ------------------------------------------------------------------------------------------
+int compile_structure(qxg_program* P) {
+    const int n = (int)P->ins.size();
+    int ntensors = 0;
+    for (const auto& I : P->ins)
+        if (I.op != QXG_OP_SAVE) ntensors = std::max(ntensors, I.dst + 1);
+    if (ntensors <= 0) return fail(QXG_ERR_INVALID, "programme defines no tensors");
+    P->base.assign(ntensors, Tensor());
+    std::vector<bool> defined(ntensors, false);
+    std::map<int, int64_t> vdim;
+    int nsave = 0;
+    auto need_def = [&](int t, int line) -> int {
+        if (t < 0 || t >= ntensors || !defined[t])
+            return fail(QXG_ERR_INVALID, "instruction " + std::to_string(line) + ": tensor " +
+                                             std::to_string(t) + " used before definition");
+        return 0;
+    };
+    for (int i = 0; i < n; i++) {
+        const qxg_instr& I = P->ins[i];
+        if (I.op != QXG_OP_SAVE) {
+            if (I.dst < 0 || I.dst >= ntensors) return fail(QXG_ERR_INVALID, "bad tensor id");
+            if (defined[I.dst])
+                return fail(QXG_ERR_INVALID, "tensor " + std::to_string(I.dst) + " defined twice");
+        }
+        Tensor& t = P->base[I.op == QXG_OP_SAVE ? 0 : I.dst];
+        switch (I.op) {
+        case QXG_OP_LOAD: {
+            if (I.a < 0 || I.a >= (int)P->ddims.size()) return fail(QXG_ERR_INVALID, "load: bad data id");
+            t.kind = I.op; t.instr = i; t.data_id = I.a;
+            t.dims = P->ddims[I.a];
+            break;
+        }
+        case QXG_OP_OUTPUT: {
+            if (I.a < 0 || I.a >= P->nqubits) return fail(QXG_ERR_INVALID, "output: qubit out of range");
+            if (I.b != 2) return fail(QXG_ERR_UNSUPPORTED, "output: only dimension 2 is supported");
+            t.kind = I.op; t.instr = i; t.qubit = I.a; t.dims = {2};
+            t.beta = true;
+            break;
+        }
+        case QXG_OP_VIEW: {
+            if (int r = need_def(I.a, i)) return r;
+            const Tensor& s = P->base[I.a];
+            if (s.kind != QXG_OP_LOAD && s.kind != QXG_OP_OUTPUT && s.kind != QXG_OP_VIEW)
+                return fail(QXG_ERR_UNSUPPORTED, "view: only leaf, output and view tensors can be viewed");
+            if (I.pos < 0 || I.pos >= (int)s.dims.size()) return fail(QXG_ERR_INVALID, "view: rank position out of range");
+            if (I.b < 0 || I.b >= kMaxViewFix * 64) return fail(QXG_ERR_INVALID, "view: bad slice variable");
+            if (I.dim <= 0 || s.dims[I.pos] != I.dim)
+                return fail(QXG_ERR_INVALID, "view: dimension does not match the viewed index");
+            auto it = vdim.find(I.b);
+            if (it != vdim.end() && it->second != I.dim)
+                return fail(QXG_ERR_INVALID, "view: slice variable used with two dimensions");
+            vdim[I.b] = I.dim;
+            t.kind = I.op; t.instr = i;
+            t.dims = s.dims; t.dims[I.pos] = 1;
+            t.view_root = s.kind == QXG_OP_VIEW ? s.view_root : I.a;
+            t.fixes = s.fixes;
+            t.fixes.push_back({I.pos, I.b});
+            if ((int)t.fixes.size() > kMaxViewFix) return fail(QXG_ERR_UNSUPPORTED, "view: too many chained views");
+            t.beta = s.beta; t.sigma = true;
+            break;
+        }
+        case QXG_OP_NCON: {
+            if (int r = need_def(I.a, i)) return r;
+            if (int r = need_def(I.b, i)) return r;
+            if (I.nc < 0 || I.na < 0 || I.nb < 0 || I.label_off < 0 ||
+                (int64_t)I.label_off + I.nc + I.na + I.nb > (int64_t)P->labels.size())
+                return fail(QXG_ERR_INVALID, "ncon: label range out of bounds");
+            const Tensor& A = P->base[I.a];
+            const Tensor& B = P->base[I.b];
+            if ((int)A.dims.size() != I.na || (int)B.dims.size() != I.nb)
+                return fail(QXG_ERR_INVALID, "ncon " + std::to_string(i) + ": label count does not match operand rank");
+            const int32_t* lc = &P->labels[I.label_off];
+            const int32_t* la = lc + I.nc;
+            const int32_t* lb = la + I.na;
+            std::map<int32_t, int64_t> ld;
+            for (int q = 0; q < I.na; q++) {
+                if (la[q] <= 0) return fail(QXG_ERR_INVALID, "ncon: labels must be positive");
+                if (ld.count(la[q])) return fail(QXG_ERR_UNSUPPORTED, "ncon: repeated label within an operand");
+                ld[la[q]] = A.dims[q];
+            }
+            std::map<int32_t, int64_t> lbm;
+            for (int q = 0; q < I.nb; q++) {
+                if (lb[q] <= 0) return fail(QXG_ERR_INVALID, "ncon: labels must be positive");
+                if (lbm.count(lb[q])) return fail(QXG_ERR_UNSUPPORTED, "ncon: repeated label within an operand");
+                lbm[lb[q]] = B.dims[q];
+                auto it = ld.find(lb[q]);
+                if (it != ld.end() && it->second != B.dims[q])
+                    return fail(QXG_ERR_INVALID, "ncon " + std::to_string(i) + ": label " + std::to_string(lb[q]) +
+                                                     " has different dimensions in the operands");
+                ld[lb[q]] = B.dims[q];
+            }
+            t.kind = I.op; t.instr = i;
+            t.dims.clear();
+            std::map<int32_t, int> seen;
+            for (int q = 0; q < I.nc; q++) {
+                auto it = ld.find(lc[q]);
+                if (it == ld.end()) return fail(QXG_ERR_INVALID, "ncon: result label not in operands");
+                if (seen.count(lc[q])) return fail(QXG_ERR_INVALID, "ncon: repeated result label");
+                seen[lc[q]] = q;
+                t.dims.push_back(it->second);
+            }
+            t.beta = A.beta || B.beta;
+            t.sigma = A.sigma || B.sigma;
+            P->base[I.a].needed = true;
+            P->base[I.b].needed = true;
+            // algorithmic flops: 8 |C| K over the unsliced dims is accumulated below
+            break;
+        }
+        case QXG_OP_SAVE: {
+            if (int r = need_def(I.a, i)) return r;
+            P->root = I.a;
+            P->base[I.a].needed = true;
+            nsave++;
+            break;
+        }
+        default:
+            return fail(QXG_ERR_INVALID, "unknown opcode " + std::to_string(I.op));
+        }
+        if (I.op != QXG_OP_SAVE) defined[I.dst] = true;
+    }
+    if (nsave != 1) return fail(QXG_ERR_INVALID, "programme must have exactly one save");
+    for (auto& t : P->base) {
+        t.pdims.clear();
+        for (int64_t d : t.dims) t.pdims.push_back(pow2ceil(d));
+        t.group = t.beta ? 2 : (t.sigma ? 1 : 0);
+        if (t.kind == QXG_OP_VIEW && t.needed) P->base[t.view_root].needed = true;
+    }
+    // slice variables: dense ids 0..V-1 required
+    P->var_dim.clear();
+    for (auto& kv : vdim) {
+        if (kv.first != (int)P->var_dim.size()) return fail(QXG_ERR_INVALID, "slice variables must be numbered 0..V-1");
+        P->var_dim.push_back(kv.second);
+    }
+    P->nslices = 1;
+    for (int64_t d : P->var_dim) {
+        if (P->nslices > (int64_t(1) << 40) / d) return fail(QXG_ERR_UNSUPPORTED, "too many slices");
+        P->nslices *= d;
+    }
+    // algorithmic flops per amplitude: each ncon's 8 |C| K with sliced dims at 1, times slices
+    double f = 0;
+    for (int i = 0; i < n; i++) {
+        const qxg_instr& I = P->ins[i];
+        if (I.op != QXG_OP_NCON) continue;
+        const int32_t* lc = &P->labels[I.label_off];
+        const int32_t* la = lc + I.nc;
+        const int32_t* lb = la + I.na;
+        std::map<int32_t, int64_t> ld;
+        for (int q = 0; q < I.na; q++) ld[la[q]] = P->base[I.a].dims[q];
+        for (int q = 0; q < I.nb; q++) ld[lb[q]] = P->base[I.b].dims[q];
+        double all = 1;
+        for (auto& kv : ld) all *= (double)kv.second;
+        f += 8.0 * all;
+    }
+    P->flops_per_amp = f * (double)P->nslices;
+    return 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// batch plan
+// ------------------------------------------------------------------------------------------
+int bits_of(const Tensor& t, int axis) { return ilog2(t.pdims[axis]); }
+
+BitMap make_map(const std::vector<std::pair<int, int>>& pairs /* (src bit, dst bit) */, int* err) {
+    std::vector<std::pair<int, int>> p = pairs;
+    std::sort(p.begin(), p.end());
+    BitMap m;
+    m.n = 0;
+    for (size_t i = 0; i < p.size();) {
+        size_t j = i + 1;
+        while (j < p.size() && p[j].first == p[j - 1].first + 1 && p[j].second == p[j - 1].second + 1) j++;
+        if (m.n >= kMaxRuns) { *err = 1; return m; }
+        m.r[m.n].src = (uint8_t)p[i].first;
+        m.r[m.n].len = (uint8_t)(j - i);
+        m.r[m.n].dst = (uint8_t)p[i].second;
+        m.r[m.n].pad = 0;
+        m.n++;
+        i = j;
+    }
+    return m;
+}
+
+int position_of(const Tensor& t, PBit b) {
+    for (size_t p = 0; p < t.layout.size(); p++)
+        if (t.layout[p] == b) return (int)p;
+    return -1;
+}
+
+int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out) {
+    auto plan = std::make_unique<Plan>();
+    plan->bc = bc;
+    plan->sc = sc;
+    plan->T = P->base;
+    auto& T = plan->T;
+    const int nbb = ilog2(bc), nsb = ilog2(sc);
+    const int ntensors = (int)T.size();
+    int err = 0;
+    // layouts in instruction order
+    for (const auto& I : P->ins) {
+        if (I.op == QXG_OP_SAVE) continue;
+        Tensor& t = T[I.dst];
+        t.layout.clear();
+        if (I.op == QXG_OP_LOAD) {
+            for (int a = 0; a < (int)t.pdims.size(); a++)
+                for (int j = 0; j < bits_of(t, a); j++) t.layout.push_back({(int16_t)a, (int16_t)j});
+        } else if (I.op == QXG_OP_OUTPUT) {
+            t.layout.push_back({0, 0});
+            for (int j = 0; j < nbb; j++) t.layout.push_back({kBeta, (int16_t)j});
+        } else if (I.op == QXG_OP_VIEW) {
+            const Tensor& r = T[t.view_root];
+            for (const PBit& b : r.layout) {
+                bool fixed = false;
+                if (b.axis >= 0)
+                    for (auto& f : t.fixes) if (f.first == b.axis) fixed = true;
+                if (!fixed) t.layout.push_back(b);
+            }
+            for (int j = 0; j < nsb; j++) t.layout.push_back({kSigma, (int16_t)j});
+        } else if (I.op == QXG_OP_NCON) {
+            const Tensor& A = T[I.a];
+            const Tensor& B = T[I.b];
+            const int32_t* lc = &P->labels[I.label_off];
+            const int32_t* la = lc + I.nc;
+            const int32_t* lb = la + I.na;
+            auto axis_in = [](const int32_t* ls, int n, int32_t L) {
+                for (int q = 0; q < n; q++) if (ls[q] == L) return q;
+                return -1;
+            };
+            // translate an operand bit into the result's bit (or mark K with axis -3)
+            auto to_c = [&](const int32_t* ls, PBit b) -> PBit {
+                if (b.axis < 0) return b;
+                const int ca = axis_in(lc, I.nc, ls[b.axis]);
+                if (ca < 0) return {-3, 0};
+                return {(int16_t)ca, b.j};
+            };
+            const bool a_big = A.layout.size() >= B.layout.size();
+            const Tensor& X = a_big ? A : B;
+            const Tensor& Y = a_big ? B : A;
+            const int32_t* lx = a_big ? la : lb;
+            const int32_t* ly = a_big ? lb : la;
+            std::vector<PBit> from_x;
+            for (const PBit& b : X.layout) { PBit c = to_c(lx, b); if (c.axis != -3) from_x.push_back(c); }
+            std::vector<PBit> fresh;
+            for (const PBit& b : Y.layout) {
+                PBit c = to_c(ly, b);
+                if (c.axis == -3) continue;
+                if (std::find(from_x.begin(), from_x.end(), c) == from_x.end()) fresh.push_back(c);
+            }
+            size_t fi = 0;
+            for (const PBit& b : X.layout) {
+                PBit c = to_c(lx, b);
+                if (c.axis != -3) t.layout.push_back(c);
+                else if (fi < fresh.size()) t.layout.push_back(fresh[fi++]);
+            }
+            while (fi < fresh.size()) t.layout.push_back(fresh[fi++]);
+        }
+        if (t.layout.size() > 46) return fail(QXG_ERR_UNSUPPORTED, "tensor with more than 2^46 elements");
+    }
+    // steps, groups and exponent slots
+    // leaves first (their slots are set once per call), then one contiguous range per group
+    // (reset before every pass of that group)
+    int slot = 0;
+    for (int i = 0; i < ntensors; i++)
+        if (T[i].kind == QXG_OP_LOAD) T[i].slot = slot++;
+    for (int g = 0; g < 3; g++) {
+        plan->slot_begin[g] = slot;
+        for (int i = 0; i < ntensors; i++)
+            if (T[i].group == g && T[i].kind != QXG_OP_LOAD) T[i].slot = slot++;
+        plan->slot_end[g] = slot;
+    }
+    for (int ii = 0; ii < (int)P->ins.size(); ii++) {
+        const qxg_instr& I = P->ins[ii];
+        if (I.op == QXG_OP_SAVE || I.op == QXG_OP_LOAD) continue;
+        Tensor& t = T[I.dst];
+        if (!t.needed) continue;
+        Step st;
+        memset(&st.sargs, 0, sizeof(st.sargs));
+        memset(&st.vargs, 0, sizeof(st.vargs));
+        memset(&st.oargs, 0, sizeof(st.oargs));
+        st.kind = I.op;
+        st.tensor = I.dst;
+        if (I.op == QXG_OP_OUTPUT) {
+            st.oargs.qubit = t.qubit;
+            st.oargs.nqubits = P->nqubits;
+            st.oargs.nbeta = bc;
+            st.oargs.exp_dst = t.slot;
+        } else if (I.op == QXG_OP_VIEW) {
+            const Tensor& r = T[t.view_root];
+            std::vector<std::pair<int, int>> pairs;
+            int sig = 0;
+            for (int p = 0; p < (int)t.layout.size(); p++) {
+                if (t.layout[p].axis == kSigma) { sig++; continue; }
+                const int q = position_of(r, t.layout[p]);
+                if (q < 0) return fail(QXG_ERR_INVALID, "internal: view layout");
+                pairs.push_back({p, q});
+            }
+            st.vargs.sigma_shift = (int)t.layout.size() - sig;
+            st.vargs.map = make_map(pairs, &err);
+            st.vargs.n = int64_t(1) << t.layout.size();
+            st.vargs.nfix = (int)t.fixes.size();
+            for (int f = 0; f < st.vargs.nfix; f++) {
+                const int ax = t.fixes[f].first, var = t.fixes[f].second;
+                st.vargs.fix_shift[f] = position_of(r, PBit{(int16_t)ax, 0});
+                if (st.vargs.fix_shift[f] < 0) return fail(QXG_ERR_INVALID, "internal: view fix");
+                int64_t stride = 1;
+                for (int v = 0; v < var; v++) stride *= P->var_dim[v];
+                st.vargs.var_stride[f] = stride;
+                st.vargs.var_dim[f] = P->var_dim[var];
+                for (int j = 1; j < bits_of(r, ax); j++)
+                    if (position_of(r, PBit{(int16_t)ax, (int16_t)j}) != st.vargs.fix_shift[f] + j)
+                        return fail(QXG_ERR_INVALID, "internal: viewed axis bits not contiguous");
+            }
+            st.vargs.exp_src = T[t.view_root].slot;
+            st.vargs.exp_dst = t.slot;
+        } else {  // NCON
+            const Tensor& A = T[I.a];
+            const Tensor& B = T[I.b];
+            const int32_t* lc = &P->labels[I.label_off];
+            const int32_t* la = lc + I.nc;
+            const int32_t* lb = la + I.na;
+            auto axis_in = [](const int32_t* ls, int n, int32_t L) {
+                for (int q = 0; q < n; q++) if (ls[q] == L) return q;
+                return -1;
+            };
+            std::vector<std::pair<int, int>> cA, cB, kA, kB;
+            for (int p = 0; p < (int)t.layout.size(); p++) {
+                const PBit b = t.layout[p];
+                PBit ba = b, bb = b;
+                if (b.axis >= 0) {
+                    ba.axis = (int16_t)axis_in(la, I.na, lc[b.axis]);
+                    bb.axis = (int16_t)axis_in(lb, I.nb, lc[b.axis]);
+                }
+                const int pa = (b.axis >= 0 && ba.axis < 0) ? -1 : position_of(A, ba);
+                const int pb = (b.axis >= 0 && bb.axis < 0) ? -1 : position_of(B, bb);
+                if (pa < 0 && pb < 0) return fail(QXG_ERR_INVALID, "internal: result bit without source");
+                if (pa >= 0) cA.push_back({p, pa});
+                if (pb >= 0) cB.push_back({p, pb});
+            }
+            // summed bits: operand bits whose label is not in the result, in the bigger
+            // operand's physical order
+            const bool a_big = A.layout.size() >= B.layout.size();
+            const Tensor& X = a_big ? A : B;
+            const Tensor& Y = a_big ? B : A;
+            const int32_t* lx = a_big ? la : lb;
+            const int32_t* ly = a_big ? lb : la;
+            const int nyl = a_big ? I.nb : I.na;
+            int kbit = 0;
+            std::vector<std::pair<int, int>>& kX = a_big ? kA : kB;
+            std::vector<std::pair<int, int>>& kY = a_big ? kB : kA;
+            for (int p = 0; p < (int)X.layout.size(); p++) {
+                const PBit b = X.layout[p];
+                if (b.axis < 0) continue;
+                if (axis_in(lc, I.nc, lx[b.axis]) >= 0) continue;
+                kX.push_back({kbit, p});
+                const int yax = axis_in(ly, nyl, lx[b.axis]);
+                if (yax >= 0) {
+                    const int q = position_of(Y, PBit{(int16_t)yax, b.j});
+                    if (q >= 0) kY.push_back({kbit, q});
+                }
+                kbit++;
+            }
+            for (int p = 0; p < (int)Y.layout.size(); p++) {   // labels summed but only in Y
+                const PBit b = Y.layout[p];
+                if (b.axis < 0) continue;
+                if (axis_in(lc, I.nc, ly[b.axis]) >= 0) continue;
+                const int32_t* lxx = lx;
+                const int nxl = a_big ? I.na : I.nb;
+                if (axis_in(lxx, nxl, ly[b.axis]) >= 0) continue;
+                kY.push_back({kbit, p});
+                kbit++;
+            }
+            st.sargs.nC = int64_t(1) << t.layout.size();
+            st.sargs.nk = kbit;
+            st.sargs.cA = make_map(cA, &err);
+            st.sargs.cB = make_map(cB, &err);
+            st.sargs.kA = make_map(kA, &err);
+            st.sargs.kB = make_map(kB, &err);
+            st.sargs.expA = A.slot;
+            st.sargs.expB = B.slot;
+            st.sargs.expC = t.slot;
+            const double s = P->fp64 ? 16.0 : 8.0;
+            st.flops = 8.0 * (double)st.sargs.nC * (double)(int64_t(1) << kbit);
+            st.bytes = s * ((double)(int64_t(1) << A.layout.size()) + (double)(int64_t(1) << B.layout.size()) +
+                            (double)st.sargs.nC);
+            if (!P->fp64 && P->opts.precision != QXG_PREC_FP32)
+                st.use_tc = tc_plan_step(st.sargs, A.layout.size(), B.layout.size(), t.layout.size(),
+                                         P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc);
+        }
+        if (err) return fail(QXG_ERR_UNSUPPORTED, "bit map needs more than the supported number of runs");
+        plan->flops_pass[t.group] += st.flops;
+        plan->bytes_pass[t.group] += st.bytes;
+        plan->steps[t.group].push_back(st);
+    }
+    // arena: lifetimes over the execution sequence group0, group1, group2
+    struct Item { int tensor; int def; int last; int64_t bytes; };
+    std::vector<int> pos_of(ntensors, -1);
+    int pos = 0;
+    for (int g = 0; g < 3; g++)
+        for (auto& st : plan->steps[g]) pos_of[st.tensor] = pos++;
+    const int end_pos = pos + 1;
+    std::vector<int> last(ntensors, -1);
+    auto use = [&](int t, int at) {
+        if (pos_of[t] < 0) return;
+        last[t] = std::max(last[t], at);
+        // used by a later group -> alive until the end (the later group repeats)
+        const int gt = T[t].group;
+        int gat = 0;
+        int acc = 0;
+        for (int g = 0; g < 3; g++) { acc += (int)plan->steps[g].size(); if (at < acc) { gat = g; break; } }
+        if (gat > gt) last[t] = end_pos;
+    };
+    pos = 0;
+    for (int g = 0; g < 3; g++) {
+        for (auto& st : plan->steps[g]) {
+            const qxg_instr& I = P->ins[T[st.tensor].instr];
+            if (st.kind == QXG_OP_NCON) { use(I.a, pos); use(I.b, pos); }
+            if (st.kind == QXG_OP_VIEW) use(T[st.tensor].view_root, pos);
+            pos++;
+        }
+    }
+    if (pos_of[P->root] >= 0) last[P->root] = end_pos;
+    std::vector<Item> items;
+    for (int t = 0; t < ntensors; t++) {
+        if (pos_of[t] < 0) continue;
+        const int64_t bytes = ((int64_t(1) << T[t].layout.size()) * (int64_t)P->esize + 255) & ~int64_t(255);
+        items.push_back({t, pos_of[t], std::max(last[t], pos_of[t]), bytes});
+    }
+    std::vector<int> order(items.size());
+    for (size_t i = 0; i < items.size(); i++) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) {
+        if (items[x].bytes != items[y].bytes) return items[x].bytes > items[y].bytes;
+        return items[x].def < items[y].def;
+    });
+    struct Placed { int64_t off, bytes; int def, last; };
+    std::vector<Placed> placed;
+    int64_t total = 0;
+    for (int oi : order) {
+        const Item& it = items[oi];
+        std::vector<std::pair<int64_t, int64_t>> busy;
+        for (auto& p : placed)
+            if (!(p.last < it.def || it.last < p.def)) busy.push_back({p.off, p.off + p.bytes});
+        std::sort(busy.begin(), busy.end());
+        int64_t off = 0;
+        for (auto& b : busy) {
+            if (off + it.bytes <= b.first) break;
+            off = std::max(off, b.second);
+        }
+        placed.push_back({off, it.bytes, it.def, it.last});
+        T[it.tensor].arena_off = off;
+        total = std::max(total, off + it.bytes);
+    }
+    plan->arena_bytes = (size_t)total;
+    size_t scratch = 0;
+    for (int g = 0; g < 3; g++)
+        for (auto& st : plan->steps[g]) if (st.use_tc) scratch = std::max(scratch, st.tc.scratch_bytes);
+    plan->tc_scratch_bytes = scratch;
+    // reduction of the root
+    {
+        const Tensor& r = T[P->root];
+        ReduceArgs& ra = plan->red;
+        memset(&ra, 0, sizeof(ra));
+        ra.naxes = (int)r.dims.size();
+        if (ra.naxes > kMaxOutAxes) return fail(QXG_ERR_UNSUPPORTED, "saved tensor has too many axes");
+        int64_t osz = 1;
+        for (int a = 0; a < ra.naxes; a++) {
+            ra.axis_dim[a] = (int32_t)r.dims[a];
+            ra.axis_nbits[a] = bits_of(r, a);
+            if (ra.axis_nbits[a] > 3) return fail(QXG_ERR_UNSUPPORTED, "saved tensor axis wider than 8");
+            for (int j = 0; j < ra.axis_nbits[a]; j++) {
+                ra.axis_bitpos[a][j] = position_of(r, PBit{(int16_t)a, (int16_t)j});
+                if (ra.axis_bitpos[a][j] < 0) return fail(QXG_ERR_INVALID, "internal: root layout");
+            }
+            osz *= r.dims[a];
+        }
+        ra.out_size = osz;
+        std::vector<std::pair<int, int>> bm, sm;
+        for (int p = 0; p < (int)r.layout.size(); p++) {
+            if (r.layout[p].axis == kBeta) bm.push_back({r.layout[p].j, p});
+            if (r.layout[p].axis == kSigma) sm.push_back({r.layout[p].j, p});
+        }
+        ra.beta_map = make_map(bm, &err);
+        ra.sigma_map = make_map(sm, &err);
+        ra.nbeta = r.beta ? bc : 1;
+        ra.nsigma = r.sigma ? sc : 1;
+        ra.broadcast = r.beta ? 0 : 1;
+        ra.exp_root = r.slot;
+        if (err) return fail(QXG_ERR_UNSUPPORTED, "root bit map too fragmented");
+    }
+    out = std::move(plan);
+    return 0;
+}
+
+// choose batch sizes that fit the workspace limit
+int ensure_plan(qxg_program* P, int nbits_call) {
+    const int64_t want_b = std::max<int64_t>(1, pow2ceil(nbits_call));
+    const int64_t max_b = P->opts.max_bitstring_batch > 0 ? pow2ceil(P->opts.max_bitstring_batch) : 256;
+    const int64_t max_s = P->opts.max_slice_batch > 0 ? pow2ceil(P->opts.max_slice_batch) : 1024;
+    int64_t bc = std::min(want_b, max_b);
+    int64_t sc = std::min(pow2ceil(P->nslices), max_s);
+    bool has_out = false;
+    for (auto& t : P->base) if (t.kind == QXG_OP_OUTPUT && t.needed) has_out = true;
+    if (!has_out) bc = 1;
+    if (P->plan && P->plan->bc == bc && P->plan->sc == sc) return 0;
+    size_t limit = (size_t)P->opts.workspace_limit;
+    if (limit == 0) {
+        size_t fr = 0, tot = 0;
+        QXG_CUDA(cudaMemGetInfo(&fr, &tot));
+        limit = fr / 4 * 3 + P->arena_cap + P->scratch_cap;
+    }
+    while (true) {
+        std::unique_ptr<Plan> pl;
+        if (int r = build_plan(P, (int)bc, (int)sc, pl)) return r;
+        if (pl->arena_bytes + pl->tc_scratch_bytes <= limit) {
+            P->plan = std::move(pl);
+            break;
+        }
+        if (sc == 1 && bc == 1)
+            return fail(QXG_ERR_OOM, "workspace of " + std::to_string(pl->arena_bytes) +
+                                         " bytes for one slice and one bitstring exceeds the limit");
+        if (sc >= bc && sc > 1) sc /= 2; else bc /= 2;
+    }
+    Plan& pl = *P->plan;
+    if (pl.arena_bytes > P->arena_cap) {
+        if (P->d_arena) cudaFree(P->d_arena);
+        P->d_arena = nullptr; P->arena_cap = 0;
+        QXG_CUDA(cudaMalloc(&P->d_arena, std::max<size_t>(pl.arena_bytes, 256)));
+        P->arena_cap = pl.arena_bytes;
+    }
+    if (pl.tc_scratch_bytes > P->scratch_cap) {
+        if (P->d_scratch) cudaFree(P->d_scratch);
+        P->d_scratch = nullptr; P->scratch_cap = 0;
+        QXG_CUDA(cudaMalloc(&P->d_scratch, pl.tc_scratch_bytes));
+        P->scratch_cap = pl.tc_scratch_bytes;
+    }
+    const int ns = pl.slot_end[2];
+    if (ns > P->nslots) {
+        if (P->d_exps) cudaFree(P->d_exps);
+        P->d_exps = nullptr;
+        QXG_CUDA(cudaMalloc(&P->d_exps, sizeof(int) * 2 * std::max(ns, 1)));
+        P->nslots = ns;
+    }
+    // bind pointers
+    char* arena = static_cast<char*>(P->d_arena);
+    auto ptr = [&](int t) -> void* {
+        const Tensor& x = pl.T[t];
+        if (x.kind == QXG_OP_LOAD) return P->d_data[x.data_id];
+        return arena + x.arena_off;
+    };
+    for (int g = 0; g < 3; g++)
+        for (auto& st : pl.steps[g]) {
+            const Tensor& t = pl.T[st.tensor];
+            const qxg_instr& I = P->ins[t.instr];
+            if (st.kind == QXG_OP_NCON) {
+                st.sargs.A = ptr(I.a); st.sargs.B = ptr(I.b); st.sargs.C = ptr(st.tensor);
+            } else if (st.kind == QXG_OP_VIEW) {
+                st.vargs.src = ptr(t.view_root); st.vargs.dst = ptr(st.tensor); st.vargs.params = P->d_params;
+            } else {
+                st.oargs.dst = ptr(st.tensor); st.oargs.params = P->d_params;
+            }
+        }
+    pl.red.root = ptr(P->root);
+    pl.red.params = P->d_params;
+    // initial exponent slots: LOAD tensors carry their data's maximum exponent
+    P->h_exps_init.assign(2 * std::max(ns, 1), 0);
+    for (auto& t : pl.T) {
+        if (t.slot < 0) continue;
+        P->h_exps_init[2 * t.slot] = 0;
+        P->h_exps_init[2 * t.slot + 1] = t.kind == QXG_OP_LOAD ? P->data_m[t.data_id] : kExpUnset;
+    }
+    return 0;
+}
+
+int run_group(qxg_program* P, int g) {
+    Plan& pl = *P->plan;
+    int* exps = P->fp64 ? nullptr : P->d_exps;
+    if (exps) QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[g], pl.slot_end[g], P->stream));
+    for (auto& st : pl.steps[g]) {
+        if (st.kind == QXG_OP_NCON) {
+            if (st.use_tc) {
+                QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
+            } else {
+                QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count));
+            }
+        } else if (st.kind == QXG_OP_VIEW) {
+            QXG_CUDA(launch_view(st.vargs, P->fp64, exps, P->stream));
+        } else {
+            st.oargs.bitstrings = P->d_bits;
+            QXG_CUDA(launch_output(st.oargs, P->fp64, exps, P->stream));
+        }
+    }
+    return 0;
+}
+
+int set_params(qxg_program* P, size_t k, const PassParams& pp) {
+    P->h_params[k] = pp;
+    QXG_CUDA(cudaMemcpyAsync(P->d_params, &P->h_params[k], sizeof(PassParams), cudaMemcpyHostToDevice, P->stream));
+    return 0;
+}
+
+int run_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d_out) {
+    Plan& pl = *P->plan;
+    const Tensor& root = pl.T[P->root];
+    const int64_t nsl = s1 - s0;
+    const int64_t nsc = (nsl + pl.sc - 1) / pl.sc;
+    const int64_t nbc = root.beta ? (nbits + pl.bc - 1) / pl.bc : 1;
+    const size_t npass = (size_t)(1 + nsc * (1 + nbc));
+    // the pinned pass parameters of a previous asynchronous call may still be in flight
+    QXG_CUDA(cudaStreamSynchronize(P->stream));
+    if (npass > P->h_params_cap) {
+        if (P->h_params) { cudaStreamSynchronize(P->stream); cudaFreeHost(P->h_params); }
+        P->h_params = nullptr;
+        QXG_CUDA(cudaMallocHost(&P->h_params, sizeof(PassParams) * npass));
+        P->h_params_cap = npass;
+    }
+    QXG_CUDA(cudaMemcpyAsync(P->d_exps, P->h_exps_init.data(), sizeof(int) * P->h_exps_init.size(),
+                             cudaMemcpyHostToDevice, P->stream));
+    size_t k = 0;
+    PassParams pp;
+    memset(&pp, 0, sizeof(pp));
+    pp.num_slices = P->nslices;
+    pp.slice_base = s0;
+    pp.slices_valid = (int32_t)std::min<int64_t>(pl.sc, nsl);
+    pp.bits_valid = root.beta ? std::min(pl.bc, nbits) : nbits;
+    if (int r = set_params(P, k++, pp)) return r;
+    if (int r = run_group(P, 0)) return r;
+    pl.red.out = d_out;
+    for (int64_t c = 0; c < nsc; c++) {
+        pp.slice_base = s0 + c * pl.sc;
+        pp.slices_valid = (int32_t)std::min<int64_t>(pl.sc, s1 - pp.slice_base);
+        pp.bit_base = 0;
+        pp.bits_valid = root.beta ? std::min(pl.bc, nbits) : nbits;
+        if (int r = set_params(P, k++, pp)) return r;
+        if (int r = run_group(P, 1)) return r;
+        if (!root.beta && root.group <= 1) {
+            QXG_CUDA(launch_reduce(pl.red, P->fp64, P->fp64 ? nullptr : P->d_exps, P->stream));
+            continue;
+        }
+        for (int64_t b = 0; b < nbc; b++) {
+            pp.bit_base = (int32_t)(b * pl.bc);
+            pp.bits_valid = root.beta ? (int32_t)std::min<int64_t>(pl.bc, nbits - pp.bit_base) : nbits;
+            if (int r = set_params(P, k++, pp)) return r;
+            if (int r = run_group(P, 2)) return r;
+            QXG_CUDA(launch_reduce(pl.red, P->fp64, P->fp64 ? nullptr : P->d_exps, P->stream));
+        }
+    }
+    return 0;
+}
+
+int check_ready(qxg_program* P) {
+    for (size_t i = 0; i < P->data_set.size(); i++) {
+        bool used = false;
+        for (auto& t : P->base) if (t.kind == QXG_OP_LOAD && t.data_id == (int)i && t.needed) used = true;
+        if (used && !P->data_set[i]) return fail(QXG_ERR_STATE, "leaf data " + std::to_string(i) + " not set");
+    }
+    return 0;
+}
+
+int validate_bits(const char* bits, int64_t n) {
+    for (int64_t i = 0; i < n; i++) {
+        const char c = bits[i];
+        if (c != '0' && c != '1' && c != '+' && c != '-')
+            return fail(QXG_ERR_INVALID, "bitstring character outside '01+-' at position " + std::to_string(i));
+    }
+    return 0;
+}
+
+}  // namespace
+
+namespace qxg {
+int ncon_fail(int code, const char* msg) { return fail(code, msg); }
+}  // namespace qxg
+
+extern "C" {
+
+const char* qxg_last_error(void) { return g_last_error.c_str(); }
+
+const char* qxg_version(void) { return "qxgpu 0.1.0 sm_103a"; }
+
+int qxg_program_create(const qxg_instr* instrs, int32_t ninstr, const int32_t* labels, int64_t nlabels,
+                       const int32_t* data_rank, const int64_t* data_dims, int32_t ndata, int32_t nqubits,
+                       const qxg_options* opts, qxg_program** out) {
+    g_last_error.clear();
+    if (!out) return fail(QXG_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!instrs || ninstr <= 0 || (nlabels > 0 && !labels) || ndata < 0 || (ndata > 0 && (!data_rank || !data_dims)) ||
+        nqubits < 0)
+        return fail(QXG_ERR_INVALID, "bad arguments");
+    auto P = std::make_unique<qxg_program>();
+    memset(&P->opts, 0, sizeof(P->opts));
+    if (opts) P->opts = *opts;
+    if (P->opts.precision < QXG_PREC_FP64 || P->opts.precision > QXG_PREC_FP32)
+        return fail(QXG_ERR_INVALID, "unknown precision");
+    P->fp64 = P->opts.precision == QXG_PREC_FP64;
+    P->esize = P->fp64 ? 16 : 8;
+    P->device = P->opts.device;
+    P->nqubits = nqubits;
+    P->ins.assign(instrs, instrs + ninstr);
+    if (nlabels > 0) P->labels.assign(labels, labels + nlabels);
+    int64_t off = 0;
+    for (int d = 0; d < ndata; d++) {
+        if (data_rank[d] < 0 || data_rank[d] > 64) return fail(QXG_ERR_INVALID, "bad data rank");
+        std::vector<int64_t> dims(data_dims + off, data_dims + off + data_rank[d]);
+        std::vector<int64_t> pd;
+        for (int64_t x : dims) {
+            if (x <= 0 || x > (1 << 20)) return fail(QXG_ERR_INVALID, "bad data dimension");
+            pd.push_back(pow2ceil(x));
+        }
+        P->ddims.push_back(dims);
+        P->dpdims.push_back(pd);
+        off += data_rank[d];
+    }
+    if (int r = compile_structure(P.get())) return r;
+    int ndev = 0;
+    QXG_CUDA(cudaGetDeviceCount(&ndev));
+    if (P->device < 0 || P->device >= ndev) return fail(QXG_ERR_INVALID, "device ordinal out of range");
+    QXG_CUDA(cudaSetDevice(P->device));
+    QXG_CUDA(cudaDeviceGetAttribute(&P->sm_count, cudaDevAttrMultiProcessorCount, P->device));
+    QXG_CUDA(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    QXG_CUDA(cudaMalloc(&P->d_params, sizeof(PassParams)));
+    P->d_data.assign(ndata, nullptr);
+    P->data_m.assign(ndata, 0);
+    P->data_set.assign(ndata, false);
+    for (int d = 0; d < ndata; d++) {
+        int64_t n = 1;
+        for (int64_t x : P->dpdims[d]) n *= x;
+        QXG_CUDA(cudaMalloc(&P->d_data[d], (size_t)std::max<int64_t>(n, 1) * P->esize));
+    }
+    *out = P.release();
+    return QXG_OK;
+}
+
+int qxg_program_set_data(qxg_program* P, int32_t id, const double* re_im, int64_t nelem) {
+    g_last_error.clear();
+    if (!P || !re_im || id < 0 || id >= (int)P->ddims.size()) return fail(QXG_ERR_INVALID, "bad arguments");
+    const auto& dims = P->ddims[id];
+    const auto& pd = P->dpdims[id];
+    int64_t n = 1, pn = 1;
+    for (int64_t x : dims) n *= x;
+    for (int64_t x : pd) pn *= x;
+    if (nelem != n) return fail(QXG_ERR_INVALID, "leaf data size does not match its dimensions");
+    QXG_CUDA(cudaSetDevice(P->device));
+    std::vector<double> padded((size_t)std::max<int64_t>(pn, 1) * 2, 0.0);
+    const int r = (int)dims.size();
+    std::vector<int64_t> idx(r, 0);
+    for (int64_t e = 0; e < n; e++) {
+        int64_t po = 0, st = 1;
+        for (int a = 0; a < r; a++) { po += idx[a] * st; st *= pd[a]; }
+        padded[2 * po] = re_im[2 * e];
+        padded[2 * po + 1] = re_im[2 * e + 1];
+        for (int a = 0; a < r; a++) { if (++idx[a] < dims[a]) break; idx[a] = 0; }
+    }
+    if (P->fp64) {
+        QXG_CUDA(cudaMemcpy(P->d_data[id], padded.data(), sizeof(double) * padded.size(), cudaMemcpyHostToDevice));
+        P->data_m[id] = 0;
+    } else {
+        std::vector<float> f(padded.size());
+        int m = kExpUnset;
+        for (size_t i = 0; i < padded.size(); i++) {
+            f[i] = (float)padded[i];
+            if (f[i] != 0.f) { int e; std::frexp(std::fabs(f[i]), &e); m = std::max(m, e); }
+        }
+        P->data_m[id] = m;
+        QXG_CUDA(cudaMemcpy(P->d_data[id], f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+    }
+    P->data_set[id] = true;
+    return QXG_OK;
+}
+
+int qxg_amplitudes_device(qxg_program* P, const char* d_bitstrings, int32_t nbits, int64_t s0, int64_t s1,
+                          double* d_out) {
+    g_last_error.clear();
+    if (!P || nbits <= 0 || (P->nqubits > 0 && !d_bitstrings) || !d_out) return fail(QXG_ERR_INVALID, "bad arguments");
+    if (s0 < 0 || s1 > P->nslices || s0 >= s1) return fail(QXG_ERR_INVALID, "slice range out of bounds");
+    if (int r = check_ready(P)) return r;
+    QXG_CUDA(cudaSetDevice(P->device));
+    if (int r = ensure_plan(P, nbits)) return r;
+    const int64_t osz = P->plan->red.out_size;
+    QXG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(double) * 2 * (size_t)osz * nbits, P->stream));
+    char* saved = P->d_bits;
+    P->d_bits = const_cast<char*>(d_bitstrings);
+    const int r = run_passes(P, nbits, s0, s1, d_out);
+    P->d_bits = saved;
+    return r;
+}
+
+int qxg_amplitudes(qxg_program* P, const char* bits, int32_t nbits, int64_t s0, int64_t s1, double* out) {
+    g_last_error.clear();
+    if (!P || nbits <= 0 || (P->nqubits > 0 && !bits) || !out) return fail(QXG_ERR_INVALID, "bad arguments");
+    if (s0 < 0 || s1 > P->nslices || s0 >= s1) return fail(QXG_ERR_INVALID, "slice range out of bounds");
+    if (int r = validate_bits(bits, (int64_t)nbits * P->nqubits)) return r;
+    if (int r = check_ready(P)) return r;
+    QXG_CUDA(cudaSetDevice(P->device));
+    if (int r = ensure_plan(P, nbits)) return r;
+    const size_t nb = (size_t)nbits * (size_t)std::max(P->nqubits, 1);
+    if (nb > P->d_bits_cap) {
+        if (P->d_bits) cudaFree(P->d_bits);
+        P->d_bits = nullptr; P->d_bits_cap = 0;
+        QXG_CUDA(cudaMalloc(&P->d_bits, nb));
+        P->d_bits_cap = nb;
+    }
+    const int64_t osz = P->plan->red.out_size;
+    const size_t ob = sizeof(double) * 2 * (size_t)osz * nbits;
+    if (ob > P->d_out_cap) {
+        if (P->d_out) cudaFree(P->d_out);
+        P->d_out = nullptr; P->d_out_cap = 0;
+        QXG_CUDA(cudaMalloc(&P->d_out, ob));
+        P->d_out_cap = ob;
+    }
+    if (P->nqubits > 0)
+        QXG_CUDA(cudaMemcpyAsync(P->d_bits, bits, (size_t)nbits * P->nqubits, cudaMemcpyHostToDevice, P->stream));
+    QXG_CUDA(cudaMemsetAsync(P->d_out, 0, ob, P->stream));
+    if (int r = run_passes(P, nbits, s0, s1, P->d_out)) return r;
+    QXG_CUDA(cudaMemcpyAsync(out, P->d_out, ob, cudaMemcpyDeviceToHost, P->stream));
+    QXG_CUDA(cudaStreamSynchronize(P->stream));
+    return QXG_OK;
+}
+
+int qxg_program_synchronize(qxg_program* P) {
+    if (!P) return fail(QXG_ERR_INVALID, "bad arguments");
+    QXG_CUDA(cudaStreamSynchronize(P->stream));
+    return QXG_OK;
+}
+
+void* qxg_program_stream(qxg_program* P) { return P ? (void*)P->stream : nullptr; }
+
+int qxg_program_info_get(const qxg_program* P, qxg_program_info* info) {
+    if (!P || !info) return fail(QXG_ERR_INVALID, "bad arguments");
+    memset(info, 0, sizeof(*info));
+    info->num_slices = P->nslices;
+    int64_t osz = 1;
+    for (int64_t d : P->base[P->root].dims) osz *= d;
+    info->output_size = osz;
+    info->num_qubits = P->nqubits;
+    int ns = 0;
+    for (auto& I : P->ins) if (I.op == QXG_OP_NCON) ns++;
+    info->num_steps = ns;
+    info->flops_per_amplitude = P->flops_per_amp;
+    if (P->plan) {
+        const Plan& pl = *P->plan;
+        info->bitstring_batch = pl.bc;
+        info->slice_batch = pl.sc;
+        info->workspace_bytes = (int64_t)(pl.arena_bytes + pl.tc_scratch_bytes);
+        info->flops_executed_per_pass = pl.flops_pass[0] + pl.flops_pass[1] + pl.flops_pass[2];
+        info->bytes_executed_per_pass = pl.bytes_pass[0] + pl.bytes_pass[1] + pl.bytes_pass[2];
+        int c[3] = {0, 0, 0};
+        for (int g = 0; g < 3; g++) for (auto& st : pl.steps[g]) if (st.kind == QXG_OP_NCON) c[g]++;
+        info->num_steps_invariant = c[0];
+        info->num_steps_slice = c[1];
+        info->num_steps_bitstring = c[2];
+    }
+    return QXG_OK;
+}
+
+void qxg_program_destroy(qxg_program* P) {
+    if (!P) return;
+    cudaSetDevice(P->device);
+    if (P->stream) cudaStreamSynchronize(P->stream);
+    for (void* p : P->d_data) if (p) cudaFree(p);
+    if (P->d_arena) cudaFree(P->d_arena);
+    if (P->d_scratch) cudaFree(P->d_scratch);
+    if (P->d_exps) cudaFree(P->d_exps);
+    if (P->d_params) cudaFree(P->d_params);
+    if (P->h_params) cudaFreeHost(P->h_params);
+    if (P->d_bits) cudaFree(P->d_bits);
+    if (P->d_out) cudaFree(P->d_out);
+    if (P->stream) cudaStreamDestroy(P->stream);
+    delete P;
+}
+
+}  // extern "C"

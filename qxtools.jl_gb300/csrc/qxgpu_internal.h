@@ -1,0 +1,113 @@
+// Internal declarations shared by the executor's host compiler and its CUDA kernels.
+//
+// Every tensor dimension on the contraction path is a power of two (qubit bonds are 2,
+// decomposed two-qubit bonds 2 or 4; other sizes are zero-padded up at upload), so a tensor's
+// linear index is a bit string and every permute/reshape of the reference's `ncon`
+// (docs/src/users_guide.md:124-146) is a bit permutation.  A permutation is stored as a few
+// "runs": bits [src, src+len) of one index land at bits [dst, dst+len) of another.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace qxg {
+
+constexpr int kMaxRuns = 24;       // runs per bit map (a contraction rarely needs more than 8)
+constexpr int kKTableBits = 8;     // K offsets tabulated in shared memory (2^8 entries)
+
+struct Run {
+    uint8_t src, len, dst, pad;
+};
+
+struct BitMap {                     // index -> offset as a sum of shifted bit fields
+    int32_t n;
+    Run r[kMaxRuns];
+};
+
+__host__ __device__ inline int64_t pdep(int64_t x, const BitMap& m) {
+    int64_t o = 0;
+    for (int i = 0; i < m.n; i++) {
+        const Run q = m.r[i];
+        o |= ((x >> q.src) & ((int64_t(1) << q.len) - 1)) << q.dst;
+    }
+    return o;
+}
+
+// Per-pass parameters read by kernels from device memory, so a captured pass can be replayed
+// for another (slice batch, bitstring batch) by rewriting this block.
+struct PassParams {
+    int64_t slice_base;        // first slice id of this pass
+    int64_t num_slices;        // total slices of the programme
+    int32_t bit_base;          // first bitstring of this pass (row in the bitstring buffer)
+    int32_t bits_valid;        // bitstrings of this pass that are real (rest are padding)
+    int32_t slices_valid;      // slices of this pass that are real
+    int32_t pad;
+};
+
+// One pairwise contraction C[c] = sum_k A[a(c,k)] B[b(c,k)] over bit-indexed tensors.
+struct StepArgs {
+    const void* A;
+    const void* B;
+    void* C;
+    int64_t nC;                // elements of C (a power of two)
+    int32_t nk;                // summed bits
+    int32_t expA, expB, expC;  // exponent slots (split / fp32 modes), -1 when unused
+    BitMap cA, cB;             // C index -> A / B offset
+    BitMap kA, kB;             // K index -> A / B offset
+};
+
+// Materialise a view of a leaf/output tensor for a batch of slices.
+constexpr int kMaxViewFix = 8;
+struct ViewArgs {
+    const void* src;
+    void* dst;
+    int64_t n;                 // elements of dst
+    int32_t sigma_shift;       // dst bits >= sigma_shift are the slice batch index
+    int32_t nfix;
+    BitMap map;                // dst index (bits below sigma_shift) -> src offset
+    int32_t fix_shift[kMaxViewFix];   // src bit position of the fixed axis' lowest bit
+    int64_t var_stride[kMaxViewFix];  // slice id / var_stride % var_dim = value of the variable
+    int64_t var_dim[kMaxViewFix];
+    int32_t exp_src, exp_dst;
+    const PassParams* params;
+};
+
+// Output (bitstring) vectors for a batch of bitstrings: dst[x + 2*beta].
+struct OutputArgs {
+    void* dst;
+    const char* bitstrings;    // device, nbitstrings x nqubits
+    int32_t qubit, nqubits, nbeta;
+    int32_t exp_dst;
+    const PassParams* params;
+};
+
+// Sum of the root tensor over the slice batch, added into the FP64 result.
+constexpr int kMaxOutAxes = 48;
+struct ReduceArgs {
+    const void* root;
+    double* out;               // (nbitstrings x out_size) complex doubles
+    int64_t out_size;          // logical elements per bitstring
+    int32_t nbeta, nsigma;     // batch sizes in the root (1 when absent)
+    BitMap beta_map;           // bitstring-batch index -> root offset
+    BitMap sigma_map;          // slice-batch index -> root offset
+    int32_t naxes;
+    int32_t axis_dim[kMaxOutAxes];        // logical (unpadded) dims of the root's axes
+    int32_t axis_nbits[kMaxOutAxes];
+    int32_t axis_bitpos[kMaxOutAxes][3];  // physical positions of each axis bit (<= 3 bits)
+    int32_t exp_root;
+    int32_t broadcast;         // 1: root has no beta; write the same value to every bitstring
+    const PassParams* params;
+};
+
+// Kernel launchers (kernels_simt.cu).  Storage: double2 when fp64 != 0, else float2.
+cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count);
+cudaError_t launch_view(const ViewArgs& a, bool fp64, int* exps, cudaStream_t s);
+cudaError_t launch_output(const OutputArgs& a, bool fp64, int* exps, cudaStream_t s);
+cudaError_t launch_reduce(const ReduceArgs& a, bool fp64, const int* exps, cudaStream_t s);
+cudaError_t launch_reset_exps(int* exps, int begin, int end, cudaStream_t s);
+
+// Exponent slots: exps[2*i] = e (true value = stored * 2^e), exps[2*i+1] = m (max stored
+// exponent, atomically raised by the producer).
+constexpr int kExpUnset = -2139062144;  // 0x80808080: memset-able "minus infinity"
+
+}  // namespace qxg

@@ -1,0 +1,314 @@
+"""ctypes binding of libqxgpu (include/qxgpu.h) and the programme builder.
+
+`Programme.from_graph(graph)` turns a `.qx` command list (compute_graph.ComputeGraph or parsed
+`.qx` text) into the C ABI's arrays: tensor symbols -> dense ids, `data_<k>` keys -> data ids,
+`v<i>` -> slice variable i-1, 1-based qubits and rank positions -> 0-based.  `Executor` owns one
+`qxg_program` on one GPU.  The library is required: importing works without it, but creating an
+Executor raises if libqxgpu.so is missing or no GPU is visible (there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from collections import OrderedDict
+from pathlib import Path
+
+import numpy as np
+
+from .compute_graph import ComputeGraph, Load, Ncon, Output, Save, View
+
+__all__ = ["QXG_OP", "PRECISION", "QXGError", "Programme", "Executor", "load_library",
+           "library_path", "ncon_device"]
+
+_HERE = Path(__file__).resolve().parent
+_LIB_PATH = _HERE / "_build" / "libqxgpu.so"
+
+QXG_OP = {"load": 1, "view": 2, "output": 3, "ncon": 4, "save": 5}
+PRECISION = {"fp64": 0, "split_bf16": 1, "split_tf32": 2, "fp32": 3}
+_STATUS = {0: "QXG_OK", -1: "QXG_ERR_INVALID", -2: "QXG_ERR_CUDA", -3: "QXG_ERR_OOM",
+           -4: "QXG_ERR_UNSUPPORTED", -5: "QXG_ERR_TIMEOUT", -6: "QXG_ERR_STATE"}
+
+
+class QXGError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class qxg_instr(ct.Structure):
+    _fields_ = [(n, ct.c_int32) for n in
+                ("op", "dst", "a", "b", "pos", "dim", "nc", "na", "nb", "label_off")]
+
+
+class qxg_options(ct.Structure):
+    _fields_ = [("precision", ct.c_int32), ("device", ct.c_int32), ("workspace_limit", ct.c_int64),
+                ("max_bitstring_batch", ct.c_int32), ("max_slice_batch", ct.c_int32),
+                ("use_graphs", ct.c_int32), ("reserved", ct.c_int32 * 7)]
+
+
+class qxg_program_info(ct.Structure):
+    _fields_ = [("num_slices", ct.c_int64), ("output_size", ct.c_int64), ("num_qubits", ct.c_int32),
+                ("num_steps", ct.c_int32), ("bitstring_batch", ct.c_int32), ("slice_batch", ct.c_int32),
+                ("workspace_bytes", ct.c_int64), ("flops_per_amplitude", ct.c_double),
+                ("flops_executed_per_pass", ct.c_double), ("bytes_executed_per_pass", ct.c_double),
+                ("num_steps_invariant", ct.c_int32), ("num_steps_slice", ct.c_int32),
+                ("num_steps_bitstring", ct.c_int32), ("reserved", ct.c_int32 * 5)]
+
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def load_library(path=None):
+    """Load libqxgpu.so and declare its signatures (no GPU needed to load)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else _LIB_PATH
+    if not p.exists():
+        raise QXGError(-6, f"{p} is missing: build it with qxtools.jl_gb300/build.py "
+                           "(or __graft_entry__.build())")
+    lib = ct.CDLL(str(p))
+    P = ct.c_void_p
+    lib.qxg_program_create.argtypes = [ct.POINTER(qxg_instr), ct.c_int32, ct.POINTER(ct.c_int32), ct.c_int64,
+                                       ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), ct.c_int32, ct.c_int32,
+                                       ct.POINTER(qxg_options), ct.POINTER(P)]
+    lib.qxg_program_set_data.argtypes = [P, ct.c_int32, ct.POINTER(ct.c_double), ct.c_int64]
+    lib.qxg_amplitudes.argtypes = [P, ct.c_char_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_double)]
+    lib.qxg_amplitudes_device.argtypes = [P, P, ct.c_int32, ct.c_int64, ct.c_int64, P]
+    lib.qxg_program_synchronize.argtypes = [P]
+    lib.qxg_program_stream.argtypes = [P]
+    lib.qxg_program_stream.restype = P
+    lib.qxg_program_info_get.argtypes = [P, ct.POINTER(qxg_program_info)]
+    lib.qxg_program_destroy.argtypes = [P]
+    lib.qxg_program_destroy.restype = None
+    lib.qxg_ncon.argtypes = [ct.c_int32, P, ct.c_int32, ct.POINTER(ct.c_int32), P, ct.c_int32,
+                             ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), P, ct.c_int32,
+                             ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), P]
+    lib.qxg_last_error.restype = ct.c_char_p
+    lib.qxg_version.restype = ct.c_char_p
+    for f in ("qxg_program_create", "qxg_program_set_data", "qxg_amplitudes", "qxg_amplitudes_device",
+              "qxg_program_synchronize", "qxg_program_info_get", "qxg_ncon"):
+        getattr(lib, f).restype = ct.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(lib, rc: int):
+    if rc != 0:
+        raise QXGError(rc, lib.qxg_last_error().decode())
+
+
+class Programme:
+    """The C ABI's view of a `.qx` programme: instruction array, labels, leaf shapes and data."""
+
+    def __init__(self, instrs: np.ndarray, labels: np.ndarray, data_keys: list, data: list,
+                 nqubits: int, tensor_ids: dict):
+        self.instrs = instrs            # (n, 10) int32
+        self.labels = labels            # int32
+        self.data_keys = data_keys
+        self.data = data                # complex128 arrays (column-major shape)
+        self.nqubits = nqubits
+        self.tensor_ids = tensor_ids
+
+    @property
+    def data_rank(self) -> np.ndarray:
+        return np.array([d.ndim for d in self.data], dtype=np.int32)
+
+    @property
+    def data_dims(self) -> np.ndarray:
+        return np.array([x for d in self.data for x in d.shape], dtype=np.int64)
+
+    def data_flat(self):
+        """(concatenated interleaved doubles, complex offsets per leaf)."""
+        offs, parts, o = [], [], 0
+        for d in self.data:
+            offs.append(o)
+            flat = np.asarray(d, dtype=np.complex128).reshape(-1, order="F")
+            parts.append(flat)
+            o += flat.size
+        cat = np.concatenate(parts) if parts else np.zeros(0, np.complex128)
+        return np.ascontiguousarray(cat.view(np.float64)), np.array(offs, dtype=np.int64)
+
+    @property
+    def num_slices(self) -> int:
+        vd = {}
+        for r in self.instrs:
+            if r[0] == QXG_OP["view"]:
+                vd[int(r[3])] = int(r[5])
+        n = 1
+        for v in vd.values():
+            n *= v
+        return n
+
+    @classmethod
+    def from_commands(cls, commands, data: "OrderedDict[str, np.ndarray]", nqubits: int) -> "Programme":
+        ids: dict = {}
+        dkeys = list(data.keys())
+        dpos = {k: i for i, k in enumerate(dkeys)}
+        rows, labels = [], []
+
+        def tid(name, define=False):
+            if define:
+                if name in ids:
+                    raise ValueError(f"tensor {name} defined twice")
+                ids[name] = len(ids)
+            if name not in ids:
+                raise ValueError(f"tensor {name} used before definition")
+            return ids[name]
+
+        for c in commands:
+            if isinstance(c, Load):
+                if c.data not in dpos:
+                    raise ValueError(f"no data {c.data}")
+                if tuple(np.shape(data[c.data])) != tuple(c.dims):
+                    raise ValueError(f"load {c.name}: dims {c.dims} do not match data {np.shape(data[c.data])}")
+                rows.append([1, tid(c.name, True), dpos[c.data], 0, 0, 0, 0, 0, 0, 0])
+            elif isinstance(c, View):
+                if not c.var.startswith("v"):
+                    raise ValueError(f"bad slice variable {c.var}")
+                src = tid(c.src)
+                rows.append([2, tid(c.name, True), src, int(c.var[1:]) - 1, c.pos - 1, c.dim, 0, 0, 0, 0])
+            elif isinstance(c, Output):
+                rows.append([3, tid(c.name, True), c.qubit - 1, c.dim, 0, 0, 0, 0, 0, 0])
+            elif isinstance(c, Ncon):
+                a, b = tid(c.a), tid(c.b)
+                off = len(labels)
+                labels += list(c.c_labels) + list(c.a_labels) + list(c.b_labels)
+                rows.append([4, tid(c.name, True), a, b, 0, 0, len(c.c_labels), len(c.a_labels),
+                             len(c.b_labels), off])
+            elif isinstance(c, Save):
+                rows.append([5, 0, tid(c.name), 0, 0, 0, 0, 0, 0, 0])
+            else:
+                raise TypeError(f"unknown command {c!r}")
+        instrs = np.array(rows, dtype=np.int32).reshape(-1, 10)
+        return cls(instrs, np.array(labels, dtype=np.int32), dkeys,
+                   [np.asarray(data[k], dtype=np.complex128) for k in dkeys], nqubits, ids)
+
+    @classmethod
+    def from_graph(cls, graph: ComputeGraph) -> "Programme":
+        return cls.from_commands(graph.commands, graph.data, graph.num_qubits)
+
+
+def _bitstring_bytes(bitstrings, nqubits: int) -> bytes:
+    if isinstance(bitstrings, str):
+        bitstrings = [bitstrings]
+    out = []
+    for b in bitstrings:
+        if len(b) != nqubits:
+            raise ValueError(f"bitstring {b!r} does not have {nqubits} characters")
+        out.append(b)
+    return "".join(out).encode("ascii")
+
+
+class Executor:
+    """One compiled programme on one GPU (a `qxg_program` handle)."""
+
+    def __init__(self, programme: Programme, precision: str = "fp64", device: int = 0,
+                 workspace_limit: int = 0, max_bitstring_batch: int = 0, max_slice_batch: int = 0,
+                 use_graphs: bool = False):
+        self.lib = load_library()
+        self.programme = programme
+        self.precision = precision
+        opts = qxg_options()
+        opts.precision = PRECISION[precision]
+        opts.device = device
+        opts.workspace_limit = workspace_limit
+        opts.max_bitstring_batch = max_bitstring_batch
+        opts.max_slice_batch = max_slice_batch
+        opts.use_graphs = int(use_graphs)
+        ins = np.ascontiguousarray(programme.instrs, dtype=np.int32)
+        n = ins.shape[0]
+        arr = (qxg_instr * n).from_buffer_copy(ins.tobytes())
+        labels = np.ascontiguousarray(programme.labels, dtype=np.int32)
+        lab_ptr = labels.ctypes.data_as(ct.POINTER(ct.c_int32)) if labels.size else None
+        rank = np.ascontiguousarray(programme.data_rank)
+        dims = np.ascontiguousarray(programme.data_dims)
+        h = ct.c_void_p()
+        _check(self.lib, self.lib.qxg_program_create(
+            arr, n, lab_ptr, labels.size, rank.ctypes.data_as(ct.POINTER(ct.c_int32)),
+            dims.ctypes.data_as(ct.POINTER(ct.c_int64)) if dims.size else ct.POINTER(ct.c_int64)(),
+            len(programme.data), programme.nqubits, ct.byref(opts), ct.byref(h)))
+        self._h = h
+        for i, d in enumerate(programme.data):
+            flat = np.ascontiguousarray(np.asarray(d, dtype=np.complex128).reshape(-1, order="F"))
+            _check(self.lib, self.lib.qxg_program_set_data(
+                h, i, flat.view(np.float64).ctypes.data_as(ct.POINTER(ct.c_double)), flat.size))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.qxg_program_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self) -> dict:
+        inf = qxg_program_info()
+        _check(self.lib, self.lib.qxg_program_info_get(self._h, ct.byref(inf)))
+        return {f: getattr(inf, f) for f, _ in qxg_program_info._fields_ if f != "reserved"}
+
+    @property
+    def num_slices(self) -> int:
+        return self.info()["num_slices"]
+
+    def amplitudes(self, bitstrings, slices=None) -> np.ndarray:
+        """Saved tensor for each bitstring, summed over slices (host buffers in and out).
+        Returns complex128 of shape (n, output_size) (output_size 1: amplitudes)."""
+        if isinstance(bitstrings, str):
+            bitstrings = [bitstrings]
+        bitstrings = list(bitstrings)
+        n = len(bitstrings)
+        info = self.info()
+        s0, s1 = (0, info["num_slices"]) if slices is None else slices
+        buf = _bitstring_bytes(bitstrings, self.programme.nqubits)
+        out = np.zeros(2 * n * info["output_size"], dtype=np.float64)
+        _check(self.lib, self.lib.qxg_amplitudes(self._h, buf, n, s0, s1,
+                                                 out.ctypes.data_as(ct.POINTER(ct.c_double))))
+        return out.view(np.complex128).reshape(n, info["output_size"])
+
+    def amplitudes_device(self, d_bitstrings_ptr: int, n: int, d_out_ptr: int, slices=None):
+        """Enqueue on the programme's stream with device-resident inputs/outputs (no sync)."""
+        s0, s1 = (0, self.num_slices) if slices is None else slices
+        _check(self.lib, self.lib.qxg_amplitudes_device(self._h, ct.c_void_p(d_bitstrings_ptr), n, s0, s1,
+                                                        ct.c_void_p(d_out_ptr)))
+
+    def synchronize(self):
+        _check(self.lib, self.lib.qxg_program_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return self.lib.qxg_program_stream(self._h) or 0
+
+
+def ncon_device(precision: str, C_ptr: int, c_labels, A_ptr: int, a_labels, a_dims, B_ptr: int, b_labels,
+                b_dims, stream: int = 0):
+    """One pairwise contraction on device buffers through qxg_ncon."""
+    lib = load_library()
+
+    def i32(x):
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.int32))
+        return a, (a.ctypes.data_as(ct.POINTER(ct.c_int32)) if a.size else None)
+
+    def i64(x):
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.int64))
+        return a, (a.ctypes.data_as(ct.POINTER(ct.c_int64)) if a.size else None)
+    lc, plc = i32(c_labels)
+    la, pla = i32(a_labels)
+    lb, plb = i32(b_labels)
+    ad, pad = i64(a_dims)
+    bd, pbd = i64(b_dims)
+    _check(lib, lib.qxg_ncon(PRECISION[precision], ct.c_void_p(C_ptr), lc.size, plc, ct.c_void_p(A_ptr), la.size,
+                             pla, pad, ct.c_void_p(B_ptr), lb.size, plb, pbd, ct.c_void_p(stream)))
