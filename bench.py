@@ -1,0 +1,395 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 contraction executor (amplitudes/s and TFLOP/s).
+
+Workload (default `rqc_5x5_d12_open6`): a seeded 5x5-grid random circuit, 12 cycles of
+{sqrt X, sqrt Y, sqrt W} + fSim(pi/2, pi/6) (pattern ABCDCDAB), two-qubit gates decomposed,
+planned and compiled into a `.qx` programme as generate_simulation_files does, with 6 qubits
+left open (a 2^6-amplitude output tensor per bitstring) and 64 seeded bitstrings of the other
+19 qubits -> 4096 amplitudes per pass.  Synthetic, seeded data.
+
+A step is one pass of the programme over one batch of bitstrings (`--bits-per-step`, default
+all 64) and all its slices.  `value` times steps with the bitstrings already in HBM (the
+device entry point qxg_amplitudes_device); `e2e` times the same steps through the host entry
+point qxg_amplitudes with pinned host buffers (bitstrings copied in, amplitudes copied out,
+every step).  Intermediates exceed L2 (largest intermediate reported in `config`).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32|split_bf16|split_tf32]
+    python bench.py --impl reference ...   # the CPU FP64 oracle on the host cores
+Under torchrun (N > 1) every rank runs its own replica on its own shard of bitstrings (the
+path shards by bitstring with no exchange) and the slowest rank's time is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "amplitudes/s & TFLOP/s: split-prec batched vs FP64 GPU path at <=1e-5 rel err"
+UNIT = "amplitudes/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="rqc_5x5_d12_open6")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "split_bf16", "split_tf32"])
+    ap.add_argument("--bits-per-step", type=int, default=0, help="bitstrings per step (0: the workload's list)")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample length")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--compare-fp64", action="store_true", help="also time the FP64 path and report the error")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(value: float, ws: int, backend_dev):
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=backend_dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"qxg_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sms.append(float(p[1]))
+                maxs.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        self.path.unlink(missing_ok=True)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxs), "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "MEASURED_PEAKS.json"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def fp64_peak_tflops(torch, dev) -> float:
+    """FP64 peak of this GPU measured here: cuBLAS DGEMM 4096^3 (torch.matmul), best of 5."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        e.synchronize()
+        best = max(best, 2 * 4096 ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def traffic_summary(workload: str, kernel: str, precision: str):
+    """DRAM bytes per launch of the dominant kernel from a committed ncu summary, if any."""
+    p = ROOT / "profiles" / f"{kernel}_{workload}_{precision}.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return d.get("dram_bytes_per_launch"), d
+        except ValueError:
+            pass
+    return None, None
+
+
+# --------------------------------------------------------------------------------------------
+def cpu_baseline(q, oracle, prog, bits, info, seconds: float):
+    """The oracle (FP64 CPU restatement) on a bounded sample: one bitstring's walk for one slice
+    with every host thread inside the contractions, stopped after `seconds`; the FLOP rate is
+    converted to amplitudes/s with the programme's FLOPs per bitstring."""
+    cores = oracle.max_threads()
+    out_size = info["amplitudes_per_bitstring"]
+    flops, sec, finished = oracle.run_timed(prog, bits[0], seconds, 0, cores, out_size=out_size)
+    rate = flops / max(sec, 1e-9)
+    amps = rate / info["flops_per_bitstring"] * out_size
+    sample = (f"one FP64 walk of bitstring 0, slice 0 of {info['name']} "
+              f"({'complete' if finished else f'stopped after {sec:.1f} s'}, {flops:.3e} FLOPs in {sec:.1f} s); "
+              f"amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per bitstring x "
+              f"{out_size} amplitudes per bitstring")
+    return {"value": amps, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+            "gflops": rate / 1e9}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    import __graft_entry__ as entry
+    q = entry.load()
+    from oracle import oracle
+    oracle.build()
+    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed)
+    cores = oracle.max_threads()
+    out_size = info["amplitudes_per_bitstring"]
+    per = max(2.0, min(args.cpu_seconds, 20.0))
+    for _ in range(args.warmup):
+        oracle.run_timed(prog, bits[0], min(per, 3.0), 0, cores, out_size=out_size)
+    fl_tot, sec_tot = 0.0, 0.0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        fl, sec, _ = oracle.run_timed(prog, bits[k % len(bits)], per, 0, cores, out_size=out_size)
+        fl_tot += fl
+        sec_tot += sec
+    wall = time.perf_counter() - t0
+    rate = fl_tot / sec_tot
+    value = rate / info["flops_per_bitstring"] * out_size
+    sample = (f"each step: one FP64 walk (bitstring k, slice 0) stopped after {per:.0f} s; amplitudes/s = "
+              f"FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per bitstring x {out_size} amplitudes")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": workload_config(info, args, None),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "tflops": rate / 1e12}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(info, args, ex_info):
+    cfg = {"workload": info["name"], "grid": f"{info['spec']['rows']}x{info['spec']['cols']}",
+           "cycles": info["spec"]["depth"], "gate_set": "sqrtX/sqrtY/sqrtW + fSim(pi/2,pi/6), ABCDCDAB",
+           "open_qubits": len(info["open_qubits"]), "bitstrings": len(info["bitstrings"]),
+           "amplitudes_per_bitstring": info["amplitudes_per_bitstring"], "slices": info["num_slices"],
+           "plan_steps": info["plan_steps"], "max_intermediate_log2": info["max_log2"],
+           "flops_per_bitstring": info["flops_per_bitstring"], "seed": info["seed"],
+           "precision": args.precision,
+           "l2": "intermediates larger than L2 (no flush needed)"}
+    if ex_info:
+        cfg.update({"bitstring_batch": ex_info["bitstring_batch"], "slice_batch": ex_info["slice_batch"],
+                    "workspace_bytes": ex_info["workspace_bytes"]})
+    return cfg
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    import __graft_entry__ as entry
+    lib_path = ROOT / "qxtools.jl_gb300" / "_build" / "libqxgpu.so"
+    if not lib_path.exists():
+        entry._load_build_module().build()
+    q = entry.load()
+    from oracle import oracle
+    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed)
+    # default batch: the whole list for the Complex64 paths, 16 bitstrings for the slower FP64 path
+    nb = args.bits_per_step or (min(16, len(bits)) if args.precision == "fp64" else len(bits))
+    # weak scaling: rank r takes its own shard of bitstrings (regenerated deterministically)
+    all_bits = list(q.amplitudes_uniform(info["nqubits"], args.seed + 7919 * rank, nb)) if rank else bits[:nb]
+    if len(all_bits) < nb:
+        all_bits = (all_bits * math.ceil(nb / len(all_bits)))[:nb]
+    out_size = info["amplitudes_per_bitstring"]
+    amps_per_step = nb * out_size
+    ex = q.Executor(prog, precision=args.precision, device=local)
+    stream = torch.cuda.ExternalStream(ex.stream, device=dev)
+    d_bits = torch.tensor(list("".join(all_bits).encode()), dtype=torch.uint8, device=dev)
+    d_out = torch.zeros(2 * nb * out_size, dtype=torch.float64, device=dev)
+    nslice = ex.num_slices
+
+    def step_device():
+        ex.amplitudes_device(d_bits.data_ptr(), nb, d_out.data_ptr(), slices=(0, nslice))
+
+    for _ in range(args.warmup):
+        step_device()
+    ex.synchronize()
+    ex_info = ex.info()
+    # ---- value: device-resident inputs --------------------------------------------------------
+    _, launches0 = ex.profile_read()
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s_ev.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step_device()
+        e_ev.record(stream)
+        ex.synchronize()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ms = s_ev.elapsed_time(e_ev)
+    barrier(ws)
+    _, launches1 = ex.profile_read()
+    ms = barrier_max(ms, ws, dev)
+    clocks = clk.summary()
+    value = ws * amps_per_step * args.steps / (ms * 1e-3)
+    # ---- e2e: host entry point with pinned host buffers ---------------------------------------
+    import ctypes as ct
+    h_bits = torch.tensor(list("".join(all_bits).encode()), dtype=torch.uint8).pin_memory()
+    h_out = torch.zeros(2 * nb * out_size, dtype=torch.float64).pin_memory()
+    lib = ex.lib
+
+    def step_host():
+        rc = lib.qxg_amplitudes(ex._h, ct.c_char_p(h_bits.data_ptr()), nb, 0, nslice,
+                                ct.cast(ct.c_void_p(h_out.data_ptr()), ct.POINTER(ct.c_double)))
+        if rc != 0:
+            raise RuntimeError(lib.qxg_last_error().decode())
+
+    step_host()
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    e2e_s = barrier_max(time.perf_counter() - t0, ws, dev)
+    e2e = {"value": ws * amps_per_step * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(h_bits.numel()), "d2h_bytes_per_step": int(h_out.numel() * 8)}
+    # ---- roofline of the dominant kernel: CUDA events on the executor's stream ---------------
+    ex.profile(True)
+    for _ in range(args.steps):
+        step_device()
+    rows, _ = ex.profile_read()
+    ex.profile(False)
+    by_kind = {}
+    for r in rows:
+        k = by_kind.setdefault(r["kernel"], {"launches": 0, "ms": 0.0, "flops": 0.0, "bytes": 0.0})
+        for f in ("launches", "ms", "flops", "bytes"):
+            k[f] += r[f]
+    total_ms = sum(v["ms"] for v in by_kind.values())
+    dom_name, dom = max(by_kind.items(), key=lambda kv: kv[1]["ms"])
+    peaks, peak_src = measured_peaks()
+    flops_exec = sum(v["flops"] for v in by_kind.values())
+    tflops = flops_exec / (total_ms * 1e-3) / 1e12 if total_ms else 0.0
+    kernel_name = {"contract_fp64": "contract_kernel_fp64", "contract_fp32": "contract_kernel_fp32",
+                   "contract_tc": "tc_contract"}.get(dom_name, dom_name)
+    traffic, _ = traffic_summary(args.workload, kernel_name, args.precision)
+    if dom_name == "contract_fp64":
+        fp64_peak = fp64_peak_tflops(torch, dev)
+        ach = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
+        roof = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                "traffic": traffic, "peak_source": "measured here: cuBLAS DGEMM 4096^3 (no FP64 entry in "
+                                                  "MEASURED_PEAKS.json; GB300 FP64 runs on CUDA cores)",
+                "kernel": kernel_name, "kernel_share": dom["ms"] / total_ms,
+                "hbm_achieved_gbs": dom["bytes"] / (dom["ms"] * 1e-3) / 1e9,
+                "hbm_peak_gbs": peaks["hbm_gbs"]}
+    elif dom_name == "contract_tc":
+        ach = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
+        pk = peaks["bf16_tflops"]
+        roof = {"bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s", "frac": ach / pk,
+                "traffic": traffic, "peak_source": f"bf16_tflops of {peak_src}", "kernel": kernel_name,
+                "kernel_share": dom["ms"] / total_ms}
+    else:
+        ach = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+        pk = peaks["hbm_gbs"]
+        roof = {"bound": "hbm", "achieved": ach, "peak": pk, "unit": "GB/s", "frac": ach / pk, "traffic": traffic,
+                "peak_source": f"hbm_gbs of {peak_src}", "kernel": kernel_name, "kernel_share": dom["ms"] / total_ms}
+    roof["kernels"] = {k: {"launches": v["launches"], "ms": round(v["ms"], 3), "share": v["ms"] / total_ms}
+                       for k, v in sorted(by_kind.items(), key=lambda kv: -kv[1]["ms"])}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+            "data": "synthetic (seeded random circuit, seeded bitstrings)",
+            "config": workload_config(info, args, ex_info) | {"parallelism": f"replicas x{ws} (bitstring shards)"},
+            "tflops": tflops, "tflops_note": "executed FLOPs (8 |C| K per contraction) / CUDA-event time of all kernels",
+            "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches1 - launches0), "roofline": roof,
+            "wall_s": wall}
+    # ---- error of this run against the FP64 path and the oracle ------------------------------
+    got = d_out.cpu().numpy().view("complex128").reshape(nb, out_size)
+    if args.compare_fp64 and args.precision != "fp64":
+        ex64 = q.Executor(prog, precision="fp64", device=local)
+        ref64 = ex64.amplitudes(all_bits)
+        line["max_rel_err_vs_fp64"] = float(abs(got - ref64).max() / abs(ref64).max())
+        ex64.close()
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(q, oracle, prog, bits, info, args.cpu_seconds)
+    ex.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

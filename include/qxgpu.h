@@ -142,6 +142,37 @@ void* qxg_program_stream(qxg_program* prog);
 /* Sizes, chosen batches and FLOP counts of a created programme. */
 int qxg_program_info_get(const qxg_program* prog, qxg_program_info* info);
 
+/* Per-kernel timing of a programme: the reference times its executor with TimerOutputs
+ * sections ("Simulation", bin/qxrun.jl:50-52 and the warm re-run at :89-96); here every
+ * launch can be bracketed with CUDA events on the programme's own stream. */
+typedef enum qxg_kernel_kind {
+    QXG_KERNEL_CONTRACT_FP64 = 0,   /* CUDA-core contraction, ComplexF64 */
+    QXG_KERNEL_CONTRACT_FP32 = 1,   /* CUDA-core contraction, Complex64 / FP32 */
+    QXG_KERNEL_CONTRACT_TC = 2,     /* tensor-core (tcgen05) split-precision contraction */
+    QXG_KERNEL_VIEW = 3,            /* slice-batch view materialisation */
+    QXG_KERNEL_OUTPUT = 4,          /* bitstring-batch output vectors */
+    QXG_KERNEL_REDUCE = 5           /* FP64 sum over the slice batch */
+} qxg_kernel_kind;
+
+typedef struct qxg_step_profile {
+    int32_t instr;      /* instruction index of the command (-1: the slice reduction) */
+    int32_t kernel;     /* qxg_kernel_kind */
+    int64_t launches;
+    double ms;          /* summed CUDA-event time of those launches */
+    double flops;       /* algorithmic FLOPs (8 |C| K) summed over the launches */
+    double bytes;       /* algorithmic bytes (s (|A|+|B|+|C|)) summed over the launches */
+} qxg_step_profile;
+
+/* enable = 1: record CUDA events around every launch from now on (clears earlier records);
+ * enable = 0: stop recording.  No counterpart in the reference beyond its timers. */
+int qxg_program_profile(qxg_program* prog, int32_t enable);
+
+/* Synchronise and aggregate the records per command: up to max_entries entries are written to
+ * out, *n_entries receives their count, *kernel_launches the number of kernels this programme
+ * launched since it was created (counted whether or not profiling is on). */
+int qxg_program_profile_read(qxg_program* prog, qxg_step_profile* out, int32_t max_entries,
+                             int32_t* n_entries, int64_t* kernel_launches);
+
 /* Free the device buffers, graphs and stream of a programme.  Accepts NULL. */
 void qxg_program_destroy(qxg_program* prog);
 

@@ -77,3 +77,28 @@ def run_programme(prog, bitstrings, slices=None, nthreads: int = 0, out_size: in
     return run(prog.instrs, prog.labels, prog.data_rank, prog.data_dims, flat, offs, prog.nqubits,
                bitstrings, slices=slices, nthreads=nthreads, out_size=out_size,
                num_slices=prog.num_slices)
+
+
+def run_timed(prog, bitstring: str, max_seconds: float, slice_id: int = 0, nthreads: int = 0,
+              out_size: int = 1):
+    """CPU-baseline sample: one FP64 walk (one bitstring, one slice) using every thread inside
+    the contractions, stopped after `max_seconds`.  -> (flops completed, seconds, finished)."""
+    lib = load()
+    flat, offs = prog.data_flat()
+    ins = np.ascontiguousarray(prog.instrs, dtype=np.int32)
+    lab = np.ascontiguousarray(prog.labels if prog.labels.size else np.zeros(1), dtype=np.int32)
+    dr = np.ascontiguousarray(prog.data_rank, dtype=np.int32)
+    dd = np.ascontiguousarray(prog.data_dims, dtype=np.int64)
+    do = np.ascontiguousarray(offs, dtype=np.int64)
+    df = np.ascontiguousarray(flat, dtype=np.float64)
+    out = np.zeros(2 * out_size, dtype=np.float64)
+    fl, sec = ct.c_double(0), ct.c_double(0)
+    P = lambda a, t: a.ctypes.data_as(ct.POINTER(t))
+    rc = lib.qxo_run_timed(P(ins, ct.c_int32), ct.c_int(ins.shape[0]), P(lab, ct.c_int32), P(dr, ct.c_int32),
+                           P(dd, ct.c_int64), P(do, ct.c_int64), P(df, ct.c_double), ct.c_int(dr.size),
+                           ct.c_int(prog.nqubits), ct.c_char_p(bitstring.encode() or b"\0"), ct.c_int64(slice_id),
+                           ct.c_int(nthreads), ct.c_double(max_seconds), P(out, ct.c_double),
+                           ct.c_int64(out_size), ct.byref(fl), ct.byref(sec))
+    if rc not in (0, 1):
+        raise RuntimeError(f"oracle failed with status {rc}")
+    return fl.value, sec.value, rc == 0

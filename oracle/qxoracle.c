@@ -48,6 +48,19 @@ typedef struct {
     int borrowed;
 } otensor;
 
+/* 1 while qxo_run executes fewer jobs than threads: contractions are then threaded inside. */
+static int qxo_inner_parallel = 0;
+/* Time-bounded sampling (qxo_run_timed): stop the walk at the deadline, count FLOPs done. */
+static double qxo_deadline = 0.0;
+static double qxo_flops_done = 0.0;
+
+#include <time.h>
+static double qxo_now(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 static int64_t prod_dims(int rank, const int64_t* d) {
     int64_t p = 1;
     for (int i = 0; i < rank; i++) p *= d[i];
@@ -97,9 +110,21 @@ static int ncon_general(otensor* C, const int32_t* lc, int nc,
     if (!C->data) return -2;
     int64_t K = 1;
     for (int j = 0; j < nk; j++) K *= ldim[kidx[j]];
+    qxo_flops_done += 8.0 * (double)C->size * (double)K;
+    /* Result elements are split into contiguous chunks; each chunk starts its odometer from
+       the digits of its first element.  Runs threaded when called outside a parallel region
+       (one job: all host threads work inside the contraction). */
+    const int64_t nchunks = (C->size >= 4096 && qxo_inner_parallel) ? 256 : 1;
+    const int64_t csz = (C->size + nchunks - 1) / nchunks;
+#ifdef _OPENMP
+    #pragma omp parallel for schedule(dynamic, 1) if (nchunks > 1)
+#endif
+    for (int64_t ch = 0; ch < nchunks; ch++) {
+    const int64_t c0 = ch * csz, c1 = (c0 + csz < C->size) ? c0 + csz : C->size;
     int64_t ci[QXO_MAX_RANK]; memset(ci, 0, sizeof(ci));
     int64_t offA = 0, offB = 0;
-    for (int64_t c = 0; c < C->size; c++) {
+    { int64_t rem = c0; for (int i = 0; i < nc; i++) { int q = cidx[i]; ci[i] = rem % ldim[q]; rem /= ldim[q]; offA += ci[i] * sA[q]; offB += ci[i] * sB[q]; } }
+    for (int64_t c = c0; c < c1; c++) {
         double re = 0.0, im = 0.0;
         int64_t ki[3 * QXO_MAX_RANK]; memset(ki, 0, sizeof(int64_t) * (size_t)(nk ? nk : 1));
         int64_t kA = 0, kB = 0;
@@ -121,6 +146,7 @@ static int ncon_general(otensor* C, const int32_t* lc, int nc,
             if (ci[i] < ldim[q]) break;
             offA -= sA[q] * ldim[q]; offB -= sB[q] * ldim[q]; ci[i] = 0;
         }
+    }
     }
     return 0;
 }
@@ -180,6 +206,7 @@ static int walk(const oprog* P, const char* bits, int64_t slice, cplx* out, int6
     int rc = 0;
     for (int n = 0; n < P->nins && rc == 0; n++) {
         const qxg_instr* I = &P->ins[n];
+        if (qxo_deadline > 0.0 && qxo_now() > qxo_deadline) { rc = 1; break; }
         switch (I->op) {
         case QXG_OP_LOAD: {
             otensor* t = &T[I->dst];
@@ -268,9 +295,15 @@ int qxo_run(const qxg_instr* ins, int nins, const int32_t* labels,
     cplx* partial = (cplx*)malloc(sizeof(cplx) * (size_t)(njobs > 0 ? njobs : 1) * (size_t)out_size);
     if (!partial) { free(P.last_use); return -2; }
     int err = 0;
+    int nthr = 1;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
-    #pragma omp parallel for schedule(dynamic, 1)
+    nthr = omp_get_max_threads();
+#endif
+    const int outer = njobs >= nthr;
+    qxo_inner_parallel = !outer;
+#ifdef _OPENMP
+    #pragma omp parallel for schedule(dynamic, 1) if (outer)
 #endif
     for (int64_t j = 0; j < njobs; j++) {
         int64_t bi = j / nsl, s = slice_begin + j % nsl;
@@ -298,6 +331,28 @@ int qxo_run(const qxg_instr* ins, int nins, const int32_t* labels,
     free(partial);
     free(P.last_use);
     return err;
+}
+
+/*
+ * CPU-baseline sample: one walk of the programme for bitstring 0 and slice `slice`, all host
+ * threads inside the contractions, stopped at the first instruction boundary after
+ * `max_seconds`.  Returns 0 (finished) or 1 (stopped at the deadline); *flops receives the
+ * FLOPs of the completed contractions (8 |C| K each), *seconds the elapsed time.
+ */
+int qxo_run_timed(const qxg_instr* ins, int nins, const int32_t* labels,
+                  const int32_t* data_rank, const int64_t* data_dims, const int64_t* data_off,
+                  const double* data, int ndata, int nqubits, const char* bitstring, int64_t slice,
+                  int nthreads, double max_seconds, double* out, int64_t out_size,
+                  double* flops, double* seconds) {
+    const double t0 = qxo_now();
+    qxo_deadline = t0 + max_seconds;
+    qxo_flops_done = 0.0;
+    const int rc = qxo_run(ins, nins, labels, data_rank, data_dims, data_off, data, ndata, nqubits,
+                           bitstring, 1, slice, slice + 1, nthreads, out, out_size);
+    *seconds = qxo_now() - t0;
+    *flops = qxo_flops_done;
+    qxo_deadline = 0.0;
+    return rc == 1 ? 1 : (rc == 0 ? 0 : rc);
 }
 
 /* Max threads OpenMP would use (for reporting the CPU baseline's core count). */

@@ -133,6 +133,13 @@ struct qxg_program {
     double* d_out = nullptr;
     size_t d_out_cap = 0;
     std::vector<int> h_exps_init;
+    // profiling: CUDA events around launches, aggregated per command on read
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    struct Rec { int instr, kind; size_t ev; double flops, bytes; };
+    std::vector<Rec> recs;
+    int64_t launches = 0;
 };
 
 namespace {
@@ -709,25 +716,67 @@ int ensure_plan(qxg_program* P, int nbits_call) {
     return 0;
 }
 
+// Event pair around one launch when profiling; returns the index of the first event.
+int prof_begin(qxg_program* P, size_t* ev) {
+    if (!P->profiling) return 0;
+    while (P->ev_pool.size() < P->ev_used + 2) {
+        cudaEvent_t e;
+        QXG_CUDA(cudaEventCreate(&e));
+        P->ev_pool.push_back(e);
+    }
+    *ev = P->ev_used;
+    P->ev_used += 2;
+    QXG_CUDA(cudaEventRecord(P->ev_pool[*ev], P->stream));
+    return 0;
+}
+
+int prof_end(qxg_program* P, size_t ev, int instr, int kind, double flops, double bytes) {
+    P->launches++;
+    if (!P->profiling) return 0;
+    QXG_CUDA(cudaEventRecord(P->ev_pool[ev + 1], P->stream));
+    P->recs.push_back({instr, kind, ev, flops, bytes});
+    return 0;
+}
+
 int run_group(qxg_program* P, int g) {
     Plan& pl = *P->plan;
     int* exps = P->fp64 ? nullptr : P->d_exps;
-    if (exps) QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[g], pl.slot_end[g], P->stream));
+    if (exps) {
+        QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[g], pl.slot_end[g], P->stream));
+        P->launches++;
+    }
     for (auto& st : pl.steps[g]) {
+        const int instr = pl.T[st.tensor].instr;
+        size_t ev = 0;
+        if (int r = prof_begin(P, &ev)) return r;
+        int kind;
         if (st.kind == QXG_OP_NCON) {
             if (st.use_tc) {
+                kind = QXG_KERNEL_CONTRACT_TC;
                 QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
             } else {
+                kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
                 QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count));
             }
         } else if (st.kind == QXG_OP_VIEW) {
+            kind = QXG_KERNEL_VIEW;
             QXG_CUDA(launch_view(st.vargs, P->fp64, exps, P->stream));
         } else {
+            kind = QXG_KERNEL_OUTPUT;
             st.oargs.bitstrings = P->d_bits;
             QXG_CUDA(launch_output(st.oargs, P->fp64, exps, P->stream));
         }
+        if (int r = prof_end(P, ev, instr, kind, st.flops, st.bytes)) return r;
     }
     return 0;
+}
+
+int run_reduce(qxg_program* P) {
+    Plan& pl = *P->plan;
+    size_t ev = 0;
+    if (int r = prof_begin(P, &ev)) return r;
+    QXG_CUDA(launch_reduce(pl.red, P->fp64, P->fp64 ? nullptr : P->d_exps, P->stream));
+    return prof_end(P, ev, -1, QXG_KERNEL_REDUCE, 0.0, 0.0);
 }
 
 int set_params(qxg_program* P, size_t k, const PassParams& pp) {
@@ -771,7 +820,7 @@ int run_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d_out)
         if (int r = set_params(P, k++, pp)) return r;
         if (int r = run_group(P, 1)) return r;
         if (!root.beta && root.group <= 1) {
-            QXG_CUDA(launch_reduce(pl.red, P->fp64, P->fp64 ? nullptr : P->d_exps, P->stream));
+            if (int r = run_reduce(P)) return r;
             continue;
         }
         for (int64_t b = 0; b < nbc; b++) {
@@ -779,7 +828,7 @@ int run_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d_out)
             pp.bits_valid = root.beta ? (int32_t)std::min<int64_t>(pl.bc, nbits - pp.bit_base) : nbits;
             if (int r = set_params(P, k++, pp)) return r;
             if (int r = run_group(P, 2)) return r;
-            QXG_CUDA(launch_reduce(pl.red, P->fp64, P->fp64 ? nullptr : P->d_exps, P->stream));
+            if (int r = run_reduce(P)) return r;
         }
     }
     return 0;
@@ -990,10 +1039,48 @@ int qxg_program_info_get(const qxg_program* P, qxg_program_info* info) {
     return QXG_OK;
 }
 
+int qxg_program_profile(qxg_program* P, int32_t enable) {
+    if (!P) return fail(QXG_ERR_INVALID, "bad arguments");
+    QXG_CUDA(cudaSetDevice(P->device));
+    QXG_CUDA(cudaStreamSynchronize(P->stream));
+    P->profiling = enable != 0;
+    P->recs.clear();
+    P->ev_used = 0;
+    return QXG_OK;
+}
+
+int qxg_program_profile_read(qxg_program* P, qxg_step_profile* out, int32_t max_entries, int32_t* n_entries,
+                             int64_t* kernel_launches) {
+    if (!P || (max_entries > 0 && !out)) return fail(QXG_ERR_INVALID, "bad arguments");
+    QXG_CUDA(cudaSetDevice(P->device));
+    QXG_CUDA(cudaStreamSynchronize(P->stream));
+    std::map<std::pair<int, int>, qxg_step_profile> agg;
+    for (const auto& r : P->recs) {
+        float ms = 0.f;
+        QXG_CUDA(cudaEventElapsedTime(&ms, P->ev_pool[r.ev], P->ev_pool[r.ev + 1]));
+        auto& a = agg[{r.instr, r.kind}];
+        a.instr = r.instr;
+        a.kernel = r.kind;
+        a.launches += 1;
+        a.ms += ms;
+        a.flops += r.flops;
+        a.bytes += r.bytes;
+    }
+    int32_t n = 0;
+    for (auto& kv : agg) {
+        if (n < max_entries) out[n] = kv.second;
+        n++;
+    }
+    if (n_entries) *n_entries = n;
+    if (kernel_launches) *kernel_launches = P->launches;
+    return QXG_OK;
+}
+
 void qxg_program_destroy(qxg_program* P) {
     if (!P) return;
     cudaSetDevice(P->device);
     if (P->stream) cudaStreamSynchronize(P->stream);
+    for (cudaEvent_t e : P->ev_pool) cudaEventDestroy(e);
     for (void* p : P->d_data) if (p) cudaFree(p);
     if (P->d_arena) cudaFree(P->d_arena);
     if (P->d_scratch) cudaFree(P->d_scratch);

@@ -54,6 +54,13 @@ class qxg_program_info(ct.Structure):
                 ("num_steps_bitstring", ct.c_int32), ("reserved", ct.c_int32 * 5)]
 
 
+class qxg_step_profile(ct.Structure):
+    _fields_ = [("instr", ct.c_int32), ("kernel", ct.c_int32), ("launches", ct.c_int64), ("ms", ct.c_double),
+                ("flops", ct.c_double), ("bytes", ct.c_double)]
+
+
+KERNEL_KINDS = {0: "contract_fp64", 1: "contract_fp32", 2: "contract_tc", 3: "view", 4: "output", 5: "reduce"}
+
 _lib = None
 
 
@@ -87,10 +94,14 @@ def load_library(path=None):
     lib.qxg_ncon.argtypes = [ct.c_int32, P, ct.c_int32, ct.POINTER(ct.c_int32), P, ct.c_int32,
                              ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), P, ct.c_int32,
                              ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), P]
+    lib.qxg_program_profile.argtypes = [P, ct.c_int32]
+    lib.qxg_program_profile_read.argtypes = [P, ct.POINTER(qxg_step_profile), ct.c_int32, ct.POINTER(ct.c_int32),
+                                             ct.POINTER(ct.c_int64)]
     lib.qxg_last_error.restype = ct.c_char_p
     lib.qxg_version.restype = ct.c_char_p
     for f in ("qxg_program_create", "qxg_program_set_data", "qxg_amplitudes", "qxg_amplitudes_device",
-              "qxg_program_synchronize", "qxg_program_info_get", "qxg_ncon"):
+              "qxg_program_synchronize", "qxg_program_info_get", "qxg_ncon", "qxg_program_profile",
+              "qxg_program_profile_read"):
         getattr(lib, f).restype = ct.c_int
     if path is None:
         _lib = lib
@@ -190,7 +201,10 @@ class Programme:
 
     @classmethod
     def from_graph(cls, graph: ComputeGraph) -> "Programme":
-        return cls.from_commands(graph.commands, graph.data, graph.num_qubits)
+        """Bitstrings carry one character per `output` command (qubit numbers 1..k), so a
+        programme without outputs (open wires only) takes empty bitstrings."""
+        nq = max([c.qubit for c in graph.commands if isinstance(c, Output)], default=0)
+        return cls.from_commands(graph.commands, graph.data, nq)
 
 
 def _bitstring_bytes(bitstrings, nqubits: int) -> bytes:
@@ -287,6 +301,22 @@ class Executor:
 
     def synchronize(self):
         _check(self.lib, self.lib.qxg_program_synchronize(self._h))
+
+    def profile(self, enable: bool = True):
+        """Start (clearing earlier records) or stop CUDA-event timing of every launch."""
+        _check(self.lib, self.lib.qxg_program_profile(self._h, int(enable)))
+
+    def profile_read(self):
+        """-> (list of per-command dicts {instr, kernel, launches, ms, flops, bytes}, total
+        kernel launches since creation)."""
+        n = ct.c_int32(0)
+        launches = ct.c_int64(0)
+        _check(self.lib, self.lib.qxg_program_profile_read(self._h, None, 0, ct.byref(n), ct.byref(launches)))
+        buf = (qxg_step_profile * max(1, n.value))()
+        _check(self.lib, self.lib.qxg_program_profile_read(self._h, buf, n.value, ct.byref(n), ct.byref(launches)))
+        rows = [{"instr": b.instr, "kernel": KERNEL_KINDS.get(b.kernel, str(b.kernel)), "launches": b.launches,
+                 "ms": b.ms, "flops": b.flops, "bytes": b.bytes} for b in buf[:n.value]]
+        return rows, launches.value
 
     @property
     def stream(self) -> int:

@@ -365,15 +365,17 @@ def netcon(tnc) -> list:
 # ---------------------------------------------------------------------------------------
 # greedy planner (seeded, randomised)
 # ---------------------------------------------------------------------------------------
-def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exclude=()) -> list:
+def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exclude=(),
+                            score: str = "size") -> list:
     """Seeded greedy contraction: repeatedly contract the pair of tensors sharing a
-    (non-excluded) label that minimises size(C) - size(A) - size(B), with optional Gumbel
-    noise of the given temperature on log-sizes.  Intermediates are named `I<k>`.
-    Disconnected components are left for the caller (build_compute_graph joins them)."""
+    (non-excluded) label with the lowest score, plus Gumbel noise of the given temperature.
+    Scores (log2 units): "size" = signed log of size(C) - size(A) - size(B) (the classic
+    greedy), "growth" = log size(C) - max(log size(A), log size(B)).  Intermediates are named
+    `I<k>`.  Disconnected components are left for the caller (build_compute_graph joins
+    them)."""
     rng = np.random.default_rng(seed)
     excl = set(exclude)
-    dims = net.dims
-    lg = {l: math.log2(d) for l, d in dims.items()}
+    lg = {l: (0.0 if l in excl else math.log2(d)) for l, d in net.dims.items()}
     tens = {n: set(ls) for n, ls in net.tensors.items()}
     holders: dict = {}
     for n, ls in tens.items():
@@ -382,7 +384,7 @@ def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exc
     opens = set(net.open)
 
     def size_lg(ls):
-        return sum(0.0 if l in excl else lg[l] for l in ls)
+        return sum(lg[l] for l in ls)
 
     def result(a, b):
         la, lb = tens[a], tens[b]
@@ -396,14 +398,20 @@ def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exc
         return out
 
     def cost(a, b):
-        lc = result(a, b)
-        c = 2.0 ** size_lg(lc) - 2.0 ** size_lg(tens[a]) - 2.0 ** size_lg(tens[b])
+        c = size_lg(result(a, b))
+        x, y = size_lg(tens[a]), size_lg(tens[b])
+        if score == "growth":
+            s = c - max(x, y)
+        else:
+            d = 2.0 ** c - 2.0 ** x - 2.0 ** y
+            s = math.copysign(math.log2(abs(d) + 1.0), d)
         if temperature > 0:
-            c -= temperature * float(rng.gumbel()) * 2.0 ** size_lg(lc)
-        return c
+            s -= temperature * float(rng.gumbel())
+        return s
 
     heap = []
     counter = itertools.count()
+    order_idx = {n: i for i, n in enumerate(tens)}
 
     def push_pairs(n):
         seen = set()
@@ -413,13 +421,8 @@ def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exc
             for m in holders[l]:
                 if m != n and m not in seen:
                     seen.add(m)
-                    a, b = (n, m) if _order_key(n) < _order_key(m) else (m, n)
+                    a, b = (n, m) if order_idx[n] < order_idx[m] else (m, n)
                     heapq.heappush(heap, (cost(a, b), next(counter), a, b))
-
-    order_idx = {n: i for i, n in enumerate(tens)}
-
-    def _order_key(n):
-        return order_idx[n]
 
     for n in list(tens):
         push_pairs(n)
@@ -436,7 +439,8 @@ def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exc
             c = f"I{k}"
         lc = result(a, b)
         for l in tens[a] | tens[b]:
-            holders[l].discard(a); holders[l].discard(b)
+            holders[l].discard(a)
+            holders[l].discard(b)
         del tens[a], tens[b]
         tens[c] = lc
         order_idx[c] = len(order_idx)
@@ -452,6 +456,18 @@ def _sort_key_cost(net, plan, sliced=()):
     return (pc["max_log2"], pc["flops"])
 
 
+_TRIAL_SETTINGS = [("size", 0.0), ("growth", 0.0), ("growth", 0.5), ("size", 0.2), ("growth", 0.3),
+                   ("size", 0.5)]
+
+
+def random_greedy_plans(net: HyperNet, trials: int, seed: int = 0, exclude=()):
+    """`trials` seeded greedy plans cycling through score functions and temperatures."""
+    for t in range(trials):
+        score, temp = _TRIAL_SETTINGS[t % len(_TRIAL_SETTINGS)]
+        yield greedy_contraction_plan(net, seed=seed * 7919 + t, temperature=temp, exclude=exclude,
+                                      score=score)
+
+
 def flow_cutter_contraction_plan(tnc, time: int = 60, seed: int = -1, hypergraph: bool = True) -> list:
     """Stand-in for FlowCutter planning (:90-113): best of the min-fill plan and
     `8 * time` seeded random-greedy plans by (largest intermediate, FLOPs).
@@ -462,9 +478,7 @@ def flow_cutter_contraction_plan(tnc, time: int = 60, seed: int = -1, hypergraph
         return base
     seed0 = 0 if seed is None or seed < 0 else int(seed)
     best, bestk = base, _sort_key_cost(net, base)
-    for trial in range(max(1, 8 * int(time))):
-        temp = 0.0 if trial == 0 else 0.05 * (1 + trial % 4)
-        p = greedy_contraction_plan(net, seed=seed0 * 7919 + trial, temperature=temp)
+    for p in random_greedy_plans(net, max(1, 8 * int(time)), seed0):
         if len(p) < len(base):
             continue
         k = _sort_key_cost(net, p)
@@ -548,7 +562,7 @@ def net_labels_in_order(tn):
     return list(tn.hyperedges().keys())
 
 
-def _scheme_by_greedy(net, num, seed0, max_log2, base_plan):
+def _scheme_by_greedy(net, num, seed0, max_log2, base_plan, replan_trials=6):
     plan = base_plan
     sliced: list = []
     widths = []
@@ -558,9 +572,7 @@ def _scheme_by_greedy(net, num, seed0, max_log2, base_plan):
             break
         best = min(cands, key=lambda l: _scheme_key(net, plan, sliced + [l]))
         sliced.append(best)
-        trials = [greedy_contraction_plan(net, seed=seed0, exclude=sliced)] + \
-            [greedy_contraction_plan(net, seed=seed0 * 31 + t, temperature=0.1, exclude=sliced) for t in range(1, 4)]
-        for p in trials:
+        for p in random_greedy_plans(net, replan_trials, seed0 * 31 + len(sliced), exclude=sliced):
             if _scheme_key(net, p, sliced) < _scheme_key(net, plan, sliced):
                 plan = p
         widths.append(plan_cost(net, plan, sliced)["max_log2"])
@@ -591,7 +603,7 @@ def contraction_scheme(tnc, num: int, time: int = 120, seed: int = -1,
     method = "min fill heuristic"
     if hypergraph and time > 0:
         base = flow_cutter_contraction_plan(tnc, time=time, seed=seed, hypergraph=hypergraph)
-        p2, s2, w2 = _scheme_by_greedy(net, num, seed0, max_log2, base)
+        p2, s2, w2 = _scheme_by_greedy(net, num, seed0, max_log2, base, replan_trials=max(6, 2 * int(time)))
         if _scheme_key(net, p2, s2) < _scheme_key(net, plan, sliced):
             plan, sliced, widths = p2, s2, w2
             method = "greedy stand-in for flow cutter"

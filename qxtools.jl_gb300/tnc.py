@@ -295,6 +295,15 @@ class TensorNetworkCircuit:
             raise ValueError("outputs already added")
         self.output_tensors = self._boundary("out", bitstring)
 
+    def add_output_subset(self, qubits):
+        """Output tensors on the listed qubits (1-based) only; the others stay open, so the
+        contraction yields a 2^k tensor per bitstring (k open qubits).  Output i of the
+        programme is qubits[i-1]; bitstrings carry one character per listed qubit."""
+        if self.output_tensors:
+            raise ValueError("outputs already added")
+        self.output_tensors = [self.tn.add_tensor([self.output_indices[q - 1]], basis_vector("0"))
+                               for q in qubits]
+
     def set_output(self, bitstring: str):
         """Replace the data of the existing output tensors with another bitstring's vectors."""
         for q, ch in enumerate(bitstring):

@@ -1,0 +1,84 @@
+"""Seeded synthetic workloads of the benchmark configurations (random grid circuits).
+
+Each workload is a `.qx` programme built the way generate_simulation_files builds one
+(src/simulation.jl:52-77: convert_to_tnc with decomposition, contraction_scheme, then
+build_compute_graph) plus a seeded list of bitstrings (the `.yml` List method).  Generated
+programmes are cached under _build/workloads/ (the planner takes seconds to a minute).
+
+  rqc_4x4_d10          4x4 grid, 10 cycles, unsliced, 64 bitstrings (the CPU-runnable case)
+  rqc_6x6_d14_s4       6x6 grid, 14 cycles, 4 sliced bonds, 256 bitstrings
+  rqc_5x5_d12_open6    5x5 grid, 12 cycles, 6 qubits open (2^6 amplitudes per bitstring),
+                       64 bitstrings of the other 19 qubits -> 4096 amplitudes
+  rqc_3x4_d8_s3        3x4 grid, 8 cycles, 3 sliced bonds, 64 bitstrings (parity size)
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+
+from . import dsl as _dsl
+from .circuits import create_rqc_circuit
+from .compute_graph import build_compute_graph
+from .executor import Programme
+from .planning import contraction_scheme, hyper_network, plan_cost
+from .simulation import amplitudes_uniform
+from .tnc import convert_to_tnc
+
+__all__ = ["WORKLOADS", "build_workload"]
+
+WORKLOADS = {
+    "rqc_4x4_d10": dict(rows=4, cols=4, depth=10, nslice=0, open=0, nbits=64),
+    "rqc_6x6_d14_s4": dict(rows=6, cols=6, depth=14, nslice=4, open=0, nbits=256),
+    "rqc_5x5_d12_open6": dict(rows=5, cols=5, depth=12, nslice=0, open=6, nbits=64),
+    "rqc_3x4_d8_s3": dict(rows=3, cols=4, depth=8, nslice=3, open=0, nbits=64),
+}
+
+_CACHE = Path(__file__).resolve().parent / "_build" / "workloads"
+
+
+def _key(name, spec, seed, time):
+    h = hashlib.sha1(json.dumps([name, spec, seed, time], sort_keys=True).encode()).hexdigest()[:12]
+    return f"{name}_{h}"
+
+
+def build_workload(name: str, seed: int = 1, time: int = 2, cache: bool = True):
+    """-> (Programme, bitstrings, info dict).  Deterministic for (name, seed, time)."""
+    spec = dict(WORKLOADS[name])
+    key = _key(name, spec, seed, time)
+    qx, npz, meta_p = (_CACHE / f"{key}.qx", _CACHE / f"{key}.npz", _CACHE / f"{key}.json")
+    if cache and qx.exists() and npz.exists() and meta_p.exists():
+        cmds, _ = _dsl.read_qx(str(qx))
+        info = json.loads(meta_p.read_text())
+        prog = Programme.from_commands(cmds, _dsl.read_data(str(npz)), info["nqubits"])
+        return prog, info["bitstrings"], info
+    circ = create_rqc_circuit(spec["rows"], spec["cols"], spec["depth"], seed=seed)
+    n = circ.num_qubits
+    tnc = convert_to_tnc(circ, decompose=True, no_output=True)
+    if spec["open"]:
+        rng = np.random.Generator(np.random.PCG64(seed + 1000))
+        open_q = sorted(int(x) + 1 for x in rng.choice(n, size=spec["open"], replace=False))
+        out_q = [q for q in range(1, n + 1) if q not in open_q]
+    else:
+        open_q, out_q = [], list(range(1, n + 1))
+    tnc.add_output_subset(out_q)
+    groups, plan, meta = contraction_scheme(tnc, spec["nslice"], seed=seed, time=time)
+    graph = build_compute_graph(tnc, plan, groups)
+    nq = len(out_q)
+    prog = Programme.from_commands(graph.commands, graph.data, nq)
+    bits = list(amplitudes_uniform(nq, seed, spec["nbits"]))
+    net = hyper_network(tnc)
+    sl = [tnc.tn.root(g[0]) for g in groups]
+    pc = plan_cost(net, plan, sl)
+    info = dict(name=name, spec=spec, seed=seed, nqubits=nq, open_qubits=open_q, bitstrings=bits,
+                num_slices=prog.num_slices, plan_steps=len(plan), max_log2=pc["max_log2"],
+                flops_per_slice=pc["flops"], flops_per_bitstring=pc["flops"] * prog.num_slices,
+                amplitudes_per_bitstring=2 ** len(open_q), metadata=meta)
+    if cache:
+        _CACHE.mkdir(parents=True, exist_ok=True)
+        _dsl.write_qx(graph, str(qx), metadata=meta)
+        _dsl.write_data(graph.data, str(npz))
+        meta_p.write_text(json.dumps(info, default=str))
+    return prog, bits, info
