@@ -102,7 +102,8 @@ typedef struct qxg_program_info {
     int32_t num_steps_invariant;  /* ncon steps computed once per call */
     int32_t num_steps_slice;      /* ncon steps computed once per slice batch */
     int32_t num_steps_bitstring;  /* ncon steps computed once per (slice batch, bitstring batch) */
-    int32_t reserved[5];
+    int32_t num_steps_tensor_core;  /* ncon steps run on the tensor cores (split modes) */
+    int32_t reserved[4];
 } qxg_program_info;
 
 /* Build a programme from the `.qx` command list.  data_rank[i] and the concatenated

@@ -834,6 +834,18 @@ int run_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d_out)
     return 0;
 }
 
+// A tensor-core kernel whose bounded wait gave up leaves a code in a device word; read and clear.
+int check_tc(qxg_program* P) {
+    if (!P->plan) return 0;
+    bool any = false;
+    for (int g = 0; g < 3; g++) for (auto& st : P->plan->steps[g]) any = any || st.use_tc;
+    if (!any) return 0;
+    int code = 0;
+    QXG_CUDA(tc_read_error(&code, P->stream));
+    if (code) return fail(QXG_ERR_TIMEOUT, "a tensor-core kernel gave up waiting (code " + std::to_string(code) + ")");
+    return 0;
+}
+
 int check_ready(qxg_program* P) {
     for (size_t i = 0; i < P->data_set.size(); i++) {
         bool used = false;
@@ -1000,12 +1012,14 @@ int qxg_amplitudes(qxg_program* P, const char* bits, int32_t nbits, int64_t s0, 
     if (int r = run_passes(P, nbits, s0, s1, P->d_out)) return r;
     QXG_CUDA(cudaMemcpyAsync(out, P->d_out, ob, cudaMemcpyDeviceToHost, P->stream));
     QXG_CUDA(cudaStreamSynchronize(P->stream));
+    if (int r = check_tc(P)) return r;
     return QXG_OK;
 }
 
 int qxg_program_synchronize(qxg_program* P) {
     if (!P) return fail(QXG_ERR_INVALID, "bad arguments");
     QXG_CUDA(cudaStreamSynchronize(P->stream));
+    if (int r = check_tc(P)) return r;
     return QXG_OK;
 }
 
@@ -1030,8 +1044,13 @@ int qxg_program_info_get(const qxg_program* P, qxg_program_info* info) {
         info->workspace_bytes = (int64_t)(pl.arena_bytes + pl.tc_scratch_bytes);
         info->flops_executed_per_pass = pl.flops_pass[0] + pl.flops_pass[1] + pl.flops_pass[2];
         info->bytes_executed_per_pass = pl.bytes_pass[0] + pl.bytes_pass[1] + pl.bytes_pass[2];
-        int c[3] = {0, 0, 0};
-        for (int g = 0; g < 3; g++) for (auto& st : pl.steps[g]) if (st.kind == QXG_OP_NCON) c[g]++;
+        int c[3] = {0, 0, 0}, ntc = 0;
+        for (int g = 0; g < 3; g++)
+            for (auto& st : pl.steps[g]) {
+                if (st.kind == QXG_OP_NCON) c[g]++;
+                if (st.use_tc) ntc++;
+            }
+        info->num_steps_tensor_core = ntc;
         info->num_steps_invariant = c[0];
         info->num_steps_slice = c[1];
         info->num_steps_bitstring = c[2];

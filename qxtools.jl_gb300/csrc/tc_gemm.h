@@ -1,6 +1,13 @@
-// Tensor-core (tcgen05) path of the split-precision executors: a contraction step whose
-// summed and free extents are large enough is run as a complex GEMM on 3xBF16 or 3xTF32
-// operand splits with FP32 accumulation in tensor memory.
+// Tensor-core (tcgen05) path of the split-precision executors.
+//
+// A contraction step C[b,m,n] = sum_k X[b,m,k] Y[b,k,n] (X the larger operand, Y the smaller)
+// runs as a real GEMM on the 5th-generation tensor cores:
+//   A_op[m, (q,k)]         = (Re X, Im X)[m, k]                  (M x 2K, K-major)
+//   B_op[(p,n), (q,k)]     = [[Re Y, -Im Y], [Im Y, Re Y]]       (2N x 2K, K-major)
+//   D[m, (p,n)]            = (Re C, Im C)[m, n]                  (FP32 in tensor memory)
+// Each operand is split into hi + lo planes (3xBF16: bf16 round-to-nearest of x and of x-hi;
+// 3xTF32 the same with tf32), scaled by 2^-(max exponent) so nothing underflows, and the three
+// products hi*hi + hi*lo + lo*hi accumulate in FP32 (the lo*lo term is dropped).
 #pragma once
 
 #include <cstddef>
@@ -10,10 +17,23 @@
 
 namespace qxg {
 
+constexpr int kTcTileM = 128;       // MMA M (rows of X per CTA)
+constexpr int kTcChunkBytes = 128;  // bytes of one operand row per K chunk (8 core-matrix columns)
+
 struct TcStep {
-    int64_t M = 0, N = 0, K = 0, batch = 0;   // GEMM extents of the step
-    size_t scratch_bytes = 0;                 // split operands staged in device scratch
+    bool x_is_a = true;             // the larger operand (M side) is the step's A
     bool tf32 = false;
+    int nb = 0, nm = 0, nn = 0, nk = 0;        // bits of batch, M, N, K
+    int64_t M = 0, N = 0, K = 0, batch = 0;
+    int ntile_n = 0;                // complex columns per N tile (N'' = 2 ntile_n)
+    int kc = 0;                     // complex K per chunk (32 bf16, 16 tf32)
+    int64_t mtiles = 0, ntiles = 0, kchunks = 0;
+    // bit maps: index space -> operand / result offsets
+    BitMap xb, xm, xk;              // X offset of batch / m / k index
+    BitMap yb, yn, yk;              // Y offset of batch / n / k index
+    BitMap cb, cm, cn;              // C offset of batch / m / n index
+    size_t a_plane_bytes = 0, b_plane_bytes = 0;
+    size_t scratch_bytes = 0;       // 2 planes of A_op + 2 planes of B_op
 };
 
 // Decide whether a step goes to the tensor cores; fills `tc` when it does.
@@ -22,5 +42,8 @@ bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits
 // Run a planned tensor-core step (scratch: at least tc.scratch_bytes of device memory).
 cudaError_t tc_run_step(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
                         int sm_count);
+
+// Device error word set by a tensor-core kernel whose bounded wait gave up (0 = none).
+cudaError_t tc_read_error(int* host_code, cudaStream_t st);
 
 }  // namespace qxg

@@ -51,7 +51,8 @@ class qxg_program_info(ct.Structure):
                 ("workspace_bytes", ct.c_int64), ("flops_per_amplitude", ct.c_double),
                 ("flops_executed_per_pass", ct.c_double), ("bytes_executed_per_pass", ct.c_double),
                 ("num_steps_invariant", ct.c_int32), ("num_steps_slice", ct.c_int32),
-                ("num_steps_bitstring", ct.c_int32), ("reserved", ct.c_int32 * 5)]
+                ("num_steps_bitstring", ct.c_int32), ("num_steps_tensor_core", ct.c_int32),
+                ("reserved", ct.c_int32 * 4)]
 
 
 class qxg_step_profile(ct.Structure):

@@ -1,0 +1,72 @@
+"""Split-precision executors (3xBF16 / 3xTF32 products on tcgen05 tensor cores, FP32
+accumulation, power-of-two operand scaling, FP64 slice sum) against exact references.
+
+Tolerances (relative to the largest result element): 3xTF32 <= 5e-6, 3xBF16 <= 1e-4 for a single
+contraction (FP32 accumulation over up to 2^8 real terms is itself ~1e-6); on whole random-circuit
+programmes <= 1e-5 (3xTF32, FP32) and <= 1e-4 (3xBF16) against the FP64 oracle.
+"""
+import math
+from collections import OrderedDict
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = {"split_tf32": 5e-6, "split_bf16": 1e-4, "fp32": 5e-6}
+
+
+def single_ncon_programme(q, nm, nk, nn, nbatch=0, seed=0, scale=1.0):
+    """C[m.., n.., b..] = sum_k A[m.., k.., b..] B[k.., n.., b..] with dim-2 labels."""
+    rng = np.random.default_rng(seed)
+    lm = list(range(1, nm + 1))
+    lk = list(range(nm + 1, nm + nk + 1))
+    ln = list(range(nm + nk + 1, nm + nk + nn + 1))
+    lb = list(range(nm + nk + nn + 1, nm + nk + nn + nbatch + 1))
+    la, lbb, lc = lm + lk + lb, lk + ln + lb, lm + ln + lb
+    A = (rng.standard_normal((2,) * len(la)) + 1j * rng.standard_normal((2,) * len(la))) * scale
+    B = (rng.standard_normal((2,) * len(lbb)) + 1j * rng.standard_normal((2,) * len(lbb))) * scale
+    cmds = [q.Load("a", "data_1", A.shape), q.Load("b", "data_2", B.shape),
+            q.Ncon("c", tuple(lc), "a", tuple(la), "b", tuple(lbb)), q.Save("output", "c")]
+    prog = q.Programme.from_commands(cmds, OrderedDict([("data_1", A), ("data_2", B)]), 0)
+    letters = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
+    sub = lambda ls: "".join(letters[l - 1] for l in ls)
+    ref = np.einsum(f"{sub(la)},{sub(lbb)}->{sub(lc)}", A, B).reshape(-1, order="F")
+    return prog, ref
+
+
+@pytest.mark.parametrize("precision", ["split_tf32", "split_bf16"])
+@pytest.mark.parametrize("nm,nk,nn,nb", [(7, 5, 4, 0), (8, 6, 8, 0), (7, 7, 2, 0), (9, 4, 5, 1), (7, 3, 5, 0)])
+def test_tensor_core_single_contraction(q, gpu_lib, precision, nm, nk, nn, nb):
+    prog, ref = single_ncon_programme(q, nm, nk, nn, nb, seed=nm * 100 + nk * 10 + nn)
+    with q.Executor(prog, precision=precision) as ex:
+        got = ex.amplitudes([""])[0]
+        assert ex.info()["num_steps_tensor_core"] == 1
+    err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    assert err <= TOL[precision], err
+
+
+@pytest.mark.parametrize("precision", ["split_tf32", "split_bf16"])
+def test_tensor_core_scaling_tiny_and_huge_values(q, gpu_lib, precision):
+    """Operands far from 1 are scaled by powers of two before the split: no underflow/overflow."""
+    for scale in (2.0 ** -60, 2.0 ** 50):
+        prog, ref = single_ncon_programme(q, 7, 5, 4, seed=3, scale=scale)
+        with q.Executor(prog, precision=precision) as ex:
+            got = ex.amplitudes([""])[0]
+        err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+        assert err <= TOL[precision], (scale, err)
+
+
+@pytest.mark.parametrize("precision", ["split_tf32", "split_bf16", "fp32"])
+def test_split_executor_on_random_circuit(q, gpu_lib, oracle, precision):
+    circ = q.create_rqc_circuit(4, 4, 8, seed=21)
+    tnc = q.convert_to_tnc(circ, decompose=True, no_output=True)
+    tnc.add_output_subset(list(range(1, 11)))          # 6 qubits open: 64 amplitudes per bitstring
+    groups, plan, _ = q.contraction_scheme(tnc, 1, seed=2, time=1)
+    prog = q.Programme.from_graph(q.build_compute_graph(tnc, plan, groups))
+    bits = list(q.amplitudes_uniform(10, 5, 12))
+    with q.Executor(prog, precision=precision) as ex:
+        got = ex.amplitudes(bits)
+    ref = oracle.run_programme(prog, bits, nthreads=8, out_size=64)
+    err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    tol = 1e-5 if precision != "split_bf16" else 1e-4
+    assert err <= tol, err
