@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="rqc_5x5_d12_open6")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "split_bf16", "split_tf32"])
+    ap.add_argument("--precision", default="split_tf32", choices=["fp64", "fp32", "split_bf16", "split_tf32"])
     ap.add_argument("--bits-per-step", type=int, default=0, help="bitstrings per step (0: the workload's list)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample length")

@@ -149,10 +149,11 @@ int qxg_program_info_get(const qxg_program* prog, qxg_program_info* info);
 typedef enum qxg_kernel_kind {
     QXG_KERNEL_CONTRACT_FP64 = 0,   /* CUDA-core contraction, ComplexF64 */
     QXG_KERNEL_CONTRACT_FP32 = 1,   /* CUDA-core contraction, Complex64 / FP32 */
-    QXG_KERNEL_CONTRACT_TC = 2,     /* tensor-core (tcgen05) split-precision contraction */
+    QXG_KERNEL_CONTRACT_TC = 2,     /* tensor-core (tcgen05) split-precision GEMM of a contraction */
     QXG_KERNEL_VIEW = 3,            /* slice-batch view materialisation */
     QXG_KERNEL_OUTPUT = 4,          /* bitstring-batch output vectors */
-    QXG_KERNEL_REDUCE = 5           /* FP64 sum over the slice batch */
+    QXG_KERNEL_REDUCE = 5,          /* FP64 sum over the slice batch */
+    QXG_KERNEL_TC_PACK = 6          /* gather + hi/lo split of both operands for the tensor cores */
 } qxg_kernel_kind;
 
 typedef struct qxg_step_profile {

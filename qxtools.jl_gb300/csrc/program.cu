@@ -752,8 +752,16 @@ int run_group(qxg_program* P, int g) {
         int kind;
         if (st.kind == QXG_OP_NCON) {
             if (st.use_tc) {
+                // pack both operands (its own record), then the tensor-core GEMM
+                QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
+                const double pack_bytes = (double)P->esize *
+                        (double)((int64_t(1) << pl.T[P->ins[instr].a].layout.size()) +
+                                 (int64_t(1) << pl.T[P->ins[instr].b].layout.size())) +
+                    (double)st.tc.scratch_bytes;
+                if (int r = prof_end(P, ev, instr, QXG_KERNEL_TC_PACK, 0.0, pack_bytes)) return r;
+                if (int r = prof_begin(P, &ev)) return r;
                 kind = QXG_KERNEL_CONTRACT_TC;
-                QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
+                QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream));
             } else {
                 kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
                 QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count));

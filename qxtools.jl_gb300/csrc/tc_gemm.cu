@@ -1,21 +1,24 @@
 // Tensor-core path of the split-precision executors (see tc_gemm.h).
 //
-// Three kernels per contraction step:
-//   pack_x: gather the larger operand X through its bit maps, scale by 2^-max exponent, split
-//           into hi/lo planes and write them as tcgen05 K-major core-matrix tiles (no swizzle:
-//           8 rows x 16 bytes per core matrix, 128-byte K chunks, tile rows 128);
-//   pack_y: the same for the smaller operand Y in the complex-doubled form [[Re,-Im],[Im,Re]];
-//   gemm:   one CTA per (batch, 128-row M tile, N tile).  A producer thread streams the K chunks
-//           of the four planes into shared memory with cp.async.bulk (two stages, mbarrier
-//           transaction counts); one thread issues tcgen05.mma (kind::f16 with BF16 planes or
-//           kind::tf32) -- hi*hi, hi*lo, lo*hi per 32-byte K step -- into an FP32 accumulator in
-//           tensor memory; four epilogue warps read it back with tcgen05.ld and scatter the complex
-//           result through the result's bit map, raising the result's exponent slot.
+// Per contraction step:
+//   pack (x2): gather an operand through its bit maps, scale by 2^-max exponent, split into hi/lo
+//           planes and write them as tcgen05 K-major core-matrix tiles (no swizzle: 8 rows x 16
+//           bytes per core matrix, 64-byte K chunks so 8-row groups are 512 bytes apart).  The
+//           larger operand X becomes the MMA's A (M side); the smaller Y is written in the
+//           complex-doubled form [[Re,-Im],[Im,Re]] as the MMA's B (N side);
+//   gemm:   one CTA per (batch, 128-row M tile, N tile), two CTAs per SM.  A producer thread
+//           streams the K chunks of the four planes into shared memory with cp.async.bulk (three
+//           stages, mbarrier transaction counts); one thread issues tcgen05.mma (kind::f16 with
+//           BF16 planes or kind::tf32) -- hi*hi, hi*lo, lo*hi per 32-byte K step -- into an FP32
+//           accumulator in tensor memory; four epilogue warps read it with tcgen05.ld and scatter
+//           the complex result through the result's bit map (offsets of the tile's columns are
+//           tabulated in shared memory), raising the result's exponent slot.
 // Every wait is bounded; a wait that gives up sets g_tc_error, the CTA skips its remaining work,
 // frees its tensor memory and returns.
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "tc_gemm.h"
@@ -26,9 +29,14 @@ __device__ int g_tc_error = 0;
 
 namespace {
 
-constexpr int kThreadsGemm = 192;       // warp 0 producer, warp 1 MMA, warps 2-5 epilogue
-constexpr int kATileBytes = kTcTileM * kTcChunkBytes;   // 16 KB
-constexpr uint32_t kWaitLimit = 1u << 20;               // try_wait polls before giving up
+constexpr int kThreadsGemm = 192;                        // warp 0 producer, 1 MMA, 2-5 epilogue
+constexpr int kStages = 3;
+constexpr int kCols16 = kTcChunkBytes / 16;              // 16-byte core-matrix columns per chunk (4)
+constexpr int kSbo = kCols16 * 128;                      // bytes between 8-row groups (512)
+constexpr int kATileBytes = kTcTileM * kTcChunkBytes;    // 8 KB
+constexpr int kKSteps = kTcChunkBytes / 32;              // MMA K steps (32 bytes each) per chunk
+constexpr uint32_t kWaitLimit = 1u << 20;                // try_wait polls before giving up
+constexpr int kKTable = 4096;                            // k offsets tabulated by the pack kernel
 
 struct PackArgs {
     const void* src;        // float2 operand
@@ -49,7 +57,7 @@ struct GemmArgs {
     float2* C;
     BitMap cb, cm, cn;
     int64_t M, N, mtiles, ntiles, kchunks, batch;
-    int ntile;              // complex columns per N tile (16..128)
+    int ntile;              // complex columns per N tile (16..64)
     uint32_t b_tile_bytes;
     uint32_t idesc;
     int exp_c;
@@ -91,9 +99,9 @@ template <> struct Split<true> {
     }
 };
 
-// Byte offset of (row, 16-byte column) inside a K-major no-swizzle tile of 128-byte rows.
+// Byte offset of (row, 16-byte column) inside a K-major no-swizzle tile of 64-byte rows.
 __device__ __forceinline__ int64_t core_off(int row, int col16) {
-    return (int64_t)(row >> 3) * 1024 + col16 * 128 + (row & 7) * 16;
+    return (int64_t)(row >> 3) * kSbo + col16 * 128 + (row & 7) * 16;
 }
 
 template <typename E, int NE>
@@ -103,27 +111,33 @@ __device__ __forceinline__ void st16(uint8_t* dst, const E (&v)[NE]) {
     *reinterpret_cast<uint4*>(dst) = w;
 }
 
-// One thread: one row, one 16-byte group g (0..3) of one K chunk: E complex values of k.
+// One thread: one row, one 16-byte group g (0..1) of one K chunk: NE complex values of k, whose
+// real parts go to column g and imaginary parts to column 2 + g.
 template <bool TF32>
 __global__ void pack_kernel(const PackArgs p, int* exps) {
     using S = Split<TF32>;
     using E = typename S::E;
     constexpr int NE = 16 / sizeof(E);          // elements per 16 bytes: 8 bf16 / 4 tf32
+    constexpr int KC = 2 * NE;                  // complex k per chunk
+    __shared__ int64_t ktab[kKTable];
     const float2* __restrict__ X = static_cast<const float2*>(p.src);
     uint8_t* __restrict__ hi = static_cast<uint8_t*>(p.hi);
     uint8_t* __restrict__ lo = static_cast<uint8_t*>(p.lo);
+    const int64_t kt = p.K < kKTable ? p.K : kKTable;
+    for (int64_t k = threadIdx.x; k < kt; k += blockDim.x) ktab[k] = pdep(k, p.mk);
+    __syncthreads();
     const float s = pow2f(-read_m(exps, p.slot_src));
     if (p.doubled && blockIdx.x == 0 && threadIdx.x == 0) {
         const int mo = read_m(exps, p.slot_other), my = read_m(exps, p.slot_src);
         exps[2 * p.exp_c] = exps[2 * p.slot_other] + exps[2 * p.slot_src] + mo + my;
     }
-    const int64_t total = p.batch * p.kchunks * p.rows_pad * 4;
+    const int64_t total = p.batch * p.kchunks * p.rows_pad * 2;
     const int64_t tile_bytes = (int64_t)p.tile_rows * kTcChunkBytes;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t r = t % p.rows_pad;
+        const int64_t r = t % p.rows_pad;
         int64_t rest = t / p.rows_pad;
-        const int g = (int)(rest & 3);
-        rest >>= 2;
+        const int g = (int)(rest & 1);
+        rest >>= 1;
         const int64_t c = rest % p.kchunks;
         const int64_t b = rest / p.kchunks;
         float re[NE], im[NE];
@@ -131,10 +145,10 @@ __global__ void pack_kernel(const PackArgs p, int* exps) {
         const int64_t base = row_ok ? pdep(b, p.mb) + pdep(r, p.mr) : 0;
 #pragma unroll
         for (int j = 0; j < NE; j++) {
-            const int64_t k = c * (4 * NE) + g * NE + j;
+            const int64_t k = c * KC + g * NE + j;
             re[j] = 0.f; im[j] = 0.f;
             if (row_ok && k < p.K) {
-                const float2 v = X[base + pdep(k, p.mk)];
+                const float2 v = X[base + (k < kKTable ? ktab[k] : pdep(k, p.mk))];
                 re[j] = v.x * s;
                 im[j] = v.y * s;
             }
@@ -143,15 +157,14 @@ __global__ void pack_kernel(const PackArgs p, int* exps) {
 #pragma unroll
         for (int j = 0; j < NE; j++) { S::go(re[j], hr[j], lr[j]); S::go(im[j], hm[j], lm[j]); }
         if (!p.doubled) {
-            // A_op row r: re parts in 16-byte columns 0..3, im parts in 4..7
             const int64_t tile = (b * p.row_tiles + r / kTcTileM) * p.kchunks + c;
             const int row = (int)(r % kTcTileM);
             uint8_t* th = hi + tile * tile_bytes;
             uint8_t* tl = lo + tile * tile_bytes;
             st16(th + core_off(row, g), hr);
             st16(tl + core_off(row, g), lr);
-            st16(th + core_off(row, 4 + g), hm);
-            st16(tl + core_off(row, 4 + g), lm);
+            st16(th + core_off(row, 2 + g), hm);
+            st16(tl + core_off(row, 2 + g), lm);
         } else {
             // B_op rows (0,n): [Re Y | -Im Y], (1,n): [Im Y | Re Y]
             E nhm[NE], nlm[NE];
@@ -164,12 +177,12 @@ __global__ void pack_kernel(const PackArgs p, int* exps) {
             const int r0 = n, r1 = p.ntile + n;
             st16(th + core_off(r0, g), hr);
             st16(tl + core_off(r0, g), lr);
-            st16(th + core_off(r0, 4 + g), nhm);
-            st16(tl + core_off(r0, 4 + g), nlm);
+            st16(th + core_off(r0, 2 + g), nhm);
+            st16(tl + core_off(r0, 2 + g), nlm);
             st16(th + core_off(r1, g), hm);
             st16(tl + core_off(r1, g), lm);
-            st16(th + core_off(r1, 4 + g), hr);
-            st16(tl + core_off(r1, 4 + g), lr);
+            st16(th + core_off(r1, 2 + g), hr);
+            st16(tl + core_off(r1, 2 + g), lr);
         }
     }
 }
@@ -208,9 +221,9 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
         : "memory");
 }
 // Shared-memory matrix descriptor: K-major, no swizzle; LBO = 128 B between core matrices along
-// K, SBO = 1024 B between 8-row groups; descriptor version 1.
+// K, SBO = 512 B between 8-row groups; descriptor version 1.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
-    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(kSbo >> 4) << 32) |
            (1ull << 46);
 }
 template <bool TF32>
@@ -246,26 +259,28 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 template <bool TF32>
-__global__ void __launch_bounds__(kThreadsGemm, 1) tc_gemm_kernel(const GemmArgs g) {
+__global__ void __launch_bounds__(kThreadsGemm, 2) tc_gemm_kernel(const GemmArgs g) {
     extern __shared__ uint8_t smem_raw[];
-    __shared__ uint64_t bars[5];              // full[2], empty[2], accum
+    __shared__ uint64_t bars[2 * kStages + 1];   // full[kStages], empty[kStages], accum
+    __shared__ int64_t noff[128];                // result offsets of this tile's columns
     __shared__ uint32_t tmem_holder;
     __shared__ int abort_flag;
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const uint32_t stage_bytes = 2u * kATileBytes + 2u * g.b_tile_bytes;
     uint64_t* full = bars;
-    uint64_t* empty = bars + 2;
-    uint64_t* accum = bars + 4;
+    uint64_t* empty = bars + kStages;
+    uint64_t* accum = bars + 2 * kStages;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t tile = blockIdx.x;
     const int64_t nt = tile % g.ntiles;
     tile /= g.ntiles;
     const int64_t mt = tile % g.mtiles;
     const int64_t b = tile / g.mtiles;
-    const uint32_t ncols = (uint32_t)(2 * g.ntile) < 32u ? 32u : (uint32_t)(2 * g.ntile);
+    // two accumulators (main, corrections) of 2*ntile FP32 columns each
+    const uint32_t ncols = (uint32_t)(4 * g.ntile) < 32u ? 32u : (uint32_t)(4 * g.ntile);
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 5; i++) mbar_init(&bars[i], 1);
+        for (int i = 0; i < 2 * kStages + 1; i++) mbar_init(&bars[i], 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -275,18 +290,24 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) tc_gemm_kernel(const GemmArgs
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    if (warp >= 2) {
+        for (int j = threadIdx.x - 64; j < g.ntile; j += 128) {
+            const int64_t n = nt * g.ntile + j;
+            noff[j] = n < g.N ? pdep(n, g.cn) : 0;
+        }
+    }
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_holder;
 
     if (warp == 0 && lane == 0) {
-        // producer: stream K chunks of the four planes into the two stages
+        // producer: stream K chunks of the four planes into the stages
         const int64_t a_tile0 = (b * g.mtiles + mt) * g.kchunks;
         const int64_t b_tile0 = (b * g.ntiles + nt) * g.kchunks;
         for (int64_t c = 0; c < g.kchunks; c++) {
-            const int s = (int)(c & 1);
-            const uint32_t u = (uint32_t)(c >> 1);
+            const int s = (int)(c % kStages);
+            const uint32_t u = (uint32_t)(c / kStages);
             if (!mbar_wait(&empty[s], (u & 1u) ^ 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 1); break; }
             if (*(volatile int*)&abort_flag) break;
             uint8_t* st = smem + s * stage_bytes;
@@ -299,23 +320,26 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) tc_gemm_kernel(const GemmArgs
                       &full[s]);
         }
     } else if (warp == 1 && lane == 0) {
-        // MMA issuer: 4 K steps of 32 bytes per chunk, three products each
+        // MMA issuer: kKSteps K steps of 32 bytes per chunk, three products each
         for (int64_t c = 0; c < g.kchunks; c++) {
-            const int s = (int)(c & 1);
-            const uint32_t u = (uint32_t)(c >> 1);
+            const int s = (int)(c % kStages);
+            const uint32_t u = (uint32_t)(c / kStages);
             if (!mbar_wait(&full[s], u & 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 2); break; }
             fence_after();
             const uint32_t st = smem_u32(smem + s * stage_bytes);
             const uint32_t ahi = st, alo = st + kATileBytes, bhi = st + 2 * kATileBytes,
                            blo = st + 2 * kATileBytes + g.b_tile_bytes;
 #pragma unroll
-            for (int ks = 0; ks < 4; ks++) {
+            for (int ks = 0; ks < kKSteps; ks++) {
                 const uint32_t off = ks * 256;     // two 16-byte core-matrix columns per K step
                 const uint64_t dah = smem_desc(ahi + off), dal = smem_desc(alo + off);
                 const uint64_t dbh = smem_desc(bhi + off), dbl = smem_desc(blo + off);
-                mma<TF32>(tmem, dah, dbh, g.idesc, (c | ks) != 0 ? 1u : 0u);
-                mma<TF32>(tmem, dah, dbl, g.idesc, 1u);
-                mma<TF32>(tmem, dal, dbh, g.idesc, 1u);
+                const uint32_t first = (c | ks) != 0 ? 1u : 0u;
+                // hi*hi into the main accumulator; the small hi*lo + lo*hi corrections into their
+                // own accumulator, so they are not rounded away against the large running sum
+                mma<TF32>(tmem, dah, dbh, g.idesc, first);
+                mma<TF32>(tmem + 2 * g.ntile, dah, dbl, g.idesc, first);
+                mma<TF32>(tmem + 2 * g.ntile, dal, dbh, g.idesc, 1u);
             }
             mma_commit(&empty[s]);
         }
@@ -328,24 +352,27 @@ __global__ void __launch_bounds__(kThreadsGemm, 1) tc_gemm_kernel(const GemmArgs
         const int q = warp & 3;
         const int row = q * 32 + lane;
         const int64_t m = mt * kTcTileM + row;
-        const bool live = ok && !*(volatile int*)&abort_flag;
+        const bool live = ok && !*(volatile int*)&abort_flag && m < g.M;
         int emax = -2139062144;
-        const int64_t cbase = (m < g.M) ? pdep(b, g.cb) + pdep(m, g.cm) : 0;
+        float2* __restrict__ Crow = g.C + ((m < g.M) ? pdep(b, g.cb) + pdep(m, g.cm) : 0);
+        const int64_t nleft = g.N - nt * g.ntile;
+        const int nvalid = nleft < g.ntile ? (int)nleft : g.ntile;
+        const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
         for (int n0 = 0; n0 < g.ntile; n0 += 16) {
-            uint32_t vr[16], vi[16];
-            const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+            uint32_t vr[16], vi[16], cr[16], ci[16];
             tmem_ld16(lane_addr + n0, vr);
             tmem_ld16(lane_addr + g.ntile + n0, vi);
+            tmem_ld16(lane_addr + 2 * g.ntile + n0, cr);
+            tmem_ld16(lane_addr + 3 * g.ntile + n0, ci);
             tmem_wait_ld();
-            if (live && m < g.M) {
+            if (live) {
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
-                    const int64_t n = nt * g.ntile + n0 + j;
-                    if (n < g.N) {
+                    if (n0 + j < nvalid) {
                         float2 v;
-                        v.x = __uint_as_float(vr[j]);
-                        v.y = __uint_as_float(vi[j]);
-                        g.C[cbase + pdep(n, g.cn)] = v;
+                        v.x = __uint_as_float(vr[j]) + __uint_as_float(cr[j]);
+                        v.y = __uint_as_float(vi[j]) + __uint_as_float(ci[j]);
+                        Crow[noff[n0 + j]] = v;
                         const float mx = fmaxf(fabsf(v.x), fabsf(v.y));
                         if (mx > 0.f) emax = max(emax, exp_of(mx));
                     }
@@ -390,12 +417,14 @@ BitMap runs(const std::vector<std::pair<int, int>>& pairs, bool* ok) {
 
 int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+constexpr size_t kMaxDynSmem = kStages * (2 * kATileBytes + 2 * (2 * 64 * kTcChunkBytes)) + 128;
+
 template <bool TF32>
 cudaError_t set_smem_attr() {
     static bool done = false;
     if (done) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         2 * (2 * kATileBytes + 2 * 2 * 128 * kTcChunkBytes) + 1024);
+                                         (int)kMaxDynSmem);
     if (e == cudaSuccess) done = true;
     return e;
 }
@@ -454,45 +483,43 @@ bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits
     t.N = int64_t(1) << t.nn;
     t.K = int64_t(1) << t.nk;
     t.batch = int64_t(1) << t.nb;
-    t.ntile_n = (int)std::min<int64_t>(128, std::max<int64_t>(16, t.N));
-    t.kc = tf32 ? 16 : 32;
+    // N tile <= 64 complex: two accumulators of 2*64 columns = 256 tensor-memory columns, so two
+    // CTAs fit in an SM's 512 columns
+    t.ntile_n = (int)std::min<int64_t>(64, std::max<int64_t>(16, t.N));
+    t.kc = (kTcChunkBytes / 2) / (tf32 ? 4 : 2);     // complex k per chunk: half the row is Re
     t.mtiles = cdiv(t.M, kTcTileM);
     t.ntiles = cdiv(t.N, t.ntile_n);
     t.kchunks = cdiv(t.K, t.kc);
     t.a_plane_bytes = (size_t)(t.batch * t.mtiles * t.kchunks) * kATileBytes;
     t.b_plane_bytes = (size_t)(t.batch * t.ntiles * t.kchunks) * (size_t)(2 * t.ntile_n * kTcChunkBytes);
     t.scratch_bytes = 2 * (t.a_plane_bytes + t.b_plane_bytes);
-    if (t.scratch_bytes > (size_t(24) << 30)) return false;
+    if (t.scratch_bytes > (size_t(96) << 30)) return false;
     if (t.batch * t.mtiles * t.ntiles > (int64_t(1) << 31) - 1) return false;
     *tc = t;
     return true;
 }
 
-cudaError_t tc_run_step(const TcStep& t, const StepArgs& s, int* exps, void* scratch, cudaStream_t st, int sm_count) {
+cudaError_t tc_run_pack(const TcStep& t, const StepArgs& s, int* exps, void* scratch, cudaStream_t st, int sm_count) {
     uint8_t* base = static_cast<uint8_t*>(scratch);
-    void* a_hi = base;
-    void* a_lo = base + t.a_plane_bytes;
-    void* b_hi = base + 2 * t.a_plane_bytes;
-    void* b_lo = base + 2 * t.a_plane_bytes + t.b_plane_bytes;
     const int slot_x = t.x_is_a ? s.expA : s.expB;
     const int slot_y = t.x_is_a ? s.expB : s.expA;
     PackArgs px;
     memset(&px, 0, sizeof(px));
     px.src = t.x_is_a ? s.A : s.B;
-    px.hi = a_hi; px.lo = a_lo;
+    px.hi = base; px.lo = base + t.a_plane_bytes;
     px.mb = t.xb; px.mr = t.xm; px.mk = t.xk;
     px.rows = t.M; px.rows_pad = t.mtiles * kTcTileM; px.K = t.K; px.batch = t.batch;
     px.kchunks = t.kchunks; px.row_tiles = t.mtiles; px.tile_rows = kTcTileM; px.ntile = 0;
     px.slot_src = slot_x; px.doubled = 0; px.exp_c = s.expC; px.slot_other = slot_y;
     PackArgs py = px;
     py.src = t.x_is_a ? s.B : s.A;
-    py.hi = b_hi; py.lo = b_lo;
+    py.hi = base + 2 * t.a_plane_bytes; py.lo = base + 2 * t.a_plane_bytes + t.b_plane_bytes;
     py.mb = t.yb; py.mr = t.yn; py.mk = t.yk;
     py.rows = t.N; py.rows_pad = t.ntiles * t.ntile_n; py.row_tiles = t.ntiles;
     py.tile_rows = 2 * t.ntile_n; py.ntile = t.ntile_n;
     py.slot_src = slot_y; py.doubled = 1; py.slot_other = slot_x;
     auto grid_of = [&](const PackArgs& p) {
-        const int64_t n = p.batch * p.kchunks * p.rows_pad * 4;
+        const int64_t n = p.batch * p.kchunks * p.rows_pad * 2;
         return (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, 256), (int64_t)sm_count * 16));
     };
     if (t.tf32) {
@@ -502,11 +529,15 @@ cudaError_t tc_run_step(const TcStep& t, const StepArgs& s, int* exps, void* scr
         pack_kernel<false><<<grid_of(px), 256, 0, st>>>(px, exps);
         pack_kernel<false><<<grid_of(py), 256, 0, st>>>(py, exps);
     }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+cudaError_t tc_run_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scratch, cudaStream_t st) {
+    uint8_t* base = static_cast<uint8_t*>(scratch);
     GemmArgs g;
     memset(&g, 0, sizeof(g));
-    g.a_hi = a_hi; g.a_lo = a_lo; g.b_hi = b_hi; g.b_lo = b_lo;
+    g.a_hi = base; g.a_lo = base + t.a_plane_bytes;
+    g.b_hi = base + 2 * t.a_plane_bytes; g.b_lo = base + 2 * t.a_plane_bytes + t.b_plane_bytes;
     g.C = static_cast<float2*>(s.C);
     g.cb = t.cb; g.cm = t.cm; g.cn = t.cn;
     g.M = t.M; g.N = t.N; g.mtiles = t.mtiles; g.ntiles = t.ntiles; g.kchunks = t.kchunks; g.batch = t.batch;
@@ -517,8 +548,9 @@ cudaError_t tc_run_step(const TcStep& t, const StepArgs& s, int* exps, void* scr
     g.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((nmma >> 3) << 17) | ((uint32_t)(kTcTileM >> 4) << 24);
     g.exp_c = s.expC;
     g.exps = exps;
-    const size_t smem = 2 * (2 * kATileBytes + 2 * (size_t)g.b_tile_bytes) + 1024;
+    const size_t smem = kStages * (2 * kATileBytes + 2 * (size_t)g.b_tile_bytes) + 128;
     const int64_t ctas = t.batch * t.mtiles * t.ntiles;
+    cudaError_t e;
     if (t.tf32) {
         if ((e = set_smem_attr<true>()) != cudaSuccess) return e;
         tc_gemm_kernel<true><<<(unsigned)ctas, kThreadsGemm, smem, st>>>(g);

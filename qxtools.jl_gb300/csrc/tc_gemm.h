@@ -7,7 +7,9 @@
 //   D[m, (p,n)]            = (Re C, Im C)[m, n]                  (FP32 in tensor memory)
 // Each operand is split into hi + lo planes (3xBF16: bf16 round-to-nearest of x and of x-hi;
 // 3xTF32 the same with tf32), scaled by 2^-(max exponent) so nothing underflows, and the three
-// products hi*hi + hi*lo + lo*hi accumulate in FP32 (the lo*lo term is dropped).
+// products hi*hi + hi*lo + lo*hi accumulate in FP32 (the lo*lo term is dropped): hi*hi in one
+// tensor-memory accumulator and the two small correction products in a second one, added in the
+// epilogue, so the corrections are not lost against the large running sum.
 #pragma once
 
 #include <cstddef>
@@ -18,7 +20,7 @@
 namespace qxg {
 
 constexpr int kTcTileM = 128;       // MMA M (rows of X per CTA)
-constexpr int kTcChunkBytes = 128;  // bytes of one operand row per K chunk (8 core-matrix columns)
+constexpr int kTcChunkBytes = 64;   // bytes of one operand row per K chunk (4 core-matrix columns)
 
 struct TcStep {
     bool x_is_a = true;             // the larger operand (M side) is the step's A
@@ -39,9 +41,11 @@ struct TcStep {
 // Decide whether a step goes to the tensor cores; fills `tc` when it does.
 bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits, bool tf32, TcStep* tc);
 
-// Run a planned tensor-core step (scratch: at least tc.scratch_bytes of device memory).
-cudaError_t tc_run_step(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
+// Run a planned tensor-core step (scratch: at least tc.scratch_bytes of device memory):
+// tc_run_pack (both operands) then tc_run_gemm.
+cudaError_t tc_run_pack(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
                         int sm_count);
+cudaError_t tc_run_gemm(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st);
 
 // Device error word set by a tensor-core kernel whose bounded wait gave up (0 = none).
 cudaError_t tc_read_error(int* host_code, cudaStream_t st);

@@ -60,7 +60,8 @@ class qxg_step_profile(ct.Structure):
                 ("flops", ct.c_double), ("bytes", ct.c_double)]
 
 
-KERNEL_KINDS = {0: "contract_fp64", 1: "contract_fp32", 2: "contract_tc", 3: "view", 4: "output", 5: "reduce"}
+KERNEL_KINDS = {0: "contract_fp64", 1: "contract_fp32", 2: "contract_tc", 3: "view", 4: "output", 5: "reduce",
+                6: "tc_pack"}
 
 _lib = None
 

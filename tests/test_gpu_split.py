@@ -70,3 +70,16 @@ def test_split_executor_on_random_circuit(q, gpu_lib, oracle, precision):
     err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
     tol = 1e-5 if precision != "split_bf16" else 1e-4
     assert err <= tol, err
+
+
+@pytest.mark.parametrize("precision", ["split_tf32", "split_bf16"])
+def test_tensor_core_error_at_large_k(q, gpu_lib, precision):
+    """K = 2^9 complex terms (2^10 real terms per accumulator): the error stays at the level of FP32
+    accumulation itself (~sqrt(2^10) * 2^-24) because the correction products accumulate apart
+    from the main products -- 3xTF32 within 5e-6 of the largest element, 3xBF16 within 5e-5."""
+    prog, ref = single_ncon_programme(q, 7, 9, 4, seed=9)
+    with q.Executor(prog, precision=precision) as ex:
+        got = ex.amplitudes([""])[0]
+    err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    print(f"{precision} K=512 error {err:.3e}")
+    assert err <= (5e-6 if precision == "split_tf32" else 5e-5), err
