@@ -190,6 +190,29 @@ int qxg_ncon(int32_t precision,
              const void* B, int32_t nb, const int32_t* b_labels, const int64_t* b_dims,
              void* stream);
 
+/* Bytes of the library's static device scratch used by qxg_ncon_tc_static (64 MiB). */
+#define QXG_TC_STATIC_SCRATCH_BYTES (64ll << 20)
+
+/* One pairwise contraction on the tensor cores (3xBF16 or 3xTF32 split products, FP32
+ * accumulation) that allocates no device memory.  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc -- code running while a CUDA graph is being captured, hosts
+ * whose allocator is owned by another runtime, or allocation-free real-time loops.  The packed
+ * hi/lo operand planes live in one file-scope device array of QXG_TC_STATIC_SCRATCH_BYTES that
+ * every GPU loading the library holds until the process exits; a shape whose planes do not fit
+ * is rejected with QXG_ERR_UNSUPPORTED and a message, and so is a shape the tensor cores do not
+ * serve (fewer than 128 free rows on the larger operand, a summed extent below 8, or a smaller
+ * operand with fewer than 4 free columns).  Arguments are those of qxg_ncon with precision
+ * QXG_PREC_SPLIT_BF16 or QXG_PREC_SPLIT_TF32 (float2 storage).  The first call on a device looks
+ * up the array's device address (make that first call before any stream capture).  Every call on
+ * a device shares that device's array, which keeps the last call's contents: calls that can
+ * overlap on one GPU (issued on different streams or from different threads) race, so the caller
+ * must order them. */
+int qxg_ncon_tc_static(int32_t precision,
+                       void* C, int32_t nc, const int32_t* c_labels,
+                       const void* A, int32_t na, const int32_t* a_labels, const int64_t* a_dims,
+                       const void* B, int32_t nb, const int32_t* b_labels, const int64_t* b_dims,
+                       void* stream);
+
 /* Thread-local description of the last error ("" when none). */
 const char* qxg_last_error(void);
 

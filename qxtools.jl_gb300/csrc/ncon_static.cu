@@ -1,0 +1,105 @@
+// qxg_ncon_tc_static: the tensor-core pairwise contraction without any device allocation.
+//
+// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is being captured,
+// hosts whose device allocator belongs to another runtime, allocation-free real-time loops.  For
+// them this entry point keeps its scratch -- the packed hi/lo operand planes and three exponent
+// slots -- in one file-scope device array of QXG_TC_STATIC_SCRATCH_BYTES.  Host code may not use
+// the array's name as a device address; the address is looked up once per device with
+// cudaGetSymbolAddress (on the first call made with that device current).  Shapes whose planes
+// do not fit are rejected.  All calls on a device share the array; it keeps the last call's
+// contents, and calls that overlap on one GPU race.
+#include <mutex>
+#include <string>
+
+#include "../../include/qxgpu.h"
+#include "qxgpu_internal.h"
+#include "tc_gemm.h"
+
+namespace qxg {
+int ncon_fail(int code, const char* msg);
+int ncon_build_args(StepArgs* s, int32_t nc, const int32_t* lc, int32_t na, const int32_t* la,
+                    const int64_t* ad, int32_t nb, const int32_t* lb, const int64_t* bd);
+}  // namespace qxg
+
+namespace {
+
+constexpr size_t kStaticBytes = (size_t)QXG_TC_STATIC_SCRATCH_BYTES;
+constexpr size_t kExpBytes = 256;   // exponent slots (A, B, C) at the start of the array
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+std::mutex g_mu;
+void* g_addr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device (looked up once per device).
+int static_scratch(int dev, void** out) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p) {
+            std::string m = std::string("qxg_ncon_tc_static: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
+            return qxg::ncon_fail(QXG_ERR_CUDA, m.c_str());
+        }
+        g_addr[dev] = p;
+    }
+    *out = g_addr[dev];
+    return 0;
+}
+
+int bits_of(const int64_t* dims, int32_t n) {
+    int b = 0;
+    for (int i = 0; i < n; i++) {
+        int x = 0;
+        while ((int64_t(1) << x) < dims[i]) x++;
+        b += x;
+    }
+    return b;
+}
+
+}  // namespace
+
+extern "C" int qxg_ncon_tc_static(int32_t precision, void* C, int32_t nc, const int32_t* c_labels, const void* A,
+                                  int32_t na, const int32_t* a_labels, const int64_t* a_dims, const void* B,
+                                  int32_t nb, const int32_t* b_labels, const int64_t* b_dims, void* stream) {
+    using namespace qxg;
+    if (precision != QXG_PREC_SPLIT_BF16 && precision != QXG_PREC_SPLIT_TF32)
+        return ncon_fail(QXG_ERR_INVALID, "qxg_ncon_tc_static: precision must be QXG_PREC_SPLIT_BF16 or _TF32");
+    if (!C || !A || !B || nc < 0 || na < 0 || nb < 0 || (nc && !c_labels) || (na && (!a_labels || !a_dims)) ||
+        (nb && (!b_labels || !b_dims)))
+        return ncon_fail(QXG_ERR_INVALID, "qxg_ncon_tc_static: bad arguments");
+    StepArgs s;
+    if (int r = ncon_build_args(&s, nc, c_labels, na, a_labels, a_dims, nb, b_labels, b_dims)) return r;
+    s.A = A; s.B = B; s.C = C;
+    s.expA = 0; s.expB = 1; s.expC = 2;
+    int cbits = 0;
+    while ((int64_t(1) << cbits) < s.nC) cbits++;
+    TcStep t;
+    if (!tc_plan_step(s, (size_t)bits_of(a_dims, na), (size_t)bits_of(b_dims, nb), (size_t)cbits,
+                      precision == QXG_PREC_SPLIT_TF32, &t))
+        return ncon_fail(QXG_ERR_UNSUPPORTED,
+                         "qxg_ncon_tc_static: shape not served by the tensor cores (needs >= 128 free rows on the "
+                         "larger operand, a summed extent >= 8 and >= 4 free columns on the smaller)");
+    if (t.scratch_bytes > kStaticBytes - kExpBytes) {
+        std::string m = "qxg_ncon_tc_static: the packed operands need " + std::to_string(t.scratch_bytes) +
+                        " bytes, more than the static scratch of " + std::to_string(kStaticBytes - kExpBytes) + " bytes";
+        return ncon_fail(QXG_ERR_UNSUPPORTED, m.c_str());
+    }
+    int dev = 0, sms = 148;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return ncon_fail(QXG_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return ncon_fail(QXG_ERR_UNSUPPORTED, "qxg_ncon_tc_static: device ordinal too large");
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void* base = nullptr;
+    if (int r = static_scratch(dev, &base)) return r;
+    int* exps = static_cast<int*>(base);
+    void* planes = static_cast<unsigned char*>(base) + kExpBytes;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // exponent slots start at zero: operands enter unscaled and the result is stored as is
+    e = cudaMemsetAsync(exps, 0, kExpBytes, st);
+    if (e == cudaSuccess) e = tc_run_pack(t, s, exps, planes, st, sms);
+    if (e == cudaSuccess) e = tc_run_gemm(t, s, exps, planes, st);
+    if (e != cudaSuccess) return ncon_fail(QXG_ERR_CUDA, cudaGetErrorString(e));
+    return QXG_OK;
+}
