@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--compare-fp64", action="store_true", help="also time the FP64 path and report the error")
+    ap.add_argument("--no-graphs", action="store_true", help="launch every kernel eagerly (no CUDA graphs)")
+    ap.add_argument("--gradient", action="store_true",
+                    help="time the reverse-mode gradient against the forward pass (parametrised 5x5 circuit)")
     return ap.parse_args()
 
 
@@ -230,7 +233,7 @@ def workload_config(info, args, ex_info):
            "amplitudes_per_bitstring": info["amplitudes_per_bitstring"], "slices": info["num_slices"],
            "plan_steps": info["plan_steps"], "max_intermediate_log2": info["max_log2"],
            "flops_per_bitstring": info["flops_per_bitstring"], "seed": info["seed"],
-           "precision": args.precision,
+           "precision": args.precision, "cuda_graphs": not args.no_graphs,
            "l2": "intermediates larger than L2 (no flush needed)"}
     if ex_info:
         cfg.update({"bitstring_batch": ex_info["bitstring_batch"], "slice_batch": ex_info["slice_batch"],
@@ -263,7 +266,7 @@ def run_ours(args):
         all_bits = (all_bits * math.ceil(nb / len(all_bits)))[:nb]
     out_size = info["amplitudes_per_bitstring"]
     amps_per_step = nb * out_size
-    ex = q.Executor(prog, precision=args.precision, device=local)
+    ex = q.Executor(prog, precision=args.precision, device=local, use_graphs=not args.no_graphs)
     stream = torch.cuda.ExternalStream(ex.stream, device=dev)
     d_bits = torch.tensor(list("".join(all_bits).encode()), dtype=torch.uint8, device=dev)
     d_out = torch.zeros(2 * nb * out_size, dtype=torch.float64, device=dev)
@@ -383,10 +386,55 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_gradient(args):
+    """Forward vs reverse-mode gradient on the parametrised 5x5, 12-layer circuit (840 angles,
+    256 bitstrings, L = sum |amplitude|^2): seconds per evaluation through the host API, the
+    ratio, and the angle gradient's error against the FP64 gradient on the first 8 bitstrings."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as entry
+    q = entry.load()
+    torch.cuda.set_device(0)
+    circ = q.create_parametrised_circuit(5, 5, 12, seed=args.seed)
+    bits = list(q.amplitudes_uniform(25, args.seed, 256))
+    f = q.gradients.ParametrisedCircuitLoss(circ, seed=args.seed, time=2, precision=args.precision)
+    for _ in range(max(1, args.warmup)):
+        f.executor.amplitudes(bits)
+        f.loss_and_grad(bits)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        f.executor.amplitudes(bits)
+    fwd = (time.perf_counter() - t0) / args.steps
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L, g, _ = f.loss_and_grad(bits)
+    grad = (time.perf_counter() - t0) / args.steps
+    sub = bits[:8]
+    ref = q.gradients.ParametrisedCircuitLoss(circ, seed=args.seed, time=2, precision="fp64")
+    _, g64, _ = ref.loss_and_grad(sub)
+    _, gs, _ = f.loss_and_grad(sub)
+    ref.close()
+    info = f.executor.info()
+    f.close()
+    line = {"metric": "gradient seconds / forward seconds (reverse-mode adjoint)", "value": grad / fwd,
+            "unit": "ratio", "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic (seeded angles, bitstrings)",
+            "config": {"workload": "param_5x5_l12", "params": circ.num_params, "bitstrings": len(bits),
+                       "precision": args.precision, "plan_steps": info["num_steps"],
+                       "flops_per_amplitude": info["flops_per_amplitude"]},
+            "forward_s": fwd, "gradient_s": grad, "amplitudes_per_s_forward": len(bits) / fwd,
+            "loss": L, "max_abs_err_vs_fp64_8bits": float(np.max(np.abs(gs - g64))),
+            "max_rel_err_vs_fp64_8bits": float(np.max(np.abs(gs - g64)) / np.max(np.abs(g64)))}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.gradient:
+        run_gradient(args)
     else:
         run_ours(args)
 

@@ -134,6 +134,23 @@ int qxg_amplitudes(qxg_program* prog, const char* bitstrings, int32_t nbitstring
 int qxg_amplitudes_device(qxg_program* prog, const char* d_bitstrings, int32_t nbitstrings,
                           int64_t slice_begin, int64_t slice_end, double* d_out_re_im);
 
+/* Gradient of a real loss L(amplitudes) with respect to every leaf tensor, by reverse-mode
+ * (adjoint) contraction through the same programme: for each `ncon` C = A.B the adjoints are
+ * A_bar = ncon(C_bar, conj B) and B_bar = ncon(conj A, C_bar) (X_bar = dL/d conj X).  No
+ * counterpart in the reference (its executor is forward only); this is the differentiable form
+ * of `single_amplitude` / QXTns.contract_tn!.
+ *   amp_bar: nbitstrings * output_size interleaved complex values dL/d conj(amplitude); NULL
+ *            means L = sum |amplitude|^2 (then the slice range must fit one slice batch).
+ *   out_re_im: the amplitudes (as qxg_amplitudes), or NULL.
+ *   leaf_grads: dL/d conj(leaf) for every `load` command in programme order, each its data's
+ *            elements in column-major order (interleaved complex doubles).
+ * Each (slice batch, bitstring batch) pass recomputes the forward sub-trees it needs and runs its
+ * backward steps; gradients are summed over passes in FP64.  Every command's result must be read
+ * by at most one command (true of programmes built by build_compute_graph). */
+int qxg_gradient(qxg_program* prog, const char* bitstrings, int32_t nbitstrings,
+                 int64_t slice_begin, int64_t slice_end, const double* amp_bar,
+                 double* out_re_im, double* leaf_grads);
+
 /* Wait for work enqueued on the programme's stream. */
 int qxg_program_synchronize(qxg_program* prog);
 

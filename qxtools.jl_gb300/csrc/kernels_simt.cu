@@ -69,6 +69,7 @@ contract_kernel(const StepArgs a, int* exps) {
             exps[2 * a.expC] = exps[2 * a.expA] + exps[2 * a.expB] + mA + mB;
     }
     int emax = kExpUnset;
+    const R sa = a.conjA ? R(-1) : R(1), sb = a.conjB ? R(-1) : R(1);   // conjugation signs
     const int64_t ntiles = a.nC >> tb;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t tbase = t << tb;
@@ -83,10 +84,11 @@ contract_kernel(const StepArgs a, int* exps) {
                 for (int k = 0; k < KT; k++) {
                     const T x = A[ah + tA[k]];
                     const T y = B[bh + tB[k]];
+                    const R xi = sa * x.y, yi = sb * y.y;
                     re = fma(x.x, y.x, re);
-                    re = fma(-x.y, y.y, re);
-                    im = fma(x.x, y.y, im);
-                    im = fma(x.y, y.x, im);
+                    re = fma(-xi, yi, re);
+                    im = fma(x.x, yi, im);
+                    im = fma(xi, y.x, im);
                 }
             }
             if (SCALED) {
@@ -191,6 +193,113 @@ __global__ void reduce_kernel(const ReduceArgs a, const int* exps) {
     }
 }
 
+template <typename T>
+__global__ void seed_kernel(const SeedArgs a, int* exps) {
+    using R = typename Real<T>::type;
+    T* __restrict__ D = static_cast<T*>(a.dst);
+    const T* __restrict__ Rt = static_cast<const T*>(a.root);
+    const PassParams p = *a.params;
+    if (exps && blockIdx.x == 0 && threadIdx.x == 0) exps[2 * a.exp_dst] = 0;
+    const double scale = (exps && !a.amp_bar) ? pow2d(exps[2 * a.exp_root]) : 1.0;
+    const int64_t total = a.out_size * a.nbeta;
+    int emax = kExpUnset;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total; idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = idx % a.out_size;
+        const int beta = (int)(idx / a.out_size);
+        if (beta >= p.bits_valid) continue;
+        int64_t off = pdep(beta, a.beta_map);
+        int64_t rem = e;
+        for (int ax = 0; ax < a.naxes; ax++) {
+            const int64_t d = rem % a.axis_dim[ax];
+            rem /= a.axis_dim[ax];
+            for (int j = 0; j < a.axis_nbits[ax]; j++)
+                if ((d >> j) & 1) off += int64_t(1) << a.axis_bitpos[ax][j];
+        }
+        const int ns = a.nsigma > 1 ? min(a.nsigma, p.slices_valid) : 1;
+        double vr, vi;
+        if (a.amp_bar) {
+            const double* s = a.amp_bar + 2 * ((int64_t)(p.bit_base + beta) * a.out_size + e);
+            vr = s[0]; vi = s[1];
+        } else {          // L = sum |a|^2: dL/d conj(a) = a, the root summed over the slice batch
+            vr = 0.0; vi = 0.0;
+            for (int s = 0; s < ns; s++) {
+                const T v = Rt[off + pdep(s, a.sigma_map)];
+                vr += (double)v.x;
+                vi += (double)v.y;
+            }
+            vr *= scale; vi *= scale;
+        }
+        T v;
+        v.x = (R)vr; v.y = (R)vi;
+        for (int s = 0; s < ns; s++) D[off + pdep(s, a.sigma_map)] = v;
+        if (exps) {
+            const float mx = fmaxf(fabsf((float)vr), fabsf((float)vi));
+            if (mx > 0.f) emax = max(emax, exp_of(mx));
+        }
+    }
+    if (exps) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.exp_dst + 1], emax);
+    }
+}
+
+template <typename T>
+__global__ void view_adjoint_kernel(const ViewAdjArgs a, int* exps) {
+    using R = typename Real<T>::type;
+    const T* __restrict__ V = static_cast<const T*>(a.vbar);
+    T* __restrict__ S = static_cast<T*>(a.sbar);
+    const PassParams p = *a.params;
+    if (exps && blockIdx.x == 0 && threadIdx.x == 0) exps[2 * a.exp_s] = exps[2 * a.exp_v];
+    const int ns = min(a.nsigma, p.slices_valid);
+    int emax = kExpUnset;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < a.ns; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t base = pdep(j, a.s2v);
+        R re = R(0), im = R(0);
+        for (int s = 0; s < ns; s++) {
+            const int64_t sid = p.slice_base + s;
+            if (sid >= p.num_slices) break;
+            bool hit = true;
+            for (int f = 0; f < a.nfix; f++) {
+                const int64_t want = (j >> a.fix_shift[f]) & ((int64_t(1) << a.fix_bits[f]) - 1);
+                if ((sid / a.var_stride[f]) % a.var_dim[f] != want) { hit = false; break; }
+            }
+            if (hit) {
+                const T v = V[base + ((int64_t)s << a.sigma_shift)];
+                re += v.x;
+                im += v.y;
+            }
+        }
+        T o;
+        o.x = re; o.y = im;
+        S[j] = o;
+        if (exps) {
+            const float mx = fmaxf(fabsf((float)re), fabsf((float)im));
+            if (mx > 0.f) emax = max(emax, exp_of(mx));
+        }
+    }
+    if (exps) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.exp_s + 1], emax);
+    }
+}
+
+template <typename T>
+__global__ void leaf_grad_kernel(const LeafGradArgs a, const int* exps) {
+    const T* __restrict__ S = static_cast<const T*>(a.sbar);
+    const double scale = exps ? pow2d(exps[2 * a.exp_s]) : 1.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t rem = i, off = 0, st = 1;
+        for (int d = 0; d < a.rank; d++) {
+            off += (rem % a.dims[d]) * st;
+            rem /= a.dims[d];
+            st *= a.pdims[d];
+        }
+        const T v = S[off];
+        a.grad[2 * i] += (double)v.x * scale;
+        a.grad[2 * i + 1] += (double)v.y * scale;
+    }
+}
+
 __global__ void reset_exps_kernel(int* exps, int begin, int end) {
     for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
         exps[2 * i] = 0;
@@ -238,6 +347,27 @@ cudaError_t launch_reduce(const ReduceArgs& a, bool fp64, const int* exps, cudaS
     const int g = grid_for(a.out_size * a.nbeta, 256, 4096);
     if (fp64) reduce_kernel<double2><<<g, 256, 0, s>>>(a, exps);
     else reduce_kernel<float2><<<g, 256, 0, s>>>(a, exps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seed(const SeedArgs& a, bool fp64, int* exps, cudaStream_t s) {
+    const int g = grid_for(a.out_size * a.nbeta, 256, 4096);
+    if (fp64) seed_kernel<double2><<<g, 256, 0, s>>>(a, exps);
+    else seed_kernel<float2><<<g, 256, 0, s>>>(a, exps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_view_adjoint(const ViewAdjArgs& a, bool fp64, int* exps, cudaStream_t s) {
+    const int g = grid_for(a.ns, 256, 1024);
+    if (fp64) view_adjoint_kernel<double2><<<g, 256, 0, s>>>(a, exps);
+    else view_adjoint_kernel<float2><<<g, 256, 0, s>>>(a, exps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_grad(const LeafGradArgs& a, bool fp64, const int* exps, cudaStream_t s) {
+    const int g = grid_for(a.n, 256, 1024);
+    if (fp64) leaf_grad_kernel<double2><<<g, 256, 0, s>>>(a, exps);
+    else leaf_grad_kernel<float2><<<g, 256, 0, s>>>(a, exps);
     return cudaGetLastError();
 }
 

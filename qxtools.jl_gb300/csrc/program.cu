@@ -74,12 +74,21 @@ struct Tensor {
     int slot = -1;                      // exponent slot
 };
 
+// Backward (adjoint) step kinds of gradient plans.
+constexpr int kBwdNcon = 1, kBwdView = 2, kBwdLeaf = 3;
+
 struct Step {                           // an executable item of a pass
-    int kind;                           // QXG_OP_NCON / VIEW / OUTPUT
-    int tensor;                         // tensor produced
+    int kind;                           // QXG_OP_NCON / VIEW / OUTPUT (forward)
+    int tensor;                         // tensor produced (table index; adjoints offset by ntensors)
+    int bkind = 0;                      // 0 forward, else kBwd*
+    int instr = -1;                     // instruction whose command this step serves
+    int reads[2] = {-1, -1};            // table indices read (arena lifetimes)
+    int64_t goff = 0;                   // leaf-gradient steps: offset in the gradient vector
     StepArgs sargs;
     ViewArgs vargs;
     OutputArgs oargs;
+    ViewAdjArgs vaargs;
+    LeafGradArgs largs;
     bool use_tc = false;                // tensor-core path (split modes)
     TcStep tc;                          // tensor-core step description
     double flops = 0, bytes = 0;
@@ -94,6 +103,13 @@ struct Plan {
     size_t tc_scratch_bytes = 0;
     ReduceArgs red;
     double flops_pass[3] = {0, 0, 0}, bytes_pass[3] = {0, 0, 0};
+    // gradient plans: adjoint tensors live at table index ntensors + t
+    bool grad = false;
+    int ntensors = 0;
+    std::vector<Step> bsteps;           // backward steps in execution order
+    SeedArgs seed;
+    int slot_all_end = 0;               // slots [slot_begin[0], slot_all_end) reset every pass
+    double flops_bwd = 0;
 };
 
 }  // namespace
@@ -117,8 +133,13 @@ struct qxg_program {
     std::vector<int64_t> var_dim;
     int64_t nslices = 1;
     double flops_per_amp = 0;
-    // batch plan and device buffers
+    // batch plans (forward; gradient) and device buffers
     std::unique_ptr<Plan> plan;
+    std::unique_ptr<Plan> gplan;
+    double* d_grad = nullptr;           // FP64 leaf gradients
+    size_t d_grad_cap = 0;
+    double* d_ampbar = nullptr;         // adjoint seed per bitstring
+    size_t d_ampbar_cap = 0;
     void* d_arena = nullptr;
     size_t arena_cap = 0;
     void* d_scratch = nullptr;
@@ -140,6 +161,10 @@ struct qxg_program {
     struct Rec { int instr, kind; size_t ev; double flops, bytes; };
     std::vector<Rec> recs;
     int64_t launches = 0;
+    // CUDA graphs: one executable graph per pass group, captured on the group's second run
+    cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+    int group_runs[3] = {0, 0, 0};
+    int64_t launches_per_group[3] = {0, 0, 0};
 };
 
 namespace {
@@ -333,7 +358,225 @@ int position_of(const Tensor& t, PBit b) {
     return -1;
 }
 
-int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out) {
+// Bit maps of R = sum X (x) Y (one `ncon`): lr / lx / ly give the label of each logical axis of
+// R, X and Y.  A bit of R comes from X and/or Y by label (axis bits) or by identity (slice and
+// bitstring batch bits); every operand bit that R lacks is summed.  Summed bits are ordered by
+// the larger operand's physical order, then the smaller operand's own.  X and Y become the
+// StepArgs' A and B.
+int build_maps(const Tensor& R, const int32_t* lr, int nr, const Tensor& X, const int32_t* lx, int nx,
+               const Tensor& Y, const int32_t* ly, int ny, StepArgs* s, int* err) {
+    auto axis_in = [](const int32_t* ls, int n, int32_t L) {
+        for (int q = 0; q < n; q++) if (ls[q] == L) return q;
+        return -1;
+    };
+    auto trans = [&](PBit b, const int32_t* ls, const int32_t* lt, int nt) -> PBit {
+        if (b.axis < 0) return b;
+        const int ax = axis_in(lt, nt, ls[b.axis]);
+        if (ax < 0) return PBit{-3, 0};
+        return PBit{(int16_t)ax, b.j};
+    };
+    std::vector<std::pair<int, int>> cX, cY, kX, kY;
+    for (int p = 0; p < (int)R.layout.size(); p++) {
+        const PBit b = R.layout[p];
+        const int px = position_of(X, trans(b, lr, lx, nx));
+        const int py = position_of(Y, trans(b, lr, ly, ny));
+        if (px < 0 && py < 0) return fail(QXG_ERR_INVALID, "internal: result bit without source");
+        if (px >= 0) cX.push_back({p, px});
+        if (py >= 0) cY.push_back({p, py});
+    }
+    const bool x_big = X.layout.size() >= Y.layout.size();
+    const Tensor& Z = x_big ? X : Y;
+    const Tensor& W = x_big ? Y : X;
+    const int32_t* lz = x_big ? lx : ly;
+    const int32_t* lw = x_big ? ly : lx;
+    const int nz = x_big ? nx : ny, nw = x_big ? ny : nx;
+    std::vector<std::pair<int, int>>& kZ = x_big ? kX : kY;
+    std::vector<std::pair<int, int>>& kW = x_big ? kY : kX;
+    int kbit = 0;
+    for (int p = 0; p < (int)Z.layout.size(); p++) {
+        const PBit b = Z.layout[p];
+        if (position_of(R, trans(b, lz, lr, nr)) >= 0) continue;
+        kZ.push_back({kbit, p});
+        const int q = position_of(W, trans(b, lz, lw, nw));
+        if (q >= 0) kW.push_back({kbit, q});
+        kbit++;
+    }
+    for (int p = 0; p < (int)W.layout.size(); p++) {
+        const PBit b = W.layout[p];
+        if (position_of(R, trans(b, lw, lr, nr)) >= 0) continue;
+        if (position_of(Z, trans(b, lw, lz, nz)) >= 0) continue;
+        kW.push_back({kbit, p});
+        kbit++;
+    }
+    s->nC = int64_t(1) << R.layout.size();
+    s->nk = kbit;
+    s->cA = make_map(cX, err);
+    s->cB = make_map(cY, err);
+    s->kA = make_map(kX, err);
+    s->kB = make_map(kY, err);
+    return 0;
+}
+
+// Complex offsets of each `load` command's gradient in the caller's gradient vector (every load,
+// in instruction order, -1 for other commands) and the vector's length.
+std::vector<int64_t> leaf_offsets(const qxg_program* P, int64_t* total) {
+    std::vector<int64_t> off(P->ins.size(), -1);
+    int64_t o = 0;
+    for (size_t i = 0; i < P->ins.size(); i++) {
+        if (P->ins[i].op != QXG_OP_LOAD) continue;
+        off[i] = o;
+        int64_t n = 1;
+        for (int64_t d : P->ddims[P->ins[i].a]) n *= d;
+        o += n;
+    }
+    *total = o;
+    return off;
+}
+
+// Backward steps of a gradient plan (reverse-mode, Wirtinger derivatives of a real loss L with
+// X_bar = dL/d conj X).  For a forward step C = ncon(A, B): A_bar = ncon(C_bar, conj B) and
+// B_bar = ncon(conj A, C_bar) -- the same einsum machinery with one operand conjugated; a view's
+// adjoint gathers the slice batch back into its leaf; every leaf's adjoint is added to its FP64
+// gradient.  Adjoint tensors are table entries ntensors + t with the forward tensor's layout.
+int build_backward(qxg_program* P, Plan& pl, int* err) {
+    auto& T = pl.T;
+    const int n = (int)T.size();
+    std::vector<int> nreads(n, 0);
+    for (int g = 0; g < 3; g++)
+        for (auto& st : pl.steps[g])
+            for (int r : st.reads) if (r >= 0) nreads[r]++;
+    for (int t = 0; t < n; t++)
+        if (nreads[t] > 1) return fail(QXG_ERR_UNSUPPORTED, "gradient: tensor " + std::to_string(t) + " is read twice");
+    std::vector<char> needs(n, 0);
+    for (const qxg_instr& I : P->ins) {
+        if (I.op == QXG_OP_SAVE) continue;
+        const int t = I.dst;
+        if (I.op == QXG_OP_LOAD) needs[t] = 1;
+        else if (I.op == QXG_OP_VIEW) needs[t] = T[T[t].view_root].kind == QXG_OP_LOAD;
+        else if (I.op == QXG_OP_NCON) needs[t] = needs[I.a] || needs[I.b];
+    }
+    if (!needs[P->root]) return fail(QXG_ERR_INVALID, "gradient: the saved tensor depends on no leaf");
+    T.resize(2 * n);
+    int slot = pl.slot_all_end;
+    for (int t = 0; t < n; t++) {
+        if (!needs[t] || !(T[t].needed || t == P->root)) continue;
+        T[n + t] = T[t];
+        T[n + t].kind = 0;              // an adjoint: always an arena buffer, never leaf data
+        T[n + t].arena_off = -1;
+        T[n + t].slot = slot++;
+    }
+    pl.slot_all_end = slot;
+    const double es = P->fp64 ? 16.0 : 8.0;
+    auto sz = [&](int t) { return (double)(int64_t(1) << T[t].layout.size()); };
+    auto add_ncon = [&](int res, const int32_t* lr, int nr, int x, const int32_t* lx, int nx, int cx, int y,
+                        const int32_t* ly, int ny, int cy, int instr) -> int {
+        Step st;
+        memset(&st.sargs, 0, sizeof(st.sargs));
+        st.kind = QXG_OP_NCON;
+        st.bkind = kBwdNcon;
+        st.tensor = res;
+        st.instr = instr;
+        st.reads[0] = x;
+        st.reads[1] = y;
+        if (int r = build_maps(T[res], lr, nr, T[x], lx, nx, T[y], ly, ny, &st.sargs, err)) return r;
+        st.sargs.conjA = cx;
+        st.sargs.conjB = cy;
+        st.sargs.expA = T[x].slot;
+        st.sargs.expB = T[y].slot;
+        st.sargs.expC = T[res].slot;
+        st.flops = 8.0 * (double)st.sargs.nC * (double)(int64_t(1) << st.sargs.nk);
+        st.bytes = es * (sz(x) + sz(y) + sz(res));
+        if (!P->fp64 && P->opts.precision != QXG_PREC_FP32)
+            st.use_tc = tc_plan_step(st.sargs, T[x].layout.size(), T[y].layout.size(), T[res].layout.size(),
+                                     P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc);
+        pl.flops_bwd += st.flops;
+        pl.bsteps.push_back(st);
+        return 0;
+    };
+    for (int g = 2; g >= 0; g--) {
+        for (auto it = pl.steps[g].rbegin(); it != pl.steps[g].rend(); ++it) {
+            const Step& f = *it;
+            const int t = f.tensor;
+            if (!needs[t]) continue;
+            const qxg_instr& I = P->ins[f.instr];
+            if (f.kind == QXG_OP_NCON) {
+                const int32_t* lc = &P->labels[I.label_off];
+                const int32_t* la = lc + I.nc;
+                const int32_t* lb = la + I.na;
+                if (needs[I.a])
+                    if (int r = add_ncon(n + I.a, la, I.na, n + t, lc, I.nc, 0, I.b, lb, I.nb, 1, f.instr)) return r;
+                if (needs[I.b])
+                    if (int r = add_ncon(n + I.b, lb, I.nb, I.a, la, I.na, 1, n + t, lc, I.nc, 0, f.instr)) return r;
+            } else if (f.kind == QXG_OP_VIEW) {
+                const int r = T[t].view_root;
+                const Tensor& S = T[r];
+                const Tensor& V = T[t];
+                Step st;
+                memset(&st.vaargs, 0, sizeof(st.vaargs));
+                st.kind = QXG_OP_VIEW;
+                st.bkind = kBwdView;
+                st.tensor = n + r;
+                st.instr = f.instr;
+                st.reads[0] = n + t;
+                ViewAdjArgs& va = st.vaargs;
+                std::vector<std::pair<int, int>> pairs;
+                for (int p = 0; p < (int)S.layout.size(); p++) {
+                    const PBit b = S.layout[p];
+                    bool fixed = false;
+                    for (auto& fx : V.fixes) if (fx.first == b.axis) fixed = true;
+                    if (fixed) continue;
+                    const int q = position_of(V, b);
+                    if (q < 0) return fail(QXG_ERR_INVALID, "internal: view adjoint layout");
+                    pairs.push_back({p, q});
+                }
+                va.s2v = make_map(pairs, err);
+                va.sigma_shift = f.vargs.sigma_shift;
+                va.nsigma = pl.sc;
+                va.ns = int64_t(1) << S.layout.size();
+                va.nfix = f.vargs.nfix;
+                for (int k = 0; k < va.nfix; k++) {
+                    va.fix_shift[k] = f.vargs.fix_shift[k];
+                    va.fix_bits[k] = bits_of(S, V.fixes[k].first);
+                    va.var_stride[k] = f.vargs.var_stride[k];
+                    va.var_dim[k] = f.vargs.var_dim[k];
+                }
+                va.exp_v = T[n + t].slot;
+                va.exp_s = T[n + r].slot;
+                pl.bsteps.push_back(st);
+            }
+        }
+    }
+    // leaf gradients in instruction order (the gradient pointer is bound with the buffers)
+    int64_t total = 0;
+    const std::vector<int64_t> goff = leaf_offsets(P, &total);
+    for (size_t ii = 0; ii < P->ins.size(); ii++) {
+        const qxg_instr& I = P->ins[ii];
+        if (I.op != QXG_OP_LOAD || T[n + I.dst].slot < 0 || !needs[I.dst] || !T[I.dst].needed) continue;
+        const Tensor& L = T[I.dst];
+        if ((int)L.dims.size() > 16) return fail(QXG_ERR_UNSUPPORTED, "gradient: leaf of rank above 16");
+        Step st;
+        memset(&st.largs, 0, sizeof(st.largs));
+        st.kind = QXG_OP_LOAD;
+        st.bkind = kBwdLeaf;
+        st.tensor = -1;
+        st.instr = (int)ii;
+        st.reads[0] = n + I.dst;
+        LeafGradArgs& la = st.largs;
+        la.rank = (int)L.dims.size();
+        la.n = 1;
+        for (int d = 0; d < la.rank; d++) {
+            la.dims[d] = (int32_t)L.dims[d];
+            la.pdims[d] = (int32_t)L.pdims[d];
+            la.n *= L.dims[d];
+        }
+        st.goff = goff[ii];             // complex offset in the gradient vector, bound at launch
+        la.exp_s = T[n + I.dst].slot;
+        pl.bsteps.push_back(st);
+    }
+    return 0;
+}
+
+int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool grad = false) {
     auto plan = std::make_unique<Plan>();
     plan->bc = bc;
     plan->sc = sc;
@@ -425,6 +668,9 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out) {
         memset(&st.oargs, 0, sizeof(st.oargs));
         st.kind = I.op;
         st.tensor = I.dst;
+        st.instr = ii;
+        if (I.op == QXG_OP_NCON) { st.reads[0] = I.a; st.reads[1] = I.b; }
+        if (I.op == QXG_OP_VIEW) st.reads[0] = t.view_root;
         if (I.op == QXG_OP_OUTPUT) {
             st.oargs.qubit = t.qubit;
             st.oargs.nqubits = P->nqubits;
@@ -464,63 +710,8 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out) {
             const int32_t* lc = &P->labels[I.label_off];
             const int32_t* la = lc + I.nc;
             const int32_t* lb = la + I.na;
-            auto axis_in = [](const int32_t* ls, int n, int32_t L) {
-                for (int q = 0; q < n; q++) if (ls[q] == L) return q;
-                return -1;
-            };
-            std::vector<std::pair<int, int>> cA, cB, kA, kB;
-            for (int p = 0; p < (int)t.layout.size(); p++) {
-                const PBit b = t.layout[p];
-                PBit ba = b, bb = b;
-                if (b.axis >= 0) {
-                    ba.axis = (int16_t)axis_in(la, I.na, lc[b.axis]);
-                    bb.axis = (int16_t)axis_in(lb, I.nb, lc[b.axis]);
-                }
-                const int pa = (b.axis >= 0 && ba.axis < 0) ? -1 : position_of(A, ba);
-                const int pb = (b.axis >= 0 && bb.axis < 0) ? -1 : position_of(B, bb);
-                if (pa < 0 && pb < 0) return fail(QXG_ERR_INVALID, "internal: result bit without source");
-                if (pa >= 0) cA.push_back({p, pa});
-                if (pb >= 0) cB.push_back({p, pb});
-            }
-            // summed bits: operand bits whose label is not in the result, in the bigger
-            // operand's physical order
-            const bool a_big = A.layout.size() >= B.layout.size();
-            const Tensor& X = a_big ? A : B;
-            const Tensor& Y = a_big ? B : A;
-            const int32_t* lx = a_big ? la : lb;
-            const int32_t* ly = a_big ? lb : la;
-            const int nyl = a_big ? I.nb : I.na;
-            int kbit = 0;
-            std::vector<std::pair<int, int>>& kX = a_big ? kA : kB;
-            std::vector<std::pair<int, int>>& kY = a_big ? kB : kA;
-            for (int p = 0; p < (int)X.layout.size(); p++) {
-                const PBit b = X.layout[p];
-                if (b.axis < 0) continue;
-                if (axis_in(lc, I.nc, lx[b.axis]) >= 0) continue;
-                kX.push_back({kbit, p});
-                const int yax = axis_in(ly, nyl, lx[b.axis]);
-                if (yax >= 0) {
-                    const int q = position_of(Y, PBit{(int16_t)yax, b.j});
-                    if (q >= 0) kY.push_back({kbit, q});
-                }
-                kbit++;
-            }
-            for (int p = 0; p < (int)Y.layout.size(); p++) {   // labels summed but only in Y
-                const PBit b = Y.layout[p];
-                if (b.axis < 0) continue;
-                if (axis_in(lc, I.nc, ly[b.axis]) >= 0) continue;
-                const int32_t* lxx = lx;
-                const int nxl = a_big ? I.na : I.nb;
-                if (axis_in(lxx, nxl, ly[b.axis]) >= 0) continue;
-                kY.push_back({kbit, p});
-                kbit++;
-            }
-            st.sargs.nC = int64_t(1) << t.layout.size();
-            st.sargs.nk = kbit;
-            st.sargs.cA = make_map(cA, &err);
-            st.sargs.cB = make_map(cB, &err);
-            st.sargs.kA = make_map(kA, &err);
-            st.sargs.kB = make_map(kB, &err);
+            if (int r = build_maps(t, lc, I.nc, A, la, I.na, B, lb, I.nb, &st.sargs, &err)) return r;
+            const int kbit = st.sargs.nk;
             st.sargs.expA = A.slot;
             st.sargs.expB = B.slot;
             st.sargs.expC = t.slot;
@@ -537,17 +728,31 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out) {
         plan->bytes_pass[t.group] += st.bytes;
         plan->steps[t.group].push_back(st);
     }
-    // arena: lifetimes over the execution sequence group0, group1, group2
+    plan->ntensors = ntensors;
+    plan->slot_all_end = slot;
+    if (grad) {
+        if (int r = build_backward(P, *plan, &err)) return r;
+        if (err) return fail(QXG_ERR_UNSUPPORTED, "adjoint bit map needs more than the supported number of runs");
+    }
+    // arena: lifetimes over the execution sequence group0, group1, group2 (then, in gradient
+    // plans, the backward steps; every group runs in every gradient pass)
+    const int ntab = (int)T.size();
     struct Item { int tensor; int def; int last; int64_t bytes; };
-    std::vector<int> pos_of(ntensors, -1);
+    std::vector<int> pos_of(ntab, -1);
     int pos = 0;
     for (int g = 0; g < 3; g++)
         for (auto& st : plan->steps[g]) pos_of[st.tensor] = pos++;
+    const int fwd_end = pos;
+    for (auto& st : plan->bsteps)
+        if (st.bkind != kBwdLeaf) { if (pos_of[st.tensor] < 0) pos_of[st.tensor] = pos; pos++; }
+        else pos++;
+    if (grad) pos_of[ntensors + P->root] = fwd_end;          // the seed, written before the backward
     const int end_pos = pos + 1;
-    std::vector<int> last(ntensors, -1);
+    std::vector<int> last(ntab, -1);
     auto use = [&](int t, int at) {
-        if (pos_of[t] < 0) return;
+        if (t < 0 || pos_of[t] < 0) return;
         last[t] = std::max(last[t], at);
+        if (grad) return;
         // used by a later group -> alive until the end (the later group repeats)
         const int gt = T[t].group;
         int gat = 0;
@@ -556,17 +761,13 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out) {
         if (gat > gt) last[t] = end_pos;
     };
     pos = 0;
-    for (int g = 0; g < 3; g++) {
-        for (auto& st : plan->steps[g]) {
-            const qxg_instr& I = P->ins[T[st.tensor].instr];
-            if (st.kind == QXG_OP_NCON) { use(I.a, pos); use(I.b, pos); }
-            if (st.kind == QXG_OP_VIEW) use(T[st.tensor].view_root, pos);
-            pos++;
-        }
-    }
-    if (pos_of[P->root] >= 0) last[P->root] = end_pos;
+    for (int g = 0; g < 3; g++)
+        for (auto& st : plan->steps[g]) { use(st.reads[0], pos); use(st.reads[1], pos); pos++; }
+    if (grad) use(P->root, fwd_end);
+    for (auto& st : plan->bsteps) { use(st.reads[0], pos); use(st.reads[1], pos); pos++; }
+    if (!grad && pos_of[P->root] >= 0) last[P->root] = end_pos;
     std::vector<Item> items;
-    for (int t = 0; t < ntensors; t++) {
+    for (int t = 0; t < ntab; t++) {
         if (pos_of[t] < 0) continue;
         const int64_t bytes = ((int64_t(1) << T[t].layout.size()) * (int64_t)P->esize + 255) & ~int64_t(255);
         items.push_back({t, pos_of[t], std::max(last[t], pos_of[t]), bytes});
@@ -599,6 +800,7 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out) {
     size_t scratch = 0;
     for (int g = 0; g < 3; g++)
         for (auto& st : plan->steps[g]) if (st.use_tc) scratch = std::max(scratch, st.tc.scratch_bytes);
+    for (auto& st : plan->bsteps) if (st.use_tc) scratch = std::max(scratch, st.tc.scratch_bytes);
     plan->tc_scratch_bytes = scratch;
     // reduction of the root
     {
@@ -631,13 +833,37 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out) {
         ra.broadcast = r.beta ? 0 : 1;
         ra.exp_root = r.slot;
         if (err) return fail(QXG_ERR_UNSUPPORTED, "root bit map too fragmented");
+        if (grad) {
+            SeedArgs& sd = plan->seed;
+            memset(&sd, 0, sizeof(sd));
+            sd.out_size = ra.out_size;
+            sd.nbeta = ra.nbeta;
+            sd.nsigma = ra.nsigma;
+            sd.beta_map = ra.beta_map;
+            sd.sigma_map = ra.sigma_map;
+            sd.naxes = ra.naxes;
+            for (int a = 0; a < ra.naxes; a++) {
+                sd.axis_dim[a] = ra.axis_dim[a];
+                sd.axis_nbits[a] = ra.axis_nbits[a];
+                for (int j = 0; j < 3; j++) sd.axis_bitpos[a][j] = ra.axis_bitpos[a][j];
+            }
+            sd.exp_root = ra.exp_root;
+            sd.exp_dst = T[ntensors + P->root].slot;
+        }
     }
+    plan->grad = grad;
     out = std::move(plan);
     return 0;
 }
 
-// choose batch sizes that fit the workspace limit
-int ensure_plan(qxg_program* P, int nbits_call) {
+void drop_graphs(qxg_program* P);
+
+// Choose batch sizes whose workspace fits the limit, (re)build the forward plan (grad = false)
+// or the gradient plan (grad = true), grow the shared device buffers and bind pointers.  Both
+// plans use the same arena and scratch: growing either drops the other plan (its bound pointers
+// are stale) and the captured graphs.
+int ensure_plan(qxg_program* P, int nbits_call, bool grad = false) {
+    std::unique_ptr<Plan>& slot = grad ? P->gplan : P->plan;
     const int64_t want_b = std::max<int64_t>(1, pow2ceil(nbits_call));
     const int64_t max_b = P->opts.max_bitstring_batch > 0 ? pow2ceil(P->opts.max_bitstring_batch) : 256;
     const int64_t max_s = P->opts.max_slice_batch > 0 ? pow2ceil(P->opts.max_slice_batch) : 1024;
@@ -646,7 +872,7 @@ int ensure_plan(qxg_program* P, int nbits_call) {
     bool has_out = false;
     for (auto& t : P->base) if (t.kind == QXG_OP_OUTPUT && t.needed) has_out = true;
     if (!has_out) bc = 1;
-    if (P->plan && P->plan->bc == bc && P->plan->sc == sc) return 0;
+    if (slot && slot->bc == bc && slot->sc == sc) return 0;
     size_t limit = (size_t)P->opts.workspace_limit;
     if (limit == 0) {
         size_t fr = 0, tot = 0;
@@ -655,9 +881,11 @@ int ensure_plan(qxg_program* P, int nbits_call) {
     }
     while (true) {
         std::unique_ptr<Plan> pl;
-        if (int r = build_plan(P, (int)bc, (int)sc, pl)) return r;
+        if (int r = build_plan(P, (int)bc, (int)sc, pl, grad)) return r;
         if (pl->arena_bytes + pl->tc_scratch_bytes <= limit) {
-            P->plan = std::move(pl);
+            if (P->stream) cudaStreamSynchronize(P->stream);
+            if (!grad) drop_graphs(P);
+            slot = std::move(pl);
             break;
         }
         if (sc == 1 && bc == 1)
@@ -665,20 +893,25 @@ int ensure_plan(qxg_program* P, int nbits_call) {
                                          " bytes for one slice and one bitstring exceeds the limit");
         if (sc >= bc && sc > 1) sc /= 2; else bc /= 2;
     }
-    Plan& pl = *P->plan;
+    Plan& pl = *slot;
+    std::unique_ptr<Plan>& other = grad ? P->plan : P->gplan;
     if (pl.arena_bytes > P->arena_cap) {
         if (P->d_arena) cudaFree(P->d_arena);
         P->d_arena = nullptr; P->arena_cap = 0;
         QXG_CUDA(cudaMalloc(&P->d_arena, std::max<size_t>(pl.arena_bytes, 256)));
         P->arena_cap = pl.arena_bytes;
+        other.reset();
+        drop_graphs(P);
     }
     if (pl.tc_scratch_bytes > P->scratch_cap) {
         if (P->d_scratch) cudaFree(P->d_scratch);
         P->d_scratch = nullptr; P->scratch_cap = 0;
         QXG_CUDA(cudaMalloc(&P->d_scratch, pl.tc_scratch_bytes));
         P->scratch_cap = pl.tc_scratch_bytes;
+        other.reset();
+        drop_graphs(P);
     }
-    const int ns = pl.slot_end[2];
+    const int ns = std::max(pl.slot_end[2], pl.slot_all_end);
     if (ns > P->nslots) {
         if (P->d_exps) cudaFree(P->d_exps);
         P->d_exps = nullptr;
@@ -706,6 +939,21 @@ int ensure_plan(qxg_program* P, int nbits_call) {
         }
     pl.red.root = ptr(P->root);
     pl.red.params = P->d_params;
+    if (grad) {
+        const int n = pl.ntensors;
+        for (auto& st : pl.bsteps) {
+            if (st.bkind == kBwdNcon) {
+                st.sargs.A = ptr(st.reads[0]); st.sargs.B = ptr(st.reads[1]); st.sargs.C = ptr(st.tensor);
+            } else if (st.bkind == kBwdView) {
+                st.vaargs.vbar = ptr(st.reads[0]); st.vaargs.sbar = ptr(st.tensor); st.vaargs.params = P->d_params;
+            } else {
+                st.largs.sbar = ptr(st.reads[0]);
+            }
+        }
+        pl.seed.dst = ptr(n + P->root);
+        pl.seed.root = ptr(P->root);
+        pl.seed.params = P->d_params;
+    }
     // initial exponent slots: LOAD tensors carry their data's maximum exponent
     P->h_exps_init.assign(2 * std::max(ns, 1), 0);
     for (auto& t : pl.T) {
@@ -738,8 +986,55 @@ int prof_end(qxg_program* P, size_t ev, int instr, int kind, double flops, doubl
     return 0;
 }
 
+int run_group_eager(qxg_program* P, int g, Plan* plp = nullptr);
+
+void drop_graphs(qxg_program* P) {
+    for (int g = 0; g < 3; g++) {
+        if (P->gexec[g]) cudaGraphExecDestroy(P->gexec[g]);
+        P->gexec[g] = nullptr;
+        P->group_runs[g] = 0;
+    }
+}
+
+// One pass group: eager launches, or (with use_graphs, outside profiling) a CUDA graph captured
+// from the group's second run and replayed afterwards.  Kernel arguments are fixed per plan (the
+// arena, leaves, bitstring buffer and pass-parameter block do not move), so the graph stays valid
+// until the plan changes.
 int run_group(qxg_program* P, int g) {
     Plan& pl = *P->plan;
+    if (pl.steps[g].empty()) return 0;
+    const bool graphs = P->opts.use_graphs && !P->profiling;
+    if (!graphs || P->group_runs[g] < 1) {
+        const int64_t before = P->launches;
+        if (int r = run_group_eager(P, g)) return r;
+        P->launches_per_group[g] = P->launches - before;
+        P->group_runs[g]++;
+        return 0;
+    }
+    if (!P->gexec[g]) {
+        cudaGraph_t graph = nullptr;
+        QXG_CUDA(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
+        const int64_t before = P->launches;
+        const int r = run_group_eager(P, g);
+        const cudaError_t e = cudaStreamEndCapture(P->stream, &graph);
+        P->launches = before;
+        if (r) { if (graph) cudaGraphDestroy(graph); return r; }
+        if (e != cudaSuccess) return fail(QXG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        const cudaError_t ei = cudaGraphInstantiate(&P->gexec[g], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            P->gexec[g] = nullptr;
+            return fail(QXG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+        }
+    }
+    QXG_CUDA(cudaGraphLaunch(P->gexec[g], P->stream));
+    P->launches += P->launches_per_group[g];
+    P->group_runs[g]++;
+    return 0;
+}
+
+int run_group_eager(qxg_program* P, int g, Plan* plp) {
+    Plan& pl = plp ? *plp : *P->plan;
     int* exps = P->fp64 ? nullptr : P->d_exps;
     if (exps) {
         QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[g], pl.slot_end[g], P->stream));
@@ -779,8 +1074,8 @@ int run_group(qxg_program* P, int g) {
     return 0;
 }
 
-int run_reduce(qxg_program* P) {
-    Plan& pl = *P->plan;
+int run_reduce(qxg_program* P, Plan* plp = nullptr) {
+    Plan& pl = plp ? *plp : *P->plan;
     size_t ev = 0;
     if (int r = prof_begin(P, &ev)) return r;
     QXG_CUDA(launch_reduce(pl.red, P->fp64, P->fp64 ? nullptr : P->d_exps, P->stream));
@@ -842,17 +1137,115 @@ int run_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d_out)
     return 0;
 }
 
+// Gradient passes.  Every (slice batch, bitstring batch) runs all forward groups (the shared
+// sub-trees are recomputed per pass instead of stored across passes), optionally adds its slice
+// sum to the amplitudes, seeds the root's adjoint and runs the backward steps; leaf adjoints are
+// added into the FP64 gradient, so the gradient is the sum over passes (the loss's seed is linear).
+int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d_out, const double* d_ampbar,
+                    double* d_grad) {
+    Plan& pl = *P->gplan;
+    const Tensor& root = pl.T[P->root];
+    const int64_t nsl = s1 - s0;
+    const int64_t nsc = (nsl + pl.sc - 1) / pl.sc;
+    const int64_t nbc = root.beta ? (nbits + pl.bc - 1) / pl.bc : 1;
+    if (!d_ampbar && nsc > 1)
+        return fail(QXG_ERR_UNSUPPORTED, "gradient of sum |amplitude|^2 needs the slice range in one pass "
+                                         "(raise max_slice_batch or pass amp_bar)");
+    if (!root.beta && nbits != 1)
+        return fail(QXG_ERR_UNSUPPORTED, "gradient: the saved tensor does not depend on the bitstring; pass one");
+    const size_t npass = (size_t)(nsc * nbc);
+    QXG_CUDA(cudaStreamSynchronize(P->stream));
+    if (npass > P->h_params_cap) {
+        if (P->h_params) cudaFreeHost(P->h_params);
+        P->h_params = nullptr;
+        QXG_CUDA(cudaMallocHost(&P->h_params, sizeof(PassParams) * npass));
+        P->h_params_cap = npass;
+    }
+    QXG_CUDA(cudaMemcpyAsync(P->d_exps, P->h_exps_init.data(), sizeof(int) * P->h_exps_init.size(),
+                             cudaMemcpyHostToDevice, P->stream));
+    int* exps = P->fp64 ? nullptr : P->d_exps;
+    pl.red.out = d_out;
+    pl.seed.amp_bar = d_ampbar;
+    const int n = pl.ntensors;
+    const size_t seed_bytes = (size_t)P->esize << pl.T[n + P->root].layout.size();
+    size_t k = 0;
+    PassParams pp;
+    memset(&pp, 0, sizeof(pp));
+    pp.num_slices = P->nslices;
+    for (int64_t c = 0; c < nsc; c++) {
+        for (int64_t b = 0; b < nbc; b++) {
+            pp.slice_base = s0 + c * pl.sc;
+            pp.slices_valid = (int32_t)std::min<int64_t>(pl.sc, s1 - pp.slice_base);
+            pp.bit_base = (int32_t)(b * pl.bc);
+            pp.bits_valid = root.beta ? (int32_t)std::min<int64_t>(pl.bc, nbits - pp.bit_base) : nbits;
+            if (int r = set_params(P, k++, pp)) return r;
+            if (exps) {
+                QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[0], pl.slot_all_end, P->stream));
+                P->launches++;
+            }
+            for (int g = 0; g < 3; g++)
+                if (int r = run_group_eager(P, g, &pl)) return r;
+            if (d_out)
+                if (int r = run_reduce(P, &pl)) return r;
+            QXG_CUDA(cudaMemsetAsync(pl.seed.dst, 0, seed_bytes, P->stream));
+            QXG_CUDA(launch_seed(pl.seed, P->fp64, exps, P->stream));
+            P->launches++;
+            for (auto& st : pl.bsteps) {
+                size_t ev = 0;
+                if (int r = prof_begin(P, &ev)) return r;
+                int kind = QXG_KERNEL_REDUCE;
+                if (st.bkind == kBwdNcon) {
+                    if (st.use_tc) {
+                        QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
+                        QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream));
+                        kind = QXG_KERNEL_CONTRACT_TC;
+                    } else {
+                        QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count));
+                        kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
+                    }
+                } else if (st.bkind == kBwdView) {
+                    QXG_CUDA(launch_view_adjoint(st.vaargs, P->fp64, exps, P->stream));
+                    kind = QXG_KERNEL_VIEW;
+                } else {
+                    LeafGradArgs la = st.largs;
+                    la.grad = d_grad + 2 * st.goff;
+                    QXG_CUDA(launch_leaf_grad(la, P->fp64, exps, P->stream));
+                }
+                if (int r = prof_end(P, ev, st.instr, kind, st.flops, st.bytes)) return r;
+            }
+        }
+    }
+    return 0;
+}
+
+// Grow the programme's bitstring buffer; captured graphs hold its address, so a new buffer
+// drops them.
+int ensure_bits(qxg_program* P, size_t nb) {
+    if (nb <= P->d_bits_cap) return 0;
+    QXG_CUDA(cudaStreamSynchronize(P->stream));
+    drop_graphs(P);
+    if (P->d_bits) cudaFree(P->d_bits);
+    P->d_bits = nullptr;
+    P->d_bits_cap = 0;
+    QXG_CUDA(cudaMalloc(&P->d_bits, nb));
+    P->d_bits_cap = nb;
+    return 0;
+}
+
 // A tensor-core kernel whose bounded wait gave up leaves a code in a device word; read and clear.
-int check_tc(qxg_program* P) {
-    if (!P->plan) return 0;
+int check_tc_plan(qxg_program* P, const Plan* pl) {
+    if (!pl) return 0;
     bool any = false;
-    for (int g = 0; g < 3; g++) for (auto& st : P->plan->steps[g]) any = any || st.use_tc;
+    for (int g = 0; g < 3; g++) for (auto& st : pl->steps[g]) any = any || st.use_tc;
+    for (auto& st : pl->bsteps) any = any || st.use_tc;
     if (!any) return 0;
     int code = 0;
     QXG_CUDA(tc_read_error(&code, P->stream));
     if (code) return fail(QXG_ERR_TIMEOUT, "a tensor-core kernel gave up waiting (code " + std::to_string(code) + ")");
     return 0;
 }
+
+int check_tc(qxg_program* P) { return check_tc_plan(P, P->plan.get()); }
 
 int check_ready(qxg_program* P) {
     for (size_t i = 0; i < P->data_set.size(); i++) {
@@ -983,12 +1376,13 @@ int qxg_amplitudes_device(qxg_program* P, const char* d_bitstrings, int32_t nbit
     QXG_CUDA(cudaSetDevice(P->device));
     if (int r = ensure_plan(P, nbits)) return r;
     const int64_t osz = P->plan->red.out_size;
+    // bitstrings are copied into the programme's own buffer, whose address captured passes keep
+    if (int r = ensure_bits(P, (size_t)nbits * (size_t)std::max(P->nqubits, 1))) return r;
+    if (P->nqubits > 0)
+        QXG_CUDA(cudaMemcpyAsync(P->d_bits, d_bitstrings, (size_t)nbits * P->nqubits, cudaMemcpyDeviceToDevice,
+                                 P->stream));
     QXG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(double) * 2 * (size_t)osz * nbits, P->stream));
-    char* saved = P->d_bits;
-    P->d_bits = const_cast<char*>(d_bitstrings);
-    const int r = run_passes(P, nbits, s0, s1, d_out);
-    P->d_bits = saved;
-    return r;
+    return run_passes(P, nbits, s0, s1, d_out);
 }
 
 int qxg_amplitudes(qxg_program* P, const char* bits, int32_t nbits, int64_t s0, int64_t s1, double* out) {
@@ -999,13 +1393,7 @@ int qxg_amplitudes(qxg_program* P, const char* bits, int32_t nbits, int64_t s0, 
     if (int r = check_ready(P)) return r;
     QXG_CUDA(cudaSetDevice(P->device));
     if (int r = ensure_plan(P, nbits)) return r;
-    const size_t nb = (size_t)nbits * (size_t)std::max(P->nqubits, 1);
-    if (nb > P->d_bits_cap) {
-        if (P->d_bits) cudaFree(P->d_bits);
-        P->d_bits = nullptr; P->d_bits_cap = 0;
-        QXG_CUDA(cudaMalloc(&P->d_bits, nb));
-        P->d_bits_cap = nb;
-    }
+    if (int r = ensure_bits(P, (size_t)nbits * (size_t)std::max(P->nqubits, 1))) return r;
     const int64_t osz = P->plan->red.out_size;
     const size_t ob = sizeof(double) * 2 * (size_t)osz * nbits;
     if (ob > P->d_out_cap) {
@@ -1021,6 +1409,54 @@ int qxg_amplitudes(qxg_program* P, const char* bits, int32_t nbits, int64_t s0, 
     QXG_CUDA(cudaMemcpyAsync(out, P->d_out, ob, cudaMemcpyDeviceToHost, P->stream));
     QXG_CUDA(cudaStreamSynchronize(P->stream));
     if (int r = check_tc(P)) return r;
+    return QXG_OK;
+}
+
+int qxg_gradient(qxg_program* P, const char* bits, int32_t nbits, int64_t s0, int64_t s1, const double* amp_bar,
+                 double* out, double* leaf_grads) {
+    g_last_error.clear();
+    if (!P || nbits <= 0 || (P->nqubits > 0 && !bits) || !leaf_grads) return fail(QXG_ERR_INVALID, "bad arguments");
+    if (s0 < 0 || s1 > P->nslices || s0 >= s1) return fail(QXG_ERR_INVALID, "slice range out of bounds");
+    if (int r = validate_bits(bits, (int64_t)nbits * P->nqubits)) return r;
+    if (int r = check_ready(P)) return r;
+    QXG_CUDA(cudaSetDevice(P->device));
+    if (int r = ensure_plan(P, nbits, true)) return r;
+    if (int r = ensure_bits(P, (size_t)nbits * (size_t)std::max(P->nqubits, 1))) return r;
+    if (P->nqubits > 0)
+        QXG_CUDA(cudaMemcpyAsync(P->d_bits, bits, (size_t)nbits * P->nqubits, cudaMemcpyHostToDevice, P->stream));
+    const int64_t osz = P->gplan->red.out_size;
+    const size_t ob = sizeof(double) * 2 * (size_t)osz * nbits;
+    auto grow = [&](double** buf, size_t* cap, size_t bytes) -> int {
+        if (bytes <= *cap) return 0;
+        QXG_CUDA(cudaStreamSynchronize(P->stream));
+        if (*buf) cudaFree(*buf);
+        *buf = nullptr;
+        *cap = 0;
+        QXG_CUDA(cudaMalloc((void**)buf, bytes));
+        *cap = bytes;
+        return 0;
+    };
+    if (out) {
+        if (int r = grow(&P->d_out, &P->d_out_cap, ob)) return r;
+        QXG_CUDA(cudaMemsetAsync(P->d_out, 0, ob, P->stream));
+    }
+    int64_t gtotal = 0;
+    leaf_offsets(P, &gtotal);
+    const size_t gb = sizeof(double) * 2 * (size_t)std::max<int64_t>(gtotal, 1);
+    if (int r = grow(&P->d_grad, &P->d_grad_cap, gb)) return r;
+    QXG_CUDA(cudaMemsetAsync(P->d_grad, 0, gb, P->stream));
+    if (amp_bar) {
+        if (int r = grow(&P->d_ampbar, &P->d_ampbar_cap, ob)) return r;
+        QXG_CUDA(cudaMemcpyAsync(P->d_ampbar, amp_bar, ob, cudaMemcpyHostToDevice, P->stream));
+    }
+    if (int r = run_grad_passes(P, nbits, s0, s1, out ? P->d_out : nullptr, amp_bar ? P->d_ampbar : nullptr,
+                                P->d_grad))
+        return r;
+    if (out) QXG_CUDA(cudaMemcpyAsync(out, P->d_out, ob, cudaMemcpyDeviceToHost, P->stream));
+    QXG_CUDA(cudaMemcpyAsync(leaf_grads, P->d_grad, sizeof(double) * 2 * (size_t)gtotal, cudaMemcpyDeviceToHost,
+                             P->stream));
+    QXG_CUDA(cudaStreamSynchronize(P->stream));
+    if (int r = check_tc_plan(P, P->gplan.get())) return r;
     return QXG_OK;
 }
 
@@ -1108,6 +1544,7 @@ void qxg_program_destroy(qxg_program* P) {
     cudaSetDevice(P->device);
     if (P->stream) cudaStreamSynchronize(P->stream);
     for (cudaEvent_t e : P->ev_pool) cudaEventDestroy(e);
+    drop_graphs(P);
     for (void* p : P->d_data) if (p) cudaFree(p);
     if (P->d_arena) cudaFree(P->d_arena);
     if (P->d_scratch) cudaFree(P->d_scratch);
@@ -1116,6 +1553,8 @@ void qxg_program_destroy(qxg_program* P) {
     if (P->h_params) cudaFreeHost(P->h_params);
     if (P->d_bits) cudaFree(P->d_bits);
     if (P->d_out) cudaFree(P->d_out);
+    if (P->d_grad) cudaFree(P->d_grad);
+    if (P->d_ampbar) cudaFree(P->d_ampbar);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
 }

@@ -52,8 +52,52 @@ struct StepArgs {
     int64_t nC;                // elements of C (a power of two)
     int32_t nk;                // summed bits
     int32_t expA, expB, expC;  // exponent slots (split / fp32 modes), -1 when unused
+    int32_t conjA, conjB;      // 1: use the complex conjugate of the operand (adjoint steps)
     BitMap cA, cB;             // C index -> A / B offset
     BitMap kA, kB;             // K index -> A / B offset
+};
+
+// Adjoint seed: dL/d conj(root) for a batch, from a caller's per-bitstring seed (amp_bar) or,
+// for L = sum |amplitude|^2, from the amplitudes themselves (sum of the root over the slice
+// batch).  The destination is zeroed first; only real (beta, sigma) entries are written.
+struct SeedArgs {
+    void* dst;                 // adjoint of the root (root layout)
+    const void* root;          // forward root (norm2 mode)
+    const double* amp_bar;     // (nbitstrings x out_size) complex; NULL -> norm2 mode
+    int64_t out_size;
+    int32_t nbeta, nsigma;
+    BitMap beta_map, sigma_map;
+    int32_t naxes;
+    int32_t axis_dim[48];
+    int32_t axis_nbits[48];
+    int32_t axis_bitpos[48][3];
+    int32_t exp_root, exp_dst;
+    const struct PassParams* params;
+};
+
+// Adjoint of a (chain of) view(s) of a leaf: S_bar[j] = sum over the slice batch of V_bar at the
+// slice's value of every fixed axis (zero where no slice of the batch selects j).
+struct ViewAdjArgs {
+    const void* vbar;          // adjoint of the view (view layout, sigma bits on top)
+    void* sbar;                // adjoint of the leaf (leaf layout)
+    int64_t ns;                // leaf elements
+    int32_t sigma_shift, nsigma;
+    BitMap s2v;                // leaf index (non-fixed bits) -> view offset
+    int32_t nfix;
+    int32_t fix_shift[8], fix_bits[8];
+    int64_t var_stride[8], var_dim[8];
+    int32_t exp_v, exp_s;
+    const struct PassParams* params;
+};
+
+// Accumulate a leaf's adjoint (padded column-major, scaled by 2^e) into its FP64 gradient.
+struct LeafGradArgs {
+    const void* sbar;
+    double* grad;              // logical (unpadded) column-major complex doubles
+    int64_t n;                 // logical elements
+    int32_t rank;
+    int32_t dims[16], pdims[16];
+    int32_t exp_s;
 };
 
 // Materialise a view of a leaf/output tensor for a batch of slices.
@@ -105,6 +149,9 @@ cudaError_t launch_view(const ViewArgs& a, bool fp64, int* exps, cudaStream_t s)
 cudaError_t launch_output(const OutputArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_reduce(const ReduceArgs& a, bool fp64, const int* exps, cudaStream_t s);
 cudaError_t launch_reset_exps(int* exps, int begin, int end, cudaStream_t s);
+cudaError_t launch_seed(const SeedArgs& a, bool fp64, int* exps, cudaStream_t s);
+cudaError_t launch_view_adjoint(const ViewAdjArgs& a, bool fp64, int* exps, cudaStream_t s);
+cudaError_t launch_leaf_grad(const LeafGradArgs& a, bool fp64, const int* exps, cudaStream_t s);
 
 // Exponent slots: exps[2*i] = e (true value = stored * 2^e), exps[2*i+1] = m (max stored
 // exponent, atomically raised by the producer).

@@ -50,6 +50,7 @@ struct PackArgs {
     int slot_src;           // exponent slot of the operand
     int doubled;            // 1: complex-doubled Y form
     int exp_c, slot_other;  // Y pack writes exps[C] = e_x + e_y + m_x + m_y
+    int conj;               // 1: pack the complex conjugate (adjoint steps)
 };
 
 struct GemmArgs {
@@ -127,6 +128,7 @@ __global__ void pack_kernel(const PackArgs p, int* exps) {
     for (int64_t k = threadIdx.x; k < kt; k += blockDim.x) ktab[k] = pdep(k, p.mk);
     __syncthreads();
     const float s = pow2f(-read_m(exps, p.slot_src));
+    const float si = p.conj ? -s : s;
     if (p.doubled && blockIdx.x == 0 && threadIdx.x == 0) {
         const int mo = read_m(exps, p.slot_other), my = read_m(exps, p.slot_src);
         exps[2 * p.exp_c] = exps[2 * p.slot_other] + exps[2 * p.slot_src] + mo + my;
@@ -150,7 +152,7 @@ __global__ void pack_kernel(const PackArgs p, int* exps) {
             if (row_ok && k < p.K) {
                 const float2 v = X[base + (k < kKTable ? ktab[k] : pdep(k, p.mk))];
                 re[j] = v.x * s;
-                im[j] = v.y * s;
+                im[j] = v.y * si;
             }
         }
         E hr[NE], lr[NE], hm[NE], lm[NE];
@@ -511,7 +513,9 @@ cudaError_t tc_run_pack(const TcStep& t, const StepArgs& s, int* exps, void* scr
     px.rows = t.M; px.rows_pad = t.mtiles * kTcTileM; px.K = t.K; px.batch = t.batch;
     px.kchunks = t.kchunks; px.row_tiles = t.mtiles; px.tile_rows = kTcTileM; px.ntile = 0;
     px.slot_src = slot_x; px.doubled = 0; px.exp_c = s.expC; px.slot_other = slot_y;
+    px.conj = t.x_is_a ? s.conjA : s.conjB;
     PackArgs py = px;
+    py.conj = t.x_is_a ? s.conjB : s.conjA;
     py.src = t.x_is_a ? s.B : s.A;
     py.hi = base + 2 * t.a_plane_bytes; py.lo = base + 2 * t.a_plane_bytes + t.b_plane_bytes;
     py.mb = t.yb; py.mr = t.yn; py.mk = t.yk;

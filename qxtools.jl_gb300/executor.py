@@ -96,6 +96,9 @@ def load_library(path=None):
     lib.qxg_ncon.argtypes = [ct.c_int32, P, ct.c_int32, ct.POINTER(ct.c_int32), P, ct.c_int32,
                              ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), P, ct.c_int32,
                              ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), P]
+    lib.qxg_gradient.argtypes = [P, ct.c_char_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_double),
+                                 ct.POINTER(ct.c_double), ct.POINTER(ct.c_double)]
+    lib.qxg_gradient.restype = ct.c_int
     lib.qxg_program_profile.argtypes = [P, ct.c_int32]
     lib.qxg_program_profile_read.argtypes = [P, ct.POINTER(qxg_step_profile), ct.c_int32, ct.POINTER(ct.c_int32),
                                              ct.POINTER(ct.c_int64)]
@@ -294,6 +297,42 @@ class Executor:
         _check(self.lib, self.lib.qxg_amplitudes(self._h, buf, n, s0, s1,
                                                  out.ctypes.data_as(ct.POINTER(ct.c_double))))
         return out.view(np.complex128).reshape(n, info["output_size"])
+
+    def leaf_slices(self) -> dict:
+        """instruction index of each `load` -> (offset, shape) of its gradient in the flat vector."""
+        out, o = {}, 0
+        for i, r in enumerate(self.programme.instrs):
+            if int(r[0]) == QXG_OP["load"]:
+                shape = tuple(self.programme.data[int(r[2])].shape)
+                out[i] = (o, shape)
+                o += int(np.prod(shape)) if shape else 1
+        self._gsize = o
+        return out
+
+    def gradient(self, bitstrings, amp_bar=None, slices=None):
+        """Reverse-mode gradient (qxg_gradient): returns (amplitudes (n, out_size), {instruction
+        index of each load: dL/d conj(leaf) as an array of the leaf's shape}).  amp_bar = dL/d
+        conj(amplitude) per bitstring, shape (n, out_size); None -> L = sum |amplitude|^2."""
+        if isinstance(bitstrings, str):
+            bitstrings = [bitstrings]
+        bitstrings = list(bitstrings)
+        n = len(bitstrings)
+        info = self.info()
+        s0, s1 = (0, info["num_slices"]) if slices is None else slices
+        lay = self.leaf_slices()
+        buf = _bitstring_bytes(bitstrings, self.programme.nqubits)
+        out = np.zeros(2 * n * info["output_size"], dtype=np.float64)
+        grads = np.zeros(2 * max(self._gsize, 1), dtype=np.float64)
+        ab = None
+        if amp_bar is not None:
+            ab = np.ascontiguousarray(np.asarray(amp_bar, dtype=np.complex128).reshape(n, info["output_size"]))
+            ab = ab.view(np.float64).reshape(-1)
+        D = ct.POINTER(ct.c_double)
+        _check(self.lib, self.lib.qxg_gradient(self._h, buf, n, s0, s1, ab.ctypes.data_as(D) if ab is not None else None,
+                                               out.ctypes.data_as(D), grads.ctypes.data_as(D)))
+        g = grads.view(np.complex128)
+        leaf = {i: g[o:o + (int(np.prod(s)) if s else 1)].reshape(s, order="F") for i, (o, s) in lay.items()}
+        return out.view(np.complex128).reshape(n, info["output_size"]), leaf
 
     def amplitudes_device(self, d_bitstrings_ptr: int, n: int, d_out_ptr: int, slices=None):
         """Enqueue on the programme's stream with device-resident inputs/outputs (no sync)."""

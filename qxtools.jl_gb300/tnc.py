@@ -99,9 +99,12 @@ class TensorNetwork:
         """Hyperedge labels (union-find roots) of the tensor, one per group."""
         return [self.root(g[0]) for g in self.groups(name)]
 
-    def reduced_data(self, name: str) -> np.ndarray:
-        """Tensor data with each tied group reduced to its diagonal (one axis per group)."""
+    def reduced_data(self, name: str, data=None) -> np.ndarray:
+        """Tensor data (or `data` of the same shape, e.g. a derivative of it) with each tied
+        group reduced to its diagonal (one axis per group)."""
         t = self.tensors[name]
+        if data is not None:
+            t = QXTensor(t.indices, data)
         grp = self.groups(name)
         pos = {ix: k for k, ix in enumerate(t.indices)}
         if all(len(g) == 1 for g in grp):

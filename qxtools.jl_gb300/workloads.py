@@ -20,7 +20,7 @@ from pathlib import Path
 import numpy as np
 
 from . import dsl as _dsl
-from .circuits import create_rqc_circuit
+from .circuits import create_parametrised_circuit, create_rqc_circuit
 from .compute_graph import build_compute_graph
 from .executor import Programme
 from .planning import contraction_scheme, hyper_network, plan_cost
@@ -34,6 +34,9 @@ WORKLOADS = {
     "rqc_6x6_d14_s4": dict(rows=6, cols=6, depth=14, nslice=4, open=0, nbits=256),
     "rqc_5x5_d12_open6": dict(rows=5, cols=5, depth=12, nslice=0, open=6, nbits=64),
     "rqc_3x4_d8_s3": dict(rows=3, cols=4, depth=8, nslice=3, open=0, nbits=64),
+    # parametrised: per layer Rx(t) Rz(t) on every qubit + fSim(t, p) on one coupler pattern;
+    # 840 angles; two-qubit gates kept whole so each gate is one differentiable leaf
+    "param_5x5_l12": dict(rows=5, cols=5, depth=12, nslice=0, open=0, nbits=256, parametrised=True),
 }
 
 _CACHE = Path(__file__).resolve().parent / "_build" / "workloads"
@@ -54,9 +57,12 @@ def build_workload(name: str, seed: int = 1, time: int = 2, cache: bool = True):
         info = json.loads(meta_p.read_text())
         prog = Programme.from_commands(cmds, _dsl.read_data(str(npz)), info["nqubits"])
         return prog, info["bitstrings"], info
-    circ = create_rqc_circuit(spec["rows"], spec["cols"], spec["depth"], seed=seed)
+    if spec.get("parametrised"):
+        circ = create_parametrised_circuit(spec["rows"], spec["cols"], spec["depth"], seed=seed)
+    else:
+        circ = create_rqc_circuit(spec["rows"], spec["cols"], spec["depth"], seed=seed)
     n = circ.num_qubits
-    tnc = convert_to_tnc(circ, decompose=True, no_output=True)
+    tnc = convert_to_tnc(circ, decompose=not spec.get("parametrised"), no_output=True)
     if spec["open"]:
         rng = np.random.Generator(np.random.PCG64(seed + 1000))
         open_q = sorted(int(x) + 1 for x in rng.choice(n, size=spec["open"], replace=False))

@@ -230,3 +230,28 @@ def test_ncon_entry_point(q, gpu_lib, precision):
         got = dC.cpu().numpy().reshape(ref.shape, order="F") if ref.ndim else dC.cpu().numpy()[0]
         tol = 1e-13 if precision == "fp64" else 2e-5
         assert np.max(np.abs(got - ref)) <= tol * max(1.0, np.max(np.abs(ref)))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split_tf32"])
+def test_graph_replay_matches_eager(q, gpu_lib, oracle, precision):
+    """Passes captured in CUDA graphs and replayed give the eager results, across repeated calls,
+    slice ranges, device-resident calls and a plan change (new batch size -> graphs rebuilt)."""
+    import torch
+    prog = rqc_programme(q, 3, 4, 8, seed=5, nslice=3)
+    bits = list(q.amplitudes_uniform(12, 2, 40))
+    ref = oracle.run_programme(prog, bits, nthreads=8)[:, 0]
+    tol = FP64_TOL if precision == "fp64" else 1e-5
+    with q.Executor(prog, precision=precision, use_graphs=True, max_bitstring_batch=16, max_slice_batch=2) as ex:
+        for _ in range(3):                                   # eager run, capture, replay
+            got = ex.amplitudes(bits)[:, 0]
+            assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) <= tol
+        part = ex.amplitudes(bits[:7], slices=(2, 6))[:, 0]   # smaller batch: new plan
+        refp = oracle.run_programme(prog, bits[:7], slices=(2, 6), nthreads=8)[:, 0]
+        assert np.max(np.abs(part - refp)) / np.max(np.abs(refp)) <= tol
+        raw = torch.tensor(list("".join(bits).encode()), dtype=torch.uint8, device="cuda")
+        out = torch.zeros(2 * len(bits), dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            ex.amplitudes_device(raw.data_ptr(), len(bits), out.data_ptr())
+            ex.synchronize()
+            dev = out.cpu().numpy().view(np.complex128)
+            assert np.max(np.abs(dev - ref)) / np.max(np.abs(ref)) <= tol
