@@ -361,6 +361,11 @@ def run_ours(args):
                 "peak_source": f"hbm_gbs of {peak_src}", "kernel": kernel_name, "kernel_share": dom["ms"] / total_ms}
     roof["kernels"] = {k: {"launches": v["launches"], "ms": round(v["ms"], 3), "share": v["ms"] / total_ms}
                        for k, v in sorted(by_kind.items(), key=lambda kv: -kv[1]["ms"])}
+    top = sorted(rows, key=lambda r: -r["ms"])[:10]
+    roof["top_steps"] = [{"instr": r["instr"], "kernel": r["kernel"], "ms_per_pass": round(r["ms"] / args.steps, 3),
+                          "gb_s": round(r["bytes"] / (r["ms"] * 1e-3) / 1e9, 1) if r["ms"] else None,
+                          "tflop_s": round(r["flops"] / (r["ms"] * 1e-3) / 1e12, 2) if r["ms"] else None}
+                         for r in top]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",

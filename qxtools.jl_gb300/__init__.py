@@ -21,6 +21,6 @@ from .simulation import (amplitudes_all, amplitudes_uniform, compile_programme, 
                          generate_parameter_file, generate_simulation_files, output_params_dict,
                          run_simulation, single_amplitude)
 from .tnc import TensorNetwork, TensorNetworkCircuit, basis_vector, convert_to_tnc
-from . import gradients, replicas, simulation, workloads
+from . import gradients, replicas, sampling, simulation, workloads
 
 __version__ = "0.1.0"

@@ -30,6 +30,7 @@ __device__ int g_tc_error = 0;
 namespace {
 
 constexpr int kThreadsGemm = 192;                        // warp 0 producer, 1 MMA, 2-5 epilogue
+constexpr int kThreadsFused = 320;                       // + warps 6-9 gather and split X rows
 constexpr int kStages = 3;
 constexpr int kCols16 = kTcChunkBytes / 16;              // 16-byte core-matrix columns per chunk (4)
 constexpr int kSbo = kCols16 * 128;                      // bytes between 8-row groups (512)
@@ -55,6 +56,10 @@ struct PackArgs {
 
 struct GemmArgs {
     const void *a_hi, *a_lo, *b_hi, *b_lo;
+    const float2* X;        // fused: the larger operand itself, gathered and split in the kernel
+    BitMap xb, xm, xk;      // fused: X offset of batch / m / k index
+    int64_t K;              // fused: complex extent of K
+    int x_slot, x_conj;     // fused: X's exponent slot, conjugation
     float2* C;
     BitMap cb, cm, cn;
     int64_t M, N, mtiles, ntiles, kchunks, batch;
@@ -260,8 +265,41 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Fused operand staging: one thread gathers row `row` of X's K chunk (2*NE complex values) through
+// the bit maps, scales, splits and stores it into the stage's hi/lo A tiles (real parts in
+// 16-byte columns 0-1, imaginary parts in 2-3).
 template <bool TF32>
-__global__ void __launch_bounds__(kThreadsGemm, 2) tc_gemm_kernel(const GemmArgs g) {
+__device__ __forceinline__ void fill_a_row(uint8_t* th, uint8_t* tl, int row, const float2* __restrict__ X,
+                                           int64_t base, bool row_ok, int64_t k0, int64_t K, const BitMap& xk,
+                                           float s, float si) {
+    using S = Split<TF32>;
+    using E = typename S::E;
+    constexpr int NE = 16 / sizeof(E);
+#pragma unroll
+    for (int g = 0; g < 2; g++) {
+        float re[NE], im[NE];
+#pragma unroll
+        for (int j = 0; j < NE; j++) {
+            const int64_t k = k0 + g * NE + j;
+            re[j] = 0.f; im[j] = 0.f;
+            if (row_ok && k < K) {
+                const float2 v = X[base + pdep(k, xk)];
+                re[j] = v.x * s;
+                im[j] = v.y * si;
+            }
+        }
+        E hr[NE], lr[NE], hm[NE], lm[NE];
+#pragma unroll
+        for (int j = 0; j < NE; j++) { S::go(re[j], hr[j], lr[j]); S::go(im[j], hm[j], lm[j]); }
+        st16(th + core_off(row, g), hr);
+        st16(tl + core_off(row, g), lr);
+        st16(th + core_off(row, 2 + g), hm);
+        st16(tl + core_off(row, 2 + g), lm);
+    }
+}
+
+template <bool TF32, bool FUSED>
+__global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreadsGemm, 2) tc_gemm_kernel(const GemmArgs g) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint64_t bars[2 * kStages + 1];   // full[kStages], empty[kStages], accum
     __shared__ int64_t noff[128];                // result offsets of this tile's columns
@@ -282,7 +320,9 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) tc_gemm_kernel(const GemmArgs
     const uint32_t ncols = (uint32_t)(4 * g.ntile) < 32u ? 32u : (uint32_t)(4 * g.ntile);
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 2 * kStages + 1; i++) mbar_init(&bars[i], 1);
+        // a full barrier completes on the bulk copies' bytes and, when fused, the four X warps
+        for (int i = 0; i < kStages; i++) mbar_init(&full[i], FUSED ? 5u : 1u);
+        for (int i = kStages; i < 2 * kStages + 1; i++) mbar_init(&bars[i], 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -292,7 +332,7 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) tc_gemm_kernel(const GemmArgs
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (warp >= 2) {
+    if (warp >= 2 && warp < 6) {
         for (int j = threadIdx.x - 64; j < g.ntile; j += 128) {
             const int64_t n = nt * g.ntile + j;
             noff[j] = n < g.N ? pdep(n, g.cn) : 0;
@@ -313,10 +353,12 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) tc_gemm_kernel(const GemmArgs
             if (!mbar_wait(&empty[s], (u & 1u) ^ 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 1); break; }
             if (*(volatile int*)&abort_flag) break;
             uint8_t* st = smem + s * stage_bytes;
-            mbar_expect_tx(&full[s], stage_bytes);
+            mbar_expect_tx(&full[s], FUSED ? 2u * g.b_tile_bytes : stage_bytes);
             const int64_t ao = (a_tile0 + c) * kATileBytes, bo = (b_tile0 + c) * (int64_t)g.b_tile_bytes;
-            bulk_copy(st, static_cast<const uint8_t*>(g.a_hi) + ao, kATileBytes, &full[s]);
-            bulk_copy(st + kATileBytes, static_cast<const uint8_t*>(g.a_lo) + ao, kATileBytes, &full[s]);
+            if (!FUSED) {
+                bulk_copy(st, static_cast<const uint8_t*>(g.a_hi) + ao, kATileBytes, &full[s]);
+                bulk_copy(st + kATileBytes, static_cast<const uint8_t*>(g.a_lo) + ao, kATileBytes, &full[s]);
+            }
             bulk_copy(st + 2 * kATileBytes, static_cast<const uint8_t*>(g.b_hi) + bo, g.b_tile_bytes, &full[s]);
             bulk_copy(st + 2 * kATileBytes + g.b_tile_bytes, static_cast<const uint8_t*>(g.b_lo) + bo, g.b_tile_bytes,
                       &full[s]);
@@ -346,7 +388,30 @@ __global__ void __launch_bounds__(kThreadsGemm, 2) tc_gemm_kernel(const GemmArgs
             mma_commit(&empty[s]);
         }
         mma_commit(accum);
-    } else if (warp >= 2) {
+    } else if (FUSED && warp >= 6) {
+        // X producers: thread r gathers row r of every K chunk into the stage's A tiles, makes its
+        // stores visible to the tensor core's async proxy, and one lane per warp arrives
+        const int row = threadIdx.x - 192;
+        const int64_t m = mt * kTcTileM + row;
+        const bool row_ok = m < g.M;
+        const int64_t base = row_ok ? pdep(b, g.xb) + pdep(m, g.xm) : 0;
+        const int mx = g.exps[2 * g.x_slot + 1];
+        const float s = pow2f(-(mx < -400 ? 0 : mx));
+        const float si = g.x_conj ? -s : s;
+        constexpr int KC = TF32 ? 8 : 16;        // complex k per 64-byte chunk
+        for (int64_t c = 0; c < g.kchunks; c++) {
+            const int st_i = (int)(c % kStages);
+            const uint32_t u = (uint32_t)(c / kStages);
+            if (!mbar_wait(&empty[st_i], (u & 1u) ^ 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 4); break; }
+            if (*(volatile int*)&abort_flag) break;
+            uint8_t* st = smem + st_i * stage_bytes;
+            fill_a_row<TF32>(st, st + kATileBytes, row, g.X, base, row_ok, c * KC, g.K, g.xk, s, si);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full[st_i])) : "memory");
+        }
+    } else if (warp >= 2 && warp < 6) {
         // epilogue: warp w reads tensor-memory lanes 32*(w%4) .. +31
         const bool ok = mbar_wait(accum, 0);
         fence_after();
@@ -421,11 +486,11 @@ int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 constexpr size_t kMaxDynSmem = kStages * (2 * kATileBytes + 2 * (2 * 64 * kTcChunkBytes)) + 128;
 
-template <bool TF32>
+template <bool TF32, bool FUSED>
 cudaError_t set_smem_attr() {
     static bool done = false;
     if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<TF32, FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kMaxDynSmem);
     if (e == cudaSuccess) done = true;
     return e;
@@ -492,7 +557,9 @@ bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits
     t.mtiles = cdiv(t.M, kTcTileM);
     t.ntiles = cdiv(t.N, t.ntile_n);
     t.kchunks = cdiv(t.K, t.kc);
-    t.a_plane_bytes = (size_t)(t.batch * t.mtiles * t.kchunks) * kATileBytes;
+    static const bool unfused = getenv("QXG_TC_UNFUSED") != nullptr;   // planes path, for comparison
+    t.fused = !unfused;
+    t.a_plane_bytes = t.fused ? 0 : (size_t)(t.batch * t.mtiles * t.kchunks) * kATileBytes;
     t.b_plane_bytes = (size_t)(t.batch * t.ntiles * t.kchunks) * (size_t)(2 * t.ntile_n * kTcChunkBytes);
     t.scratch_bytes = 2 * (t.a_plane_bytes + t.b_plane_bytes);
     if (t.scratch_bytes > (size_t(96) << 30)) return false;
@@ -526,11 +593,12 @@ cudaError_t tc_run_pack(const TcStep& t, const StepArgs& s, int* exps, void* scr
         const int64_t n = p.batch * p.kchunks * p.rows_pad * 2;
         return (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, 256), (int64_t)sm_count * 16));
     };
+    // fused steps pack only Y: the GEMM gathers and splits X itself
     if (t.tf32) {
-        pack_kernel<true><<<grid_of(px), 256, 0, st>>>(px, exps);
+        if (!t.fused) pack_kernel<true><<<grid_of(px), 256, 0, st>>>(px, exps);
         pack_kernel<true><<<grid_of(py), 256, 0, st>>>(py, exps);
     } else {
-        pack_kernel<false><<<grid_of(px), 256, 0, st>>>(px, exps);
+        if (!t.fused) pack_kernel<false><<<grid_of(px), 256, 0, st>>>(px, exps);
         pack_kernel<false><<<grid_of(py), 256, 0, st>>>(py, exps);
     }
     return cudaGetLastError();
@@ -552,15 +620,26 @@ cudaError_t tc_run_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scr
     g.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((nmma >> 3) << 17) | ((uint32_t)(kTcTileM >> 4) << 24);
     g.exp_c = s.expC;
     g.exps = exps;
+    g.X = static_cast<const float2*>(t.x_is_a ? s.A : s.B);
+    g.xb = t.xb; g.xm = t.xm; g.xk = t.xk;
+    g.K = t.K;
+    g.x_slot = t.x_is_a ? s.expA : s.expB;
+    g.x_conj = t.x_is_a ? s.conjA : s.conjB;
     const size_t smem = kStages * (2 * kATileBytes + 2 * (size_t)g.b_tile_bytes) + 128;
     const int64_t ctas = t.batch * t.mtiles * t.ntiles;
     cudaError_t e;
-    if (t.tf32) {
-        if ((e = set_smem_attr<true>()) != cudaSuccess) return e;
-        tc_gemm_kernel<true><<<(unsigned)ctas, kThreadsGemm, smem, st>>>(g);
+    if (t.tf32 && t.fused) {
+        if ((e = set_smem_attr<true, true>()) != cudaSuccess) return e;
+        tc_gemm_kernel<true, true><<<(unsigned)ctas, kThreadsFused, smem, st>>>(g);
+    } else if (t.tf32) {
+        if ((e = set_smem_attr<true, false>()) != cudaSuccess) return e;
+        tc_gemm_kernel<true, false><<<(unsigned)ctas, kThreadsGemm, smem, st>>>(g);
+    } else if (t.fused) {
+        if ((e = set_smem_attr<false, true>()) != cudaSuccess) return e;
+        tc_gemm_kernel<false, true><<<(unsigned)ctas, kThreadsFused, smem, st>>>(g);
     } else {
-        if ((e = set_smem_attr<false>()) != cudaSuccess) return e;
-        tc_gemm_kernel<false><<<(unsigned)ctas, kThreadsGemm, smem, st>>>(g);
+        if ((e = set_smem_attr<false, false>()) != cudaSuccess) return e;
+        tc_gemm_kernel<false, false><<<(unsigned)ctas, kThreadsGemm, smem, st>>>(g);
     }
     return cudaGetLastError();
 }

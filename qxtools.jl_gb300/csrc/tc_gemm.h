@@ -25,6 +25,7 @@ constexpr int kTcChunkBytes = 64;   // bytes of one operand row per K chunk (4 c
 struct TcStep {
     bool x_is_a = true;             // the larger operand (M side) is the step's A
     bool tf32 = false;
+    bool fused = true;              // the GEMM gathers and splits X itself (no X planes in scratch)
     int nb = 0, nm = 0, nn = 0, nk = 0;        // bits of batch, M, N, K
     int64_t M = 0, N = 0, K = 0, batch = 0;
     int ntile_n = 0;                // complex columns per N tile (N'' = 2 ntile_n)
