@@ -70,7 +70,8 @@ def test_static_scratch_contraction_matches_allocating_entry_point(q, gpu_lib, p
 def test_static_scratch_rejects_oversized_shapes(q, gpu_lib):
     import torch
     lib = _declare(gpu_lib)
-    la, ad, lb, bd, lc = _shapes(17, 5, 4)         # packed planes larger than the static array
+    # the smaller operand's packed planes (2^11 x 2^11 complex: 134 MB) exceed the static array
+    la, ad, lb, bd, lc = _shapes(11, 11, 11)
     A = torch.zeros(2 ** len(la), dtype=torch.complex64, device="cuda")
     B = torch.zeros(2 ** len(lb), dtype=torch.complex64, device="cuda")
     C = torch.zeros(2 ** len(lc), dtype=torch.complex64, device="cuda")
