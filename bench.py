@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--compare-fp64", action="store_true", help="also time the FP64 path and report the error")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel eagerly (no CUDA graphs)")
+    ap.add_argument("--tc-tuning", default="auto",
+                    help="tensor-core tile variants: 'auto' (timed per step) or candidate number k >= 1")
     ap.add_argument("--gradient", action="store_true",
                     help="time the reverse-mode gradient against the forward pass (parametrised 5x5 circuit)")
     return ap.parse_args()
@@ -237,7 +239,10 @@ def workload_config(info, args, ex_info):
            "l2": "intermediates larger than L2 (no flush needed)"}
     if ex_info:
         cfg.update({"bitstring_batch": ex_info["bitstring_batch"], "slice_batch": ex_info["slice_batch"],
-                    "workspace_bytes": ex_info["workspace_bytes"]})
+                    "workspace_bytes": ex_info["workspace_bytes"],
+                    "tensor_core_steps": ex_info["num_steps_tensor_core"],
+                    "fused_gather_steps": ex_info["num_steps_fused"],
+                    "autotuned_steps": ex_info["num_steps_tuned"], "tc_tuning": args.tc_tuning})
     return cfg
 
 
@@ -266,7 +271,9 @@ def run_ours(args):
         all_bits = (all_bits * math.ceil(nb / len(all_bits)))[:nb]
     out_size = info["amplitudes_per_bitstring"]
     amps_per_step = nb * out_size
-    ex = q.Executor(prog, precision=args.precision, device=local, use_graphs=not args.no_graphs)
+    tuning = args.tc_tuning if args.tc_tuning == "auto" else int(args.tc_tuning)
+    ex = q.Executor(prog, precision=args.precision, device=local, use_graphs=not args.no_graphs,
+                    tc_tuning=tuning)
     stream = torch.cuda.ExternalStream(ex.stream, device=dev)
     d_bits = torch.tensor(list("".join(all_bits).encode()), dtype=torch.uint8, device=dev)
     d_out = torch.zeros(2 * nb * out_size, dtype=torch.float64, device=dev)

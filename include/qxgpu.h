@@ -82,7 +82,11 @@ typedef struct qxg_options {
     int32_t max_bitstring_batch;  /* bitstrings per pass through the programme; 0 = automatic */
     int32_t max_slice_batch;      /* slices per pass; 0 = automatic */
     int32_t use_graphs;           /* capture each pass in a CUDA graph (1) or launch eagerly (0) */
-    int32_t reserved[7];
+    int32_t tc_tuning;            /* tensor-core tile variants: 0 = time the candidates of each step
+                                     the first time it runs and keep the fastest (default);
+                                     k >= 1 = candidate k of every step (1: fused X gather, widest
+                                     N tile; then narrower tiles, then the X-planes variants) */
+    int32_t reserved[6];
 } qxg_options;
 
 typedef struct qxg_program qxg_program;
@@ -103,7 +107,9 @@ typedef struct qxg_program_info {
     int32_t num_steps_slice;      /* ncon steps computed once per slice batch */
     int32_t num_steps_bitstring;  /* ncon steps computed once per (slice batch, bitstring batch) */
     int32_t num_steps_tensor_core;  /* ncon steps run on the tensor cores (split modes) */
-    int32_t reserved[4];
+    int32_t num_steps_fused;      /* of those, steps whose GEMM gathers the larger operand itself */
+    int32_t num_steps_tuned;      /* tensor-core steps whose variant was chosen by timing */
+    int32_t reserved[2];
 } qxg_program_info;
 
 /* Build a programme from the `.qx` command list.  data_rank[i] and the concatenated

@@ -90,6 +90,7 @@ struct Step {                           // an executable item of a pass
     ViewAdjArgs vaargs;
     LeafGradArgs largs;
     bool use_tc = false;                // tensor-core path (split modes)
+    bool tc_tuned = false;              // the tile variant has been chosen
     TcStep tc;                          // tensor-core step description
     double flops = 0, bytes = 0;
 };
@@ -154,6 +155,10 @@ struct qxg_program {
     double* d_out = nullptr;
     size_t d_out_cap = 0;
     std::vector<int> h_exps_init;
+    // tensor-core autotuner: chosen variant per step shape + bit maps, events for timing
+    std::map<std::string, TcVariant> tune_cache;
+    cudaEvent_t tune_ev[2] = {nullptr, nullptr};
+    int tuned_steps = 0;                // steps whose variant was picked by timing
     // profiling: CUDA events around launches, aggregated per command on read
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -438,6 +443,16 @@ std::vector<int64_t> leaf_offsets(const qxg_program* P, int64_t* total) {
 // B_bar = ncon(conj A, C_bar) -- the same einsum machinery with one operand conjugated; a view's
 // adjoint gathers the slice batch back into its leaf; every leaf's adjoint is added to its FP64
 // gradient.  Adjoint tensors are table entries ntensors + t with the forward tensor's layout.
+// tc_tuning = k >= 1: candidate k-1 of every tensor-core step (the last one where a step has
+// fewer), chosen at plan time; 0 leaves the choice to the autotuner.
+void tc_fix_variant(const qxg_program* P, Step& st) {
+    if (P->opts.tc_tuning <= 0) return;
+    TcVariant cand[kTcMaxVariants];
+    const int nc = tc_variants(st.tc, cand);
+    tc_set_variant(st.tc, cand[std::min(P->opts.tc_tuning, nc) - 1]);
+    st.tc_tuned = true;
+}
+
 int build_backward(qxg_program* P, Plan& pl, int* err) {
     auto& T = pl.T;
     const int n = (int)T.size();
@@ -489,6 +504,7 @@ int build_backward(qxg_program* P, Plan& pl, int* err) {
         if (!P->fp64 && P->opts.precision != QXG_PREC_FP32)
             st.use_tc = tc_plan_step(st.sargs, T[x].layout.size(), T[y].layout.size(), T[res].layout.size(),
                                      P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc);
+            if (st.use_tc) tc_fix_variant(P, st);
         pl.flops_bwd += st.flops;
         pl.bsteps.push_back(st);
         return 0;
@@ -574,6 +590,11 @@ int build_backward(qxg_program* P, Plan& pl, int* err) {
         pl.bsteps.push_back(st);
     }
     return 0;
+}
+
+// Scratch a tensor-core step may use: any candidate variant when the autotuner is on.
+size_t tc_scratch_need(const qxg_program* P, const Step& st) {
+    return P->opts.tc_tuning == 0 && !st.tc_tuned ? st.tc.scratch_max : st.tc.scratch_bytes;
 }
 
 int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool grad = false) {
@@ -722,6 +743,7 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
             if (!P->fp64 && P->opts.precision != QXG_PREC_FP32)
                 st.use_tc = tc_plan_step(st.sargs, A.layout.size(), B.layout.size(), t.layout.size(),
                                          P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc);
+                if (st.use_tc) tc_fix_variant(P, st);
         }
         if (err) return fail(QXG_ERR_UNSUPPORTED, "bit map needs more than the supported number of runs");
         plan->flops_pass[t.group] += st.flops;
@@ -799,8 +821,8 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
     plan->arena_bytes = (size_t)total;
     size_t scratch = 0;
     for (int g = 0; g < 3; g++)
-        for (auto& st : plan->steps[g]) if (st.use_tc) scratch = std::max(scratch, st.tc.scratch_bytes);
-    for (auto& st : plan->bsteps) if (st.use_tc) scratch = std::max(scratch, st.tc.scratch_bytes);
+        for (auto& st : plan->steps[g]) if (st.use_tc) scratch = std::max(scratch, tc_scratch_need(P, st));
+    for (auto& st : plan->bsteps) if (st.use_tc) scratch = std::max(scratch, tc_scratch_need(P, st));
     plan->tc_scratch_bytes = scratch;
     // reduction of the root
     {
@@ -988,6 +1010,56 @@ int prof_end(qxg_program* P, size_t ev, int instr, int kind, double flops, doubl
 
 int run_group_eager(qxg_program* P, int g, Plan* plp = nullptr);
 
+// Autotuner: the first time a tensor-core step runs (its operands are in place), time each
+// candidate variant (fused X gather or X planes; N tiles of 16/32/64) on the step itself, twice
+// each, and keep the fastest of the second runs.  Re-running a step is harmless: it overwrites
+// its result and re-raises the same exponent slot, which is cleared before every candidate.
+// Identical steps (shape and bit maps) share the choice.  Not done under stream capture, and
+// the tuning launches are not counted as pass launches.
+int tune_tc_step(qxg_program* P, Step& st, int* exps) {
+    if (st.tc_tuned) return 0;
+    st.tc_tuned = true;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    QXG_CUDA(cudaStreamIsCapturing(P->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return 0;
+    const std::string key = tc_key(st.tc);
+    auto it = P->tune_cache.find(key);
+    if (it != P->tune_cache.end()) {
+        tc_set_variant(st.tc, it->second);
+        return 0;
+    }
+    TcVariant cand[kTcMaxVariants];
+    const int nc = tc_variants(st.tc, cand);
+    TcVariant best = cand[0];
+    if (nc > 1) {
+        for (auto& e : P->tune_ev)
+            if (!e) QXG_CUDA(cudaEventCreate(&e));
+        float best_ms = 0.f;
+        bool have = false;
+        int* cslot = exps + 2 * st.sargs.expC + 1;
+        for (int i = 0; i < nc; i++) {
+            tc_set_variant(st.tc, cand[i]);
+            if (st.tc.scratch_bytes > P->scratch_cap) continue;
+            float ms = 0.f;
+            for (int rep = 0; rep < 2; rep++) {
+                QXG_CUDA(cudaMemsetAsync(cslot, 0x80, sizeof(int), P->stream));   // kExpUnset
+                QXG_CUDA(cudaEventRecord(P->tune_ev[0], P->stream));
+                QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
+                QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream));
+                QXG_CUDA(cudaEventRecord(P->tune_ev[1], P->stream));
+            }
+            QXG_CUDA(cudaEventSynchronize(P->tune_ev[1]));
+            QXG_CUDA(cudaEventElapsedTime(&ms, P->tune_ev[0], P->tune_ev[1]));
+            if (!have || ms < best_ms) { best_ms = ms; best = cand[i]; have = true; }
+        }
+        QXG_CUDA(cudaMemsetAsync(cslot, 0x80, sizeof(int), P->stream));
+        P->tuned_steps++;
+    }
+    tc_set_variant(st.tc, best);
+    P->tune_cache[key] = best;
+    return 0;
+}
+
 void drop_graphs(qxg_program* P) {
     for (int g = 0; g < 3; g++) {
         if (P->gexec[g]) cudaGraphExecDestroy(P->gexec[g]);
@@ -1042,6 +1114,8 @@ int run_group_eager(qxg_program* P, int g, Plan* plp) {
     }
     for (auto& st : pl.steps[g]) {
         const int instr = pl.T[st.tensor].instr;
+        if (st.use_tc)
+            if (int r = tune_tc_step(P, st, exps)) return r;
         size_t ev = 0;
         if (int r = prof_begin(P, &ev)) return r;
         int kind;
@@ -1191,6 +1265,8 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
             QXG_CUDA(launch_seed(pl.seed, P->fp64, exps, P->stream));
             P->launches++;
             for (auto& st : pl.bsteps) {
+                if (st.use_tc)
+                    if (int r = tune_tc_step(P, st, exps)) return r;
                 size_t ev = 0;
                 if (int r = prof_begin(P, &ev)) return r;
                 int kind = QXG_KERNEL_REDUCE;
@@ -1495,6 +1571,11 @@ int qxg_program_info_get(const qxg_program* P, qxg_program_info* info) {
                 if (st.use_tc) ntc++;
             }
         info->num_steps_tensor_core = ntc;
+        int nf = 0;
+        for (int g = 0; g < 3; g++)
+            for (auto& st : pl.steps[g]) if (st.use_tc && st.tc.fused) nf++;
+        info->num_steps_fused = nf;
+        info->num_steps_tuned = P->tuned_steps;
         info->num_steps_invariant = c[0];
         info->num_steps_slice = c[1];
         info->num_steps_bitstring = c[2];
@@ -1547,6 +1628,8 @@ void qxg_program_destroy(qxg_program* P) {
     drop_graphs(P);
     for (void* p : P->d_data) if (p) cudaFree(p);
     if (P->d_arena) cudaFree(P->d_arena);
+    for (auto& e : P->tune_ev)
+        if (e) cudaEventDestroy(e);
     if (P->d_scratch) cudaFree(P->d_scratch);
     if (P->d_exps) cudaFree(P->d_exps);
     if (P->d_params) cudaFree(P->d_params);

@@ -31,7 +31,9 @@ namespace {
 
 constexpr int kThreadsGemm = 192;                        // warp 0 producer, 1 MMA, 2-5 epilogue
 constexpr int kThreadsFused = 320;                       // + warps 6-9 gather and split X rows
-constexpr int kStages = 3;
+constexpr int kStages = 3;                               // operand stages, planes kernel
+constexpr int kStagesFused = 2;                          // operand stages, fused kernel
+constexpr int kRingBytes = 32 * 1024;                    // fused: raw X rows in flight per CTA
 constexpr int kCols16 = kTcChunkBytes / 16;              // 16-byte core-matrix columns per chunk (4)
 constexpr int kSbo = kCols16 * 128;                      // bytes between 8-row groups (512)
 constexpr int kATileBytes = kTcTileM * kTcChunkBytes;    // 8 KB
@@ -265,13 +267,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Fused operand staging: one thread gathers row `row` of X's K chunk (2*NE complex values) through
-// the bit maps, scales, splits and stores it into the stage's hi/lo A tiles (real parts in
-// 16-byte columns 0-1, imaginary parts in 2-3).
+// 8-byte asynchronous global -> shared copies (the fused X gather keeps several K chunks in flight
+// without holding registers for them).
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Fused operand staging: one thread takes row `row` of X's K chunk (2*NE complex values, already
+// gathered into the raw ring: element j at raw[j * kTcTileM]), scales, splits and stores it into
+// the stage's hi/lo A tiles (real parts in 16-byte columns 0-1, imaginary parts in 2-3).
 template <bool TF32>
-__device__ __forceinline__ void fill_a_row(uint8_t* th, uint8_t* tl, int row, const float2* __restrict__ X,
-                                           int64_t base, bool row_ok, int64_t k0, int64_t K, const BitMap& xk,
-                                           float s, float si) {
+__device__ __forceinline__ void split_a_row(uint8_t* th, uint8_t* tl, int row, const float2* raw, bool row_ok,
+                                            int64_t k0, int64_t K, float s, float si) {
     using S = Split<TF32>;
     using E = typename S::E;
     constexpr int NE = 16 / sizeof(E);
@@ -283,7 +294,7 @@ __device__ __forceinline__ void fill_a_row(uint8_t* th, uint8_t* tl, int row, co
             const int64_t k = k0 + g * NE + j;
             re[j] = 0.f; im[j] = 0.f;
             if (row_ok && k < K) {
-                const float2 v = X[base + pdep(k, xk)];
+                const float2 v = raw[(g * NE + j) * kTcTileM];
                 re[j] = v.x * s;
                 im[j] = v.y * si;
             }
@@ -300,16 +311,19 @@ __device__ __forceinline__ void fill_a_row(uint8_t* th, uint8_t* tl, int row, co
 
 template <bool TF32, bool FUSED>
 __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreadsGemm, 2) tc_gemm_kernel(const GemmArgs g) {
+    constexpr int NS = FUSED ? kStagesFused : kStages;
+    constexpr int KC = TF32 ? 8 : 16;            // complex k per 64-byte chunk
     extern __shared__ uint8_t smem_raw[];
-    __shared__ uint64_t bars[2 * kStages + 1];   // full[kStages], empty[kStages], accum
+    __shared__ uint64_t bars[2 * NS + 1];        // full[NS], empty[NS], accum
     __shared__ int64_t noff[128];                // result offsets of this tile's columns
+    __shared__ int64_t xkoff[KC];                // fused: X offsets of the k values inside a chunk
     __shared__ uint32_t tmem_holder;
     __shared__ int abort_flag;
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const uint32_t stage_bytes = 2u * kATileBytes + 2u * g.b_tile_bytes;
     uint64_t* full = bars;
-    uint64_t* empty = bars + kStages;
-    uint64_t* accum = bars + 2 * kStages;
+    uint64_t* empty = bars + NS;
+    uint64_t* accum = bars + 2 * NS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t tile = blockIdx.x;
     const int64_t nt = tile % g.ntiles;
@@ -321,8 +335,8 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreadsGemm, 2) tc_ge
 
     if (threadIdx.x == 0) {
         // a full barrier completes on the bulk copies' bytes and, when fused, the four X warps
-        for (int i = 0; i < kStages; i++) mbar_init(&full[i], FUSED ? 5u : 1u);
-        for (int i = kStages; i < 2 * kStages + 1; i++) mbar_init(&bars[i], 1);
+        for (int i = 0; i < NS; i++) mbar_init(&full[i], FUSED ? 5u : 1u);
+        for (int i = NS; i < 2 * NS + 1; i++) mbar_init(&bars[i], 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -338,6 +352,8 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreadsGemm, 2) tc_ge
             noff[j] = n < g.N ? pdep(n, g.cn) : 0;
         }
     }
+    // chunk k0 has its low log2(KC) bits clear, so X's offset of k0 + j is pdep(k0) + pdep(j)
+    if (FUSED && threadIdx.x >= 192 && threadIdx.x < 192 + KC) xkoff[threadIdx.x - 192] = pdep(threadIdx.x - 192, g.xk);
     fence_before();
     __syncthreads();
     fence_after();
@@ -348,8 +364,8 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreadsGemm, 2) tc_ge
         const int64_t a_tile0 = (b * g.mtiles + mt) * g.kchunks;
         const int64_t b_tile0 = (b * g.ntiles + nt) * g.kchunks;
         for (int64_t c = 0; c < g.kchunks; c++) {
-            const int s = (int)(c % kStages);
-            const uint32_t u = (uint32_t)(c / kStages);
+            const int s = (int)(c % NS);
+            const uint32_t u = (uint32_t)(c / NS);
             if (!mbar_wait(&empty[s], (u & 1u) ^ 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 1); break; }
             if (*(volatile int*)&abort_flag) break;
             uint8_t* st = smem + s * stage_bytes;
@@ -366,8 +382,8 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreadsGemm, 2) tc_ge
     } else if (warp == 1 && lane == 0) {
         // MMA issuer: kKSteps K steps of 32 bytes per chunk, three products each
         for (int64_t c = 0; c < g.kchunks; c++) {
-            const int s = (int)(c % kStages);
-            const uint32_t u = (uint32_t)(c / kStages);
+            const int s = (int)(c % NS);
+            const uint32_t u = (uint32_t)(c / NS);
             if (!mbar_wait(&full[s], u & 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 2); break; }
             fence_after();
             const uint32_t st = smem_u32(smem + s * stage_bytes);
@@ -389,28 +405,49 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreadsGemm, 2) tc_ge
         }
         mma_commit(accum);
     } else if (FUSED && warp >= 6) {
-        // X producers: thread r gathers row r of every K chunk into the stage's A tiles, makes its
-        // stores visible to the tensor core's async proxy, and one lane per warp arrives
+        // X producers: thread r gathers row r of X's K chunks with 8-byte cp.async into a ring of
+        // R raw chunks ([R][KC][128 rows], R - 1 chunks in flight ahead of the one being split),
+        // then scales, splits and stores each chunk into the stage's A tiles, makes the stores
+        // visible to the tensor core's async proxy, and one lane per warp arrives.  Each thread
+        // reads back only its own copies, so waiting on its own copy groups is enough.
+        constexpr int R = kRingBytes / (kTcTileM * KC * 8);
+        float2* ring = reinterpret_cast<float2*>(smem + NS * stage_bytes);
         const int row = threadIdx.x - 192;
         const int64_t m = mt * kTcTileM + row;
         const bool row_ok = m < g.M;
         const int64_t base = row_ok ? pdep(b, g.xb) + pdep(m, g.xm) : 0;
-        const int mx = g.exps[2 * g.x_slot + 1];
-        const float s = pow2f(-(mx < -400 ? 0 : mx));
+        const float s = pow2f(-read_m(g.exps, g.x_slot));
         const float si = g.x_conj ? -s : s;
-        constexpr int KC = TF32 ? 8 : 16;        // complex k per 64-byte chunk
+        auto issue = [&](int64_t c) {       // one copy group per chunk (empty past the end)
+            if (row_ok && c < g.kchunks) {
+                float2* slot = ring + (c % R) * (KC * kTcTileM) + row;
+                const int64_t k0 = c * KC;
+                const float2* src = g.X + base + pdep(k0, g.xk);
+#pragma unroll
+                for (int j = 0; j < KC; j++)
+                    if (k0 + j < g.K) cp_async8(slot + j * kTcTileM, src + xkoff[j]);
+            }
+            cp_async_commit();
+        };
+        for (int c = 0; c < R - 1; c++) issue(c);
         for (int64_t c = 0; c < g.kchunks; c++) {
-            const int st_i = (int)(c % kStages);
-            const uint32_t u = (uint32_t)(c / kStages);
-            if (!mbar_wait(&empty[st_i], (u & 1u) ^ 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 4); break; }
-            if (*(volatile int*)&abort_flag) break;
+            issue(c + R - 1);
+            cp_async_wait<R - 1>();
+            const int st_i = (int)(c % NS);
+            const uint32_t u = (uint32_t)(c / NS);
+            const bool ok = mbar_wait(&empty[st_i], (u & 1u) ^ 1u);
+            // leave the loop as a whole warp (the __syncwarp below needs every lane)
+            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 4); break; }
+            if (__any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) break;
             uint8_t* st = smem + st_i * stage_bytes;
-            fill_a_row<TF32>(st, st + kATileBytes, row, g.X, base, row_ok, c * KC, g.K, g.xk, s, si);
+            split_a_row<TF32>(st, st + kATileBytes, row, ring + (c % R) * (KC * kTcTileM) + row, row_ok, c * KC,
+                              g.K, s, si);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             if (lane == 0)
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full[st_i])) : "memory");
         }
+        cp_async_wait_all();                // no copy may land after the CTA has left
     } else if (warp >= 2 && warp < 6) {
         // epilogue: warp w reads tensor-memory lanes 32*(w%4) .. +31
         const bool ok = mbar_wait(accum, 0);
@@ -484,7 +521,8 @@ BitMap runs(const std::vector<std::pair<int, int>>& pairs, bool* ok) {
 
 int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
-constexpr size_t kMaxDynSmem = kStages * (2 * kATileBytes + 2 * (2 * 64 * kTcChunkBytes)) + 128;
+constexpr size_t kMaxStageBytes = 2 * kATileBytes + 2 * (2 * 64 * kTcChunkBytes);
+constexpr size_t kMaxDynSmem = std::max(kStages * kMaxStageBytes, kStagesFused * kMaxStageBytes + kRingBytes) + 128;
 
 template <bool TF32, bool FUSED>
 cudaError_t set_smem_attr() {
@@ -550,22 +588,60 @@ bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits
     t.N = int64_t(1) << t.nn;
     t.K = int64_t(1) << t.nk;
     t.batch = int64_t(1) << t.nb;
-    // N tile <= 64 complex: two accumulators of 2*64 columns = 256 tensor-memory columns, so two
-    // CTAs fit in an SM's 512 columns
-    t.ntile_n = (int)std::min<int64_t>(64, std::max<int64_t>(16, t.N));
     t.kc = (kTcChunkBytes / 2) / (tf32 ? 4 : 2);     // complex k per chunk: half the row is Re
     t.mtiles = cdiv(t.M, kTcTileM);
-    t.ntiles = cdiv(t.N, t.ntile_n);
     t.kchunks = cdiv(t.K, t.kc);
-    static const bool unfused = getenv("QXG_TC_UNFUSED") != nullptr;   // planes path, for comparison
-    t.fused = !unfused;
+    TcVariant v[kTcMaxVariants];
+    const int nv = tc_variants(t, v);
+    if (nv == 0) return false;
+    t.planes_ok = false;
+    t.scratch_max = 0;
+    for (int i = 0; i < nv; i++) {
+        tc_set_variant(t, v[i]);
+        t.scratch_max = std::max(t.scratch_max, t.scratch_bytes);
+        if (!v[i].fused) t.planes_ok = true;
+    }
+    tc_set_variant(t, v[0]);
+    *tc = t;
+    return true;
+}
+
+void tc_set_variant(TcStep& t, TcVariant v) {
+    t.fused = v.fused;
+    t.ntile_n = v.ntile;
+    t.ntiles = cdiv(t.N, t.ntile_n);
     t.a_plane_bytes = t.fused ? 0 : (size_t)(t.batch * t.mtiles * t.kchunks) * kATileBytes;
     t.b_plane_bytes = (size_t)(t.batch * t.ntiles * t.kchunks) * (size_t)(2 * t.ntile_n * kTcChunkBytes);
     t.scratch_bytes = 2 * (t.a_plane_bytes + t.b_plane_bytes);
-    if (t.scratch_bytes > (size_t(96) << 30)) return false;
-    if (t.batch * t.mtiles * t.ntiles > (int64_t(1) << 31) - 1) return false;
-    *tc = t;
-    return true;
+}
+
+// N tiles of 16, 32 or 64 complex columns (two accumulators of 2*ntile FP32 columns: at 64 two
+// CTAs fill an SM's 512 tensor-memory columns), no wider than N needs; fused first, then the
+// planes variants whose scratch stays under 96 GB.  The first entry is the default.
+int tc_variants(const TcStep& t, TcVariant* out) {
+    const int widest = (int)std::min<int64_t>(64, std::max<int64_t>(16, t.N));
+    int n = 0;
+    for (int f = 1; f >= 0; f--)
+        for (int nt = widest; nt >= 16; nt /= 2) {
+            TcStep u = t;
+            tc_set_variant(u, TcVariant{f == 1, nt});
+            if (u.batch * u.mtiles * u.ntiles > (int64_t(1) << 31) - 1) continue;
+            if (u.scratch_bytes > (size_t(96) << 30)) continue;
+            if (n < kTcMaxVariants) out[n++] = TcVariant{f == 1, nt};
+        }
+    return n;
+}
+
+std::string tc_key(const TcStep& t) {
+    std::string k;
+    auto put = [&](int64_t x) { k.append(reinterpret_cast<const char*>(&x), sizeof(x)); };
+    auto map = [&](const BitMap& m) {
+        put(m.n);
+        for (int i = 0; i < m.n; i++) put(m.r[i].src | (m.r[i].len << 8) | (m.r[i].dst << 16));
+    };
+    put(t.tf32); put(t.nb); put(t.nm); put(t.nn); put(t.nk);
+    map(t.xb); map(t.xm); map(t.xk); map(t.yb); map(t.yn); map(t.yk); map(t.cb); map(t.cm); map(t.cn);
+    return k;
 }
 
 cudaError_t tc_run_pack(const TcStep& t, const StepArgs& s, int* exps, void* scratch, cudaStream_t st, int sm_count) {
@@ -625,7 +701,8 @@ cudaError_t tc_run_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scr
     g.K = t.K;
     g.x_slot = t.x_is_a ? s.expA : s.expB;
     g.x_conj = t.x_is_a ? s.conjA : s.conjB;
-    const size_t smem = kStages * (2 * kATileBytes + 2 * (size_t)g.b_tile_bytes) + 128;
+    const size_t stage = 2 * kATileBytes + 2 * (size_t)g.b_tile_bytes;
+    const size_t smem = (t.fused ? kStagesFused * stage + kRingBytes : kStages * stage) + 128;
     const int64_t ctas = t.batch * t.mtiles * t.ntiles;
     cudaError_t e;
     if (t.tf32 && t.fused) {

@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cstddef>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "qxgpu_internal.h"
@@ -26,21 +27,41 @@ struct TcStep {
     bool x_is_a = true;             // the larger operand (M side) is the step's A
     bool tf32 = false;
     bool fused = true;              // the GEMM gathers and splits X itself (no X planes in scratch)
+    bool planes_ok = false;         // the planes variant's scratch fits the cap
     int nb = 0, nm = 0, nn = 0, nk = 0;        // bits of batch, M, N, K
     int64_t M = 0, N = 0, K = 0, batch = 0;
     int ntile_n = 0;                // complex columns per N tile (N'' = 2 ntile_n)
-    int kc = 0;                     // complex K per chunk (32 bf16, 16 tf32)
+    int kc = 0;                     // complex K per chunk (16 bf16, 8 tf32)
     int64_t mtiles = 0, ntiles = 0, kchunks = 0;
     // bit maps: index space -> operand / result offsets
     BitMap xb, xm, xk;              // X offset of batch / m / k index
     BitMap yb, yn, yk;              // Y offset of batch / n / k index
     BitMap cb, cm, cn;              // C offset of batch / m / n index
     size_t a_plane_bytes = 0, b_plane_bytes = 0;
-    size_t scratch_bytes = 0;       // 2 planes of A_op + 2 planes of B_op
+    size_t scratch_bytes = 0;       // 2 planes of A_op (planes variant) + 2 planes of B_op
+    size_t scratch_max = 0;         // the largest scratch of any candidate variant
 };
 
-// Decide whether a step goes to the tensor cores; fills `tc` when it does.
+// A tile variant of a tensor-core step: X gathered in the GEMM (fused) or packed into planes
+// first, and the complex columns per N tile.
+struct TcVariant {
+    bool fused;
+    int ntile;
+};
+
+// Decide whether a step goes to the tensor cores; fills `tc` (default variant: fused, the
+// widest N tile) when it does.
 bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits, bool tf32, TcStep* tc);
+
+// Candidate variants of a planned step (at most kTcMaxVariants), for the autotuner.
+constexpr int kTcMaxVariants = 6;
+int tc_variants(const TcStep& t, TcVariant* out);
+
+// Switch a planned step to a variant (recomputes tile counts and scratch sizes).
+void tc_set_variant(TcStep& t, TcVariant v);
+
+// Autotuner cache key: the step's shape and bit maps (identical steps share a choice).
+std::string tc_key(const TcStep& t);
 
 // Run a planned tensor-core step (scratch: at least tc.scratch_bytes of device memory):
 // tc_run_pack (both operands) then tc_run_gemm.

@@ -42,7 +42,7 @@ class qxg_instr(ct.Structure):
 class qxg_options(ct.Structure):
     _fields_ = [("precision", ct.c_int32), ("device", ct.c_int32), ("workspace_limit", ct.c_int64),
                 ("max_bitstring_batch", ct.c_int32), ("max_slice_batch", ct.c_int32),
-                ("use_graphs", ct.c_int32), ("reserved", ct.c_int32 * 7)]
+                ("use_graphs", ct.c_int32), ("tc_tuning", ct.c_int32), ("reserved", ct.c_int32 * 6)]
 
 
 class qxg_program_info(ct.Structure):
@@ -52,7 +52,8 @@ class qxg_program_info(ct.Structure):
                 ("flops_executed_per_pass", ct.c_double), ("bytes_executed_per_pass", ct.c_double),
                 ("num_steps_invariant", ct.c_int32), ("num_steps_slice", ct.c_int32),
                 ("num_steps_bitstring", ct.c_int32), ("num_steps_tensor_core", ct.c_int32),
-                ("reserved", ct.c_int32 * 4)]
+                ("num_steps_fused", ct.c_int32), ("num_steps_tuned", ct.c_int32),
+                ("reserved", ct.c_int32 * 2)]
 
 
 class qxg_step_profile(ct.Structure):
@@ -228,7 +229,7 @@ class Executor:
 
     def __init__(self, programme: Programme, precision: str = "fp64", device: int = 0,
                  workspace_limit: int = 0, max_bitstring_batch: int = 0, max_slice_batch: int = 0,
-                 use_graphs: bool = False):
+                 use_graphs: bool = False, tc_tuning="auto"):
         self.lib = load_library()
         self.programme = programme
         self.precision = precision
@@ -239,6 +240,16 @@ class Executor:
         opts.max_bitstring_batch = max_bitstring_batch
         opts.max_slice_batch = max_slice_batch
         opts.use_graphs = int(use_graphs)
+        # "auto": time each tensor-core step's tile variants once and keep the fastest;
+        # "fixed" (= 1) or k >= 1: candidate k of every step
+        if tc_tuning == "auto":
+            opts.tc_tuning = 0
+        elif tc_tuning == "fixed":
+            opts.tc_tuning = 1
+        elif isinstance(tc_tuning, int) and tc_tuning >= 1:
+            opts.tc_tuning = tc_tuning
+        else:
+            raise ValueError("tc_tuning must be 'auto', 'fixed' or a candidate number >= 1")
         ins = np.ascontiguousarray(programme.instrs, dtype=np.int32)
         n = ins.shape[0]
         arr = (qxg_instr * n).from_buffer_copy(ins.tobytes())

@@ -83,3 +83,22 @@ def test_tensor_core_error_at_large_k(q, gpu_lib, precision):
     err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
     print(f"{precision} K=512 error {err:.3e}")
     assert err <= (5e-6 if precision == "split_tf32" else 5e-5), err
+
+
+@pytest.mark.parametrize("precision", ["split_tf32", "split_bf16"])
+@pytest.mark.parametrize("nm,nk,nn,nb", [(8, 9, 6, 0), (7, 3, 7, 1), (9, 6, 2, 0)])
+def test_every_tile_variant_matches(q, gpu_lib, precision, nm, nk, nn, nb):
+    """Each candidate tile variant (fused X gather or X planes; N tiles of 16/32/64), forced with
+    tc_tuning = k, and the autotuned choice give the einsum result within the split tolerance.
+    Shapes cover K chunks beyond the gather ring (nk=9), K below one chunk (nk=3 with 3xBF16),
+    a batch bit, and N narrower than the smallest tile (nn=2)."""
+    prog, ref = single_ncon_programme(q, nm, nk, nn, nb, seed=nm + 7 * nk + 31 * nn)
+    for k in ["auto", 1, 2, 3, 4, 5, 6]:
+        with q.Executor(prog, precision=precision, tc_tuning=k) as ex:
+            got = ex.amplitudes([""])[0]
+            info = ex.info()
+        assert info["num_steps_tensor_core"] == 1
+        err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+        assert err <= TOL[precision], (k, err)
+        if k == "auto":                         # fused and planes candidates at least
+            assert info["num_steps_tuned"] == 1
