@@ -9,6 +9,10 @@
 // offset(tile | lo) = offset(tile) + offset(lo), so the low-bit offsets of the result and all
 // K offsets (up to 2^kKTableBits) are tabulated once per block in shared memory and each
 // element costs two table reads instead of a full bit deposit.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "qxgpu_internal.h"
 
 namespace qxg {
@@ -41,7 +45,9 @@ __device__ __forceinline__ int read_m(const int* exps, int slot) {
     return m < -400 ? 0 : m;            // all-zero tensor: no scaling
 }
 
-template <typename T, bool SCALED>
+// CONJ bit 0 / bit 1: use the complex conjugate of A / B (adjoint steps).  A compile-time sign
+// folds into the FMA operands, so the forward path pays nothing for it.
+template <typename T, bool SCALED, int CONJ>
 __global__ void __launch_bounds__(kThreads)
 contract_kernel(const StepArgs a, int* exps) {
     using R = typename Real<T>::type;
@@ -69,7 +75,6 @@ contract_kernel(const StepArgs a, int* exps) {
             exps[2 * a.expC] = exps[2 * a.expA] + exps[2 * a.expB] + mA + mB;
     }
     int emax = kExpUnset;
-    const R sa = a.conjA ? R(-1) : R(1), sb = a.conjB ? R(-1) : R(1);   // conjugation signs
     const int64_t ntiles = a.nC >> tb;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t tbase = t << tb;
@@ -84,7 +89,7 @@ contract_kernel(const StepArgs a, int* exps) {
                 for (int k = 0; k < KT; k++) {
                     const T x = A[ah + tA[k]];
                     const T y = B[bh + tB[k]];
-                    const R xi = sa * x.y, yi = sb * y.y;
+                    const R xi = (CONJ & 1) ? -x.y : x.y, yi = (CONJ & 2) ? -y.y : y.y;
                     re = fma(x.x, y.x, re);
                     re = fma(-xi, yi, re);
                     im = fma(x.x, yi, im);
@@ -98,6 +103,103 @@ contract_kernel(const StepArgs a, int* exps) {
             }
             T out; out.x = re; out.y = im;
             C[tbase + i] = out;
+        }
+    }
+    if (SCALED) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.expC + 1], emax);
+    }
+}
+
+// Row form of a contraction whose smaller operand Y fits in shared memory (gate-like steps:
+// C[b,m,n] = sum_k X[b,m,k] Y[b,k,n] with K and N small).  A thread owns one row (b,m): it loads
+// the row's K values of X once into registers and writes all N results, so X is read once and C
+// written once, and Y is read from its shared-memory copy.  Rows enumerate the result's bits
+// other than the n bits (rowmap), consecutive rows are consecutive result bits, so the X loads
+// and C stores of a warp fall on consecutive addresses whenever the layouts allow it.
+struct RowArgs {
+    const void* X;
+    const void* Y;
+    void* C;
+    int64_t nrows;
+    int32_t N, K, ny;          // result columns, summed extent, elements of Y
+    int32_t conjX, conjY;
+    int32_t expX, expY, expC;
+    BitMap rowmap, nmap;       // row index / n index -> result index
+    BitMap cX, cY;             // result index -> X / Y offset
+    BitMap kX, kY;             // k -> X / Y offset
+};
+constexpr int kRowMaxY = 2048;          // elements of Y staged in shared memory
+constexpr int kRowMaxN = 1024;          // result columns per row (tabulated offsets)
+
+template <typename T, bool SCALED, int KMAX>
+__global__ void __launch_bounds__(kThreads) contract_rows_kernel(const RowArgs a, int* exps) {
+    using R = typename Real<T>::type;
+    extern __shared__ __align__(16) unsigned char rows_smem[];
+    T* Ys = reinterpret_cast<T*>(rows_smem);
+    int64_t* kx = reinterpret_cast<int64_t*>(Ys + a.ny);
+    int64_t* cn = kx + KMAX;
+    int32_t* ky = reinterpret_cast<int32_t*>(cn + a.N);
+    int32_t* cyn = ky + KMAX;
+    const T* __restrict__ X = static_cast<const T*>(a.X);
+    const T* __restrict__ Y = static_cast<const T*>(a.Y);
+    T* __restrict__ C = static_cast<T*>(a.C);
+    for (int j = threadIdx.x; j < a.ny; j += kThreads) {
+        T y = Y[j];
+        if (a.conjY) y.y = -y.y;                 // the shared copy holds conj(Y) when asked
+        Ys[j] = y;
+    }
+    for (int k = threadIdx.x; k < KMAX; k += kThreads) {
+        kx[k] = k < a.K ? pdep(k, a.kX) : 0;
+        ky[k] = k < a.K ? (int32_t)pdep(k, a.kY) : 0;
+    }
+    for (int n = threadIdx.x; n < a.N; n += kThreads) {
+        cn[n] = pdep(n, a.nmap);
+        cyn[n] = (int32_t)pdep(cn[n], a.cY);
+    }
+    __syncthreads();
+    R scale = R(1);
+    if (SCALED) {
+        const int mX = read_m(exps, a.expX), mY = read_m(exps, a.expY);
+        scale = (R)pow2f(-(mX + mY));
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            exps[2 * a.expC] = exps[2 * a.expX] + exps[2 * a.expY] + mX + mY;
+    }
+    int emax = kExpUnset;
+    const R sx = a.conjX ? R(-1) : R(1);
+    for (int64_t r = blockIdx.x * (int64_t)kThreads + threadIdx.x; r < a.nrows; r += (int64_t)gridDim.x * kThreads) {
+        const int64_t ir = pdep(r, a.rowmap);
+        const int64_t xo = pdep(ir, a.cX);
+        const int yo = (int)pdep(ir, a.cY);
+        R xr[KMAX], xi[KMAX];
+#pragma unroll
+        for (int k = 0; k < KMAX; k++) {
+            xr[k] = R(0); xi[k] = R(0);
+            if (k < a.K) {
+                const T v = X[xo + kx[k]];
+                xr[k] = v.x; xi[k] = sx * v.y;
+            }
+        }
+        for (int n = 0; n < a.N; n++) {
+            const T* yrow = Ys + yo + cyn[n];
+            R re = R(0), im = R(0);
+#pragma unroll
+            for (int k = 0; k < KMAX; k++) {
+                if (k < a.K) {
+                    const T y = yrow[ky[k]];
+                    re = fma(xr[k], y.x, re);
+                    re = fma(-xi[k], y.y, re);
+                    im = fma(xr[k], y.y, im);
+                    im = fma(xi[k], y.x, im);
+                }
+            }
+            if (SCALED) {
+                re *= scale; im *= scale;
+                const float mx = fmaxf(fabsf((float)re), fabsf((float)im));
+                if (mx > 0.f) emax = max(emax, exp_of(mx));
+            }
+            T out; out.x = re; out.y = im;
+            C[ir + cn[n]] = out;
         }
     }
     if (SCALED) {
@@ -314,18 +416,126 @@ int grid_for(int64_t n, int threads, int cap) {
     return (int)g;
 }
 
+// ---- host: choosing the row form ----------------------------------------------------------
+void expand_map(const BitMap& m, std::vector<std::pair<int, int>>& out) {
+    for (int i = 0; i < m.n; i++)
+        for (int j = 0; j < m.r[i].len; j++) out.push_back({m.r[i].src + j, m.r[i].dst + j});
+}
+
+int dst_bits(const BitMap& c, const BitMap& k) {
+    std::vector<std::pair<int, int>> v;
+    expand_map(c, v);
+    expand_map(k, v);
+    uint64_t used = 0;
+    for (auto& p : v) used |= uint64_t(1) << p.second;
+    return __builtin_popcountll(used);
+}
+
+// Consecutive (src, dst) pairs with both sides increasing by one collapse into one run.
+bool make_runs(const std::vector<std::pair<int, int>>& pairs, BitMap* m) {
+    m->n = 0;
+    for (size_t i = 0; i < pairs.size();) {
+        size_t j = i + 1;
+        while (j < pairs.size() && pairs[j].first == pairs[j - 1].first + 1 && pairs[j].second == pairs[j - 1].second + 1)
+            j++;
+        if (m->n >= kMaxRuns) return false;
+        m->r[m->n] = Run{(uint8_t)pairs[i].first, (uint8_t)(j - i), (uint8_t)pairs[i].second, 0};
+        m->n++;
+        i = j;
+    }
+    return true;
+}
+
+// Fill the row form of a step when its smaller operand fits in shared memory and K <= kmax.
+bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra) {
+    if (a.nk > 31 || (int64_t(1) << a.nk) > kmax) return false;
+    const int abits = dst_bits(a.cA, a.kA), bbits = dst_bits(a.cB, a.kB);
+    const bool x_is_a = abits >= bbits;
+    const int ybits = x_is_a ? bbits : abits;
+    if (ybits > 11 || (int64_t(1) << ybits) > kRowMaxY) return false;
+    const BitMap& cX = x_is_a ? a.cA : a.cB;
+    const BitMap& cY = x_is_a ? a.cB : a.cA;
+    int ncb = 0;
+    while ((int64_t(1) << ncb) < a.nC) ncb++;
+    std::vector<int> inx(ncb, 0), iny(ncb, 0);
+    std::vector<std::pair<int, int>> v;
+    expand_map(cX, v);
+    for (auto& p : v) if (p.first < ncb) inx[p.first] = 1;
+    v.clear();
+    expand_map(cY, v);
+    for (auto& p : v) if (p.first < ncb) iny[p.first] = 1;
+    std::vector<std::pair<int, int>> rows, cols;
+    for (int p = 0; p < ncb; p++) {
+        if (iny[p] && !inx[p]) cols.push_back({(int)cols.size(), p});
+        else rows.push_back({(int)rows.size(), p});
+    }
+    if ((int64_t(1) << cols.size()) > kRowMaxN) return false;
+    // a thread writes its N results one after another: wide rows need many of them
+    if (cols.size() > 5 && rows.size() < 16) return false;
+    memset(ra, 0, sizeof(*ra));
+    if (!make_runs(rows, &ra->rowmap) || !make_runs(cols, &ra->nmap)) return false;
+    ra->X = x_is_a ? a.A : a.B;
+    ra->Y = x_is_a ? a.B : a.A;
+    ra->C = a.C;
+    ra->nrows = int64_t(1) << rows.size();
+    ra->N = 1 << (int)cols.size();
+    ra->K = 1 << a.nk;
+    ra->ny = 1 << ybits;
+    ra->conjX = x_is_a ? a.conjA : a.conjB;
+    ra->conjY = x_is_a ? a.conjB : a.conjA;
+    ra->expX = x_is_a ? a.expA : a.expB;
+    ra->expY = x_is_a ? a.expB : a.expA;
+    ra->expC = a.expC;
+    ra->cX = cX;
+    ra->cY = cY;
+    ra->kX = x_is_a ? a.kA : a.kB;
+    ra->kY = x_is_a ? a.kB : a.kA;
+    return true;
+}
+
+template <int CONJ>
+void launch_general(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int grid) {
+    if (fp64) contract_kernel<double2, false, CONJ><<<grid, kThreads, 0, s>>>(a, exps);
+    else if (exps) contract_kernel<float2, true, CONJ><<<grid, kThreads, 0, s>>>(a, exps);
+    else contract_kernel<float2, false, CONJ><<<grid, kThreads, 0, s>>>(a, exps);
+}
+
+template <typename T, int KMAX>
+cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_count) {
+    const size_t smem = (size_t)ra.ny * sizeof(T) + (size_t)KMAX * 12 + (size_t)ra.N * 12;
+    const int64_t want = (ra.nrows + kThreads - 1) / kThreads;
+    const int64_t cap = (int64_t)sm_count * 8;
+    const int grid = (int)std::max<int64_t>(1, std::min(want, cap));
+    if (sizeof(T) == 16) contract_rows_kernel<T, false, KMAX><<<grid, kThreads, smem, s>>>(ra, exps);
+    else if (exps) contract_rows_kernel<T, true, KMAX><<<grid, kThreads, smem, s>>>(ra, exps);
+    else contract_rows_kernel<T, false, KMAX><<<grid, kThreads, smem, s>>>(ra, exps);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count) {
+    RowArgs ra;
+    if (plan_rows(a, fp64 ? 16 : 32, &ra)) {
+        if (fp64) return ra.K <= 4 ? launch_rows<double2, 4>(ra, exps, s, sm_count)
+                                   : launch_rows<double2, 16>(ra, exps, s, sm_count);
+        if (ra.K <= 4) return launch_rows<float2, 4>(ra, exps, s, sm_count);
+        if (ra.K <= 16) return launch_rows<float2, 16>(ra, exps, s, sm_count);
+        return launch_rows<float2, 32>(ra, exps, s, sm_count);
+    }
     int ncb = 0;
     while ((int64_t(1) << ncb) < a.nC) ncb++;
     const int tb = ncb < kTileBits ? ncb : kTileBits;
     const int64_t ntiles = a.nC >> tb;
     const int64_t cap = (int64_t)sm_count * 8;
     const int grid = (int)(ntiles < cap ? ntiles : cap);
-    if (fp64) contract_kernel<double2, false><<<grid, kThreads, 0, s>>>(a, exps);
-    else if (exps) contract_kernel<float2, true><<<grid, kThreads, 0, s>>>(a, exps);
-    else contract_kernel<float2, false><<<grid, kThreads, 0, s>>>(a, exps);
+    const int conj = (a.conjA ? 1 : 0) | (a.conjB ? 2 : 0);
+    switch (conj) {
+        case 0: launch_general<0>(a, fp64, exps, s, grid); break;
+        case 1: launch_general<1>(a, fp64, exps, s, grid); break;
+        case 2: launch_general<2>(a, fp64, exps, s, grid); break;
+        default: launch_general<3>(a, fp64, exps, s, grid); break;
+    }
     return cudaGetLastError();
 }
 
