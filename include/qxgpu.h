@@ -198,6 +198,14 @@ int qxg_program_profile(qxg_program* prog, int32_t enable);
 int qxg_program_profile_read(qxg_program* prog, qxg_step_profile* out, int32_t max_entries,
                              int32_t* n_entries, int64_t* kernel_launches);
 
+/* Describe, as one line of text, how the current forward plan executes command `instr`: the
+ * kernel path (tensor-core variant, row form or general CUDA-core contraction), the batch / free /
+ * summed bit counts, and for tensor-core steps which index bit of the larger operand lies at each
+ * of its address bits (from the lowest).  Writes at most len bytes (NUL-terminated) to buf and
+ * returns 0; QXG_ERR_INVALID when the command is not an executed `ncon` of the plan (no plan is
+ * built before the first amplitudes call).  A diagnostic with no counterpart in the reference. */
+int qxg_program_explain(const qxg_program* prog, int32_t instr, char* buf, int32_t len);
+
 /* Free the device buffers, graphs and stream of a programme.  Accepts NULL. */
 void qxg_program_destroy(qxg_program* prog);
 

@@ -62,7 +62,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> Path:
     with ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = BUILD / "libqxgpu.so.tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcuda"]
+    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

@@ -514,6 +514,11 @@ cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_cou
 
 }  // namespace
 
+bool contract_uses_rows(const StepArgs& a, bool fp64) {
+    RowArgs ra;
+    return plan_rows(a, fp64 ? 16 : 32, &ra);
+}
+
 cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count) {
     RowArgs ra;
     if (plan_rows(a, fp64 ? 16 : 32, &ra)) {

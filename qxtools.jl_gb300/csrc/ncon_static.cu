@@ -99,7 +99,7 @@ extern "C" int qxg_ncon_tc_static(int32_t precision, void* C, int32_t nc, const 
     // exponent slots start at zero: operands enter unscaled and the result is stored as is
     e = cudaMemsetAsync(exps, 0, kExpBytes, st);
     if (e == cudaSuccess) e = tc_run_pack(t, s, exps, planes, st, sms);
-    if (e == cudaSuccess) e = tc_run_gemm(t, s, exps, planes, st);
+    if (e == cudaSuccess) e = tc_run_gemm(t, s, exps, planes, st, sms);
     if (e != cudaSuccess) return ncon_fail(QXG_ERR_CUDA, cudaGetErrorString(e));
     return QXG_OK;
 }

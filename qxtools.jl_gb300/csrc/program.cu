@@ -91,6 +91,7 @@ struct Step {                           // an executable item of a pass
     LeafGradArgs largs;
     bool use_tc = false;                // tensor-core path (split modes)
     bool tc_tuned = false;              // the tile variant has been chosen
+    std::string tune_note;              // autotuner: milliseconds per candidate variant
     TcStep tc;                          // tensor-core step description
     double flops = 0, bytes = 0;
 };
@@ -157,6 +158,7 @@ struct qxg_program {
     std::vector<int> h_exps_init;
     // tensor-core autotuner: chosen variant per step shape + bit maps, events for timing
     std::map<std::string, TcVariant> tune_cache;
+    std::map<std::string, std::string> tune_notes;
     cudaEvent_t tune_ev[2] = {nullptr, nullptr};
     int tuned_steps = 0;                // steps whose variant was picked by timing
     // profiling: CUDA events around launches, aggregated per command on read
@@ -1026,6 +1028,7 @@ int tune_tc_step(qxg_program* P, Step& st, int* exps) {
     auto it = P->tune_cache.find(key);
     if (it != P->tune_cache.end()) {
         tc_set_variant(st.tc, it->second);
+        st.tune_note = P->tune_notes[key];
         return 0;
     }
     TcVariant cand[kTcMaxVariants];
@@ -1045,18 +1048,25 @@ int tune_tc_step(qxg_program* P, Step& st, int* exps) {
                 QXG_CUDA(cudaMemsetAsync(cslot, 0x80, sizeof(int), P->stream));   // kExpUnset
                 QXG_CUDA(cudaEventRecord(P->tune_ev[0], P->stream));
                 QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
-                QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream));
+                QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
                 QXG_CUDA(cudaEventRecord(P->tune_ev[1], P->stream));
             }
             QXG_CUDA(cudaEventSynchronize(P->tune_ev[1]));
             QXG_CUDA(cudaEventElapsedTime(&ms, P->tune_ev[0], P->tune_ev[1]));
             if (!have || ms < best_ms) { best_ms = ms; best = cand[i]; have = true; }
+            char note[64];
+            snprintf(note, sizeof(note), "%s%s%d:%.3fms", st.tune_note.empty() ? "" : ",",
+                     cand[i].fused ? (cand[i].tma ? "tma" : (cand[i].tmem ? "tmem" : (cand[i].bulk ? "bulk" : "rows")))
+                                   : "planes",
+                     cand[i].ntile, ms);
+            st.tune_note += note;
         }
         QXG_CUDA(cudaMemsetAsync(cslot, 0x80, sizeof(int), P->stream));
         P->tuned_steps++;
     }
     tc_set_variant(st.tc, best);
     P->tune_cache[key] = best;
+    P->tune_notes[key] = st.tune_note;
     return 0;
 }
 
@@ -1130,7 +1140,7 @@ int run_group_eager(qxg_program* P, int g, Plan* plp) {
                 if (int r = prof_end(P, ev, instr, QXG_KERNEL_TC_PACK, 0.0, pack_bytes)) return r;
                 if (int r = prof_begin(P, &ev)) return r;
                 kind = QXG_KERNEL_CONTRACT_TC;
-                QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream));
+                QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
             } else {
                 kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
                 QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count));
@@ -1273,7 +1283,7 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
                 if (st.bkind == kBwdNcon) {
                     if (st.use_tc) {
                         QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
-                        QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream));
+                        QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
                         kind = QXG_KERNEL_CONTRACT_TC;
                     } else {
                         QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count));
@@ -1618,6 +1628,51 @@ int qxg_program_profile_read(qxg_program* P, qxg_step_profile* out, int32_t max_
     if (n_entries) *n_entries = n;
     if (kernel_launches) *kernel_launches = P->launches;
     return QXG_OK;
+}
+
+int qxg_program_explain(const qxg_program* P, int32_t instr, char* buf, int32_t len) {
+    if (!P || !buf || len <= 0) return fail(QXG_ERR_INVALID, "explain: null programme or buffer");
+    if (!P->plan) return fail(QXG_ERR_INVALID, "explain: no plan yet (run amplitudes first)");
+    const Plan& pl = *P->plan;
+    const Step* found = nullptr;
+    int group = -1;
+    for (int g = 0; g < 3 && !found; g++)
+        for (auto& st : pl.steps[g])
+            if (st.kind == QXG_OP_NCON && pl.T[st.tensor].instr == instr) { found = &st; group = g; break; }
+    if (!found) return fail(QXG_ERR_INVALID, "explain: instruction " + std::to_string(instr) + " is not an executed ncon");
+    const Step& st = *found;
+    static const char* gname[3] = {"invariant", "slice", "bitstring"};
+    std::string d = "instr " + std::to_string(instr) + " group " + gname[group] + " ";
+    auto bits_of_map = [](const BitMap& m, char cls, std::vector<std::string>& at) {
+        for (int i = 0; i < m.n; i++)
+            for (int j = 0; j < m.r[i].len; j++) {
+                const int dst = m.r[i].dst + j;
+                if ((int)at.size() <= dst) at.resize(dst + 1, "-");
+                at[dst] = std::string(1, cls) + std::to_string(m.r[i].src + j);
+            }
+    };
+    if (st.use_tc) {
+        const TcStep& t = st.tc;
+        d += std::string("tensor-core ") + (t.tf32 ? "3xTF32 " : "3xBF16 ") + (t.fused ? (t.tma ? "tma-gather" : (t.tmem ? "tmem-gather" : (t.bulk ? "bulk-gather" : "row-gather"))) : "planes") +
+             " ntile=" + std::to_string(t.ntile_n) + " nb=" + std::to_string(t.nb) + " nm=" + std::to_string(t.nm) +
+             " nn=" + std::to_string(t.nn) + " nk=" + std::to_string(t.nk) + " X=" + (t.x_is_a ? "A" : "B") +
+             " x_bits=";
+        std::vector<std::string> at;
+        bits_of_map(t.xb, 'b', at); bits_of_map(t.xm, 'm', at); bits_of_map(t.xk, 'k', at);
+        for (size_t i = 0; i < at.size(); i++) d += (i ? "," : "") + at[i];
+        d += " c_bits=";
+        at.clear();
+        bits_of_map(t.cb, 'b', at); bits_of_map(t.cm, 'm', at); bits_of_map(t.cn, 'n', at);
+        for (size_t i = 0; i < at.size(); i++) d += (i ? "," : "") + at[i];
+        if (!st.tune_note.empty()) d += " tuned=" + st.tune_note;
+    } else {
+        d += contract_uses_rows(st.sargs, P->fp64) ? "cuda-core row-form" : "cuda-core general";
+        int ncb = 0;
+        while ((int64_t(1) << ncb) < st.sargs.nC) ncb++;
+        d += " c_bits=" + std::to_string(ncb) + " nk=" + std::to_string(st.sargs.nk);
+    }
+    snprintf(buf, (size_t)len, "%s", d.c_str());
+    return 0;
 }
 
 void qxg_program_destroy(qxg_program* P) {

@@ -145,6 +145,8 @@ struct ReduceArgs {
 
 // Kernel launchers (kernels_simt.cu).  Storage: double2 when fp64 != 0, else float2.
 cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count);
+// Whether launch_contract runs a step in the row form (smaller operand staged in shared memory).
+bool contract_uses_rows(const StepArgs& a, bool fp64);
 cudaError_t launch_view(const ViewArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_output(const OutputArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_reduce(const ReduceArgs& a, bool fp64, const int* exps, cudaStream_t s);

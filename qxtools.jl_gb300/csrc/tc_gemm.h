@@ -27,6 +27,17 @@ struct TcStep {
     bool x_is_a = true;             // the larger operand (M side) is the step's A
     bool tf32 = false;
     bool fused = true;              // the GEMM gathers and splits X itself (no X planes in scratch)
+    bool bulk = false;              // fused, with X's contiguous segments fetched by cp.async.bulk
+    bool tmem = false;              // fused row gather, A tiles in tensor memory
+    bool tma = false;               // fused TMA tensor gather, A tiles in tensor memory
+    bool tma_ok = false;            // X's blocks fit one 5-D TMA box (see tc_gemm.cu)
+    int tma_npiece = 0;             // TMA box: runs of the block's address bits (<= 4 pieces of <= 8 bits)
+    int tma_pos[4] = {0, 0, 0, 0}, tma_len[4] = {0, 0, 0, 0};
+    int tma_lead = 0;               // the block holds X's address bits 0 .. tma_lead-1
+    bool bulk_ok = false;           // X's (128 rows x chunk) blocks are segments of >= 16 elements
+    bool bfast = false;             // X's lowest address bit is a batch bit (tile order: batch first)
+    BitMap segmap, rowmap_c, kmap_c;   // bulk gather plan (see tc_gemm.cu)
+    int seg_bits = 0, nseg = 0;
     bool planes_ok = false;         // the planes variant's scratch fits the cap
     int nb = 0, nm = 0, nn = 0, nk = 0;        // bits of batch, M, N, K
     int64_t M = 0, N = 0, K = 0, batch = 0;
@@ -42,11 +53,14 @@ struct TcStep {
     size_t scratch_max = 0;         // the largest scratch of any candidate variant
 };
 
-// A tile variant of a tensor-core step: X gathered in the GEMM (fused) or packed into planes
-// first, and the complex columns per N tile.
+// A tile variant of a tensor-core step: X gathered in the GEMM (fused: by rows or by contiguous
+// segments) or packed into planes first, and the complex columns per N tile.
 struct TcVariant {
     bool fused;
     int ntile;
+    bool bulk;                      // fused only: bulk segment gather instead of row gather
+    bool tmem;                      // fused only: row gather with the A tiles in tensor memory
+    bool tma;                       // fused only: TMA tensor gather, A tiles in tensor memory
 };
 
 // Decide whether a step goes to the tensor cores; fills `tc` (default variant: fused, the
@@ -54,7 +68,7 @@ struct TcVariant {
 bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits, bool tf32, TcStep* tc);
 
 // Candidate variants of a planned step (at most kTcMaxVariants), for the autotuner.
-constexpr int kTcMaxVariants = 6;
+constexpr int kTcMaxVariants = 12;
 int tc_variants(const TcStep& t, TcVariant* out);
 
 // Switch a planned step to a variant (recomputes tile counts and scratch sizes).
@@ -67,7 +81,8 @@ std::string tc_key(const TcStep& t);
 // tc_run_pack (both operands) then tc_run_gemm.
 cudaError_t tc_run_pack(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
                         int sm_count);
-cudaError_t tc_run_gemm(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st);
+cudaError_t tc_run_gemm(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
+                        int sm_count);
 
 // Device error word set by a tensor-core kernel whose bounded wait gave up (0 = none).
 cudaError_t tc_read_error(int* host_code, cudaStream_t st);

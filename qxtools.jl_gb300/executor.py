@@ -101,6 +101,7 @@ def load_library(path=None):
                                  ct.POINTER(ct.c_double), ct.POINTER(ct.c_double)]
     lib.qxg_gradient.restype = ct.c_int
     lib.qxg_program_profile.argtypes = [P, ct.c_int32]
+    lib.qxg_program_explain.argtypes = [P, ct.c_int32, ct.c_char_p, ct.c_int32]
     lib.qxg_program_profile_read.argtypes = [P, ct.POINTER(qxg_step_profile), ct.c_int32, ct.POINTER(ct.c_int32),
                                              ct.POINTER(ct.c_int64)]
     lib.qxg_last_error.restype = ct.c_char_p
@@ -369,6 +370,12 @@ class Executor:
         rows = [{"instr": b.instr, "kernel": KERNEL_KINDS.get(b.kernel, str(b.kernel)), "launches": b.launches,
                  "ms": b.ms, "flops": b.flops, "bytes": b.bytes} for b in buf[:n.value]]
         return rows, launches.value
+
+    def explain(self, instr: int) -> str:
+        """One line on how the current plan executes `ncon` command `instr` (qxg_program_explain)."""
+        buf = ct.create_string_buffer(4096)
+        _check(self.lib, self.lib.qxg_program_explain(self._h, int(instr), buf, len(buf)))
+        return buf.value.decode()
 
     @property
     def stream(self) -> int:

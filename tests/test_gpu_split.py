@@ -15,14 +15,17 @@ pytestmark = pytest.mark.gpu
 TOL = {"split_tf32": 5e-6, "split_bf16": 1e-4, "fp32": 5e-6}
 
 
-def single_ncon_programme(q, nm, nk, nn, nbatch=0, seed=0, scale=1.0):
-    """C[m.., n.., b..] = sum_k A[m.., k.., b..] B[k.., n.., b..] with dim-2 labels."""
+def single_ncon_programme(q, nm, nk, nn, nbatch=0, seed=0, scale=1.0, a_order="mkb"):
+    """C[m.., n.., b..] = sum_k A[m.., k.., b..] B[k.., n.., b..] with dim-2 labels; a_order
+    permutes A's label groups (its lowest address bits: m, k or batch)."""
     rng = np.random.default_rng(seed)
     lm = list(range(1, nm + 1))
     lk = list(range(nm + 1, nm + nk + 1))
     ln = list(range(nm + nk + 1, nm + nk + nn + 1))
     lb = list(range(nm + nk + nn + 1, nm + nk + nn + nbatch + 1))
-    la, lbb, lc = lm + lk + lb, lk + ln + lb, lm + ln + lb
+    groups = {"m": lm, "k": lk, "b": lb}
+    la = [l for g in a_order for l in groups[g]]
+    lbb, lc = lk + ln + lb, lm + ln + lb
     A = (rng.standard_normal((2,) * len(la)) + 1j * rng.standard_normal((2,) * len(la))) * scale
     B = (rng.standard_normal((2,) * len(lbb)) + 1j * rng.standard_normal((2,) * len(lbb))) * scale
     cmds = [q.Load("a", "data_1", A.shape), q.Load("b", "data_2", B.shape),
@@ -86,17 +89,22 @@ def test_tensor_core_error_at_large_k(q, gpu_lib, precision):
 
 
 @pytest.mark.parametrize("precision", ["split_tf32", "split_bf16"])
-@pytest.mark.parametrize("nm,nk,nn,nb", [(8, 9, 6, 0), (7, 3, 7, 1), (9, 6, 2, 0)])
-def test_every_tile_variant_matches(q, gpu_lib, precision, nm, nk, nn, nb):
-    """Each candidate tile variant (fused X gather or X planes; N tiles of 16/32/64), forced with
-    tc_tuning = k, and the autotuned choice give the einsum result within the split tolerance.
-    Shapes cover K chunks beyond the gather ring (nk=9), K below one chunk (nk=3 with 3xBF16),
-    a batch bit, and N narrower than the smallest tile (nn=2)."""
-    prog, ref = single_ncon_programme(q, nm, nk, nn, nb, seed=nm + 7 * nk + 31 * nn)
-    for k in ["auto", 1, 2, 3, 4, 5, 6]:
+@pytest.mark.parametrize("nm,nk,nn,nb,order", [(8, 9, 6, 0, "mkb"), (7, 3, 7, 1, "mkb"), (9, 6, 2, 0, "mkb"),
+                                               (7, 6, 6, 0, "kmb"), (8, 4, 5, 2, "bmk"), (8, 5, 6, 1, "kbm")])
+def test_every_tile_variant_matches(q, gpu_lib, precision, nm, nk, nn, nb, order):
+    """Each candidate tile variant (X gathered in the GEMM by contiguous segments or by rows, or
+    packed into planes first; N tiles of 16/32/64), forced with tc_tuning = k, and the autotuned
+    choice give the einsum result within the split tolerance.  Shapes cover K chunks beyond the
+    gather ring (nk=9), K below one chunk (nk=3 with 3xBF16), batch bits, N narrower than the
+    smallest tile (nn=2), and larger operands whose lowest address bits are summed (segments of
+    rows and k values interleaved) or batch bits (batch-first tile order, no segment gather)."""
+    prog, ref = single_ncon_programme(q, nm, nk, nn, nb, seed=nm + 7 * nk + 31 * nn, a_order=order)
+    for k in ["auto"] + list(range(1, 13)):
         with q.Executor(prog, precision=precision, tc_tuning=k) as ex:
             got = ex.amplitudes([""])[0]
             info = ex.info()
+            desc = ex.explain(2)                 # the ncon command
+        assert "tensor-core" in desc and f"nk={nk}" in desc, desc
         assert info["num_steps_tensor_core"] == 1
         err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
         assert err <= TOL[precision], (k, err)
