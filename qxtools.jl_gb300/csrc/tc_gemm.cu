@@ -37,8 +37,9 @@ constexpr int kModeRows = 1;      // X rows gathered by 8-byte cp.async in the k
 constexpr int kModeBulk = 2;      // X's contiguous segments fetched by cp.async.bulk, then split
 constexpr int kModeTmem = 3;      // as kModeRows, but the split A tiles go to tensor memory
 constexpr int kModeTma = 4;       // X's blocks fetched by one TMA tensor copy each, split into tensor memory
+// kModeTma runs two groups of four split warps (7-10 and 11-14) on alternate chunks
 constexpr int threads_of(int mode) {
-    return mode == kModePlanes ? 192 : ((mode == kModeBulk || mode == kModeTma) ? 352 : 320);
+    return mode == kModePlanes ? 192 : (mode == kModeBulk ? 352 : (mode == kModeTma ? 480 : 320));
 }
 constexpr int kATmemCols = 32;    // tensor-memory columns of one A stage (hi and lo, 16 each)
 constexpr int kMaxRing = 8;                              // raw X chunks in a gather ring
@@ -418,7 +419,7 @@ __device__ __forceinline__ void split_row_words(Get get, bool row_ok, int64_t k0
 //   warp 6          (kModeBulk) fetch X's contiguous segments into a ring with cp.async.bulk
 //   warps 7-10      (kModeBulk) split the ring's chunks and store the A tiles
 template <bool TF32, int MODE>
-__global__ void __launch_bounds__(threads_of(MODE), 2)
+__global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
     tc_gemm_kernel(const GemmArgs g, const __grid_constant__ CUtensorMap tmap) {
     constexpr bool FUSED = MODE != kModePlanes;
     constexpr bool ROWS = MODE == kModeRows || MODE == kModeTmem;
@@ -493,7 +494,7 @@ __global__ void __launch_bounds__(threads_of(MODE), 2)
         for (int j = threadIdx.x - 64; j < g.ntile; j += 128) jtab[j] = pdep(j, g.cn);
     if (ROWS && threadIdx.x >= 192 && threadIdx.x < 192 + KC)
         xkoff[threadIdx.x - 192] = pdep(threadIdx.x - 192, g.xk);
-    if (SEGS && threadIdx.x >= 224) {
+    if (SEGS && threadIdx.x >= 224 && threadIdx.x < 224 + 128) {
         // byte of compact index c in a slot: segment c >> seg_bits, element c & (2^seg_bits - 1)
         const int r = threadIdx.x - 224;
         auto slot_byte = [&](int64_t c) {
@@ -770,11 +771,15 @@ __global__ void __launch_bounds__(threads_of(MODE), 2)
         const float s = pow2f(-read_m(g.exps, g.x_slot));
         const float si = g.x_conj ? -s : s;
         const int rb = rtab[row];
-        int slot = 0, st_i = 0;
+        // group grp of NG takes chunks grp, grp + NG, ...; slot, stage and chunk advance by NG
+        constexpr int NG = MODE == kModeTma ? 2 : 1;
+        const int grp = (warp - 7) / 4;
+        int slot = grp, st_i = grp;
         uint32_t rph = 0, ph = 0;
-        int64_t c = 0;
+        int64_t c = grp;
+        while (c >= g.kchunks) c -= g.kchunks;
         const int64_t Q = ntl * g.kchunks;
-        for (int64_t qq = 0; qq < Q; qq++) {
+        for (int64_t qq = grp; qq < Q; qq += NG) {
             const bool ok = mbar_wait(&rfull[slot], rph) && mbar_wait(&empty[st_i], ph ^ 1u);
             if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 7); break; }
             if (__any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) break;
@@ -799,9 +804,12 @@ __global__ void __launch_bounds__(threads_of(MODE), 2)
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&fullA[st_i])) : "memory");
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&rempty[slot])) : "memory");
             }
-            if (++slot == R) { slot = 0; rph ^= 1u; }
-            if (++st_i == NS) { st_i = 0; ph ^= 1u; }
-            if (++c == g.kchunks) c = 0;
+            slot += NG;
+            if (slot >= R) { slot -= R; rph ^= 1u; }
+            st_i += NG;
+            if (st_i >= NS) { st_i -= NS; ph ^= 1u; }
+            c += NG;
+            while (c >= g.kchunks) c -= g.kchunks;
         }
     } else if (warp >= 2 && warp < 6) {
         // epilogue: warp w reads tensor-memory lanes 32*(w%4) .. +31 of buffer (tile & 1)
@@ -1274,8 +1282,8 @@ cudaError_t tc_run_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scr
         g.rowmap_c = t.rowmap_c;
         g.kmap_c = t.kmap_c;
         g.slot_bytes = (g.box_bytes + 127) / 128 * 128;
-        g.ring_chunks = std::min(kMaxRing, sh.ring_bytes / g.slot_bytes);
-        if (g.ring_chunks < 2) return cudaErrorInvalidValue;
+        g.ring_chunks = std::min(kMaxRing, sh.ring_bytes / g.slot_bytes) & ~1;   // even: two split groups
+        if (g.ring_chunks < 2 || (g.stages & 1)) return cudaErrorInvalidValue;
         sh.ring_bytes = g.ring_chunks * g.slot_bytes;
     }
     if (mode == kModeRows || mode == kModeTmem) g.ring_chunks = sh.ring_bytes / (kTcTileM * t.kc * 8);
