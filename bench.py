@@ -409,7 +409,9 @@ def run_gradient(args):
     torch.cuda.set_device(0)
     circ = q.create_parametrised_circuit(5, 5, 12, seed=args.seed)
     bits = list(q.amplitudes_uniform(25, args.seed, 256))
-    f = q.gradients.ParametrisedCircuitLoss(circ, seed=args.seed, time=2, precision=args.precision)
+    # planned like the param_5x5_l12 workload: 8 x 16 greedy trials, FLOPs first within 2^28
+    plan_opts = dict(seed=args.seed, time=16, width_cap=q.workloads.WIDTH_CAP)
+    f = q.gradients.ParametrisedCircuitLoss(circ, precision=args.precision, **plan_opts)
     for _ in range(max(1, args.warmup)):
         f.executor.amplitudes(bits)
         f.loss_and_grad(bits)
@@ -423,7 +425,7 @@ def run_gradient(args):
         L, g, _ = f.loss_and_grad(bits)
     grad = (time.perf_counter() - t0) / args.steps
     sub = bits[:8]
-    ref = q.gradients.ParametrisedCircuitLoss(circ, seed=args.seed, time=2, precision="fp64")
+    ref = q.gradients.ParametrisedCircuitLoss(circ, precision="fp64", **plan_opts)
     _, g64, _ = ref.loss_and_grad(sub)
     _, gs, _ = f.loss_and_grad(sub)
     ref.close()

@@ -86,7 +86,9 @@ typedef struct qxg_options {
                                      the first time it runs and keep the fastest (default);
                                      k >= 1 = candidate k of every step (1: fused X gather, widest
                                      N tile; then narrower tiles, then the X-planes variants) */
-    int32_t reserved[6];
+    int32_t tc_plane_budget_mb;   /* packed planes of a tensor-core step's smaller operand beyond which
+                                     its free columns are processed in blocks; 0 = 4096 MiB */
+    int32_t reserved[5];
 } qxg_options;
 
 typedef struct qxg_program qxg_program;
@@ -231,8 +233,9 @@ int qxg_ncon(int32_t precision,
  * hi/lo operand planes live in one file-scope device array of QXG_TC_STATIC_SCRATCH_BYTES that
  * every GPU loading the library holds until the process exits; a shape whose planes do not fit
  * is rejected with QXG_ERR_UNSUPPORTED and a message, and so is a shape the tensor cores do not
- * serve (fewer than 128 free rows on the larger operand, a summed extent below 8, or a smaller
- * operand with fewer than 4 free columns).  Arguments are those of qxg_ncon with precision
+ * serve (fewer than 128 free rows on the larger operand -- 16 when the summed extent is above
+ * 1024 --, a summed extent below 8, or a smaller operand with fewer than 4 free columns); sums
+ * longer than 1024 are cut into blocks whose partial results are added in a fixed order.  Arguments are those of qxg_ncon with precision
  * QXG_PREC_SPLIT_BF16 or QXG_PREC_SPLIT_TF32 (float2 storage).  The first call on a device looks
  * up the array's device address (make that first call before any stream capture).  Every call on
  * a device shares that device's array, which keeps the last call's contents: calls that can

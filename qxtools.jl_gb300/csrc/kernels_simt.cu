@@ -208,6 +208,95 @@ __global__ void __launch_bounds__(kThreads) contract_rows_kernel(const RowArgs a
     }
 }
 
+// Split-K form of a contraction with few results and a long sum (the adjoint steps that end in
+// gate-sized leaf gradients sum over every other index of the network).  Pass 1: block
+// (result tile, split) sums the split's range of the high K index (all 2^nkt low K values) for
+// up to kSplitTile results, its threads grouped by result, and writes one partial per result;
+// pass 2 adds the partials of each result in split order (deterministic), scales, stores and
+// raises the exponent slot like the general kernel.
+constexpr int kSplitTile = 256;         // results per block of pass 1
+
+template <typename T, int CONJ>
+__global__ void __launch_bounds__(kThreads) contract_splitk_kernel(const StepArgs a, int nsplit, T* partial) {
+    using R = typename Real<T>::type;
+    __shared__ int64_t tA[1 << kKTableBits], tB[1 << kKTableBits];
+    __shared__ R red[2][kThreads];
+    const int nkt = a.nk < kKTableBits ? a.nk : kKTableBits;
+    const int KT = 1 << nkt;
+    const int64_t KO = int64_t(1) << (a.nk - nkt);
+    for (int k = threadIdx.x; k < KT; k += kThreads) { tA[k] = pdep(k, a.kA); tB[k] = pdep(k, a.kB); }
+    __syncthreads();
+    const int64_t ntile = (a.nC + kSplitTile - 1) / kSplitTile;
+    const int64_t tile = blockIdx.x % ntile;
+    const int split = (int)(blockIdx.x / ntile);
+    const int64_t c0 = tile * kSplitTile;
+    const int nres = (int)(a.nC - c0 < kSplitTile ? a.nC - c0 : kSplitTile);
+    const int per = kThreads / nres;        // threads per result (>= 1)
+    const int r = threadIdx.x % nres, sub = threadIdx.x / nres;
+    const bool active = sub < per;
+    const int64_t ko0 = KO * split / nsplit, ko1 = KO * (split + 1) / nsplit;
+    R re = R(0), im = R(0);
+    if (active) {
+        const int64_t c = c0 + r;
+        const int64_t a0 = pdep(c, a.cA), b0 = pdep(c, a.cB);
+        for (int64_t ko = ko0; ko < ko1; ko++) {
+            const int64_t ah = a0 + (ko ? pdep(ko << nkt, a.kA) : 0);
+            const int64_t bh = b0 + (ko ? pdep(ko << nkt, a.kB) : 0);
+            for (int k = sub; k < KT; k += per) {
+                const T x = static_cast<const T*>(a.A)[ah + tA[k]];
+                const T y = static_cast<const T*>(a.B)[bh + tB[k]];
+                const R xi = (CONJ & 1) ? -x.y : x.y, yi = (CONJ & 2) ? -y.y : y.y;
+                re = fma(x.x, y.x, re);
+                re = fma(-xi, yi, re);
+                im = fma(x.x, yi, im);
+                im = fma(xi, y.x, im);
+            }
+        }
+    }
+    red[0][threadIdx.x] = re;
+    red[1][threadIdx.x] = im;
+    __syncthreads();
+    if (threadIdx.x < nres) {               // fixed order over the result's threads
+        R sr = R(0), si = R(0);
+        for (int j = 0; j < per; j++) { sr += red[0][threadIdx.x + j * nres]; si += red[1][threadIdx.x + j * nres]; }
+        T out; out.x = sr; out.y = si;
+        partial[(int64_t)split * a.nC + c0 + threadIdx.x] = out;
+    }
+}
+
+template <typename T, bool SCALED>
+__global__ void splitk_reduce_kernel(const StepArgs a, int nsplit, const T* partial, int* exps) {
+    using R = typename Real<T>::type;
+    R scale = R(1);
+    if (SCALED) {
+        const int mA = read_m(exps, a.expA), mB = read_m(exps, a.expB);
+        scale = (R)pow2f(-(mA + mB));
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            exps[2 * a.expC] = exps[2 * a.expA] + exps[2 * a.expB] + mA + mB;
+    }
+    int emax = kExpUnset;
+    T* C = static_cast<T*>(a.C);
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < a.nC; c += (int64_t)gridDim.x * blockDim.x) {
+        R re = R(0), im = R(0);
+        for (int j = 0; j < nsplit; j++) {
+            const T v = partial[(int64_t)j * a.nC + c];
+            re += v.x;
+            im += v.y;
+        }
+        if (SCALED) {
+            re *= scale; im *= scale;
+            const float mx = fmaxf(fabsf((float)re), fabsf((float)im));
+            if (mx > 0.f) emax = max(emax, exp_of(mx));
+        }
+        T out; out.x = re; out.y = im;
+        C[c] = out;
+    }
+    if (SCALED) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.expC + 1], emax);
+    }
+}
+
 template <typename T>
 __global__ void view_kernel(const ViewArgs a, int* exps) {
     const T* __restrict__ S = static_cast<const T*>(a.src);
@@ -493,6 +582,21 @@ bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra) {
     return true;
 }
 
+// Splits of the split-K form: used when the results are few (<= 2^14) and each sums at least
+// 2^14 terms; enough splits of the high K index to give about 8 blocks per SM, at least 2^12
+// terms per split, and at most 2^22 partials in all.
+int splitk_count(const StepArgs& a, int sm_count) {
+    if (a.nC > (int64_t(1) << 14) || a.nk < 14) return 0;
+    const int nkt = a.nk < kKTableBits ? a.nk : kKTableBits;
+    const int64_t KO = int64_t(1) << (a.nk - nkt);
+    const int64_t ntile = (a.nC + kSplitTile - 1) / kSplitTile;
+    int64_t want = std::max<int64_t>(1, (int64_t)sm_count * 8 / ntile);
+    want = std::min<int64_t>(want, std::max<int64_t>(1, (int64_t(1) << a.nk) >> 12));
+    want = std::min<int64_t>(want, KO);
+    want = std::min<int64_t>(want, std::max<int64_t>(1, (int64_t(1) << 22) / a.nC));
+    return (int)want;
+}
+
 template <int CONJ>
 void launch_general(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int grid) {
     if (fp64) contract_kernel<double2, false, CONJ><<<grid, kThreads, 0, s>>>(a, exps);
@@ -514,13 +618,50 @@ cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_cou
 
 }  // namespace
 
+size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
+    RowArgs ra;
+    if (plan_rows(a, fp64 ? 16 : 32, &ra)) return 0;
+    const int ns = splitk_count(a, sm_count);
+    return ns > 0 ? (size_t)ns * (size_t)a.nC * (fp64 ? 16 : 8) : 0;
+}
+
+template <typename T, int CONJ>
+void launch_splitk_t(const StepArgs& a, int ns, T* partial, int* exps, cudaStream_t s) {
+    const int64_t ntile = (a.nC + kSplitTile - 1) / kSplitTile;
+    contract_splitk_kernel<T, CONJ><<<(unsigned)(ntile * ns), kThreads, 0, s>>>(a, ns, partial);
+}
+
+template <typename T>
+cudaError_t launch_splitk(const StepArgs& a, int ns, void* scratch, int* exps, cudaStream_t s) {
+    T* partial = static_cast<T*>(scratch);
+    switch ((a.conjA ? 1 : 0) | (a.conjB ? 2 : 0)) {
+        case 0: launch_splitk_t<T, 0>(a, ns, partial, exps, s); break;
+        case 1: launch_splitk_t<T, 1>(a, ns, partial, exps, s); break;
+        case 2: launch_splitk_t<T, 2>(a, ns, partial, exps, s); break;
+        default: launch_splitk_t<T, 3>(a, ns, partial, exps, s); break;
+    }
+    const int g = grid_for(a.nC, 256, 1024);
+    if (exps && sizeof(T) == 8) splitk_reduce_kernel<T, true><<<g, 256, 0, s>>>(a, ns, partial, exps);
+    else splitk_reduce_kernel<T, false><<<g, 256, 0, s>>>(a, ns, partial, exps);
+    return cudaGetLastError();
+}
+
 bool contract_uses_rows(const StepArgs& a, bool fp64) {
     RowArgs ra;
     return plan_rows(a, fp64 ? 16 : 32, &ra);
 }
 
-cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count) {
+cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count, void* scratch,
+                            size_t scratch_bytes, int* launches) {
+    if (launches) *launches = 1;
     RowArgs ra;
+    if (!plan_rows(a, fp64 ? 16 : 32, &ra)) {
+        const int ns = splitk_count(a, sm_count);
+        if (ns > 0 && scratch && scratch_bytes >= (size_t)ns * (size_t)a.nC * (fp64 ? 16 : 8)) {
+            if (launches) *launches = 2;
+            return fp64 ? launch_splitk<double2>(a, ns, scratch, exps, s) : launch_splitk<float2>(a, ns, scratch, exps, s);
+        }
+    }
     if (plan_rows(a, fp64 ? 16 : 32, &ra)) {
         if (fp64) return ra.K <= 4 ? launch_rows<double2, 4>(ra, exps, s, sm_count)
                                    : launch_rows<double2, 16>(ra, exps, s, sm_count);

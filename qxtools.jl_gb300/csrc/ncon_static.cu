@@ -80,7 +80,8 @@ extern "C" int qxg_ncon_tc_static(int32_t precision, void* C, int32_t nc, const 
                       precision == QXG_PREC_SPLIT_TF32, &t))
         return ncon_fail(QXG_ERR_UNSUPPORTED,
                          "qxg_ncon_tc_static: shape not served by the tensor cores (needs >= 128 free rows on the "
-                         "larger operand, a summed extent >= 8 and >= 4 free columns on the smaller)");
+                         "larger operand, or >= 16 with a summed extent above 1024, a summed extent >= 8 and "
+                         ">= 4 free columns on the smaller)");
     if (t.scratch_bytes > kStaticBytes - kExpBytes) {
         std::string m = "qxg_ncon_tc_static: the packed operands need " + std::to_string(t.scratch_bytes) +
                         " bytes, more than the static scratch of " + std::to_string(kStaticBytes - kExpBytes) + " bytes";
@@ -98,8 +99,7 @@ extern "C" int qxg_ncon_tc_static(int32_t precision, void* C, int32_t nc, const 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // exponent slots start at zero: operands enter unscaled and the result is stored as is
     e = cudaMemsetAsync(exps, 0, kExpBytes, st);
-    if (e == cudaSuccess) e = tc_run_pack(t, s, exps, planes, st, sms);
-    if (e == cudaSuccess) e = tc_run_gemm(t, s, exps, planes, st, sms);
+    if (e == cudaSuccess) e = tc_run_step(t, s, exps, planes, st, sms, nullptr);
     if (e != cudaSuccess) return ncon_fail(QXG_ERR_CUDA, cudaGetErrorString(e));
     return QXG_OK;
 }

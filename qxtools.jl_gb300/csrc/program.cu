@@ -505,7 +505,8 @@ int build_backward(qxg_program* P, Plan& pl, int* err) {
         st.bytes = es * (sz(x) + sz(y) + sz(res));
         if (!P->fp64 && P->opts.precision != QXG_PREC_FP32)
             st.use_tc = tc_plan_step(st.sargs, T[x].layout.size(), T[y].layout.size(), T[res].layout.size(),
-                                     P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc);
+                                     P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc,
+                                     (double)P->opts.tc_plane_budget_mb * (1 << 20));
             if (st.use_tc) tc_fix_variant(P, st);
         pl.flops_bwd += st.flops;
         pl.bsteps.push_back(st);
@@ -744,7 +745,8 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
                             (double)st.sargs.nC);
             if (!P->fp64 && P->opts.precision != QXG_PREC_FP32)
                 st.use_tc = tc_plan_step(st.sargs, A.layout.size(), B.layout.size(), t.layout.size(),
-                                         P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc);
+                                         P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc,
+                                     (double)P->opts.tc_plane_budget_mb * (1 << 20));
                 if (st.use_tc) tc_fix_variant(P, st);
         }
         if (err) return fail(QXG_ERR_UNSUPPORTED, "bit map needs more than the supported number of runs");
@@ -825,6 +827,14 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
     for (int g = 0; g < 3; g++)
         for (auto& st : plan->steps[g]) if (st.use_tc) scratch = std::max(scratch, tc_scratch_need(P, st));
     for (auto& st : plan->bsteps) if (st.use_tc) scratch = std::max(scratch, tc_scratch_need(P, st));
+    // split-K partials of CUDA-core steps with few results and a long sum share the scratch
+    for (int g = 0; g < 3; g++)
+        for (auto& st : plan->steps[g])
+            if (st.kind == QXG_OP_NCON && !st.use_tc)
+                scratch = std::max(scratch, contract_scratch_bytes(st.sargs, P->fp64, P->sm_count));
+    for (auto& st : plan->bsteps)
+        if (st.bkind == kBwdNcon && !st.use_tc)
+            scratch = std::max(scratch, contract_scratch_bytes(st.sargs, P->fp64, P->sm_count));
     plan->tc_scratch_bytes = scratch;
     // reduction of the root
     {
@@ -1047,8 +1057,7 @@ int tune_tc_step(qxg_program* P, Step& st, int* exps) {
             for (int rep = 0; rep < 2; rep++) {
                 QXG_CUDA(cudaMemsetAsync(cslot, 0x80, sizeof(int), P->stream));   // kExpUnset
                 QXG_CUDA(cudaEventRecord(P->tune_ev[0], P->stream));
-                QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
-                QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
+                QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count, nullptr));
                 QXG_CUDA(cudaEventRecord(P->tune_ev[1], P->stream));
             }
             QXG_CUDA(cudaEventSynchronize(P->tune_ev[1]));
@@ -1130,7 +1139,13 @@ int run_group_eager(qxg_program* P, int g, Plan* plp) {
         if (int r = prof_begin(P, &ev)) return r;
         int kind;
         if (st.kind == QXG_OP_NCON) {
-            if (st.use_tc) {
+            if (st.use_tc && st.tc.nouter > 0) {
+                // outer N blocks: pack and GEMM per block under one record
+                kind = QXG_KERNEL_CONTRACT_TC;
+                int nl = 0;
+                QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count, &nl));
+                P->launches += nl - 1;
+            } else if (st.use_tc) {
                 // pack both operands (its own record), then the tensor-core GEMM
                 QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
                 const double pack_bytes = (double)P->esize *
@@ -1138,12 +1153,17 @@ int run_group_eager(qxg_program* P, int g, Plan* plp) {
                                  (int64_t(1) << pl.T[P->ins[instr].b].layout.size())) +
                     (double)st.tc.scratch_bytes;
                 if (int r = prof_end(P, ev, instr, QXG_KERNEL_TC_PACK, 0.0, pack_bytes)) return r;
+                if (!st.tc.fused) P->launches++;             // X and Y both packed
                 if (int r = prof_begin(P, &ev)) return r;
                 kind = QXG_KERNEL_CONTRACT_TC;
                 QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
+                if (st.tc.ks > 0) P->launches++;            // the split-K sum
             } else {
                 kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
-                QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count));
+                int nl = 1;
+                QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count, P->d_scratch, P->scratch_cap,
+                                         &nl));
+                P->launches += nl - 1;
             }
         } else if (st.kind == QXG_OP_VIEW) {
             kind = QXG_KERNEL_VIEW;
@@ -1282,11 +1302,15 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
                 int kind = QXG_KERNEL_REDUCE;
                 if (st.bkind == kBwdNcon) {
                     if (st.use_tc) {
-                        QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
-                        QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
+                        int nl = 0;
+                        QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count, &nl));
+                        P->launches += nl - 1;
                         kind = QXG_KERNEL_CONTRACT_TC;
                     } else {
-                        QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count));
+                        int nl = 1;
+                        QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count, P->d_scratch,
+                                                 P->scratch_cap, &nl));
+                        P->launches += nl - 1;
                         kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
                     }
                 } else if (st.bkind == kBwdView) {
@@ -1630,19 +1654,35 @@ int qxg_program_profile_read(qxg_program* P, qxg_step_profile* out, int32_t max_
     return QXG_OK;
 }
 
+namespace {
+std::string describe_step(const qxg_program* P, const Step& st, int group, int instr);
+}
+
 int qxg_program_explain(const qxg_program* P, int32_t instr, char* buf, int32_t len) {
     if (!P || !buf || len <= 0) return fail(QXG_ERR_INVALID, "explain: null programme or buffer");
-    if (!P->plan) return fail(QXG_ERR_INVALID, "explain: no plan yet (run amplitudes first)");
-    const Plan& pl = *P->plan;
+    // the forward plan, else the gradient plan (which holds the forward steps too)
+    const Plan* fpl = P->plan ? P->plan.get() : P->gplan.get();
+    if (!fpl) return fail(QXG_ERR_INVALID, "explain: no plan yet (run amplitudes or a gradient first)");
+    const Plan& pl = *fpl;
     const Step* found = nullptr;
     int group = -1;
     for (int g = 0; g < 3 && !found; g++)
         for (auto& st : pl.steps[g])
             if (st.kind == QXG_OP_NCON && pl.T[st.tensor].instr == instr) { found = &st; group = g; break; }
     if (!found) return fail(QXG_ERR_INVALID, "explain: instruction " + std::to_string(instr) + " is not an executed ncon");
-    const Step& st = *found;
+    std::string d = describe_step(P, *found, group, instr);
+    // the gradient plan's adjoint contractions of the same command
+    if (P->gplan)
+        for (const auto& bs : P->gplan->bsteps)
+            if (bs.bkind == kBwdNcon && bs.instr == instr) d += " | adjoint: " + describe_step(P, bs, -1, instr);
+    snprintf(buf, (size_t)len, "%s", d.c_str());
+    return 0;
+}
+
+namespace {
+std::string describe_step(const qxg_program* P, const Step& st, int group, int instr) {
     static const char* gname[3] = {"invariant", "slice", "bitstring"};
-    std::string d = "instr " + std::to_string(instr) + " group " + gname[group] + " ";
+    std::string d = group >= 0 ? "instr " + std::to_string(instr) + " group " + gname[group] + " " : std::string();
     auto bits_of_map = [](const BitMap& m, char cls, std::vector<std::string>& at) {
         for (int i = 0; i < m.n; i++)
             for (int j = 0; j < m.r[i].len; j++) {
@@ -1653,6 +1693,8 @@ int qxg_program_explain(const qxg_program* P, int32_t instr, char* buf, int32_t 
     };
     if (st.use_tc) {
         const TcStep& t = st.tc;
+        if (t.ks > 0) d += "split-K=" + std::to_string(1 << t.ks) + " ";
+        if (t.nouter > 0) d += "n-blocks=" + std::to_string(1 << t.nouter) + " ";
         d += std::string("tensor-core ") + (t.tf32 ? "3xTF32 " : "3xBF16 ") + (t.fused ? (t.tma ? "tma-gather" : (t.tmem ? "tmem-gather" : (t.bulk ? "bulk-gather" : "row-gather"))) : "planes") +
              " ntile=" + std::to_string(t.ntile_n) + " nb=" + std::to_string(t.nb) + " nm=" + std::to_string(t.nm) +
              " nn=" + std::to_string(t.nn) + " nk=" + std::to_string(t.nk) + " X=" + (t.x_is_a ? "A" : "B") +
@@ -1666,14 +1708,16 @@ int qxg_program_explain(const qxg_program* P, int32_t instr, char* buf, int32_t 
         for (size_t i = 0; i < at.size(); i++) d += (i ? "," : "") + at[i];
         if (!st.tune_note.empty()) d += " tuned=" + st.tune_note;
     } else {
-        d += contract_uses_rows(st.sargs, P->fp64) ? "cuda-core row-form" : "cuda-core general";
+        d += contract_uses_rows(st.sargs, P->fp64)
+                 ? "cuda-core row-form"
+                 : (contract_scratch_bytes(st.sargs, P->fp64, P->sm_count) > 0 ? "cuda-core split-K" : "cuda-core general");
         int ncb = 0;
         while ((int64_t(1) << ncb) < st.sargs.nC) ncb++;
         d += " c_bits=" + std::to_string(ncb) + " nk=" + std::to_string(st.sargs.nk);
     }
-    snprintf(buf, (size_t)len, "%s", d.c_str());
-    return 0;
+    return d;
 }
+}  // namespace
 
 void qxg_program_destroy(qxg_program* P) {
     if (!P) return;

@@ -144,7 +144,11 @@ struct ReduceArgs {
 };
 
 // Kernel launchers (kernels_simt.cu).  Storage: double2 when fp64 != 0, else float2.
-cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count);
+// scratch (may be null): device memory for the split-K partials of steps with few results and a
+// long sum (contract_scratch_bytes); *launches receives the kernels launched (1 or 2).
+cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count,
+                            void* scratch = nullptr, size_t scratch_bytes = 0, int* launches = nullptr);
+size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count);
 // Whether launch_contract runs a step in the row form (smaller operand staged in shared memory).
 bool contract_uses_rows(const StepArgs& a, bool fp64);
 cudaError_t launch_view(const ViewArgs& a, bool fp64, int* exps, cudaStream_t s);

@@ -861,7 +861,7 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acce[buf])) : "memory");
         }
         for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-        if (lane == 0 && emax != -2139062144) atomicMax(&g.exps[2 * g.exp_c + 1], emax);
+        if (lane == 0 && emax != -2139062144 && g.exp_c >= 0) atomicMax(&g.exps[2 * g.exp_c + 1], emax);
     }
     fence_before();
     __syncthreads();
@@ -869,6 +869,26 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
     }
+}
+
+// Split-K sum: C[c] = sum over the K blocks s (in order) of partial[s * nC + c], raising the
+// result's exponent slot (the partials share the result's scale).
+__global__ void tc_ksum_kernel(const float2* __restrict__ partial, float2* __restrict__ C, int64_t nC, int nsplit,
+                               int* exps, int exp_c) {
+    int emax = -2139062144;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nC; c += (int64_t)gridDim.x * blockDim.x) {
+        float re = 0.f, im = 0.f;
+        for (int j = 0; j < nsplit; j++) {
+            const float2 v = partial[(int64_t)j * nC + c];
+            re += v.x;
+            im += v.y;
+        }
+        C[c] = make_float2(re, im);
+        const float mx = fmaxf(fabsf(re), fabsf(im));
+        if (mx > 0.f) emax = max(emax, exp_of(mx));
+    }
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if ((threadIdx.x & 31) == 0 && emax != -2139062144 && exp_c >= 0) atomicMax(&exps[2 * exp_c + 1], emax);
 }
 
 // ---- host helpers --------------------------------------------------------------------------------
@@ -933,7 +953,9 @@ cudaError_t set_smem_attr() {
 
 void plan_bulk(TcStep& t);
 
-bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits, bool tf32, TcStep* tc) {
+bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits, bool tf32, TcStep* tc,
+                  double plane_budget) {
+    if (plane_budget <= 0) plane_budget = 4.0 * (1 << 30);
     std::vector<int> ca, cb, ka, kb;
     expand(s.cA, ca);
     expand(s.cB, cb);
@@ -973,8 +995,67 @@ bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits
     t.nm = (int)cm.size();
     t.nn = (int)cn.size();
     t.nk = s.nk;
-    // eligibility: a real GEMM (M >= 128 rows, enough K x N reuse to leave the HBM roofline)
-    if (t.nm < 7 || t.nk < 3 || t.nn < 2 || t.nn + t.nk < 8) return false;
+    // eligibility: a real GEMM (M >= 128 rows, enough K x N reuse to leave the HBM roofline); a
+    // long sum (K > 1024) also with 16 to 64 rows -- the tile's other rows stay zero, which costs
+    // tensor time only, while the CUDA-core alternative would re-read both operands per result
+    if ((t.nm < 7 && !(t.nm >= 4 && t.nk > 10)) || t.nk < 3 || t.nn < 2 || t.nn + t.nk < 8) return false;
+    // split K: the tensor cores accumulate in FP32 with an error that grows about linearly with
+    // the number of K steps (2^-24 per step of 8 products: 1e-5 of the result near K = 1024), so
+    // K is cut into blocks of at most 2^10 -- and of down to 2^8 while the tiles are fewer than
+    // 512.  The high K bits become batch bits, each block writes its own partial result (the
+    // partials' index bits sit above the result's), and tc_run_gemm sums the partials in order.
+    {
+        const int64_t tiles = (int64_t(1) << t.nb) * std::max<int64_t>(1, (int64_t(1) << t.nm) / kTcTileM) *
+                              std::max<int64_t>(1, (int64_t(1) << t.nn) / 64);
+        int ks = std::max(0, t.nk - 10);
+        while (ks < t.nk - 8 && (tiles << ks) < 512) ks++;
+        t.ks = ks;
+        t.c_elems = int64_t(1) << c_bits;
+        if (ks > 0) {
+            const int k0 = t.nk - ks;
+            std::vector<std::pair<int, int>> xk2, yk2;
+            for (auto& pr : xk) {
+                if (pr.first >= k0) xb.push_back({t.nb + pr.first - k0, pr.second});
+                else xk2.push_back(pr);
+            }
+            for (auto& pr : yk) {
+                if (pr.first >= k0) yb.push_back({t.nb + pr.first - k0, pr.second});
+                else yk2.push_back(pr);
+            }
+            for (int i = 0; i < ks; i++) cbm.push_back({t.nb + i, (int)c_bits + i});
+            xk.swap(xk2);
+            yk.swap(yk2);
+            t.nb += ks;
+            t.nk -= ks;
+        }
+    }
+    // outer N blocks: when Y's packed planes (complex-doubled hi/lo: 4 words per element of Y)
+    // would pass the budget, the high n bits become a loop on the host; each block packs only its part
+    // of Y and runs the GEMM on pointers offset by the block's Y and C offsets (bit maps are
+    // additive over disjoint bits)
+    {
+        const int es = tf32 ? 4 : 2;
+        int no = 0;
+        auto ybytes = [&](int nn) {
+            return 4.0 * es * std::ldexp(1.0, t.nb + nn + t.nk);
+        };
+        while (ybytes(t.nn - no) > plane_budget && t.nn - no > 6) no++;
+        if (no > 0) {
+            std::vector<std::pair<int, int>> yo, co;
+            const int n0 = t.nn - no;
+            std::vector<std::pair<int, int>> yn2, cn2;
+            for (auto& pr : yn) (pr.first >= n0 ? yo.push_back({pr.first - n0, pr.second}) : yn2.push_back(pr));
+            for (auto& pr : cn) (pr.first >= n0 ? co.push_back({pr.first - n0, pr.second}) : cn2.push_back(pr));
+            bool ok2 = true;
+            t.yo = runs(yo, &ok2);
+            t.co = runs(co, &ok2);
+            if (!ok2) return false;
+            yn.swap(yn2);
+            cn.swap(cn2);
+            t.nn = n0;
+            t.nouter = no;
+        }
+    }
     bool ok = true;
     t.xb = runs(xb, &ok); t.yb = runs(yb, &ok); t.cb = runs(cbm, &ok);
     t.xm = runs(xm, &ok); t.cm = runs(cm, &ok);
@@ -998,11 +1079,15 @@ bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits
     TcVariant v[kTcMaxVariants];
     const int nv = tc_variants(t, v);
     if (nv == 0) return false;
+    // the autotuner tries a candidate only when the workspace holds its scratch: reserve up to
+    // kTuneScratch for candidates beyond the default, so tuning never shrinks the batches much
+    constexpr size_t kTuneScratch = size_t(4) << 30;
     t.planes_ok = false;
-    t.scratch_max = 0;
-    for (int i = 0; i < nv; i++) {
+    tc_set_variant(t, v[0]);
+    t.scratch_max = t.scratch_bytes;
+    for (int i = 1; i < nv; i++) {
         tc_set_variant(t, v[i]);
-        t.scratch_max = std::max(t.scratch_max, t.scratch_bytes);
+        if (t.scratch_bytes <= kTuneScratch) t.scratch_max = std::max(t.scratch_max, t.scratch_bytes);
         if (!v[i].fused) t.planes_ok = true;
     }
     tc_set_variant(t, v[0]);
@@ -1019,7 +1104,8 @@ void tc_set_variant(TcStep& t, TcVariant v) {
     t.ntiles = cdiv(t.N, t.ntile_n);
     t.a_plane_bytes = t.fused ? 0 : (size_t)(t.batch * t.mtiles * t.kchunks) * kATileBytes;
     t.b_plane_bytes = (size_t)(t.batch * t.ntiles * t.kchunks) * (size_t)(2 * t.ntile_n * kTcChunkBytes);
-    t.scratch_bytes = 2 * (t.a_plane_bytes + t.b_plane_bytes);
+    t.partial_bytes = t.ks > 0 ? ((size_t)t.c_elems << t.ks) * sizeof(float2) : 0;
+    t.scratch_bytes = 2 * (t.a_plane_bytes + t.b_plane_bytes) + t.partial_bytes;
 }
 
 // N tiles of 16, 32 or 64 complex columns (two accumulators of 2*ntile FP32 columns: at 64 two
@@ -1034,6 +1120,7 @@ int tc_variants(const TcStep& t, TcVariant* out) {
     for (int f = 4; f >= 0; f--) {
         if (f == 2 && !t.bulk_ok) continue;
         if (f == 4 && !t.tma_ok) continue;
+        if (f == 0 && t.nouter > 0) continue;      // X would be packed again for every block
         for (int nt = widest; nt >= 16; nt /= 2) {
             if (f >= 1 && nt == 16 && widest > 16) continue;
             const TcVariant v{f >= 1, nt, f == 2, f == 3, f == 4};
@@ -1219,14 +1306,45 @@ bool make_x_map(const TcStep& t, const void* X, CUtensorMap* map, GemmArgs* g) {
     return true;
 }
 
+cudaError_t tc_launch_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
+                           int sm_count, int64_t c_off, bool ksum);
+
 cudaError_t tc_run_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
                         int sm_count) {
+    return tc_launch_gemm(t, s, exps, scratch, st, sm_count, 0, true);
+}
+
+cudaError_t tc_run_step(const TcStep& t, const StepArgs& s, int* exps, void* scratch, cudaStream_t st, int sm_count,
+                        int* launches) {
+    const int64_t nblk = int64_t(1) << t.nouter;
+    int nl = 0;
+    for (int64_t o = 0; o < nblk; o++) {
+        StepArgs so = s;
+        const int64_t yoff = pdep(o, t.yo), coff = pdep(o, t.co);
+        if (t.x_is_a) so.B = static_cast<const float2*>(s.B) + yoff;
+        else so.A = static_cast<const float2*>(s.A) + yoff;
+        so.C = static_cast<float2*>(s.C) + coff;
+        cudaError_t e = tc_run_pack(t, so, exps, scratch, st, sm_count);
+        if (e != cudaSuccess) return e;
+        e = tc_launch_gemm(t, so, exps, scratch, st, sm_count, coff, o == nblk - 1);
+        if (e != cudaSuccess) return e;
+        nl += (t.fused ? 1 : 2) + 1;
+    }
+    if (t.ks > 0) nl++;
+    if (launches) *launches = nl;
+    return cudaSuccess;
+}
+
+cudaError_t tc_launch_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
+                           int sm_count, int64_t c_off, bool ksum) {
     uint8_t* base = static_cast<uint8_t*>(scratch);
     GemmArgs g;
     memset(&g, 0, sizeof(g));
     g.a_hi = base; g.a_lo = base + t.a_plane_bytes;
     g.b_hi = base + 2 * t.a_plane_bytes; g.b_lo = base + 2 * t.a_plane_bytes + t.b_plane_bytes;
-    g.C = static_cast<float2*>(s.C);
+    // split K: the GEMM writes the partials after the planes; the sum below writes C
+    float2* partial = reinterpret_cast<float2*>(base + 2 * (t.a_plane_bytes + t.b_plane_bytes));
+    g.C = t.ks > 0 ? partial + c_off : static_cast<float2*>(s.C);
     g.cb = t.cb; g.cm = t.cm; g.cn = t.cn;
     g.M = t.M; g.N = t.N; g.mtiles = t.mtiles; g.ntiles = t.ntiles; g.kchunks = t.kchunks; g.batch = t.batch;
     g.ntile = t.ntile_n;
@@ -1234,7 +1352,7 @@ cudaError_t tc_run_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scr
     const uint32_t nmma = (uint32_t)(2 * t.ntile_n);
     const uint32_t fmt = t.tf32 ? 2u : 1u;           // TF32 : BF16 operand format
     g.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((nmma >> 3) << 17) | ((uint32_t)(kTcTileM >> 4) << 24);
-    g.exp_c = s.expC;
+    g.exp_c = t.ks > 0 ? -1 : s.expC;
     g.exps = exps;
     g.X = static_cast<const float2*>(t.x_is_a ? s.A : s.B);
     g.xb = t.xb; g.xm = t.xm; g.xk = t.xk;
@@ -1314,6 +1432,12 @@ cudaError_t tc_run_gemm(const TcStep& t, const StepArgs& s, int* exps, void* scr
         else QXG_LAUNCH_GEMM(false, kModeTma);
     }
 #undef QXG_LAUNCH_GEMM
+    if (t.ks > 0 && ksum) {
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        const int64_t blocks = std::min<int64_t>(cdiv(t.c_elems, 256), (int64_t)sm_count * 8);
+        tc_ksum_kernel<<<(unsigned)std::max<int64_t>(1, blocks), 256, 0, st>>>(
+            partial, static_cast<float2*>(s.C) - c_off, t.c_elems, 1 << t.ks, exps, s.expC);
+    }
     return cudaGetLastError();
 }
 

@@ -36,7 +36,7 @@ struct TcStep {
     int tma_lead = 0;               // the block holds X's address bits 0 .. tma_lead-1
     bool bulk_ok = false;           // X's (128 rows x chunk) blocks are segments of >= 16 elements
     bool bfast = false;             // X's lowest address bit is a batch bit (tile order: batch first)
-    BitMap segmap, rowmap_c, kmap_c;   // bulk gather plan (see tc_gemm.cu)
+    BitMap segmap{}, rowmap_c{}, kmap_c{};   // bulk gather plan (see tc_gemm.cu)
     int seg_bits = 0, nseg = 0;
     bool planes_ok = false;         // the planes variant's scratch fits the cap
     int nb = 0, nm = 0, nn = 0, nk = 0;        // bits of batch, M, N, K
@@ -45,11 +45,15 @@ struct TcStep {
     int kc = 0;                     // complex K per chunk (16 bf16, 8 tf32)
     int64_t mtiles = 0, ntiles = 0, kchunks = 0;
     // bit maps: index space -> operand / result offsets
-    BitMap xb, xm, xk;              // X offset of batch / m / k index
-    BitMap yb, yn, yk;              // Y offset of batch / n / k index
-    BitMap cb, cm, cn;              // C offset of batch / m / n index
-    size_t a_plane_bytes = 0, b_plane_bytes = 0;
-    size_t scratch_bytes = 0;       // 2 planes of A_op (planes variant) + 2 planes of B_op
+    BitMap xb{}, xm{}, xk{};        // X offset of batch / m / k index
+    BitMap yb{}, yn{}, yk{};        // Y offset of batch / n / k index
+    BitMap cb{}, cm{}, cn{};        // C offset of batch / m / n index
+    int ks = 0;                     // split K: K blocks = 2^ks (their index bits count in nb)
+    int nouter = 0;                 // outer N blocks = 2^nouter, looped on the host
+    BitMap yo{}, co{};              // outer block index -> Y / C offset (n = 0: no blocks)
+    int64_t c_elems = 0;            // elements of the result
+    size_t a_plane_bytes = 0, b_plane_bytes = 0, partial_bytes = 0;
+    size_t scratch_bytes = 0;       // 2 planes of A_op (planes variant) + 2 planes of B_op + partials
     size_t scratch_max = 0;         // the largest scratch of any candidate variant
 };
 
@@ -65,7 +69,9 @@ struct TcVariant {
 
 // Decide whether a step goes to the tensor cores; fills `tc` (default variant: fused, the
 // widest N tile) when it does.
-bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits, bool tf32, TcStep* tc);
+// plane_budget: bytes of Y planes above which the N range is cut into outer blocks (0: 4 GiB).
+bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits, bool tf32, TcStep* tc,
+                  double plane_budget = 0);
 
 // Candidate variants of a planned step (at most kTcMaxVariants), for the autotuner.
 constexpr int kTcMaxVariants = 12;
@@ -83,6 +89,11 @@ cudaError_t tc_run_pack(const TcStep& tc, const StepArgs& s, int* exps, void* sc
                         int sm_count);
 cudaError_t tc_run_gemm(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
                         int sm_count);
+
+// The whole step, outer N blocks included (pack and GEMM per block, then the split-K sum);
+// *launches receives the kernels launched.  Steps with nouter == 0 may use the two calls above.
+cudaError_t tc_run_step(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
+                        int sm_count, int* launches);
 
 // Device error word set by a tensor-core kernel whose bounded wait gave up (0 = none).
 cudaError_t tc_read_error(int* host_code, cudaStream_t st);

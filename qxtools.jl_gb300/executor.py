@@ -42,7 +42,8 @@ class qxg_instr(ct.Structure):
 class qxg_options(ct.Structure):
     _fields_ = [("precision", ct.c_int32), ("device", ct.c_int32), ("workspace_limit", ct.c_int64),
                 ("max_bitstring_batch", ct.c_int32), ("max_slice_batch", ct.c_int32),
-                ("use_graphs", ct.c_int32), ("tc_tuning", ct.c_int32), ("reserved", ct.c_int32 * 6)]
+                ("use_graphs", ct.c_int32), ("tc_tuning", ct.c_int32),
+                ("tc_plane_budget_mb", ct.c_int32), ("reserved", ct.c_int32 * 5)]
 
 
 class qxg_program_info(ct.Structure):
@@ -230,7 +231,7 @@ class Executor:
 
     def __init__(self, programme: Programme, precision: str = "fp64", device: int = 0,
                  workspace_limit: int = 0, max_bitstring_batch: int = 0, max_slice_batch: int = 0,
-                 use_graphs: bool = False, tc_tuning="auto"):
+                 use_graphs: bool = False, tc_tuning="auto", tc_plane_budget_mb: int = 0):
         self.lib = load_library()
         self.programme = programme
         self.precision = precision
@@ -241,6 +242,7 @@ class Executor:
         opts.max_bitstring_batch = max_bitstring_batch
         opts.max_slice_batch = max_slice_batch
         opts.use_graphs = int(use_graphs)
+        opts.tc_plane_budget_mb = int(tc_plane_budget_mb)
         # "auto": time each tensor-core step's tile variants once and keep the fastest;
         # "fixed" (= 1) or k >= 1: candidate k of every step
         if tc_tuning == "auto":

@@ -49,10 +49,11 @@ class ParametrisedCircuitLoss:
     The circuit is converted without decomposition, planned (with `nslice` sliced bonds) and
     compiled once; each evaluation runs one reverse-mode pass per (slice batch, bitstring batch)."""
 
-    def __init__(self, circ, nslice: int = 0, seed: int = 1, time: int = 1, precision: str = "fp64", **opts):
+    def __init__(self, circ, nslice: int = 0, seed: int = 1, time: int = 1, precision: str = "fp64",
+                 width_cap: float | None = None, **opts):
         self.circ = circ
         self.tnc = convert_to_tnc(circ, decompose=False)
-        groups, plan, _ = contraction_scheme(self.tnc, nslice, seed=seed, time=time)
+        groups, plan, _ = contraction_scheme(self.tnc, nslice, seed=seed, time=time, width_cap=width_cap)
         self.graph = build_compute_graph(self.tnc, plan, groups)
         self.programme = Programme.from_graph(self.graph)
         self.executor = Executor(self.programme, precision=precision, **opts)

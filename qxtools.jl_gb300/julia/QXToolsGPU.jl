@@ -27,7 +27,8 @@ struct QxgOptions          # qxg_options
     precision::Int32; device::Int32; workspace_limit::Int64
     max_bitstring_batch::Int32; max_slice_batch::Int32; use_graphs::Int32
     tc_tuning::Int32        # 0: autotune tensor-core tile variants, 1: fixed default
-    reserved::NTuple{6,Int32}
+    tc_plane_budget_mb::Int32   # 0: 4096 MiB of packed planes before blocking the free columns
+    reserved::NTuple{5,Int32}
 end
 
 mutable struct QxgProgram
@@ -77,7 +78,7 @@ function load_qx(qx_file::String, data::AbstractDict; precision::Symbol=:fp64, d
     arrays = [ComplexF64.(data[k]) for k in dkeys]
     rank = Int32[ndims(x) for x in arrays]
     dims = Int64[d for x in arrays for d in size(x)]
-    opts = Ref(QxgOptions(PREC[precision], device, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 6)))
+    opts = Ref(QxgOptions(PREC[precision], device, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 5)))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:qxg_program_create, libqxgpu), Cint,
                 (Ptr{QxgInstr}, Int32, Ptr{Int32}, Int64, Ptr{Int32}, Ptr{Int64}, Int32, Int32,

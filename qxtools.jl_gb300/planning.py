@@ -414,11 +414,13 @@ def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exc
     order_idx = {n: i for i, n in enumerate(tens)}
 
     def push_pairs(n):
+        # sets are walked in a fixed order (labels by name, tensors by creation): the pushes and
+        # the random draws must not depend on string hashing
         seen = set()
-        for l in tens[n]:
+        for l in sorted(tens[n], key=str):
             if l in excl:
                 continue
-            for m in holders[l]:
+            for m in sorted(holders[l], key=order_idx.__getitem__):
                 if m != n and m not in seen:
                     seen.add(m)
                     a, b = (n, m) if order_idx[n] < order_idx[m] else (m, n)
@@ -451,9 +453,12 @@ def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exc
     return plan
 
 
-def _sort_key_cost(net, plan, sliced=()):
+def _sort_key_cost(net, plan, sliced=(), width_cap=None):
+    """(largest intermediate, FLOPs); with `width_cap`, every plan whose largest intermediate
+    is at most 2^width_cap ranks by FLOPs alone."""
     pc = plan_cost(net, plan, sliced)
-    return (pc["max_log2"], pc["flops"])
+    w = pc["max_log2"]
+    return (max(w, width_cap) if width_cap is not None else w, pc["flops"])
 
 
 _TRIAL_SETTINGS = [("size", 0.0), ("growth", 0.0), ("growth", 0.5), ("size", 0.2), ("growth", 0.3),
@@ -468,20 +473,23 @@ def random_greedy_plans(net: HyperNet, trials: int, seed: int = 0, exclude=()):
                                       score=score)
 
 
-def flow_cutter_contraction_plan(tnc, time: int = 60, seed: int = -1, hypergraph: bool = True) -> list:
+def flow_cutter_contraction_plan(tnc, time: int = 60, seed: int = -1, hypergraph: bool = True,
+                                 width_cap: float | None = None) -> list:
     """Stand-in for FlowCutter planning (:90-113): best of the min-fill plan and
-    `8 * time` seeded random-greedy plans by (largest intermediate, FLOPs).
-    `time=0` returns the min-fill plan (the reference's fall-back, :102-106)."""
+    `8 * time` seeded random-greedy plans by (largest intermediate, FLOPs) -- the reference
+    minimises the tree width first; `width_cap` (log2 elements) ranks every plan within the
+    cap by FLOPs alone.  `time=0` returns the min-fill plan (the reference's fall-back,
+    :102-106)."""
     net = hyper_network(tnc) if not isinstance(tnc, HyperNet) else tnc
     base = min_fill_contraction_plan(tnc, hypergraph=hypergraph)
     if time <= 0:
         return base
     seed0 = 0 if seed is None or seed < 0 else int(seed)
-    best, bestk = base, _sort_key_cost(net, base)
+    best, bestk = base, _sort_key_cost(net, base, width_cap=width_cap)
     for p in random_greedy_plans(net, max(1, 8 * int(time)), seed0):
         if len(p) < len(base):
             continue
-        k = _sort_key_cost(net, p)
+        k = _sort_key_cost(net, p, width_cap=width_cap)
         if k < bestk:
             best, bestk = p, k
     return best
@@ -510,10 +518,11 @@ def _slice_candidates(net, plan, sliced):
     return sorted(scored, key=lambda l: (-scored[l], l))[:24]
 
 
-def _scheme_key(net, plan, sliced):
+def _scheme_key(net, plan, sliced, width_cap=None):
     q = plan_cost(net, plan, sliced)
     nsl = math.prod(net.dims[x] for x in sliced) if sliced else 1
-    return (q["max_log2"], q["flops"] * nsl)
+    w = q["max_log2"]
+    return (max(w, width_cap) if width_cap is not None else w, q["flops"] * nsl)
 
 
 def _done(net, plan, sliced, num, max_log2):
@@ -581,7 +590,7 @@ def _scheme_by_greedy(net, num, seed0, max_log2, base_plan, replan_trials=6):
 
 def contraction_scheme(tnc, num: int, time: int = 120, seed: int = -1,
                        score_function: str = "tree_trimming", hypergraph: bool = True,
-                       max_log2: float | None = None):
+                       max_log2: float | None = None, width_cap: float | None = None):
     """Plan plus bonds to slice (:219-299) -> (index_groups_to_slice, plan, metadata).
 
     Two greedy slicers, the cheaper result (largest intermediate, then FLOPs x slices) wins:
@@ -593,7 +602,9 @@ def contraction_scheme(tnc, num: int, time: int = 120, seed: int = -1,
         intermediates that gives the cheapest plan, then re-plan with seeded greedy searches
         that ignore the sliced hyperedges.
     Stops after `num` bonds, or, when `max_log2` is given, once the largest intermediate is at
-    most 2^max_log2 elements.  Index groups are the plain index ids of each sliced hyperedge
+    most 2^max_log2 elements.  With `width_cap` (log2 elements), candidate plans whose largest
+    intermediate is within the cap rank by FLOPs alone (default: largest intermediate first, like
+    the reference's tree-width minimisation).  Index groups are the plain index ids of each sliced hyperedge
     (`expand_slice_bonds_to_hyperindices`, :190-203).  Tensors left disconnected by slicing are
     joined by build_compute_graph (compute_graph.jl:77-90)."""
     tn = getattr(tnc, "tn", tnc)
@@ -602,9 +613,9 @@ def contraction_scheme(tnc, num: int, time: int = 120, seed: int = -1,
     plan, sliced, widths = _scheme_by_order(tnc, net, num, hypergraph, max_log2)
     method = "min fill heuristic"
     if hypergraph and time > 0:
-        base = flow_cutter_contraction_plan(tnc, time=time, seed=seed, hypergraph=hypergraph)
+        base = flow_cutter_contraction_plan(tnc, time=time, seed=seed, hypergraph=hypergraph, width_cap=width_cap)
         p2, s2, w2 = _scheme_by_greedy(net, num, seed0, max_log2, base, replan_trials=max(6, 2 * int(time)))
-        if _scheme_key(net, p2, s2) < _scheme_key(net, plan, sliced):
+        if _scheme_key(net, p2, s2, width_cap) < _scheme_key(net, plan, sliced, width_cap):
             plan, sliced, widths = p2, s2, w2
             method = "greedy stand-in for flow cutter"
     groups = []

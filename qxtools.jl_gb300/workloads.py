@@ -2,8 +2,11 @@
 
 Each workload is a `.qx` programme built the way generate_simulation_files builds one
 (src/simulation.jl:52-77: convert_to_tnc with decomposition, contraction_scheme, then
-build_compute_graph) plus a seeded list of bitstrings (the `.yml` List method).  Generated
-programmes are cached under _build/workloads/ (the planner takes seconds to a minute).
+build_compute_graph) plus a seeded list of bitstrings (the `.yml` List method).  The planner
+runs 8 x `time` seeded greedy trials (default time 16) and, among plans whose largest
+intermediate is at most 2^28 elements, keeps the one with the fewest FLOPs.  Plans are
+deterministic for (name, seed, time).  Generated programmes are cached under _build/workloads/
+(the planner takes seconds to a minute).
 
   rqc_4x4_d10          4x4 grid, 10 cycles, unsliced, 64 bitstrings (the CPU-runnable case)
   rqc_6x6_d14_s4       6x6 grid, 14 cycles, 4 sliced bonds, 256 bitstrings
@@ -40,14 +43,17 @@ WORKLOADS = {
 }
 
 _CACHE = Path(__file__).resolve().parent / "_build" / "workloads"
+_PLANNER_VERSION = 2          # bump when the planner's choices change (invalidates the cache)
+WIDTH_CAP = 28.0              # log2 elements: plans within it rank by FLOPs
 
 
 def _key(name, spec, seed, time):
-    h = hashlib.sha1(json.dumps([name, spec, seed, time], sort_keys=True).encode()).hexdigest()[:12]
+    h = hashlib.sha1(json.dumps([name, spec, seed, time, _PLANNER_VERSION, WIDTH_CAP],
+                                sort_keys=True).encode()).hexdigest()[:12]
     return f"{name}_{h}"
 
 
-def build_workload(name: str, seed: int = 1, time: int = 2, cache: bool = True):
+def build_workload(name: str, seed: int = 1, time: int = 16, cache: bool = True):
     """-> (Programme, bitstrings, info dict).  Deterministic for (name, seed, time)."""
     spec = dict(WORKLOADS[name])
     key = _key(name, spec, seed, time)
@@ -70,7 +76,7 @@ def build_workload(name: str, seed: int = 1, time: int = 2, cache: bool = True):
     else:
         open_q, out_q = [], list(range(1, n + 1))
     tnc.add_output_subset(out_q)
-    groups, plan, meta = contraction_scheme(tnc, spec["nslice"], seed=seed, time=time)
+    groups, plan, meta = contraction_scheme(tnc, spec["nslice"], seed=seed, time=time, width_cap=WIDTH_CAP)
     graph = build_compute_graph(tnc, plan, groups)
     nq = len(out_q)
     prog = Programme.from_commands(graph.commands, graph.data, nq)

@@ -104,9 +104,45 @@ def test_every_tile_variant_matches(q, gpu_lib, precision, nm, nk, nn, nb, order
             got = ex.amplitudes([""])[0]
             info = ex.info()
             desc = ex.explain(2)                 # the ncon command
-        assert "tensor-core" in desc and f"nk={nk}" in desc, desc
+        assert "tensor-core" in desc, desc
         assert info["num_steps_tensor_core"] == 1
         err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
         assert err <= TOL[precision], (k, err)
         if k == "auto":                         # fused and planes candidates at least
             assert info["num_steps_tuned"] == 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "split_tf32"])
+@pytest.mark.parametrize("nm,nk,nn", [(2, 16, 2), (7, 14, 6), (0, 15, 3)])
+def test_long_sum_small_result(q, gpu_lib, precision, nm, nk, nn):
+    """Few results, long sums (the shape of adjoint steps ending in leaf gradients): the split-K
+    CUDA-core form and, for (7, 14, 6) in 3xTF32, the tensor cores with K cut into blocks of at
+    most 1024 (partials summed in a fixed order) against einsum; FP64 to 1e-12, the Complex64
+    modes to 1e-5 of the largest result."""
+    prog, ref = single_ncon_programme(q, nm, nk, nn, 0, seed=nm + nk + nn)
+    with q.Executor(prog, precision=precision) as ex:
+        got = ex.amplitudes([""])[0]
+        got2 = ex.amplitudes([""])[0]
+        if precision != "split_tf32" or nm < 7:
+            assert ex.info()["num_steps_tensor_core"] == 0
+        else:                                   # K = 2^14 on the tensor cores: split into blocks
+            assert "split-K" in ex.explain(2)
+    err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    assert err <= (1e-12 if precision == "fp64" else 1e-5), err
+    assert np.array_equal(got, got2)                   # deterministic: fixed partition and order
+
+
+@pytest.mark.parametrize("precision", ["split_tf32", "split_bf16"])
+@pytest.mark.parametrize("nm,nk,nn", [(11, 7, 11), (8, 11, 8)])
+def test_outer_column_blocks(q, gpu_lib, precision, nm, nk, nn):
+    """A planes budget of 1 MiB forces the smaller operand's free columns into blocks looped on
+    the host (each block packs its part of Y and runs the GEMM on offset pointers), alone and with
+    split K (nk=11); results against einsum within the split tolerance."""
+    prog, ref = single_ncon_programme(q, nm, nk, nn, 0, seed=nm * nk + nn)
+    for k in ["auto", 1]:
+        with q.Executor(prog, precision=precision, tc_tuning=k, tc_plane_budget_mb=1) as ex:
+            got = ex.amplitudes([""])[0]
+            desc = ex.explain(2)
+        assert "n-blocks=" in desc, desc
+        err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+        assert err <= TOL[precision], (k, err)

@@ -70,8 +70,9 @@ def test_static_scratch_contraction_matches_allocating_entry_point(q, gpu_lib, p
 def test_static_scratch_rejects_oversized_shapes(q, gpu_lib):
     import torch
     lib = _declare(gpu_lib)
-    # the smaller operand's packed planes (2^11 x 2^11 complex: 134 MB) exceed the static array
-    la, ad, lb, bd, lc = _shapes(11, 11, 11)
+    # the smaller operand's packed planes (2^12 columns x 2^10 summed, 3xTF32: 64 MiB) exceed the
+    # static array less its exponent slots
+    la, ad, lb, bd, lc = _shapes(12, 10, 12)
     A = torch.zeros(2 ** len(la), dtype=torch.complex64, device="cuda")
     B = torch.zeros(2 ** len(lb), dtype=torch.complex64, device="cuda")
     C = torch.zeros(2 ** len(lc), dtype=torch.complex64, device="cuda")
