@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--precision", default="split_tf32", choices=["fp64", "fp32", "split_bf16", "split_tf32"])
     ap.add_argument("--bits-per-step", type=int, default=0, help="bitstrings per step (0: the workload's list)")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--plan-seed", type=int, default=None, help="planner seed (default: the workload's pinned one)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--compare-fp64", action="store_true", help="also time the FP64 path and report the error")
@@ -201,7 +202,7 @@ def run_reference(args):
     q = entry.load()
     from oracle import oracle
     oracle.build()
-    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed)
+    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed, plan_seed=args.plan_seed)
     cores = oracle.max_threads()
     out_size = info["amplitudes_per_bitstring"]
     per = max(2.0, min(args.cpu_seconds, 20.0))
@@ -262,7 +263,7 @@ def run_ours(args):
         entry._load_build_module().build()
     q = entry.load()
     from oracle import oracle
-    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed)
+    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed, plan_seed=args.plan_seed)
     # default batch: the whole list for the Complex64 paths, 16 bitstrings for the slower FP64 path
     nb = args.bits_per_step or (min(16, len(bits)) if args.precision == "fp64" else len(bits))
     # weak scaling: rank r takes its own shard of bitstrings (regenerated deterministically)
@@ -409,8 +410,11 @@ def run_gradient(args):
     torch.cuda.set_device(0)
     circ = q.create_parametrised_circuit(5, 5, 12, seed=args.seed)
     bits = list(q.amplitudes_uniform(25, args.seed, 256))
-    # planned like the param_5x5_l12 workload: 8 x 16 greedy trials, FLOPs first within 2^28
-    plan_opts = dict(seed=args.seed, time=16, width_cap=q.workloads.WIDTH_CAP)
+    # planned like the param_5x5_l12 workload (its pinned plan seed and trials, ranked by plan_cost
+    # with the bitstring batch)
+    spec = q.workloads.WORKLOADS["param_5x5_l12"]
+    plan_opts = dict(seed=args.plan_seed if args.plan_seed is not None else spec["plan_seed"], time=spec["plan_time"],
+                     width_cap=q.workloads.WIDTH_CAP, beta=spec["nbits"])
     f = q.gradients.ParametrisedCircuitLoss(circ, precision=args.precision, **plan_opts)
     for _ in range(max(1, args.warmup)):
         f.executor.amplitudes(bits)

@@ -50,10 +50,11 @@ class ParametrisedCircuitLoss:
     compiled once; each evaluation runs one reverse-mode pass per (slice batch, bitstring batch)."""
 
     def __init__(self, circ, nslice: int = 0, seed: int = 1, time: int = 1, precision: str = "fp64",
-                 width_cap: float | None = None, **opts):
+                 width_cap: float | None = None, beta: int = 1, **opts):
         self.circ = circ
         self.tnc = convert_to_tnc(circ, decompose=False)
-        groups, plan, _ = contraction_scheme(self.tnc, nslice, seed=seed, time=time, width_cap=width_cap)
+        groups, plan, _ = contraction_scheme(self.tnc, nslice, seed=seed, time=time, width_cap=width_cap,
+                                             batched=self.tnc.output_tensors, beta=beta)
         self.graph = build_compute_graph(self.tnc, plan, groups)
         self.programme = Programme.from_graph(self.graph)
         self.executor = Executor(self.programme, precision=precision, **opts)

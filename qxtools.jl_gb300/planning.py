@@ -117,24 +117,48 @@ def _lg(net: HyperNet, labels, sliced=()) -> float:
     return sum(0.0 if l in sliced else math.log2(net.dims[l]) for l in labels)
 
 
-def plan_cost(net: HyperNet, plan, sliced=()) -> dict:
+# roofline of one step on the GPU executor, for ranking plans: FLOPs at 1e14 /s (split-precision
+# tensor cores) against Complex64 bytes (|A| + |B| + |C|) at 5e12 /s, whichever is longer
+_RANK_FLOPS = 1e14
+_RANK_BYTES = 5e12
+
+
+def plan_cost(net: HyperNet, plan, sliced=(), batched=(), beta: int = 1) -> dict:
     """FLOPs (8 |C| K per step, complex), largest intermediate (log2 elements) and the
-    per-step shapes of `plan` on `net` with `sliced` labels at dimension 1 (one slice)."""
+    per-step shapes of `plan` on `net` with `sliced` labels at dimension 1 (one slice).
+
+    For ranking plans on the GPU executor, which runs `beta` bitstrings at once: the tensors
+    that depend on the `batched` tensors (the outputs) carry a batch of `beta`; "time" is the
+    sum over steps of max(FLOPs / 1e14, 8 (|A| + |B| + |C|) / 5e12) seconds with those batches,
+    and "max_log2_batched" the largest batched intermediate."""
     st = net.copy()
+    dep = set(batched)
+    lbeta = math.log2(beta) if beta > 1 else 0.0
     flops = 0.0
+    est = 0.0
     max_lg = 0.0
+    max_lgb = 0.0
     steps = []
     for (a, b, c) in plan:
         lc, la, lb = contraction_indices(st, a, b)
         every = set(la) | set(lb)
         lg_all = _lg(st, every, sliced)
         lg_c = _lg(st, lc, sliced)
+        lg_a, lg_b = _lg(st, la, sliced), _lg(st, lb, sliced)
         f = 8.0 * 2.0 ** lg_all
         flops += f
+        da, db = a in dep, b in dep
+        dc = da or db
+        if dc:
+            dep.add(c)
+        ba, bb, bc = (lbeta if da else 0.0), (lbeta if db else 0.0), (lbeta if dc else 0.0)
+        est += max(f * 2.0 ** bc / _RANK_FLOPS,
+                   8.0 * (2.0 ** (lg_a + ba) + 2.0 ** (lg_b + bb) + 2.0 ** (lg_c + bc)) / _RANK_BYTES)
         max_lg = max(max_lg, lg_c)
-        steps.append((lg_c, _lg(st, la, sliced), _lg(st, lb, sliced), lg_all - lg_c))
+        max_lgb = max(max_lgb, lg_c + bc)
+        steps.append((lg_c, lg_a, lg_b, lg_all - lg_c))
         mock_contract(st, a, b, c)
-    return {"flops": flops, "max_log2": max_lg, "steps": steps}
+    return {"flops": flops, "max_log2": max_lg, "time": est, "max_log2_batched": max_lgb, "steps": steps}
 
 
 # ---------------------------------------------------------------------------------------
@@ -453,12 +477,13 @@ def greedy_contraction_plan(net: HyperNet, seed=0, temperature: float = 0.0, exc
     return plan
 
 
-def _sort_key_cost(net, plan, sliced=(), width_cap=None):
-    """(largest intermediate, FLOPs); with `width_cap`, every plan whose largest intermediate
-    is at most 2^width_cap ranks by FLOPs alone."""
-    pc = plan_cost(net, plan, sliced)
-    w = pc["max_log2"]
-    return (max(w, width_cap) if width_cap is not None else w, pc["flops"])
+def _sort_key_cost(net, plan, sliced=(), width_cap=None, batched=(), beta=1):
+    """(largest intermediate, FLOPs); with `width_cap`, every plan whose largest batched
+    intermediate is at most 2^width_cap ranks by its estimated time alone (plan_cost)."""
+    pc = plan_cost(net, plan, sliced, batched, beta)
+    if width_cap is not None:
+        return (max(pc["max_log2_batched"], width_cap), pc["time"])
+    return (pc["max_log2"], pc["flops"])
 
 
 _TRIAL_SETTINGS = [("size", 0.0), ("growth", 0.0), ("growth", 0.5), ("size", 0.2), ("growth", 0.3),
@@ -474,22 +499,23 @@ def random_greedy_plans(net: HyperNet, trials: int, seed: int = 0, exclude=()):
 
 
 def flow_cutter_contraction_plan(tnc, time: int = 60, seed: int = -1, hypergraph: bool = True,
-                                 width_cap: float | None = None) -> list:
+                                 width_cap: float | None = None, batched=(), beta: int = 1) -> list:
     """Stand-in for FlowCutter planning (:90-113): best of the min-fill plan and
     `8 * time` seeded random-greedy plans by (largest intermediate, FLOPs) -- the reference
-    minimises the tree width first; `width_cap` (log2 elements) ranks every plan within the
-    cap by FLOPs alone.  `time=0` returns the min-fill plan (the reference's fall-back,
+    minimises the tree width first; `width_cap` (log2 elements) ranks every plan whose largest
+    intermediate, batched by `beta` bitstrings where it depends on the `batched` (output)
+    tensors, is within the cap by its estimated time alone (plan_cost).  `time=0` returns the min-fill plan (the reference's fall-back,
     :102-106)."""
     net = hyper_network(tnc) if not isinstance(tnc, HyperNet) else tnc
     base = min_fill_contraction_plan(tnc, hypergraph=hypergraph)
     if time <= 0:
         return base
     seed0 = 0 if seed is None or seed < 0 else int(seed)
-    best, bestk = base, _sort_key_cost(net, base, width_cap=width_cap)
+    best, bestk = base, _sort_key_cost(net, base, (), width_cap, batched, beta)
     for p in random_greedy_plans(net, max(1, 8 * int(time)), seed0):
         if len(p) < len(base):
             continue
-        k = _sort_key_cost(net, p, width_cap=width_cap)
+        k = _sort_key_cost(net, p, (), width_cap, batched, beta)
         if k < bestk:
             best, bestk = p, k
     return best
@@ -518,11 +544,12 @@ def _slice_candidates(net, plan, sliced):
     return sorted(scored, key=lambda l: (-scored[l], l))[:24]
 
 
-def _scheme_key(net, plan, sliced, width_cap=None):
-    q = plan_cost(net, plan, sliced)
+def _scheme_key(net, plan, sliced, width_cap=None, batched=(), beta=1):
+    q = plan_cost(net, plan, sliced, batched, beta)
     nsl = math.prod(net.dims[x] for x in sliced) if sliced else 1
-    w = q["max_log2"]
-    return (max(w, width_cap) if width_cap is not None else w, q["flops"] * nsl)
+    if width_cap is not None:
+        return (max(q["max_log2_batched"], width_cap), q["time"] * nsl)
+    return (q["max_log2"], q["flops"] * nsl)
 
 
 def _done(net, plan, sliced, num, max_log2):
@@ -590,7 +617,8 @@ def _scheme_by_greedy(net, num, seed0, max_log2, base_plan, replan_trials=6):
 
 def contraction_scheme(tnc, num: int, time: int = 120, seed: int = -1,
                        score_function: str = "tree_trimming", hypergraph: bool = True,
-                       max_log2: float | None = None, width_cap: float | None = None):
+                       max_log2: float | None = None, width_cap: float | None = None,
+                       batched=(), beta: int = 1):
     """Plan plus bonds to slice (:219-299) -> (index_groups_to_slice, plan, metadata).
 
     Two greedy slicers, the cheaper result (largest intermediate, then FLOPs x slices) wins:
@@ -603,8 +631,9 @@ def contraction_scheme(tnc, num: int, time: int = 120, seed: int = -1,
         that ignore the sliced hyperedges.
     Stops after `num` bonds, or, when `max_log2` is given, once the largest intermediate is at
     most 2^max_log2 elements.  With `width_cap` (log2 elements), candidate plans whose largest
-    intermediate is within the cap rank by FLOPs alone (default: largest intermediate first, like
-    the reference's tree-width minimisation).  Index groups are the plain index ids of each sliced hyperedge
+    intermediate -- batched by `beta` bitstrings where it depends on the `batched` (output)
+    tensors -- is within the cap rank by estimated time alone (plan_cost; default: largest
+    intermediate first, like the reference's tree-width minimisation).  Index groups are the plain index ids of each sliced hyperedge
     (`expand_slice_bonds_to_hyperindices`, :190-203).  Tensors left disconnected by slicing are
     joined by build_compute_graph (compute_graph.jl:77-90)."""
     tn = getattr(tnc, "tn", tnc)
@@ -613,9 +642,11 @@ def contraction_scheme(tnc, num: int, time: int = 120, seed: int = -1,
     plan, sliced, widths = _scheme_by_order(tnc, net, num, hypergraph, max_log2)
     method = "min fill heuristic"
     if hypergraph and time > 0:
-        base = flow_cutter_contraction_plan(tnc, time=time, seed=seed, hypergraph=hypergraph, width_cap=width_cap)
+        base = flow_cutter_contraction_plan(tnc, time=time, seed=seed, hypergraph=hypergraph, width_cap=width_cap,
+                                            batched=batched, beta=beta)
         p2, s2, w2 = _scheme_by_greedy(net, num, seed0, max_log2, base, replan_trials=max(6, 2 * int(time)))
-        if _scheme_key(net, p2, s2, width_cap) < _scheme_key(net, plan, sliced, width_cap):
+        if (_scheme_key(net, p2, s2, width_cap, batched, beta) <
+                _scheme_key(net, plan, sliced, width_cap, batched, beta)):
             plan, sliced, widths = p2, s2, w2
             method = "greedy stand-in for flow cutter"
     groups = []
