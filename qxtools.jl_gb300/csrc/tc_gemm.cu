@@ -1184,7 +1184,10 @@ void plan_bulk(TcStep& t) {
         c = e;
     }
     t.tma_lead = lead;
-    t.tma_ok = true;
+    // the innermost box dimension holds the leading run: at least 16 elements (128 bytes), and
+    // every box coordinate below 2^31
+    const int xbits = t.nb + t.nm + t.nk;
+    t.tma_ok = lead >= 4 && xbits - lead <= 31;
 }
 
 std::string tc_key(const TcStep& t) {
@@ -1288,7 +1291,8 @@ bool make_x_map(const TcStep& t, const void* X, CUtensorMap* map, GemmArgs* g) {
         strides[nd - 1] = (cuuint64_t)(8ll << t.tma_lead);
         nd++;
     }
-    if (nd > 5 || xbits - t.tma_lead > 32) return false;
+    // box coordinates are signed 32-bit: the outer coordinate (offset >> tma_lead) must stay below 2^31
+    if (nd > 5 || xbits - t.tma_lead > 31) return false;
     while (nd < 5) {
         dims[nd] = 1;
         box[nd] = 1;
