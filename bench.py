@@ -415,7 +415,9 @@ def run_gradient(args):
     spec = q.workloads.WORKLOADS["param_5x5_l12"]
     plan_opts = dict(seed=args.plan_seed if args.plan_seed is not None else spec["plan_seed"], time=spec["plan_time"],
                      width_cap=q.workloads.WIDTH_CAP, beta=spec["nbits"])
-    f = q.gradients.ParametrisedCircuitLoss(circ, precision=args.precision, **plan_opts)
+    # forward and gradient passes both replayed from CUDA graphs (unless --no-graphs)
+    f = q.gradients.ParametrisedCircuitLoss(circ, precision=args.precision, use_graphs=not args.no_graphs,
+                                            **plan_opts)
     for _ in range(max(1, args.warmup)):
         f.executor.amplitudes(bits)
         f.loss_and_grad(bits)

@@ -172,6 +172,12 @@ struct qxg_program {
     cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
     int group_runs[3] = {0, 0, 0};
     int64_t launches_per_group[3] = {0, 0, 0};
+    // gradient pass graph: captured on the second pass with the same output, seed and gradient
+    // buffers (its kernels' arguments), replayed afterwards
+    cudaGraphExec_t grad_exec = nullptr;
+    int grad_runs = 0;
+    int64_t launches_per_gradpass = 0;
+    const void* grad_key[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -891,6 +897,7 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
 }
 
 void drop_graphs(qxg_program* P);
+void drop_grad_graph(qxg_program* P);
 
 // Choose batch sizes whose workspace fits the limit, (re)build the forward plan (grad = false)
 // or the gradient plan (grad = true), grow the shared device buffers and bind pointers.  Both
@@ -919,6 +926,7 @@ int ensure_plan(qxg_program* P, int nbits_call, bool grad = false) {
         if (pl->arena_bytes + pl->tc_scratch_bytes <= limit) {
             if (P->stream) cudaStreamSynchronize(P->stream);
             if (!grad) drop_graphs(P);
+            else drop_grad_graph(P);
             slot = std::move(pl);
             break;
         }
@@ -1079,12 +1087,19 @@ int tune_tc_step(qxg_program* P, Step& st, int* exps) {
     return 0;
 }
 
+void drop_grad_graph(qxg_program* P) {
+    if (P->grad_exec) cudaGraphExecDestroy(P->grad_exec);
+    P->grad_exec = nullptr;
+    P->grad_runs = 0;
+}
+
 void drop_graphs(qxg_program* P) {
     for (int g = 0; g < 3; g++) {
         if (P->gexec[g]) cudaGraphExecDestroy(P->gexec[g]);
         P->gexec[g] = nullptr;
         P->group_runs[g] = 0;
     }
+    drop_grad_graph(P);
 }
 
 // One pass group: eager launches, or (with use_graphs, outside profiling) a CUDA graph captured
@@ -1272,6 +1287,59 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
     pl.seed.amp_bar = d_ampbar;
     const int n = pl.ntensors;
     const size_t seed_bytes = (size_t)P->esize << pl.T[n + P->root].layout.size();
+    // one pass: forward recomputation, seed, adjoint steps (kernel arguments: the plan's buffers
+    // and d_out / d_ampbar / d_grad)
+    auto body = [&]() -> int {
+        if (exps) {
+            QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[0], pl.slot_all_end, P->stream));
+            P->launches++;
+        }
+        for (int g = 0; g < 3; g++)
+            if (int r = run_group_eager(P, g, &pl)) return r;
+        if (d_out)
+            if (int r = run_reduce(P, &pl)) return r;
+        QXG_CUDA(cudaMemsetAsync(pl.seed.dst, 0, seed_bytes, P->stream));
+        QXG_CUDA(launch_seed(pl.seed, P->fp64, exps, P->stream));
+        P->launches++;
+        for (auto& st : pl.bsteps) {
+            if (st.use_tc)
+                if (int r = tune_tc_step(P, st, exps)) return r;
+            size_t ev = 0;
+            if (int r = prof_begin(P, &ev)) return r;
+            int kind = QXG_KERNEL_REDUCE;
+            if (st.bkind == kBwdNcon) {
+                if (st.use_tc) {
+                    int nl = 0;
+                    QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count, &nl));
+                    P->launches += nl - 1;
+                    kind = QXG_KERNEL_CONTRACT_TC;
+                } else {
+                    int nl = 1;
+                    QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count, P->d_scratch,
+                                             P->scratch_cap, &nl));
+                    P->launches += nl - 1;
+                    kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
+                }
+            } else if (st.bkind == kBwdView) {
+                QXG_CUDA(launch_view_adjoint(st.vaargs, P->fp64, exps, P->stream));
+                kind = QXG_KERNEL_VIEW;
+            } else {
+                LeafGradArgs la = st.largs;
+                la.grad = d_grad + 2 * st.goff;
+                QXG_CUDA(launch_leaf_grad(la, P->fp64, exps, P->stream));
+            }
+            if (int r = prof_end(P, ev, st.instr, kind, st.flops, st.bytes)) return r;
+        }
+        return 0;
+    };
+    // with use_graphs (outside profiling) the pass is captured on its second run with the same
+    // buffers and replayed for every later pass
+    const bool graphs = P->opts.use_graphs && !P->profiling;
+    const void* key[3] = {d_out, d_ampbar, d_grad};
+    if (graphs && (key[0] != P->grad_key[0] || key[1] != P->grad_key[1] || key[2] != P->grad_key[2])) {
+        drop_grad_graph(P);
+        for (int i = 0; i < 3; i++) P->grad_key[i] = key[i];
+    }
     size_t k = 0;
     PassParams pp;
     memset(&pp, 0, sizeof(pp));
@@ -1283,46 +1351,32 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
             pp.bit_base = (int32_t)(b * pl.bc);
             pp.bits_valid = root.beta ? (int32_t)std::min<int64_t>(pl.bc, nbits - pp.bit_base) : nbits;
             if (int r = set_params(P, k++, pp)) return r;
-            if (exps) {
-                QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[0], pl.slot_all_end, P->stream));
-                P->launches++;
+            if (!graphs || P->grad_runs < 1) {
+                const int64_t before = P->launches;
+                if (int r = body()) return r;
+                P->launches_per_gradpass = P->launches - before;
+                P->grad_runs++;
+                continue;
             }
-            for (int g = 0; g < 3; g++)
-                if (int r = run_group_eager(P, g, &pl)) return r;
-            if (d_out)
-                if (int r = run_reduce(P, &pl)) return r;
-            QXG_CUDA(cudaMemsetAsync(pl.seed.dst, 0, seed_bytes, P->stream));
-            QXG_CUDA(launch_seed(pl.seed, P->fp64, exps, P->stream));
-            P->launches++;
-            for (auto& st : pl.bsteps) {
-                if (st.use_tc)
-                    if (int r = tune_tc_step(P, st, exps)) return r;
-                size_t ev = 0;
-                if (int r = prof_begin(P, &ev)) return r;
-                int kind = QXG_KERNEL_REDUCE;
-                if (st.bkind == kBwdNcon) {
-                    if (st.use_tc) {
-                        int nl = 0;
-                        QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count, &nl));
-                        P->launches += nl - 1;
-                        kind = QXG_KERNEL_CONTRACT_TC;
-                    } else {
-                        int nl = 1;
-                        QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count, P->d_scratch,
-                                                 P->scratch_cap, &nl));
-                        P->launches += nl - 1;
-                        kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
-                    }
-                } else if (st.bkind == kBwdView) {
-                    QXG_CUDA(launch_view_adjoint(st.vaargs, P->fp64, exps, P->stream));
-                    kind = QXG_KERNEL_VIEW;
-                } else {
-                    LeafGradArgs la = st.largs;
-                    la.grad = d_grad + 2 * st.goff;
-                    QXG_CUDA(launch_leaf_grad(la, P->fp64, exps, P->stream));
+            if (!P->grad_exec) {
+                cudaGraph_t graph = nullptr;
+                QXG_CUDA(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
+                const int64_t before = P->launches;
+                const int r = body();
+                const cudaError_t e = cudaStreamEndCapture(P->stream, &graph);
+                P->launches = before;
+                if (r) { if (graph) cudaGraphDestroy(graph); return r; }
+                if (e != cudaSuccess) return fail(QXG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+                const cudaError_t ei = cudaGraphInstantiate(&P->grad_exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ei != cudaSuccess) {
+                    P->grad_exec = nullptr;
+                    return fail(QXG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
                 }
-                if (int r = prof_end(P, ev, st.instr, kind, st.flops, st.bytes)) return r;
             }
+            QXG_CUDA(cudaGraphLaunch(P->grad_exec, P->stream));
+            P->launches += P->launches_per_gradpass;
+            P->grad_runs++;
         }
     }
     return 0;

@@ -111,6 +111,27 @@ def test_gradient_over_several_bitstring_batches(q, gpu_lib):
         assert np.max(np.abs(g1[i] - g2[i])) <= 1e-12 * (np.max(np.abs(g1[i])) + 1e-300)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "split_tf32"])
+def test_gradient_graph_replay_matches_eager(q, gpu_lib, precision):
+    """With use_graphs the gradient pass is captured on its second run and replayed for later
+    passes (5 bitstring batches of 4); three calls in a row give the eager executor's results."""
+    circ = q.create_rqc_circuit(3, 3, 4, seed=5)
+    tnc = q.convert_to_tnc(circ, decompose=True)
+    plan = q.flow_cutter_contraction_plan(tnc, time=1)
+    prog = q.compile_programme(tnc, plan)
+    bits = list(q.amplitudes_uniform(9, 1, 19))
+    with q.Executor(prog, precision=precision, max_bitstring_batch=4) as ex1, \
+            q.Executor(prog, precision=precision, max_bitstring_batch=4, use_graphs=True) as ex2:
+        a1, g1 = ex1.gradient(bits)
+        for _ in range(3):
+            a2, g2 = ex2.gradient(bits)
+            assert np.array_equal(a1, a2)
+            for i in g1:
+                assert np.array_equal(g1[i], g2[i]), i
+        a3 = ex2.amplitudes(bits)                     # the forward still matches after replays
+        assert np.max(np.abs(a3[:, 0] - a1[:, 0])) <= 1e-12 * np.max(np.abs(a1))
+
+
 def _loss(q, circ_fn, angles, bits):
     circ = circ_fn(angles)
     tnc = q.convert_to_tnc(circ, decompose=False)
