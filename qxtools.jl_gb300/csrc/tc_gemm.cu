@@ -996,10 +996,12 @@ bool tc_plan_step(const StepArgs& s, size_t a_bits, size_t b_bits, size_t c_bits
     t.nn = (int)cn.size();
     t.nk = s.nk;
     // eligibility: a real GEMM (M >= 128 rows, enough K x N reuse to leave the HBM roofline); a
-    // long sum (K > 1024) also with 16 to 64 rows when N >= 16 and M N >= 512 -- the tile's
-    // other rows stay zero, which costs tensor time only, while the CUDA-core alternative would
-    // re-read both operands per result.  Fewer results go to the CUDA-core split-K reduction.
-    const bool short_m = t.nm >= 4 && t.nk > 10 && t.nn >= 4 && t.nm + t.nn >= 9;
+    // long sum (K > 1024) also with 16 to 64 rows when the result has >= 4096 elements -- the
+    // tile's other rows stay zero, which costs tensor time only, while the CUDA-core general
+    // form would re-read both operands per result.  Smaller results of long sums go to the
+    // CUDA-core split-K reduction (a 64-element result of a 2^27-term sum would otherwise be
+    // 2^17 one-tile K blocks).
+    const bool short_m = t.nm >= 4 && t.nk > 10 && t.nb + t.nm + t.nn >= 12;
     if ((t.nm < 7 && !short_m) || t.nk < 3 || t.nn < 2 || t.nn + t.nk < 8) return false;
     // split K: the tensor cores accumulate in FP32 with an error that grows about linearly with
     // the number of K steps (2^-24 per step of 8 products: 1e-5 of the result near K = 1024), so

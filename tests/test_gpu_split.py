@@ -15,17 +15,23 @@ pytestmark = pytest.mark.gpu
 TOL = {"split_tf32": 5e-6, "split_bf16": 1e-4, "fp32": 5e-6}
 
 
-def single_ncon_programme(q, nm, nk, nn, nbatch=0, seed=0, scale=1.0, a_order="mkb"):
+def single_ncon_programme(q, nm, nk, nn, nbatch=0, seed=0, scale=1.0, a_order="mkb", c_order="mnb"):
     """C[m.., n.., b..] = sum_k A[m.., k.., b..] B[k.., n.., b..] with dim-2 labels; a_order
-    permutes A's label groups (its lowest address bits: m, k or batch)."""
+    permutes A's label groups (its lowest address bits: m, k or batch), c_order C's ("i" for
+    m and n labels interleaved from the lowest bit)."""
     rng = np.random.default_rng(seed)
     lm = list(range(1, nm + 1))
     lk = list(range(nm + 1, nm + nk + 1))
     ln = list(range(nm + nk + 1, nm + nk + nn + 1))
     lb = list(range(nm + nk + nn + 1, nm + nk + nn + nbatch + 1))
-    groups = {"m": lm, "k": lk, "b": lb}
+    groups = {"m": lm, "k": lk, "b": lb, "n": ln}
     la = [l for g in a_order for l in groups[g]]
-    lbb, lc = lk + ln + lb, lm + ln + lb
+    lbb = lk + ln + lb
+    if c_order == "i":
+        inter = [l for pair in zip(ln, lm) for l in pair]
+        lc = inter + lm[len(ln):] + ln[len(lm):] + lb
+    else:
+        lc = [l for g in c_order for l in groups[g]]
     A = (rng.standard_normal((2,) * len(la)) + 1j * rng.standard_normal((2,) * len(la))) * scale
     B = (rng.standard_normal((2,) * len(lbb)) + 1j * rng.standard_normal((2,) * len(lbb))) * scale
     cmds = [q.Load("a", "data_1", A.shape), q.Load("b", "data_2", B.shape),
@@ -89,16 +95,20 @@ def test_tensor_core_error_at_large_k(q, gpu_lib, precision):
 
 
 @pytest.mark.parametrize("precision", ["split_tf32", "split_bf16"])
-@pytest.mark.parametrize("nm,nk,nn,nb,order", [(8, 9, 6, 0, "mkb"), (7, 3, 7, 1, "mkb"), (9, 6, 2, 0, "mkb"),
-                                               (7, 6, 6, 0, "kmb"), (8, 4, 5, 2, "bmk"), (8, 5, 6, 1, "kbm")])
-def test_every_tile_variant_matches(q, gpu_lib, precision, nm, nk, nn, nb, order):
+@pytest.mark.parametrize("nm,nk,nn,nb,order,corder", [(8, 9, 6, 0, "mkb", "mnb"), (7, 3, 7, 1, "mkb", "mnb"),
+                                                       (9, 6, 2, 0, "mkb", "mnb"), (7, 6, 6, 0, "kmb", "mnb"),
+                                                       (8, 4, 5, 2, "bmk", "mnb"), (8, 5, 6, 1, "kbm", "mnb"),
+                                                       (8, 6, 7, 1, "mkb", "nmb"), (9, 5, 6, 0, "kmb", "i"),
+                                                       (7, 7, 4, 2, "mkb", "bnm")])
+def test_every_tile_variant_matches(q, gpu_lib, precision, nm, nk, nn, nb, order, corder):
     """Each candidate tile variant (X gathered in the GEMM by contiguous segments or by rows, or
     packed into planes first; N tiles of 16/32/64), forced with tc_tuning = k, and the autotuned
     choice give the einsum result within the split tolerance.  Shapes cover K chunks beyond the
     gather ring (nk=9), K below one chunk (nk=3 with 3xBF16), batch bits, N narrower than the
-    smallest tile (nn=2), and larger operands whose lowest address bits are summed (segments of
-    rows and k values interleaved) or batch bits (batch-first tile order, no segment gather)."""
-    prog, ref = single_ncon_programme(q, nm, nk, nn, nb, seed=nm + 7 * nk + 31 * nn, a_order=order)
+    smallest tile (nn=2), larger operands whose lowest address bits are summed (segments of
+    rows and k values interleaved) or batch bits (batch-first tile order, no segment gather), and
+    results whose lowest address bits are columns, interleaved rows and columns, or batch bits."""
+    prog, ref = single_ncon_programme(q, nm, nk, nn, nb, seed=nm + 7 * nk + 31 * nn, a_order=order, c_order=corder)
     for k in ["auto"] + list(range(1, 13)):
         with q.Executor(prog, precision=precision, tc_tuning=k) as ex:
             got = ex.amplitudes([""])[0]
