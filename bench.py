@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--compare-fp64", action="store_true", help="also time the FP64 path and report the error")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel eagerly (no CUDA graphs)")
+    ap.add_argument("--tuning-file", default=None,
+                    help="read the autotuner's decisions from this file if it exists, else write them after warm-up "
+                         "(so a profiler run repeats the plain run's variants)")
     ap.add_argument("--tc-tuning", default="auto",
                     help="tensor-core tile variants: 'auto' (timed per step) or candidate number k >= 1")
     ap.add_argument("--gradient", action="store_true",
@@ -283,9 +286,14 @@ def run_ours(args):
     def step_device():
         ex.amplitudes_device(d_bits.data_ptr(), nb, d_out.data_ptr(), slices=(0, nslice))
 
+    tuning_path = Path(args.tuning_file) if args.tuning_file else None
+    if tuning_path is not None and tuning_path.exists():
+        ex.set_tuning(tuning_path.read_text())
     for _ in range(args.warmup):
         step_device()
     ex.synchronize()
+    if tuning_path is not None and not tuning_path.exists() and rank == 0:
+        tuning_path.write_text(ex.tuning())
     ex_info = ex.info()
     # ---- value: device-resident inputs --------------------------------------------------------
     _, launches0 = ex.profile_read()
@@ -346,7 +354,11 @@ def run_ours(args):
     tflops = flops_exec / (total_ms * 1e-3) / 1e12 if total_ms else 0.0
     kernel_name = {"contract_fp64": "contract_kernel_fp64", "contract_fp32": "contract_kernel_fp32",
                    "contract_tc": "tc_contract"}.get(dom_name, dom_name)
-    traffic, _ = traffic_summary(args.workload, kernel_name, args.precision)
+    traffic, tsum = traffic_summary(args.workload, kernel_name, args.precision)
+    if tsum and "dram_over_algorithmic" in tsum and dom["launches"]:
+        # measured on a smaller case: DRAM bytes per algorithmic byte of this kernel class, applied
+        # to this run's algorithmic bytes per launch
+        traffic = tsum["dram_over_algorithmic"] * dom["bytes"] / dom["launches"]
     if dom_name == "contract_fp64":
         fp64_peak = fp64_peak_tflops(torch, dev)
         ach = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
@@ -367,7 +379,8 @@ def run_ours(args):
         pk = peaks["hbm_gbs"]
         roof = {"bound": "hbm", "achieved": ach, "peak": pk, "unit": "GB/s", "frac": ach / pk, "traffic": traffic,
                 "peak_source": f"hbm_gbs of {peak_src}", "kernel": kernel_name, "kernel_share": dom["ms"] / total_ms}
-    roof["kernels"] = {k: {"launches": v["launches"], "ms": round(v["ms"], 3), "share": v["ms"] / total_ms}
+    roof["kernels"] = {k: {"launches": v["launches"], "ms": round(v["ms"], 3), "share": v["ms"] / total_ms,
+                           "algorithmic_bytes": v["bytes"], "algorithmic_flops": v["flops"]}
                        for k, v in sorted(by_kind.items(), key=lambda kv: -kv[1]["ms"])}
     top = sorted(rows, key=lambda r: -r["ms"])[:10]
     roof["top_steps"] = [{"instr": r["instr"], "kernel": r["kernel"], "ms_per_pass": round(r["ms"] / args.steps, 3),

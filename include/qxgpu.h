@@ -208,6 +208,15 @@ int qxg_program_profile_read(qxg_program* prog, qxg_step_profile* out, int32_t m
  * built before the first amplitudes call).  A diagnostic with no counterpart in the reference. */
 int qxg_program_explain(const qxg_program* prog, int32_t instr, char* buf, int32_t len);
 
+/* The autotuner's decisions (tensor-core tile variant per step shape), as text, so that a later
+ * programme -- in another process -- runs the same variants without timing them again.
+ * qxg_program_tuning_get writes at most len bytes (NUL-terminated) and returns the length the
+ * whole text needs (excluding the NUL), or a negative status; qxg_program_tuning_set merges a
+ * text written by qxg_program_tuning_get (unknown shapes are ignored when planning).  No
+ * counterpart in the reference. */
+int qxg_program_tuning_get(const qxg_program* prog, char* buf, int64_t len);
+int qxg_program_tuning_set(qxg_program* prog, const char* text);
+
 /* Free the device buffers, graphs and stream of a programme.  Accepts NULL. */
 void qxg_program_destroy(qxg_program* prog);
 

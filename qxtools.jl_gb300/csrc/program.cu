@@ -1712,6 +1712,46 @@ namespace {
 std::string describe_step(const qxg_program* P, const Step& st, int group, int instr);
 }
 
+// Tuning text: one line per decision, "<hex of the shape key> <fused> <ntile> <bulk> <tmem> <tma>".
+int qxg_program_tuning_get(const qxg_program* P, char* buf, int64_t len) {
+    if (!P) return fail(QXG_ERR_INVALID, "tuning: null programme");
+    std::string out;
+    static const char* hex = "0123456789abcdef";
+    for (const auto& kv : P->tune_cache) {
+        for (unsigned char ch : kv.first) { out += hex[ch >> 4]; out += hex[ch & 15]; }
+        const TcVariant& v = kv.second;
+        out += " " + std::to_string((int)v.fused) + " " + std::to_string(v.ntile) + " " + std::to_string((int)v.bulk) +
+               " " + std::to_string((int)v.tmem) + " " + std::to_string((int)v.tma) + "\n";
+    }
+    if (buf && len > 0) snprintf(buf, (size_t)len, "%s", out.c_str());
+    return (int)out.size();
+}
+
+int qxg_program_tuning_set(qxg_program* P, const char* text) {
+    if (!P || !text) return fail(QXG_ERR_INVALID, "tuning: null programme or text");
+    const char* p = text;
+    while (*p) {
+        const char* e = p;
+        while (*e && *e != ' ' && *e != '\n') e++;
+        std::string key;
+        for (const char* h = p; h + 1 < e; h += 2) {
+            auto nib = [](char c) { return c >= 'a' ? c - 'a' + 10 : c - '0'; };
+            key += (char)((nib(h[0]) << 4) | nib(h[1]));
+        }
+        int f = 0, nt = 0, b = 0, tm = 0, ta = 0, used = 0;
+        if (*e == ' ' && sscanf(e, " %d %d %d %d %d%n", &f, &nt, &b, &tm, &ta, &used) == 5 &&
+            (nt == 16 || nt == 32 || nt == 64) && !key.empty()) {
+            P->tune_cache[key] = TcVariant{f != 0, nt, b != 0, tm != 0, ta != 0};
+            e += used;
+        } else {
+            return fail(QXG_ERR_INVALID, "tuning: malformed line");
+        }
+        while (*e && *e != '\n') e++;
+        p = *e ? e + 1 : e;
+    }
+    return 0;
+}
+
 int qxg_program_explain(const qxg_program* P, int32_t instr, char* buf, int32_t len) {
     if (!P || !buf || len <= 0) return fail(QXG_ERR_INVALID, "explain: null programme or buffer");
     // the forward plan, else the gradient plan (which holds the forward steps too)

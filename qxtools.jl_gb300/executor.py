@@ -103,6 +103,8 @@ def load_library(path=None):
     lib.qxg_gradient.restype = ct.c_int
     lib.qxg_program_profile.argtypes = [P, ct.c_int32]
     lib.qxg_program_explain.argtypes = [P, ct.c_int32, ct.c_char_p, ct.c_int32]
+    lib.qxg_program_tuning_get.argtypes = [P, ct.c_char_p, ct.c_int64]
+    lib.qxg_program_tuning_set.argtypes = [P, ct.c_char_p]
     lib.qxg_program_profile_read.argtypes = [P, ct.POINTER(qxg_step_profile), ct.c_int32, ct.POINTER(ct.c_int32),
                                              ct.POINTER(ct.c_int64)]
     lib.qxg_last_error.restype = ct.c_char_p
@@ -372,6 +374,19 @@ class Executor:
         rows = [{"instr": b.instr, "kernel": KERNEL_KINDS.get(b.kernel, str(b.kernel)), "launches": b.launches,
                  "ms": b.ms, "flops": b.flops, "bytes": b.bytes} for b in buf[:n.value]]
         return rows, launches.value
+
+    def tuning(self) -> str:
+        """The autotuner's decisions as text (qxg_program_tuning_get)."""
+        n = self.lib.qxg_program_tuning_get(self._h, None, 0)
+        if n < 0:
+            _check(self.lib, n)
+        buf = ct.create_string_buffer(n + 1)
+        self.lib.qxg_program_tuning_get(self._h, buf, n + 1)
+        return buf.value.decode()
+
+    def set_tuning(self, text: str):
+        """Preload decisions written by tuning(), here or in another process."""
+        _check(self.lib, self.lib.qxg_program_tuning_set(self._h, text.encode()))
 
     def explain(self, instr: int) -> str:
         """One line on how the current plan executes `ncon` command `instr` (qxg_program_explain)."""

@@ -156,3 +156,24 @@ def test_outer_column_blocks(q, gpu_lib, precision, nm, nk, nn):
         assert "n-blocks=" in desc, desc
         err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
         assert err <= TOL[precision], (k, err)
+
+
+def test_tuning_decisions_carry_over(q, gpu_lib):
+    """qxg_program_tuning_get / _set: a second programme preloaded with the first one's decisions
+    times no candidate and runs the same variant, with the same result."""
+    prog, ref = single_ncon_programme(q, 9, 7, 6, 1, seed=11, a_order="kmb")
+    with q.Executor(prog, precision="split_tf32") as ex1:
+        got1 = ex1.amplitudes([""])[0]
+        text = ex1.tuning()
+        desc1 = ex1.explain(2)
+        assert ex1.info()["num_steps_tuned"] == 1 and text.count("\n") == 1
+    with q.Executor(prog, precision="split_tf32") as ex2:
+        ex2.set_tuning(text)
+        got2 = ex2.amplitudes([""])[0]
+        desc2 = ex2.explain(2)
+        assert ex2.info()["num_steps_tuned"] == 0
+    variant = lambda d: d.split("tensor-core ")[1].split(" nb=")[0]
+    assert variant(desc1) == variant(desc2)
+    assert np.array_equal(got1, got2)
+    with pytest.raises(q.QXGError):
+        q.Executor(prog, precision="split_tf32").set_tuning("zz 1 7 0 0 0\n")
