@@ -36,8 +36,14 @@ __device__ __forceinline__ double pow2d(int n) {
     return __longlong_as_double((long long)(n + 1023) << 52);
 }
 // Binary exponent e of |x| with |x| in [2^(e-1), 2^e) for normal floats (frexp convention).
-__device__ __forceinline__ int exp_of(float x) {
-    return (int)((__float_as_uint(x) >> 23) & 0xffu) - 126;
+__host__ __device__ __forceinline__ int exp_of(float x) {
+#ifdef __CUDA_ARCH__
+    const unsigned u = __float_as_uint(x);
+#else
+    unsigned u;
+    std::memcpy(&u, &x, sizeof(u));
+#endif
+    return (int)((u >> 23) & 0xffu) - 126;
 }
 
 __device__ __forceinline__ int read_m(const int* exps, int slot) {
@@ -201,6 +207,431 @@ __global__ void __launch_bounds__(kThreads) contract_rows_kernel(const RowArgs a
             T out; out.x = re; out.y = im;
             C[ir + cn[n]] = out;
         }
+    }
+    if (SCALED) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.expC + 1], emax);
+    }
+}
+
+// Row form, compact: the row form with the loop work cut to the arithmetic, for FP32 steps with
+// compile-time K and N.  The row kernel above spends most of its issue slots on index work (bit
+// deposits per row, table reads and address arithmetic per (k, n)); here
+//   * a warp walks a contiguous range of 32-row groups (lanes = the 5 lowest row bits) and moves
+//     from one group to the next by adding per-bit offset deltas (the bits of g+1 that differ
+//     from g are 0..ctz(g+1)), so a row costs a few integer adds instead of three deposits;
+//   * Y is restaged densely as [batch][k][n] of (re, im, im, re) quadruples, so every (k, n)
+//     reads one 16-byte word at a compile-time offset from the row's batch base (batches padded
+//     by one word so lanes of different batches fall in different banks);
+//   * the complex product uses paired FP32 FMAs (fma.rn.f32x2): acc += (xr, xr) * (yr, yi) and
+//     acc += (-xi, xi) * (yi, yr), the same roundings in the same order as four scalar FMAs;
+//   * X pairs (k, k+1) and C pairs (n, n+1) move as 16-byte words when k bit 0 / n bit 0 is the
+//     operand's / result's lowest address bit.
+struct Rows2Args {
+    const void* X;
+    const void* Y;
+    void* C;
+    int64_t ngroups;           // 32-row groups
+    int32_t nbatch;            // Y batches (values of the row bits Y has)
+    int32_t conjX, conjY;
+    int32_t expX, expY, expC;
+    int32_t xpair, cpair;
+    BitMap laneX, laneC, laneB;    // lane -> X offset / C offset / batch index
+    BitMap grpX, grpC, grpB;       // group index -> X / C offset / batch index
+    BitMap kX, kY, nC, nY;         // k -> X / Y offset, n -> C / Y offset
+    BitMap bY;                     // batch index -> Y offset
+};
+constexpr int kRows2MaxY = 2048;
+
+__host__ __device__ __forceinline__ unsigned f2u(float x) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(x);
+#else
+    unsigned u;
+    std::memcpy(&u, &x, sizeof(u));
+    return u;
+#endif
+}
+__host__ __device__ __forceinline__ float u2f(unsigned u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float x;
+    std::memcpy(&x, &u, sizeof(x));
+    return x;
+#endif
+}
+__host__ __device__ __forceinline__ unsigned long long f2pack(float lo, float hi) {
+    return (unsigned long long)f2u(lo) | ((unsigned long long)f2u(hi) << 32);
+}
+// d += a * b on both FP32 halves, each rounded once (fused).
+__host__ __device__ __forceinline__ void fma2(unsigned long long& d, unsigned long long a, unsigned long long b) {
+#ifdef __CUDA_ARCH__
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(d) : "l"(a), "l"(b));
+#else
+    const float lo = std::fmaf(u2f((unsigned)a), u2f((unsigned)b), u2f((unsigned)d));
+    const float hi = std::fmaf(u2f((unsigned)(a >> 32)), u2f((unsigned)(b >> 32)), u2f((unsigned)(d >> 32)));
+    d = f2pack(lo, hi);
+#endif
+}
+
+// Shared tables of the compact row form: Y quadruples [batch][k][n] (batches padded by one),
+// per group-bit deltas of the X / C offsets and batch index, X offsets of k, C offsets of n.
+struct Rows2Smem {
+    float4* Ys;
+    int64_t *dX, *dC, *dB, *kx, *cn;
+};
+template <int K, int N>
+__host__ __device__ __forceinline__ Rows2Smem rows2_carve(const Rows2Args& a, unsigned char* base) {
+    Rows2Smem t;
+    t.Ys = reinterpret_cast<float4*>(base);
+    t.dX = reinterpret_cast<int64_t*>(t.Ys + (size_t)a.nbatch * (K * N + 1));
+    t.dC = t.dX + 48;
+    t.dB = t.dC + 48;
+    t.kx = t.dB + 48;
+    t.cn = t.kx + K;
+    return t;
+}
+
+// Table entries written by thread tid of nthr.
+template <int K, int N>
+__host__ __device__ __forceinline__ void rows2_fill(const Rows2Args& a, const Rows2Smem& t, int tid, int nthr) {
+    constexpr int KN = K * N, BS = K * N + 1;
+    const float* __restrict__ Yg = static_cast<const float*>(a.Y);
+    for (int i = tid; i < a.nbatch * KN; i += nthr) {
+        const int b = i / KN, k = (i % KN) / N, n = i % N;
+        const int64_t yo = pdep(b, a.bY) + pdep(k, a.kY) + pdep(n, a.nY);
+        const float yr = Yg[2 * yo], yi = a.conjY ? -Yg[2 * yo + 1] : Yg[2 * yo + 1];
+        t.Ys[b * BS + k * N + n] = make_float4(yr, yi, yi, yr);
+    }
+    for (int j = tid; j < 46; j += nthr) {
+        const int64_t bit = int64_t(1) << j, low = bit - 1;
+        t.dX[j] = pdep(bit, a.grpX) - pdep(low, a.grpX);
+        t.dC[j] = pdep(bit, a.grpC) - pdep(low, a.grpC);
+        t.dB[j] = pdep(bit, a.grpB) - pdep(low, a.grpB);
+    }
+    for (int k = tid; k < K; k += nthr) t.kx[k] = pdep(k, a.kX);
+    for (int n = tid; n < N; n += nthr) t.cn[n] = pdep(n, a.nC);
+}
+
+// The rows of lane `lane` of warp w (of nwarps): its 32-row groups one after another.
+template <int K, int N, bool SCALED>
+__host__ __device__ __forceinline__ void rows2_walk(const Rows2Args& a, const Rows2Smem& t, int64_t w, int64_t nwarps,
+                                                    int lane, float scale, int& emax) {
+    constexpr int BS = K * N + 1;
+    const int64_t lx = pdep(lane, a.laneX), lc = pdep(lane, a.laneC), lb = pdep(lane, a.laneB);
+    const int64_t g0 = a.ngroups * w / nwarps, g1 = a.ngroups * (w + 1) / nwarps;
+    int64_t ox = pdep(g0, a.grpX), oc = pdep(g0, a.grpC), ob = pdep(g0, a.grpB);
+    const float2* __restrict__ X = static_cast<const float2*>(a.X);
+    float2* __restrict__ C = static_cast<float2*>(a.C);
+    const float sx = a.conjX ? -1.f : 1.f;
+    for (int64_t g = g0; g < g1; g++) {
+        const float2* xrow = X + (lx + ox);
+        const float4* yb = t.Ys + (lb + ob) * BS;
+        float xr[K], xi[K];
+        bool paired = false;
+        if constexpr (K > 1) {
+            if (a.xpair) {                                  // k, k+1 adjacent in X
+                paired = true;
+#pragma unroll
+                for (int k = 0; k < K; k += 2) {
+                    const float4 v = *reinterpret_cast<const float4*>(xrow + t.kx[k]);
+                    xr[k] = v.x; xi[k] = v.y; xr[k + 1] = v.z; xi[k + 1] = v.w;
+                }
+            }
+        }
+        if (!paired) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float2 v = xrow[t.kx[k]];
+                xr[k] = v.x; xi[k] = v.y;
+            }
+        }
+        unsigned long long acc[N];
+#pragma unroll
+        for (int n = 0; n < N; n++) acc[n] = 0ull;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float xik = sx * xi[k];
+            const unsigned long long xx = f2pack(xr[k], xr[k]), xj = f2pack(-xik, xik);
+#pragma unroll
+            for (int n = 0; n < N; n++) {
+                const float4 y = yb[k * N + n];
+                fma2(acc[n], xx, f2pack(y.x, y.y));
+                fma2(acc[n], xj, f2pack(y.z, y.w));
+            }
+        }
+        float re[N], im[N];
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            re[n] = u2f((unsigned)(acc[n] & 0xffffffffull));
+            im[n] = u2f((unsigned)(acc[n] >> 32));
+            if (SCALED) {
+                re[n] *= scale; im[n] *= scale;
+                const float mx = fmaxf(fabsf(re[n]), fabsf(im[n]));
+                if (mx > 0.f) emax = emax > exp_of(mx) ? emax : exp_of(mx);
+            }
+        }
+        float2* crow = C + (lc + oc);
+        bool cpaired = false;
+        if constexpr (N > 1) {
+            if (a.cpair) {                                  // n, n+1 adjacent in C
+                cpaired = true;
+#pragma unroll
+                for (int n = 0; n < N; n += 2)
+                    *reinterpret_cast<float4*>(crow + t.cn[n]) = make_float4(re[n], im[n], re[n + 1], im[n + 1]);
+            }
+        }
+        if (!cpaired) {
+#pragma unroll
+            for (int n = 0; n < N; n++) crow[t.cn[n]] = make_float2(re[n], im[n]);
+        }
+        const unsigned long long next = (unsigned long long)(g + 1);
+#ifdef __CUDA_ARCH__
+        const int j = __ffsll((long long)next) - 1;        // bits 0..j of g flip
+#else
+        const int j = __builtin_ctzll(next);
+#endif
+        ox += t.dX[j];
+        oc += t.dC[j];
+        ob += t.dB[j];
+    }
+}
+
+// Launched with kThreads threads; dynamic shared memory: rows2_smem_bytes.
+template <int K, int N, bool SCALED>
+__global__ void __launch_bounds__(kThreads) contract_rows2_kernel(const Rows2Args a, int* exps) {
+    extern __shared__ __align__(16) unsigned char rows2_smem[];
+    const Rows2Smem t = rows2_carve<K, N>(a, rows2_smem);
+    rows2_fill<K, N>(a, t, threadIdx.x, kThreads);
+    __syncthreads();
+    float scale = 1.f;
+    if (SCALED) {
+        const int mX = read_m(exps, a.expX), mY = read_m(exps, a.expY);
+        scale = pow2f(-(mX + mY));
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            exps[2 * a.expC] = exps[2 * a.expX] + exps[2 * a.expY] + mX + mY;
+    }
+    int emax = kExpUnset;
+    rows2_walk<K, N, SCALED>(a, t, (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5),
+                             (int64_t)gridDim.x * (kThreads / 32), threadIdx.x & 31, scale, emax);
+    if (SCALED) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.expC + 1], emax);
+    }
+}
+
+size_t rows2_smem_bytes(const Rows2Args& a, int K, int N) {
+    return sizeof(float4) * (size_t)a.nbatch * (size_t)(K * N + 1) + sizeof(int64_t) * (3 * 48 + K + N);
+}
+
+// Elements of the shared-memory tiles of the tiled long sum (log2, fp32; fp64 one less).
+constexpr int kTileSmemTiles = 11;
+
+// Element index inside a shared-memory tile: the low bits of each 128-byte line XOR the line's
+// low bits, so 32 lanes that differ only in higher bits still fall in distinct banks.
+template <typename T>
+__host__ __device__ __forceinline__ int tile_swz(int e) {
+    constexpr int B = sizeof(T) == 8 ? 4 : 3;
+    return e ^ ((e >> B) & ((1 << B) - 1));
+}
+
+// Tiled long sum with a small result: C[a, b, g] = sum_r A[a, g, r] B[b, g, r] where the summed
+// index r is long (the adjoint steps that end in a gate's gradient sum over every other index of
+// the network), "a" are the result bits only A has, "b" those only B has and "g" those both have.
+// A tile is 2^T values of r (the T summed bits lowest in A); per tile a block loads A's and B's
+// elements of the tile into shared memory in address order (as the tiled row form does), then
+// every thread adds the products of its rows into its results: one a value and up to four
+// consecutive b values, the tile's rows divided among the threads of each result group.  Each
+// block owns one g value and every G-th tile of it; per-thread FP32 sums of one tile are added
+// into FP64 block sums, and a second kernel adds the blocks' FP64 partials of each result in
+// block order (deterministic), scales and stores.  Every element of A and B is read once.
+struct SumTileArgs {
+    const void* A;
+    const void* B;
+    void* C;
+    int64_t ntiles;            // tiles per g value
+    int32_t G;                 // blocks per g value
+    int32_t ng;                // g values
+    int32_t T, na, nb;         // summed bits per tile, bits of a, bits of b
+    int32_t conjA, conjB;
+    int32_t expA, expB, expC;
+    BitMap hiA, hiB;           // tile index (within a g value) -> A / B offset
+    BitMap gA, gB, gC;         // g -> A / B / C offset
+    BitMap eA, fB;             // A tile element (e order) / B tile element (f order) -> offset
+    BitMap sE, sF;             // tile row -> e / f index
+    BitMap aE, aC;             // a -> e index / C offset
+    BitMap bF, bC;             // b -> f index / C offset
+};
+constexpr int kSumMaxOut = 1024;        // a x b results per g value
+constexpr int kSumGroup = 4;            // b values per thread
+
+__host__ __device__ __forceinline__ int sum_groups(const SumTileArgs& a) {
+    const int nbv = 1 << a.nb;
+    return (1 << a.na) * ((nbv + kSumGroup - 1) / kSumGroup);
+}
+
+template <typename T>
+size_t sum_smem_bytes(const SumTileArgs& a) {
+    const size_t tiles = sizeof(T) * ((size_t(1) << (a.T + a.na)) + (size_t(1) << (a.T + a.nb)));
+    const size_t red = sizeof(double) * 2 * kSumGroup * kThreads;
+    return std::max(tiles, red) + sizeof(int) * ((size_t(1) << a.na) + (size_t(1) << a.nb));
+}
+
+// One tile's rows for thread (group og, row lane rl): products into FP32 sums.
+template <typename T>
+__host__ __device__ __forceinline__ void sum_tile_rows(const SumTileArgs& a, int og, int rl, int rt, const T* As,
+                                                       const T* Bs, const int* aE_t, const int* bF_t,
+                                                       typename Real<T>::type* sr, typename Real<T>::type* si) {
+    using R = typename Real<T>::type;
+    const int nbv = 1 << a.nb;
+    const int bgroups = (nbv + kSumGroup - 1) / kSumGroup;
+    const int av = og / bgroups, b0 = (og % bgroups) * kSumGroup;
+    const int ea = aE_t[av];
+    const R ca = a.conjA ? R(-1) : R(1), cb = a.conjB ? R(-1) : R(1);
+    for (int s = rl; s < (1 << a.T); s += rt) {
+        const T u = As[tile_swz<T>((int)pdep(s, a.sE) + ea)];
+        const R ur = u.x, ui = ca * u.y;
+        const int fs = (int)pdep(s, a.sF);
+#pragma unroll
+        for (int j = 0; j < kSumGroup; j++) {
+            if (b0 + j < nbv) {
+                const T v = Bs[tile_swz<T>(fs + bF_t[b0 + j])];
+                const R vr = v.x, vi = cb * v.y;
+                sr[j] = fma(ur, vr, sr[j]);
+                sr[j] = fma(-ui, vi, sr[j]);
+                si[j] = fma(ur, vi, si[j]);
+                si[j] = fma(ui, vr, si[j]);
+            }
+        }
+    }
+}
+
+template <typename T>
+__host__ __device__ __forceinline__ void sum_tile_load(const SumTileArgs& a, int64_t ao, int64_t bo, int tid, int nthr,
+                                                       T* As, T* Bs) {
+    const T* __restrict__ Ag = static_cast<const T*>(a.A) + ao;
+    const T* __restrict__ Bg = static_cast<const T*>(a.B) + bo;
+    const int EA = 1 << (a.T + a.na), E = EA + (1 << (a.T + a.nb));
+    constexpr int U = 8;                    // loads in flight per thread before the stores
+    for (int base = tid; base < E; base += U * nthr) {
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int e = base + u * nthr;
+            if (e < EA) v[u] = Ag[pdep(e, a.eA)];
+            else if (e < E) v[u] = Bg[pdep(e - EA, a.fB)];
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int e = base + u * nthr;
+            if (e < EA) As[tile_swz<T>(e)] = v[u];
+            else if (e < E) Bs[tile_swz<T>(e - EA)] = v[u];
+        }
+    }
+}
+
+// The block's partial of each result: its row lanes' FP64 sums (red: 2 kSumGroup planes of
+// kThreads values) added in lane order.
+__host__ __device__ __forceinline__ void sum_block_out(const SumTileArgs& a, const double* red, int tid, int nthr,
+                                                       double2* pblock) {
+    const int og_n = sum_groups(a), rt = kThreads / og_n;
+    const int nbv = 1 << a.nb, bgroups = (nbv + kSumGroup - 1) / kSumGroup;
+    for (int o = tid; o < og_n * kSumGroup; o += nthr) {
+        const int grp = o / kSumGroup, j = o % kSumGroup;
+        if ((grp % bgroups) * kSumGroup + j >= nbv) continue;
+        double r = 0.0, i = 0.0;
+        for (int l = 0; l < rt; l++) {
+            r += red[(2 * j) * kThreads + l * og_n + grp];
+            i += red[(2 * j + 1) * kThreads + l * og_n + grp];
+        }
+        pblock[o] = make_double2(r, i);
+    }
+}
+
+// Launched with kThreads threads.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) contract_sumtile_kernel(const SumTileArgs a, double2* partial) {
+    using R = typename Real<T>::type;
+    extern __shared__ __align__(16) unsigned char sum_smem[];
+    T* As = reinterpret_cast<T*>(sum_smem);
+    T* Bs = As + (1 << (a.T + a.na));
+    const size_t tiles = sizeof(T) * ((size_t(1) << (a.T + a.na)) + (size_t(1) << (a.T + a.nb)));
+    const size_t red_bytes = sizeof(double) * 2 * kSumGroup * kThreads;
+    double* red = reinterpret_cast<double*>(sum_smem);          // reused after the last tile
+    int* aE_t = reinterpret_cast<int*>(sum_smem + (tiles > red_bytes ? tiles : red_bytes));
+    int* bF_t = aE_t + (1 << a.na);
+    for (int i = threadIdx.x; i < (1 << a.na); i += kThreads) aE_t[i] = (int)pdep(i, a.aE);
+    for (int i = threadIdx.x; i < (1 << a.nb); i += kThreads) bF_t[i] = (int)pdep(i, a.bF);
+    const int g = blockIdx.x / a.G, part = blockIdx.x % a.G;
+    const int og_n = sum_groups(a);
+    const int rt = kThreads / og_n;                              // threads per result group (>= 1)
+    const int og = threadIdx.x % og_n, rl = threadIdx.x / og_n;
+    const bool active = rl < rt;
+    const int64_t abase = pdep(g, a.gA), bbase = pdep(g, a.gB);
+    double dr[kSumGroup], di[kSumGroup];
+    for (int j = 0; j < kSumGroup; j++) { dr[j] = 0.0; di[j] = 0.0; }
+    for (int64_t t = part; t < a.ntiles; t += a.G) {
+        sum_tile_load<T>(a, abase + pdep(t, a.hiA), bbase + pdep(t, a.hiB), threadIdx.x, kThreads, As, Bs);
+        __syncthreads();                                         // tiles (and tables) in place
+        if (active) {
+            R sr[kSumGroup], si[kSumGroup];
+            for (int j = 0; j < kSumGroup; j++) { sr[j] = R(0); si[j] = R(0); }
+            sum_tile_rows<T>(a, og, rl, rt, As, Bs, aE_t, bF_t, sr, si);
+            for (int j = 0; j < kSumGroup; j++) { dr[j] += (double)sr[j]; di[j] += (double)si[j]; }
+        }
+        __syncthreads();                                         // tiles free for the next loads
+    }
+    for (int j = 0; j < kSumGroup; j++) {
+        red[(2 * j) * kThreads + threadIdx.x] = dr[j];
+        red[(2 * j + 1) * kThreads + threadIdx.x] = di[j];
+    }
+    __syncthreads();
+    sum_block_out(a, red, threadIdx.x, kThreads, partial + (int64_t)blockIdx.x * (og_n * kSumGroup));
+}
+
+// One result of the reduce: the blocks' partials in block order, scaled.
+template <typename T>
+__host__ __device__ __forceinline__ bool sum_reduce_one(const SumTileArgs& a, const double2* partial, int64_t idx,
+                                                        double scale, T* C, float* mag) {
+    using R = typename Real<T>::type;
+    const int og_n = sum_groups(a), per = og_n * kSumGroup;
+    const int nbv = 1 << a.nb, bgroups = (nbv + kSumGroup - 1) / kSumGroup;
+    const int g = (int)(idx / per), o = (int)(idx % per);
+    const int grp = o / kSumGroup, j = o % kSumGroup;
+    const int av = grp / bgroups, bv = (grp % bgroups) * kSumGroup + j;
+    if (bv >= nbv) return false;
+    double r = 0.0, i = 0.0;
+    for (int p = 0; p < a.G; p++) {
+        const double2 v = partial[((int64_t)g * a.G + p) * per + o];
+        r += v.x;
+        i += v.y;
+    }
+    r *= scale; i *= scale;
+    *mag = fmaxf(fabsf((float)r), fabsf((float)i));
+    T out; out.x = (R)r; out.y = (R)i;
+    C[pdep(g, a.gC) + pdep(av, a.aC) + pdep(bv, a.bC)] = out;
+    return true;
+}
+
+// Adds the blocks' partials of each result, scales into the result's exponent and stores;
+// raises the result's exponent slot like the other contraction kernels.
+template <typename T, bool SCALED>
+__global__ void sumtile_reduce_kernel(const SumTileArgs a, const double2* partial, int* exps) {
+    double scale = 1.0;
+    if (SCALED) {
+        const int mA = read_m(exps, a.expA), mB = read_m(exps, a.expB);
+        scale = pow2d(-(mA + mB));
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            exps[2 * a.expC] = exps[2 * a.expA] + exps[2 * a.expB] + mA + mB;
+    }
+    const int64_t total = (int64_t)a.ng * sum_groups(a) * kSumGroup;
+    int emax = kExpUnset;
+    T* __restrict__ C = static_cast<T*>(a.C);
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        float mx = 0.f;
+        if (sum_reduce_one<T>(a, partial, idx, scale, C, &mx) && SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
     }
     if (SCALED) {
         for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
@@ -582,6 +1013,160 @@ bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra) {
     return true;
 }
 
+// Fill the compact row form (FP32) from a row form: K <= 32, N <= 16, K N <= 256, >= 32 rows.
+bool plan_rows2(const RowArgs& ra, Rows2Args* r2) {
+    auto lg = [](int64_t v) { int b = 0; while ((int64_t(1) << b) < v) b++; return b; };
+    auto pos_of = [](const BitMap& m, int64_t bit) {
+        const int64_t o = pdep(bit, m);
+        return o ? __builtin_ctzll((unsigned long long)o) : -1;
+    };
+    const int R = lg(ra.nrows);
+    if (R < 5 || ra.K > 32 || ra.N > 16 || ra.K * ra.N > 256) return false;
+    std::vector<std::pair<int, int>> lX, lC, lB, gX, gC, gB, nY, bY;
+    int nb = 0;
+    for (int i = 0; i < R; i++) {
+        const int c = pos_of(ra.rowmap, int64_t(1) << i);
+        const int x = pos_of(ra.cX, int64_t(1) << c), y = pos_of(ra.cY, int64_t(1) << c);
+        if (c < 0 || x < 0) return false;
+        auto& mx = i < 5 ? lX : gX;
+        auto& mc = i < 5 ? lC : gC;
+        auto& mb = i < 5 ? lB : gB;
+        const int src = i < 5 ? i : i - 5;
+        mx.push_back({src, x});
+        mc.push_back({src, c});
+        if (y >= 0) {
+            mb.push_back({src, nb});
+            bY.push_back({nb, y});
+            nb++;
+        }
+    }
+    for (int j = 0; (1 << j) < ra.N; j++) {
+        const int c = pos_of(ra.nmap, int64_t(1) << j);
+        const int y = c < 0 ? -1 : pos_of(ra.cY, int64_t(1) << c);
+        if (y < 0) return false;
+        nY.push_back({j, y});
+    }
+    memset(r2, 0, sizeof(*r2));
+    if (!make_runs(lX, &r2->laneX) || !make_runs(lC, &r2->laneC) || !make_runs(lB, &r2->laneB) ||
+        !make_runs(gX, &r2->grpX) || !make_runs(gC, &r2->grpC) || !make_runs(gB, &r2->grpB) ||
+        !make_runs(nY, &r2->nY) || !make_runs(bY, &r2->bY))
+        return false;
+    r2->kX = ra.kX;
+    r2->kY = ra.kY;
+    r2->nC = ra.nmap;
+    r2->X = ra.X;
+    r2->Y = ra.Y;
+    r2->C = ra.C;
+    r2->ngroups = int64_t(1) << (R - 5);
+    r2->nbatch = 1 << nb;
+    if ((int64_t)r2->nbatch * ra.K * ra.N > kRows2MaxY) return false;
+    r2->conjX = ra.conjX;
+    r2->conjY = ra.conjY;
+    r2->expX = ra.expX;
+    r2->expY = ra.expY;
+    r2->expC = ra.expC;
+    r2->xpair = ra.K > 1 && pdep(1, ra.kX) == 1 && (reinterpret_cast<uintptr_t>(ra.X) & 15) == 0;
+    r2->cpair = ra.N > 1 && pdep(1, ra.nmap) == 1 && (reinterpret_cast<uintptr_t>(ra.C) & 15) == 0;
+    return true;
+}
+
+// Fill the tiled long sum: at least 2^12 summed terms, at most 2^6 values of each of the a and
+// b bits and kSumMaxOut results per g value.  blocks: the blocks the launch should fill.
+bool plan_sumtiles(const StepArgs& s, int esize, int64_t blocks, SumTileArgs* sa) {
+    if (s.nk < 12 || s.nk > 46) return false;
+    auto one = [](const BitMap& m, int bit) {              // destination bit of one index bit, or -1
+        const int64_t o = pdep(int64_t(1) << bit, m);
+        return o ? __builtin_ctzll((unsigned long long)o) : -1;
+    };
+    int ncb = 0;
+    while ((int64_t(1) << ncb) < s.nC) ncb++;
+    std::vector<int> ab, bb, gb;                            // result bits by owner
+    for (int p = 0; p < ncb; p++) {
+        const bool ia = one(s.cA, p) >= 0, ib = one(s.cB, p) >= 0;
+        if (ia && ib) gb.push_back(p);
+        else if (ia) ab.push_back(p);
+        else if (ib) bb.push_back(p);
+        else return false;
+    }
+    const int na = (int)ab.size(), nb = (int)bb.size(), nk = s.nk;
+    if (na > 6 || nb > 6 || (int64_t(1) << (na + nb)) > kSumMaxOut) return false;
+    const int budget = esize == 8 ? kTileSmemTiles : kTileSmemTiles - 1;
+    const int T = std::min({8, nk, budget - na, budget - nb});
+    if (T < 4) return false;
+    // summed bits by position in the larger operand
+    int amax = 0, bmax = 0;
+    for (int j = 0; j < nk; j++) {
+        if (one(s.kA, j) < 0 || one(s.kB, j) < 0) return false;
+        amax = std::max(amax, one(s.kA, j));
+        bmax = std::max(bmax, one(s.kB, j));
+    }
+    for (int p : ab) amax = std::max(amax, one(s.cA, p));
+    for (int p : bb) bmax = std::max(bmax, one(s.cB, p));
+    const bool by_a = amax >= bmax;
+    std::vector<int> ks(nk);
+    for (int j = 0; j < nk; j++) ks[j] = j;
+    std::sort(ks.begin(), ks.end(), [&](int x, int y) {
+        return by_a ? one(s.kA, x) < one(s.kA, y) : one(s.kB, x) < one(s.kB, y);
+    });
+    struct TB { int pos, kind, idx; };
+    std::vector<TB> xe, xf;
+    for (int i = 0; i < T; i++) { xe.push_back({one(s.kA, ks[i]), 0, i}); xf.push_back({one(s.kB, ks[i]), 0, i}); }
+    for (int j = 0; j < na; j++) xe.push_back({one(s.cA, ab[j]), 1, j});
+    for (int j = 0; j < nb; j++) xf.push_back({one(s.cB, bb[j]), 1, j});
+    auto bypos = [](const TB& p, const TB& q) { return p.pos < q.pos; };
+    std::sort(xe.begin(), xe.end(), bypos);
+    std::sort(xf.begin(), xf.end(), bypos);
+    std::vector<std::pair<int, int>> pe, pf, psE(T), psF(T), paE(na), pbF(nb), paC, pbC, phA, phB, pgA, pgB, pgC;
+    for (int i = 0; i < (int)xe.size(); i++) {
+        pe.push_back({i, xe[i].pos});
+        if (xe[i].kind == 0) psE[xe[i].idx] = {xe[i].idx, i};
+        else paE[xe[i].idx] = {xe[i].idx, i};
+    }
+    for (int i = 0; i < (int)xf.size(); i++) {
+        pf.push_back({i, xf[i].pos});
+        if (xf[i].kind == 0) psF[xf[i].idx] = {xf[i].idx, i};
+        else pbF[xf[i].idx] = {xf[i].idx, i};
+    }
+    for (int j = 0; j < na; j++) paC.push_back({j, ab[j]});
+    for (int j = 0; j < nb; j++) pbC.push_back({j, bb[j]});
+    for (int i = T; i < nk; i++) { phA.push_back({i - T, one(s.kA, ks[i])}); phB.push_back({i - T, one(s.kB, ks[i])}); }
+    for (int i = 0; i < (int)gb.size(); i++) {
+        pgA.push_back({i, one(s.cA, gb[i])});
+        pgB.push_back({i, one(s.cB, gb[i])});
+        pgC.push_back({i, gb[i]});
+    }
+    memset(sa, 0, sizeof(*sa));
+    if (!make_runs(pe, &sa->eA) || !make_runs(pf, &sa->fB) || !make_runs(psE, &sa->sE) || !make_runs(psF, &sa->sF) ||
+        !make_runs(paE, &sa->aE) || !make_runs(pbF, &sa->bF) || !make_runs(paC, &sa->aC) || !make_runs(pbC, &sa->bC) ||
+        !make_runs(phA, &sa->hiA) || !make_runs(phB, &sa->hiB) || !make_runs(pgA, &sa->gA) || !make_runs(pgB, &sa->gB) ||
+        !make_runs(pgC, &sa->gC))
+        return false;
+    if (gb.size() > 20) return false;
+    sa->A = s.A;
+    sa->B = s.B;
+    sa->C = s.C;
+    sa->T = T;
+    sa->na = na;
+    sa->nb = nb;
+    sa->ng = 1 << (int)gb.size();
+    sa->ntiles = int64_t(1) << (nk - T);
+    const int64_t want = (blocks + sa->ng - 1) / sa->ng;
+    sa->G = (int)std::max<int64_t>(1, std::min<int64_t>(want, sa->ntiles));
+    sa->conjA = s.conjA;
+    sa->conjB = s.conjB;
+    sa->expA = s.expA;
+    sa->expB = s.expB;
+    sa->expC = s.expC;
+    return true;
+}
+
+size_t sum_partial_bytes(const SumTileArgs& sa) {
+    return (size_t)sa.ng * (size_t)sa.G * (size_t)sum_groups(sa) * kSumGroup * sizeof(double2);
+}
+
+// Blocks a tiled long sum aims at: eight per SM.
+int64_t sum_blocks(int sm_count) { return (int64_t)sm_count * 8; }
+
 // Splits of the split-K form: used when the results are few (<= 2^14) and each sums at least
 // 2^14 terms; enough splits of the high K index to give about 8 blocks per SM, at least 2^12
 // terms per split, and at most 2^22 partials in all.
@@ -604,6 +1189,47 @@ void launch_general(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int
     else contract_kernel<float2, false, CONJ><<<grid, kThreads, 0, s>>>(a, exps);
 }
 
+template <int K, int N>
+cudaError_t launch_rows2_kn(const Rows2Args& r2, int* exps, cudaStream_t s, int sm_count) {
+    const size_t smem = rows2_smem_bytes(r2, K, N);
+    auto launch = [&](auto kern) -> cudaError_t {
+        int per_sm = 0;
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+        if (e != cudaSuccess) return e;
+        const int64_t cap = (int64_t)sm_count * std::max(per_sm, 1);
+        const int64_t want = (r2.ngroups + kThreads / 32 - 1) / (kThreads / 32);
+        const int grid = (int)std::max<int64_t>(1, std::min(want, cap));
+        kern<<<grid, kThreads, smem, s>>>(r2, exps);
+        return cudaGetLastError();
+    };
+    return exps ? launch(contract_rows2_kernel<K, N, true>) : launch(contract_rows2_kernel<K, N, false>);
+}
+
+template <int K>
+cudaError_t launch_rows2_k(const Rows2Args& r2, int N, int* exps, cudaStream_t s, int sm_count) {
+    switch (N) {
+        case 1: return launch_rows2_kn<K, 1>(r2, exps, s, sm_count);
+        case 2: return launch_rows2_kn<K, 2>(r2, exps, s, sm_count);
+        case 4: return launch_rows2_kn<K, 4>(r2, exps, s, sm_count);
+        case 8: if constexpr (K <= 32) return launch_rows2_kn<K, 8>(r2, exps, s, sm_count); break;
+        case 16: if constexpr (K <= 16) return launch_rows2_kn<K, 16>(r2, exps, s, sm_count); break;
+        default: break;
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_rows2(const Rows2Args& r2, int K, int N, int* exps, cudaStream_t s, int sm_count) {
+    switch (K) {
+        case 1: return launch_rows2_k<1>(r2, N, exps, s, sm_count);
+        case 2: return launch_rows2_k<2>(r2, N, exps, s, sm_count);
+        case 4: return launch_rows2_k<4>(r2, N, exps, s, sm_count);
+        case 8: return launch_rows2_k<8>(r2, N, exps, s, sm_count);
+        case 16: return launch_rows2_k<16>(r2, N, exps, s, sm_count);
+        case 32: return launch_rows2_k<32>(r2, N, exps, s, sm_count);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 template <typename T, int KMAX>
 cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_count) {
     const size_t smem = (size_t)ra.ny * sizeof(T) + (size_t)KMAX * 12 + (size_t)ra.N * 12;
@@ -621,8 +1247,32 @@ cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_cou
 size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
     RowArgs ra;
     if (plan_rows(a, fp64 ? 16 : 32, &ra)) return 0;
+    SumTileArgs sa;
+    if (plan_sumtiles(a, fp64 ? 16 : 8, sum_blocks(sm_count), &sa)) return sum_partial_bytes(sa);
     const int ns = splitk_count(a, sm_count);
     return ns > 0 ? (size_t)ns * (size_t)a.nC * (fp64 ? 16 : 8) : 0;
+}
+
+bool contract_prefers_cuda_cores(const StepArgs& a, bool fp64, int sm_count) {
+    SumTileArgs sa;
+    return plan_sumtiles(a, fp64 ? 16 : 8, sum_blocks(sm_count), &sa) && sa.na + sa.nb <= 7;
+}
+
+template <typename T>
+cudaError_t launch_sumtiles(const SumTileArgs& sa, void* scratch, int* exps, cudaStream_t s) {
+    const size_t smem = sum_smem_bytes<T>(sa);
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(contract_sumtile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    double2* partial = static_cast<double2*>(scratch);
+    contract_sumtile_kernel<T><<<(unsigned)((int64_t)sa.ng * sa.G), kThreads, smem, s>>>(sa, partial);
+    const int64_t total = (int64_t)sa.ng * sum_groups(sa) * kSumGroup;
+    const int g = grid_for(total, 256, 1024);
+    if (exps && sizeof(T) == 8) sumtile_reduce_kernel<T, true><<<g, 256, 0, s>>>(sa, partial, exps);
+    else sumtile_reduce_kernel<T, false><<<g, 256, 0, s>>>(sa, partial, exps);
+    return cudaGetLastError();
 }
 
 template <typename T, int CONJ>
@@ -651,11 +1301,29 @@ bool contract_uses_rows(const StepArgs& a, bool fp64) {
     return plan_rows(a, fp64 ? 16 : 32, &ra);
 }
 
+const char* contract_form(const StepArgs& a, bool fp64, int sm_count) {
+    RowArgs ra;
+    if (plan_rows(a, fp64 ? 16 : 32, &ra)) {
+        Rows2Args r2;
+        return !fp64 && plan_rows2(ra, &r2) ? "cuda-core compact row-form" : "cuda-core row-form";
+    }
+    SumTileArgs sa;
+    if (plan_sumtiles(a, fp64 ? 16 : 8, sum_blocks(sm_count), &sa)) return "cuda-core tiled long-sum";
+    return splitk_count(a, sm_count) > 0 ? "cuda-core split-K" : "cuda-core general";
+}
+
 cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count, void* scratch,
                             size_t scratch_bytes, int* launches) {
     if (launches) *launches = 1;
     RowArgs ra;
     if (!plan_rows(a, fp64 ? 16 : 32, &ra)) {
+        SumTileArgs sa;
+        if (plan_sumtiles(a, fp64 ? 16 : 8, sum_blocks(sm_count), &sa)) {
+            if (scratch && scratch_bytes >= sum_partial_bytes(sa)) {
+                if (launches) *launches = 2;
+                return fp64 ? launch_sumtiles<double2>(sa, scratch, exps, s) : launch_sumtiles<float2>(sa, scratch, exps, s);
+            }
+        }
         const int ns = splitk_count(a, sm_count);
         if (ns > 0 && scratch && scratch_bytes >= (size_t)ns * (size_t)a.nC * (fp64 ? 16 : 8)) {
             if (launches) *launches = 2;
@@ -663,6 +1331,8 @@ cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_
         }
     }
     if (plan_rows(a, fp64 ? 16 : 32, &ra)) {
+        Rows2Args r2;
+        if (!fp64 && plan_rows2(ra, &r2)) return launch_rows2(r2, ra.K, ra.N, exps, s, sm_count);
         if (fp64) return ra.K <= 4 ? launch_rows<double2, 4>(ra, exps, s, sm_count)
                                    : launch_rows<double2, 16>(ra, exps, s, sm_count);
         if (ra.K <= 4) return launch_rows<float2, 4>(ra, exps, s, sm_count);

@@ -120,7 +120,16 @@ extern "C" int qxg_ncon(int32_t precision, void* C, int32_t nc, const int32_t* c
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const cudaError_t e = launch_contract(s, precision == QXG_PREC_FP64, nullptr, (cudaStream_t)stream, sms);
+    // steps with few results and a long sum keep per-block partials in stream-ordered scratch
+    const bool fp64 = precision == QXG_PREC_FP64;
+    const size_t need = contract_scratch_bytes(s, fp64, sms);
+    void* scratch = nullptr;
+    if (need) {
+        const cudaError_t ea = cudaMallocAsync(&scratch, need, (cudaStream_t)stream);
+        if (ea != cudaSuccess) return ncon_fail(QXG_ERR_CUDA, cudaGetErrorString(ea));
+    }
+    const cudaError_t e = launch_contract(s, fp64, nullptr, (cudaStream_t)stream, sms, scratch, need);
+    if (scratch) cudaFreeAsync(scratch, (cudaStream_t)stream);
     if (e != cudaSuccess) return ncon_fail(QXG_ERR_CUDA, cudaGetErrorString(e));
     return QXG_OK;
 }

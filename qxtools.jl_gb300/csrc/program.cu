@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -178,6 +179,9 @@ struct qxg_program {
     int grad_runs = 0;
     int64_t launches_per_gradpass = 0;
     const void* grad_key[3] = {nullptr, nullptr, nullptr};
+    // streams and events of captures with concurrent branches (created on first capture)
+    std::vector<cudaStream_t> cap_streams;
+    std::vector<cudaEvent_t> cap_ev;
 };
 
 namespace {
@@ -509,7 +513,8 @@ int build_backward(qxg_program* P, Plan& pl, int* err) {
         st.sargs.expC = T[res].slot;
         st.flops = 8.0 * (double)st.sargs.nC * (double)(int64_t(1) << st.sargs.nk);
         st.bytes = es * (sz(x) + sz(y) + sz(res));
-        if (!P->fp64 && P->opts.precision != QXG_PREC_FP32)
+        if (!P->fp64 && P->opts.precision != QXG_PREC_FP32 &&
+            !contract_prefers_cuda_cores(st.sargs, P->fp64, P->sm_count))
             st.use_tc = tc_plan_step(st.sargs, T[x].layout.size(), T[y].layout.size(), T[res].layout.size(),
                                      P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc,
                                      (double)P->opts.tc_plane_budget_mb * (1 << 20));
@@ -749,7 +754,8 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
             st.flops = 8.0 * (double)st.sargs.nC * (double)(int64_t(1) << kbit);
             st.bytes = s * ((double)(int64_t(1) << A.layout.size()) + (double)(int64_t(1) << B.layout.size()) +
                             (double)st.sargs.nC);
-            if (!P->fp64 && P->opts.precision != QXG_PREC_FP32)
+            if (!P->fp64 && P->opts.precision != QXG_PREC_FP32 &&
+                !contract_prefers_cuda_cores(st.sargs, P->fp64, P->sm_count))
                 st.use_tc = tc_plan_step(st.sargs, A.layout.size(), B.layout.size(), t.layout.size(),
                                          P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc,
                                      (double)P->opts.tc_plane_budget_mb * (1 << 20));
@@ -1139,6 +1145,183 @@ int run_group(qxg_program* P, int g) {
     return 0;
 }
 
+// ---- launches with their dependencies ------------------------------------------------------
+// Under stream capture a pass becomes a graph whose edges are the launches' true dependencies
+// instead of one chain.  Each unit of work names the device ranges it reads and writes (arena
+// bytes of its tensors, the shared scratch, its span of the gradient vector, the amplitude
+// output); work j follows work i < j when one of them writes what the other touches.  The
+// independent sub-trees of the contraction tree (the many small gate-absorption steps, whose
+// kernels fill a fraction of the GPU) then run side by side.  Eager runs, and profiling, keep
+// one stream and the plan's order.
+struct Span { int space; int64_t lo, hi; };
+constexpr int kSpanArena = 0, kSpanScratch = 1, kSpanGrad = 2, kSpanOut = 3;
+constexpr int kCaptureStreams = 8;
+
+struct Work {
+    std::function<int(cudaStream_t)> launch;
+    std::vector<Span> rd, wr;
+};
+
+bool spans_meet(const std::vector<Span>& a, const std::vector<Span>& b) {
+    for (const Span& x : a)
+        for (const Span& y : b)
+            if (x.space == y.space && x.lo < y.hi && y.lo < x.hi) return true;
+    return false;
+}
+
+void add_tensor_span(const qxg_program* P, const Plan& pl, int t, std::vector<Span>& out) {
+    if (t < 0 || pl.T[t].arena_off < 0) return;          // leaves live outside the arena, read-only
+    const int64_t bytes = ((int64_t(1) << pl.T[t].layout.size()) * (int64_t)P->esize + 255) & ~int64_t(255);
+    out.push_back({kSpanArena, pl.T[t].arena_off, pl.T[t].arena_off + bytes});
+}
+
+bool step_uses_scratch(const qxg_program* P, const Step& st) {
+    if (st.kind != QXG_OP_NCON) return false;
+    return st.use_tc || contract_scratch_bytes(st.sargs, P->fp64, P->sm_count) > 0;
+}
+
+void add_step_spans(const qxg_program* P, const Plan& pl, const Step& st, Work& w) {
+    add_tensor_span(P, pl, st.reads[0], w.rd);
+    add_tensor_span(P, pl, st.reads[1], w.rd);
+    add_tensor_span(P, pl, st.tensor, w.wr);
+    if (step_uses_scratch(P, st)) w.wr.push_back({kSpanScratch, 0, 1});
+    if (st.bkind == kBwdLeaf) w.wr.push_back({kSpanGrad, st.goff, st.goff + st.largs.n});
+}
+
+int launch_works(qxg_program* P, std::vector<Work>& w) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    QXG_CUDA(cudaStreamIsCapturing(P->stream, &cs));
+    const int n = (int)w.size();
+    if (cs != cudaStreamCaptureStatusActive || n < 2) {
+        for (auto& x : w)
+            if (int r = x.launch(P->stream)) return r;
+        return 0;
+    }
+    // direct dependencies, less those implied through another dependency (ancestor bit sets)
+    const int words = (n + 63) / 64;
+    std::vector<uint64_t> anc((size_t)n * words, 0), cover(words);
+    std::vector<std::vector<int>> deps(n);
+    std::vector<int> cand;
+    for (int j = 0; j < n; j++) {
+        cand.clear();
+        for (int i = 0; i < j; i++)
+            if (spans_meet(w[j].wr, w[i].rd) || spans_meet(w[j].wr, w[i].wr) || spans_meet(w[j].rd, w[i].wr))
+                cand.push_back(i);
+        std::fill(cover.begin(), cover.end(), 0);
+        for (int i : cand)
+            for (int q = 0; q < words; q++) cover[q] |= anc[(size_t)i * words + q];
+        uint64_t* aj = &anc[(size_t)j * words];
+        for (int q = 0; q < words; q++) aj[q] = cover[q];
+        for (int i : cand) {
+            if (!((cover[i / 64] >> (i % 64)) & 1)) deps[j].push_back(i);
+            aj[i / 64] |= uint64_t(1) << (i % 64);
+        }
+    }
+    while ((int)P->cap_streams.size() < kCaptureStreams) {
+        cudaStream_t s;
+        QXG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        P->cap_streams.push_back(s);
+    }
+    while ((int)P->cap_ev.size() < n + 1 + kCaptureStreams) {
+        cudaEvent_t e;
+        QXG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        P->cap_ev.push_back(e);
+    }
+    // stream 0 is the capturing stream; the others fork from it and join it at the end
+    cudaStream_t streams[kCaptureStreams];
+    streams[0] = P->stream;
+    for (int s = 1; s < kCaptureStreams; s++) streams[s] = P->cap_streams[s];
+    cudaEvent_t fork = P->cap_ev[n];
+    QXG_CUDA(cudaEventRecord(fork, P->stream));
+    int last[kCaptureStreams];
+    bool joined[kCaptureStreams];
+    for (int s = 0; s < kCaptureStreams; s++) { last[s] = -1; joined[s] = s == 0; }
+    std::vector<int> on(n, 0);
+    for (int j = 0; j < n; j++) {
+        int s = -1;
+        for (int i : deps[j])                           // continue the chain of a dependency
+            if (last[on[i]] == i && (s < 0 || i > last[s])) s = on[i];
+        if (s < 0) {                                    // else the stream idle the longest
+            s = 0;
+            for (int q = 1; q < kCaptureStreams; q++) if (last[q] < last[s]) s = q;
+        }
+        if (!joined[s]) {
+            QXG_CUDA(cudaStreamWaitEvent(streams[s], fork, 0));
+            joined[s] = true;
+        }
+        for (int i : deps[j])
+            if (on[i] != s) QXG_CUDA(cudaStreamWaitEvent(streams[s], P->cap_ev[i], 0));
+        if (int r = w[j].launch(streams[s])) return r;
+        QXG_CUDA(cudaEventRecord(P->cap_ev[j], streams[s]));
+        on[j] = s;
+        last[s] = j;
+    }
+    for (int s = 1; s < kCaptureStreams; s++) {
+        if (!joined[s]) continue;
+        cudaEvent_t e = P->cap_ev[n + s];
+        QXG_CUDA(cudaEventRecord(e, streams[s]));
+        QXG_CUDA(cudaStreamWaitEvent(P->stream, e, 0));
+    }
+    return 0;
+}
+
+// The launches of one forward step on stream `s` (profiled in eager runs, where s is the
+// programme's stream).
+int launch_fwd_step(qxg_program* P, Plan& pl, Step& st, int* exps, cudaStream_t s) {
+    const int instr = pl.T[st.tensor].instr;
+    if (st.use_tc)
+        if (int r = tune_tc_step(P, st, exps)) return r;
+    size_t ev = 0;
+    if (int r = prof_begin(P, &ev)) return r;
+    int kind;
+    if (st.kind == QXG_OP_NCON) {
+        if (st.use_tc && st.tc.nouter > 0) {
+            // outer N blocks: pack and GEMM per block under one record
+            kind = QXG_KERNEL_CONTRACT_TC;
+            int nl = 0;
+            QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, s, P->sm_count, &nl));
+            P->launches += nl - 1;
+        } else if (st.use_tc) {
+            // pack both operands (its own record), then the tensor-core GEMM
+            QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, s, P->sm_count));
+            const double pack_bytes = (double)P->esize *
+                    (double)((int64_t(1) << pl.T[P->ins[instr].a].layout.size()) +
+                             (int64_t(1) << pl.T[P->ins[instr].b].layout.size())) +
+                (double)st.tc.scratch_bytes;
+            if (int r = prof_end(P, ev, instr, QXG_KERNEL_TC_PACK, 0.0, pack_bytes)) return r;
+            if (!st.tc.fused) P->launches++;             // X and Y both packed
+            if (int r = prof_begin(P, &ev)) return r;
+            kind = QXG_KERNEL_CONTRACT_TC;
+            QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, s, P->sm_count));
+            if (st.tc.ks > 0) P->launches++;            // the split-K sum
+        } else {
+            kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
+            int nl = 1;
+            QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, s, P->sm_count, P->d_scratch, P->scratch_cap, &nl));
+            P->launches += nl - 1;
+        }
+    } else if (st.kind == QXG_OP_VIEW) {
+        kind = QXG_KERNEL_VIEW;
+        QXG_CUDA(launch_view(st.vargs, P->fp64, exps, s));
+    } else {
+        kind = QXG_KERNEL_OUTPUT;
+        st.oargs.bitstrings = P->d_bits;
+        QXG_CUDA(launch_output(st.oargs, P->fp64, exps, s));
+    }
+    return prof_end(P, ev, instr, kind, st.flops, st.bytes);
+}
+
+void append_group_works(qxg_program* P, Plan& pl, int g, int* exps, std::vector<Work>& w) {
+    for (auto& st : pl.steps[g]) {
+        Work x;
+        Step* sp = &st;
+        Plan* pp = &pl;
+        x.launch = [P, pp, sp, exps](cudaStream_t s) { return launch_fwd_step(P, *pp, *sp, exps, s); };
+        add_step_spans(P, pl, st, x);
+        w.push_back(std::move(x));
+    }
+}
+
 int run_group_eager(qxg_program* P, int g, Plan* plp) {
     Plan& pl = plp ? *plp : *P->plan;
     int* exps = P->fp64 ? nullptr : P->d_exps;
@@ -1146,51 +1329,9 @@ int run_group_eager(qxg_program* P, int g, Plan* plp) {
         QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[g], pl.slot_end[g], P->stream));
         P->launches++;
     }
-    for (auto& st : pl.steps[g]) {
-        const int instr = pl.T[st.tensor].instr;
-        if (st.use_tc)
-            if (int r = tune_tc_step(P, st, exps)) return r;
-        size_t ev = 0;
-        if (int r = prof_begin(P, &ev)) return r;
-        int kind;
-        if (st.kind == QXG_OP_NCON) {
-            if (st.use_tc && st.tc.nouter > 0) {
-                // outer N blocks: pack and GEMM per block under one record
-                kind = QXG_KERNEL_CONTRACT_TC;
-                int nl = 0;
-                QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count, &nl));
-                P->launches += nl - 1;
-            } else if (st.use_tc) {
-                // pack both operands (its own record), then the tensor-core GEMM
-                QXG_CUDA(tc_run_pack(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
-                const double pack_bytes = (double)P->esize *
-                        (double)((int64_t(1) << pl.T[P->ins[instr].a].layout.size()) +
-                                 (int64_t(1) << pl.T[P->ins[instr].b].layout.size())) +
-                    (double)st.tc.scratch_bytes;
-                if (int r = prof_end(P, ev, instr, QXG_KERNEL_TC_PACK, 0.0, pack_bytes)) return r;
-                if (!st.tc.fused) P->launches++;             // X and Y both packed
-                if (int r = prof_begin(P, &ev)) return r;
-                kind = QXG_KERNEL_CONTRACT_TC;
-                QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count));
-                if (st.tc.ks > 0) P->launches++;            // the split-K sum
-            } else {
-                kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
-                int nl = 1;
-                QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count, P->d_scratch, P->scratch_cap,
-                                         &nl));
-                P->launches += nl - 1;
-            }
-        } else if (st.kind == QXG_OP_VIEW) {
-            kind = QXG_KERNEL_VIEW;
-            QXG_CUDA(launch_view(st.vargs, P->fp64, exps, P->stream));
-        } else {
-            kind = QXG_KERNEL_OUTPUT;
-            st.oargs.bitstrings = P->d_bits;
-            QXG_CUDA(launch_output(st.oargs, P->fp64, exps, P->stream));
-        }
-        if (int r = prof_end(P, ev, instr, kind, st.flops, st.bytes)) return r;
-    }
-    return 0;
+    std::vector<Work> w;
+    append_group_works(P, pl, g, exps, w);
+    return launch_works(P, w);
 }
 
 int run_reduce(qxg_program* P, Plan* plp = nullptr) {
@@ -1289,48 +1430,73 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
     const size_t seed_bytes = (size_t)P->esize << pl.T[n + P->root].layout.size();
     // one pass: forward recomputation, seed, adjoint steps (kernel arguments: the plan's buffers
     // and d_out / d_ampbar / d_grad)
+    auto bwd_step = [&](Step& st, cudaStream_t s) -> int {
+        if (st.use_tc)
+            if (int r = tune_tc_step(P, st, exps)) return r;
+        size_t ev = 0;
+        if (int r = prof_begin(P, &ev)) return r;
+        int kind = QXG_KERNEL_REDUCE;
+        if (st.bkind == kBwdNcon) {
+            if (st.use_tc) {
+                int nl = 0;
+                QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, s, P->sm_count, &nl));
+                P->launches += nl - 1;
+                kind = QXG_KERNEL_CONTRACT_TC;
+            } else {
+                int nl = 1;
+                QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, s, P->sm_count, P->d_scratch, P->scratch_cap, &nl));
+                P->launches += nl - 1;
+                kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
+            }
+        } else if (st.bkind == kBwdView) {
+            QXG_CUDA(launch_view_adjoint(st.vaargs, P->fp64, exps, s));
+            kind = QXG_KERNEL_VIEW;
+        } else {
+            LeafGradArgs la = st.largs;
+            la.grad = d_grad + 2 * st.goff;
+            QXG_CUDA(launch_leaf_grad(la, P->fp64, exps, s));
+        }
+        return prof_end(P, ev, st.instr, kind, st.flops, st.bytes);
+    };
     auto body = [&]() -> int {
         if (exps) {
             QXG_CUDA(launch_reset_exps(exps, pl.slot_begin[0], pl.slot_all_end, P->stream));
             P->launches++;
         }
-        for (int g = 0; g < 3; g++)
-            if (int r = run_group_eager(P, g, &pl)) return r;
-        if (d_out)
-            if (int r = run_reduce(P, &pl)) return r;
-        QXG_CUDA(cudaMemsetAsync(pl.seed.dst, 0, seed_bytes, P->stream));
-        QXG_CUDA(launch_seed(pl.seed, P->fp64, exps, P->stream));
-        P->launches++;
-        for (auto& st : pl.bsteps) {
-            if (st.use_tc)
-                if (int r = tune_tc_step(P, st, exps)) return r;
-            size_t ev = 0;
-            if (int r = prof_begin(P, &ev)) return r;
-            int kind = QXG_KERNEL_REDUCE;
-            if (st.bkind == kBwdNcon) {
-                if (st.use_tc) {
-                    int nl = 0;
-                    QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, P->stream, P->sm_count, &nl));
-                    P->launches += nl - 1;
-                    kind = QXG_KERNEL_CONTRACT_TC;
-                } else {
-                    int nl = 1;
-                    QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, P->stream, P->sm_count, P->d_scratch,
-                                             P->scratch_cap, &nl));
-                    P->launches += nl - 1;
-                    kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
-                }
-            } else if (st.bkind == kBwdView) {
-                QXG_CUDA(launch_view_adjoint(st.vaargs, P->fp64, exps, P->stream));
-                kind = QXG_KERNEL_VIEW;
-            } else {
-                LeafGradArgs la = st.largs;
-                la.grad = d_grad + 2 * st.goff;
-                QXG_CUDA(launch_leaf_grad(la, P->fp64, exps, P->stream));
-            }
-            if (int r = prof_end(P, ev, st.instr, kind, st.flops, st.bytes)) return r;
+        std::vector<Work> w;
+        for (int g = 0; g < 3; g++) append_group_works(P, pl, g, exps, w);
+        if (d_out) {
+            Work x;
+            x.launch = [&](cudaStream_t s) -> int {
+                size_t ev = 0;
+                if (int r = prof_begin(P, &ev)) return r;
+                QXG_CUDA(launch_reduce(pl.red, P->fp64, exps, s));
+                return prof_end(P, ev, -1, QXG_KERNEL_REDUCE, 0.0, 0.0);
+            };
+            add_tensor_span(P, pl, P->root, x.rd);
+            x.wr.push_back({kSpanOut, 0, 1});
+            w.push_back(std::move(x));
         }
-        return 0;
+        {
+            Work x;
+            x.launch = [&](cudaStream_t s) -> int {
+                QXG_CUDA(cudaMemsetAsync(pl.seed.dst, 0, seed_bytes, s));
+                QXG_CUDA(launch_seed(pl.seed, P->fp64, exps, s));
+                P->launches++;
+                return 0;
+            };
+            add_tensor_span(P, pl, P->root, x.rd);
+            add_tensor_span(P, pl, n + P->root, x.wr);
+            w.push_back(std::move(x));
+        }
+        for (auto& st : pl.bsteps) {
+            Work x;
+            Step* sp = &st;
+            x.launch = [&bwd_step, sp](cudaStream_t s) { return bwd_step(*sp, s); };
+            add_step_spans(P, pl, st, x);
+            w.push_back(std::move(x));
+        }
+        return launch_works(P, w);
     };
     // with use_graphs (outside profiling) the pass is captured on its second run with the same
     // buffers and replayed for every later pass
@@ -1802,9 +1968,7 @@ std::string describe_step(const qxg_program* P, const Step& st, int group, int i
         for (size_t i = 0; i < at.size(); i++) d += (i ? "," : "") + at[i];
         if (!st.tune_note.empty()) d += " tuned=" + st.tune_note;
     } else {
-        d += contract_uses_rows(st.sargs, P->fp64)
-                 ? "cuda-core row-form"
-                 : (contract_scratch_bytes(st.sargs, P->fp64, P->sm_count) > 0 ? "cuda-core split-K" : "cuda-core general");
+        d += contract_form(st.sargs, P->fp64, P->sm_count);
         int ncb = 0;
         while ((int64_t(1) << ncb) < st.sargs.nC) ncb++;
         d += " c_bits=" + std::to_string(ncb) + " nk=" + std::to_string(st.sargs.nk);
@@ -1819,6 +1983,8 @@ void qxg_program_destroy(qxg_program* P) {
     if (P->stream) cudaStreamSynchronize(P->stream);
     for (cudaEvent_t e : P->ev_pool) cudaEventDestroy(e);
     drop_graphs(P);
+    for (cudaEvent_t e : P->cap_ev) cudaEventDestroy(e);
+    for (cudaStream_t s : P->cap_streams) cudaStreamDestroy(s);
     for (void* p : P->d_data) if (p) cudaFree(p);
     if (P->d_arena) cudaFree(P->d_arena);
     for (auto& e : P->tune_ev)

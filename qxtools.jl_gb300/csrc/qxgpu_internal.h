@@ -144,13 +144,18 @@ struct ReduceArgs {
 };
 
 // Kernel launchers (kernels_simt.cu).  Storage: double2 when fp64 != 0, else float2.
-// scratch (may be null): device memory for the split-K partials of steps with few results and a
-// long sum (contract_scratch_bytes); *launches receives the kernels launched (1 or 2).
+// scratch (may be null): device memory for the partials of steps with few results and a long
+// sum (contract_scratch_bytes); *launches receives the kernels launched (1 or 2).
 cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count,
                             void* scratch = nullptr, size_t scratch_bytes = 0, int* launches = nullptr);
 size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count);
 // Whether launch_contract runs a step in the row form (smaller operand staged in shared memory).
 bool contract_uses_rows(const StepArgs& a, bool fp64);
+// The CUDA-core form launch_contract picks for a step (for diagnostics).
+const char* contract_form(const StepArgs& a, bool fp64, int sm_count);
+// Whether a step with few results and a long sum is better served by the tiled long sum on the
+// CUDA cores than by a tensor-core GEMM (at most 2^7 results per value of the batch bits).
+bool contract_prefers_cuda_cores(const StepArgs& a, bool fp64, int sm_count);
 cudaError_t launch_view(const ViewArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_output(const OutputArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_reduce(const ReduceArgs& a, bool fp64, const int* exps, cudaStream_t s);

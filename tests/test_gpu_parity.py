@@ -232,6 +232,94 @@ def test_ncon_entry_point(q, gpu_lib, precision):
         assert np.max(np.abs(got - ref)) <= tol * max(1.0, np.max(np.abs(ref)))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_gate_steps_random_layouts(q, gpu_lib, precision):
+    """Gate-like contractions (X of 2^14..2^16 elements; Y with 0..5 summed, 0..6 new and 0..2
+    batch labels) under random label orders of X, Y and C, conjugation-free: the row forms
+    (tiled through shared memory, or one row per thread) against numpy."""
+    import torch
+    rng = np.random.default_rng(11)
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    letters = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
+    for case in range(24):
+        nk = int(rng.integers(0, 5 if precision == "fp64" else 6))
+        nn = int(rng.integers(0, 7))
+        nb = int(rng.integers(0, 3))
+        nx = int(rng.integers(14, 17))
+        if nx - nk + nn > 20:
+            nn = 20 - nx + nk
+        xl = list(range(1, nx + 1))
+        kl, bl, fl = xl[:nk], xl[nk:nk + nb], xl[nk + nb:]
+        nl = list(range(100, 100 + nn))
+        la = [int(v) for v in rng.permutation(xl)]
+        lb = [int(v) for v in rng.permutation(kl + bl + nl)]
+        lc = [int(v) for v in rng.permutation(bl + fl + nl)]
+        ad, bd = (2,) * len(la), (2,) * len(lb)
+        A = rng.standard_normal(ad) + 1j * rng.standard_normal(ad)
+        B = rng.standard_normal(bd) + 1j * rng.standard_normal(bd)
+        idx = {v: letters[i] for i, v in enumerate(sorted(set(la + lb)))}
+        ref = np.einsum("".join(idx[v] for v in la) + "," + "".join(idx[v] for v in lb) + "->" +
+                        "".join(idx[v] for v in lc), A, B)
+        dA = torch.tensor(A.reshape(-1, order="F"), dtype=cdt, device="cuda")
+        dB = torch.tensor(B.reshape(-1, order="F"), dtype=cdt, device="cuda")
+        dC = torch.full((ref.size,), float("nan"), dtype=cdt, device="cuda")
+        q.ncon_device(precision, dC.data_ptr(), lc, dA.data_ptr(), la, ad, dB.data_ptr(), lb, bd)
+        torch.cuda.synchronize()
+        got = dC.cpu().numpy().reshape(ref.shape, order="F")
+        tol = 1e-13 if precision == "fp64" else 2e-5
+        assert np.max(np.abs(got - ref)) <= tol * max(1.0, np.max(np.abs(ref))), (case, nk, nn, nb, nx)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_long_sums_random_layouts(q, gpu_lib, precision):
+    """Contractions with few results and a long sum (2^12..2^14 summed terms; 0..4 bits only in
+    A, 0..4 only in B, 0..2 in both and in the result) under random label orders: the tiled long
+    sum (per-block FP64 partials added in block order) against numpy."""
+    import torch
+    rng = np.random.default_rng(5)
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    letters = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
+    for case in range(16):
+        nk, na, nb, ng = (int(rng.integers(12, 15)), int(rng.integers(0, 5)), int(rng.integers(0, 5)),
+                          int(rng.integers(0, 3)))
+        kl = list(range(1, nk + 1))
+        al = list(range(100, 100 + na))
+        bl = list(range(200, 200 + nb))
+        gl = list(range(300, 300 + ng))
+        la = [int(v) for v in rng.permutation(al + gl + kl)]
+        lb = [int(v) for v in rng.permutation(bl + gl + kl)]
+        lc = [int(v) for v in rng.permutation(al + bl + gl)]
+        ad, bd = (2,) * len(la), (2,) * len(lb)
+        A = rng.standard_normal(ad) + 1j * rng.standard_normal(ad)
+        B = rng.standard_normal(bd) + 1j * rng.standard_normal(bd)
+        idx = {v: letters[i] for i, v in enumerate(sorted(set(la + lb)))}
+        ref = np.einsum("".join(idx[v] for v in la) + "," + "".join(idx[v] for v in lb) + "->" +
+                        "".join(idx[v] for v in lc), A, B)
+        ref = np.asarray(ref)
+        dA = torch.tensor(A.reshape(-1, order="F"), dtype=cdt, device="cuda")
+        dB = torch.tensor(B.reshape(-1, order="F"), dtype=cdt, device="cuda")
+        dC = torch.full((max(ref.size, 1),), float("nan"), dtype=cdt, device="cuda")
+        q.ncon_device(precision, dC.data_ptr(), lc, dA.data_ptr(), la, ad, dB.data_ptr(), lb, bd)
+        torch.cuda.synchronize()
+        got = dC.cpu().numpy().reshape(ref.shape, order="F") if ref.ndim else dC.cpu().numpy()[0]
+        tol = 1e-12 if precision == "fp64" else 2e-5
+        assert np.max(np.abs(got - ref)) <= tol * np.sqrt(2.0 ** nk), (case, nk, na, nb, ng)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "split_tf32"])
+def test_graph_branches_match_eager_exactly(q, gpu_lib, precision):
+    """Captured passes run independent sub-trees concurrently (graph edges from the launches'
+    read/write ranges, the shared scratch serialising tensor-core steps).  Every kernel is
+    deterministic, so replays must reproduce the eager first call bit for bit; a missing edge
+    shows up as a difference."""
+    prog = rqc_programme(q, 4, 4, 10, seed=3)
+    bits = list(q.amplitudes_uniform(16, 1, 32))
+    with q.Executor(prog, precision=precision, use_graphs=True, max_bitstring_batch=32) as ex:
+        first = ex.amplitudes(bits)                           # eager (and autotuning)
+        for _ in range(4):                                    # capture, then replays
+            assert np.array_equal(ex.amplitudes(bits), first)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "split_tf32"])
 def test_graph_replay_matches_eager(q, gpu_lib, oracle, precision):
     """Passes captured in CUDA graphs and replayed give the eager results, across repeated calls,
