@@ -17,6 +17,10 @@
 
 namespace qxg {
 
+// Resident blocks per SM of the long-sum kernel instance (NA, NB) with `smem` bytes (2 when the
+// query fails, e.g. without a device).
+int lsum_blocks_per_sm(int NA, int NB, size_t smem);
+
 namespace {
 
 template <typename T> struct Real;
@@ -425,182 +429,239 @@ size_t rows2_smem_bytes(const Rows2Args& a, int K, int N) {
     return sizeof(float4) * (size_t)a.nbatch * (size_t)(K * N + 1) + sizeof(int64_t) * (3 * 48 + K + N);
 }
 
-// Elements of the shared-memory tiles of the tiled long sum (log2, fp32; fp64 one less).
-constexpr int kTileSmemTiles = 11;
-
-// Element index inside a shared-memory tile: the low bits of each 128-byte line XOR the line's
-// low bits, so 32 lanes that differ only in higher bits still fall in distinct banks.
-template <typename T>
-__host__ __device__ __forceinline__ int tile_swz(int e) {
-    constexpr int B = sizeof(T) == 8 ? 4 : 3;
-    return e ^ ((e >> B) & ((1 << B) - 1));
-}
-
-// Tiled long sum with a small result: C[a, b, g] = sum_r A[a, g, r] B[b, g, r] where the summed
-// index r is long (the adjoint steps that end in a gate's gradient sum over every other index of
-// the network), "a" are the result bits only A has, "b" those only B has and "g" those both have.
-// A tile is 2^T values of r (the T summed bits lowest in A); per tile a block loads A's and B's
-// elements of the tile into shared memory in address order (as the tiled row form does), then
-// every thread adds the products of its rows into its results: one a value and up to four
-// consecutive b values, the tile's rows divided among the threads of each result group.  Each
-// block owns one g value and every G-th tile of it; per-thread FP32 sums of one tile are added
-// into FP64 block sums, and a second kernel adds the blocks' FP64 partials of each result in
-// block order (deterministic), scales and stores.  Every element of A and B is read once.
-struct SumTileArgs {
+// Long sum with a small result (FP32): C[a, b, g] = sum_r A[a, g, r] B[b, g, r], the summed index
+// r long (the adjoint steps that end in a gate's gradient sum over every other index of the
+// network); "a" are the result bits only A has, "b" those only B has, "g" those both have.  It
+// walks r the way the compact row form walks rows: a warp takes a contiguous range of groups of
+// 2^LR values of r (the LR summed bits lowest in the larger operand), two groups per step, and
+// moves between groups by per-bit offset deltas.  The results are cut into lane blocks of NA a
+// values x NB b values: the 32 lanes of a warp are 2^LR values of r times S = 32 / 2^LR
+// sub-lanes (consecutive a blocks), and the CW = CA x CB warps of a block that share a row range
+// take different a and b blocks (8 / CW such warp sets divide the block's rows).  A lane loads
+// its r's NA values of A and NB of B (16-byte pairs where a / b bit 0 is the lowest address
+// bit) and adds their outer product into NA x NB registers with paired FP32 FMAs; elements that
+// several lanes need come from memory once per warp instruction or from L1.  Block (g, part)
+// sums its lanes in FP64 (fixed butterfly, then its warps in order) into one partial per result;
+// a second kernel adds the parts in order, scales and stores: deterministic.  At most
+// kLSumRowsPerLane values of r per lane go through FP32 sums.
+struct LSumArgs {
     const void* A;
     const void* B;
     void* C;
-    int64_t ntiles;            // tiles per g value
+    int64_t ngroups;           // groups of 2^LR values of r
+    int32_t LR;                // r bits per lane group (2..5)
+    int32_t CA, CB;            // a / b blocks across the warps of one row range
     int32_t G;                 // blocks per g value
     int32_t ng;                // g values
-    int32_t T, na, nb;         // summed bits per tile, bits of a, bits of b
+    int32_t apair, bpair;
     int32_t conjA, conjB;
     int32_t expA, expB, expC;
-    BitMap hiA, hiB;           // tile index (within a g value) -> A / B offset
-    BitMap gA, gB, gC;         // g -> A / B / C offset
-    BitMap eA, fB;             // A tile element (e order) / B tile element (f order) -> offset
-    BitMap sE, sF;             // tile row -> e / f index
-    BitMap aE, aC;             // a -> e index / C offset
-    BitMap bF, bC;             // b -> f index / C offset
+    BitMap laneA, laneB, grpA, grpB;   // lane / group index of r -> A / B offset
+    BitMap gA, gB, gC;                 // g -> A / B / C offset
+    BitMap aA, aC, bB, bC;             // a -> A / C offset; b -> B / C offset
 };
-constexpr int kSumMaxOut = 1024;        // a x b results per g value
-constexpr int kSumGroup = 4;            // b values per thread
+constexpr int kLSumOut = 16;            // results per lane (NA x NB)
+constexpr int kLSumRowsPerLane = 512;
+constexpr int kLSumWarps = kThreads / 32;
 
-__host__ __device__ __forceinline__ int sum_groups(const SumTileArgs& a) {
-    const int nbv = 1 << a.nb;
-    return (1 << a.na) * ((nbv + kSumGroup - 1) / kSumGroup);
+__host__ __device__ __forceinline__ int lsum_na(const LSumArgs& a, int NA) { return a.CA * (32 >> a.LR) * NA; }
+
+struct LSumSmem {
+    int64_t *dA, *dB, *ao, *bo;
+    double* red;                       // [warp][lane-block result][re, im]
+};
+__host__ __device__ __forceinline__ LSumSmem lsum_carve(unsigned char* base, int Na, int Nb) {
+    LSumSmem t;
+    t.dA = reinterpret_cast<int64_t*>(base);
+    t.dB = t.dA + 48;
+    t.bo = t.dB + 48;
+    t.ao = t.bo + Nb;
+    t.red = reinterpret_cast<double*>(t.ao + Na);
+    return t;
+}
+// per warp: S NA NB results
+inline size_t lsum_smem_bytes(int Na, int Nb, int per_warp) {
+    return sizeof(int64_t) * (96 + Na + Nb) + sizeof(double) * 2 * per_warp * kLSumWarps;
 }
 
-template <typename T>
-size_t sum_smem_bytes(const SumTileArgs& a) {
-    const size_t tiles = sizeof(T) * ((size_t(1) << (a.T + a.na)) + (size_t(1) << (a.T + a.nb)));
-    const size_t red = sizeof(double) * 2 * kSumGroup * kThreads;
-    return std::max(tiles, red) + sizeof(int) * ((size_t(1) << a.na) + (size_t(1) << a.nb));
+__host__ __device__ __forceinline__ void lsum_fill(const LSumArgs& a, const LSumSmem& t, int Na, int Nb, int tid,
+                                                   int nthr) {
+    for (int j = tid; j < 46; j += nthr) {
+        const int64_t bit = int64_t(1) << j, low = bit - 1;
+        t.dA[j] = pdep(bit, a.grpA) - pdep(low, a.grpA);
+        t.dB[j] = pdep(bit, a.grpB) - pdep(low, a.grpB);
+    }
+    for (int i = tid; i < Na; i += nthr) t.ao[i] = pdep(i, a.aA);
+    for (int i = tid; i < Nb; i += nthr) t.bo[i] = pdep(i, a.bB);
 }
 
-// One tile's rows for thread (group og, row lane rl): products into FP32 sums.
-template <typename T>
-__host__ __device__ __forceinline__ void sum_tile_rows(const SumTileArgs& a, int og, int rl, int rt, const T* As,
-                                                       const T* Bs, const int* aE_t, const int* bF_t,
-                                                       typename Real<T>::type* sr, typename Real<T>::type* si) {
-    using R = typename Real<T>::type;
-    const int nbv = 1 << a.nb;
-    const int bgroups = (nbv + kSumGroup - 1) / kSumGroup;
-    const int av = og / bgroups, b0 = (og % bgroups) * kSumGroup;
-    const int ea = aE_t[av];
-    const R ca = a.conjA ? R(-1) : R(1), cb = a.conjB ? R(-1) : R(1);
-    for (int s = rl; s < (1 << a.T); s += rt) {
-        const T u = As[tile_swz<T>((int)pdep(s, a.sE) + ea)];
-        const R ur = u.x, ui = ca * u.y;
-        const int fs = (int)pdep(s, a.sF);
+template <int NA, int NB>
+__host__ __device__ __forceinline__ void lsum_load(const LSumArgs& a, const float2* arow, const float2* brow,
+                                                   const int64_t* ao, const int64_t* bo, float* ar, float* ai,
+                                                   float* br, float* bi) {
+    bool done = false;
+    if constexpr (NA > 1) {
+        if (a.apair) {
+            done = true;
 #pragma unroll
-        for (int j = 0; j < kSumGroup; j++) {
-            if (b0 + j < nbv) {
-                const T v = Bs[tile_swz<T>(fs + bF_t[b0 + j])];
-                const R vr = v.x, vi = cb * v.y;
-                sr[j] = fma(ur, vr, sr[j]);
-                sr[j] = fma(-ui, vi, sr[j]);
-                si[j] = fma(ur, vi, si[j]);
-                si[j] = fma(ui, vr, si[j]);
+            for (int i = 0; i < NA; i += 2) {
+                const float4 v = *reinterpret_cast<const float4*>(arow + ao[i]);
+                ar[i] = v.x; ai[i] = v.y; ar[i + 1] = v.z; ai[i + 1] = v.w;
             }
         }
     }
-}
-
-template <typename T>
-__host__ __device__ __forceinline__ void sum_tile_load(const SumTileArgs& a, int64_t ao, int64_t bo, int tid, int nthr,
-                                                       T* As, T* Bs) {
-    const T* __restrict__ Ag = static_cast<const T*>(a.A) + ao;
-    const T* __restrict__ Bg = static_cast<const T*>(a.B) + bo;
-    const int EA = 1 << (a.T + a.na), E = EA + (1 << (a.T + a.nb));
-    constexpr int U = 8;                    // loads in flight per thread before the stores
-    for (int base = tid; base < E; base += U * nthr) {
-        T v[U];
+    if (!done) {
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            const int e = base + u * nthr;
-            if (e < EA) v[u] = Ag[pdep(e, a.eA)];
-            else if (e < E) v[u] = Bg[pdep(e - EA, a.fB)];
-        }
+        for (int i = 0; i < NA; i++) { const float2 v = arow[ao[i]]; ar[i] = v.x; ai[i] = v.y; }
+    }
+    done = false;
+    if constexpr (NB > 1) {
+        if (a.bpair) {
+            done = true;
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            const int e = base + u * nthr;
-            if (e < EA) As[tile_swz<T>(e)] = v[u];
-            else if (e < E) Bs[tile_swz<T>(e - EA)] = v[u];
+            for (int i = 0; i < NB; i += 2) {
+                const float4 v = *reinterpret_cast<const float4*>(brow + bo[i]);
+                br[i] = v.x; bi[i] = v.y; br[i + 1] = v.z; bi[i + 1] = v.w;
+            }
+        }
+    }
+    if (!done) {
+#pragma unroll
+        for (int i = 0; i < NB; i++) { const float2 v = brow[bo[i]]; br[i] = v.x; bi[i] = v.y; }
+    }
+}
+
+template <int NA, int NB>
+__host__ __device__ __forceinline__ void lsum_madd(const float* ar, const float* ai, const float* br, const float* bi,
+                                                   float sa, float sb, unsigned long long (&acc)[NA][NB]) {
+    unsigned long long y1[NB], y2[NB];
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+        const float bij = sb * bi[j];
+        y1[j] = f2pack(br[j], bij);
+        y2[j] = f2pack(bij, br[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < NA; i++) {
+        const float aii = sa * ai[i];
+        const unsigned long long xx = f2pack(ar[i], ar[i]), xj = f2pack(-aii, aii);
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            fma2(acc[i][j], xx, y1[j]);
+            fma2(acc[i][j], xj, y2[j]);
         }
     }
 }
 
-// The block's partial of each result: its row lanes' FP64 sums (red: 2 kSumGroup planes of
-// kThreads values) added in lane order.
-__host__ __device__ __forceinline__ void sum_block_out(const SumTileArgs& a, const double* red, int tid, int nthr,
-                                                       double2* pblock) {
-    const int og_n = sum_groups(a), rt = kThreads / og_n;
-    const int nbv = 1 << a.nb, bgroups = (nbv + kSumGroup - 1) / kSumGroup;
-    for (int o = tid; o < og_n * kSumGroup; o += nthr) {
-        const int grp = o / kSumGroup, j = o % kSumGroup;
-        if ((grp % bgroups) * kSumGroup + j >= nbv) continue;
-        double r = 0.0, i = 0.0;
-        for (int l = 0; l < rt; l++) {
-            r += red[(2 * j) * kThreads + l * og_n + grp];
-            i += red[(2 * j + 1) * kThreads + l * og_n + grp];
+__host__ __device__ __forceinline__ int lsum_ctz(unsigned long long v) {
+#ifdef __CUDA_ARCH__
+    return __ffsll((long long)v) - 1;
+#else
+    return __builtin_ctzll(v);
+#endif
+}
+
+// Lane `lane` of warp slot w (of nwarps sharing the g value's rows), lane block (a0, b0): FP32
+// sums into acc (re, im pairs), two groups of r per step.
+template <int NA, int NB>
+__host__ __device__ __forceinline__ void lsum_walk(const LSumArgs& a, const LSumSmem& t, int64_t abase, int64_t bbase,
+                                                   int64_t w, int64_t nwarps, int lane, int a0, int b0,
+                                                   unsigned long long (&acc)[NA][NB]) {
+    const int rl = lane & ((1 << a.LR) - 1);
+    const int64_t lA = pdep(rl, a.laneA), lB = pdep(rl, a.laneB);
+    const int64_t g0 = a.ngroups * w / nwarps, g1 = a.ngroups * (w + 1) / nwarps;
+    int64_t oA = pdep(g0, a.grpA), oB = pdep(g0, a.grpB);
+    const float2* __restrict__ Ag = static_cast<const float2*>(a.A) + abase + lA;
+    const float2* __restrict__ Bg = static_cast<const float2*>(a.B) + bbase + lB;
+    const int64_t* ao = t.ao + a0;
+    const int64_t* bo = t.bo + b0;
+    const float sa = a.conjA ? -1.f : 1.f, sb = a.conjB ? -1.f : 1.f;
+    for (int64_t g = g0; g < g1; g += 2) {
+        const bool two = g + 1 < g1;
+        const int j1 = lsum_ctz((unsigned long long)(g + 1));
+        const int64_t oA1 = oA + t.dA[j1], oB1 = oB + t.dB[j1];
+        float ar[NA], ai[NA], br[NB], bi[NB], ar1[NA], ai1[NA], br1[NB], bi1[NB];
+        lsum_load<NA, NB>(a, Ag + oA, Bg + oB, ao, bo, ar, ai, br, bi);
+        if (two) lsum_load<NA, NB>(a, Ag + oA1, Bg + oB1, ao, bo, ar1, ai1, br1, bi1);
+        lsum_madd<NA, NB>(ar, ai, br, bi, sa, sb, acc);
+        if (two) {
+            lsum_madd<NA, NB>(ar1, ai1, br1, bi1, sa, sb, acc);
+            const int j2 = lsum_ctz((unsigned long long)(g + 2));
+            oA = oA1 + t.dA[j2];
+            oB = oB1 + t.dB[j2];
         }
-        pblock[o] = make_double2(r, i);
     }
 }
 
-// Launched with kThreads threads.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) contract_sumtile_kernel(const SumTileArgs a, double2* partial) {
-    using R = typename Real<T>::type;
-    extern __shared__ __align__(16) unsigned char sum_smem[];
-    T* As = reinterpret_cast<T*>(sum_smem);
-    T* Bs = As + (1 << (a.T + a.na));
-    const size_t tiles = sizeof(T) * ((size_t(1) << (a.T + a.na)) + (size_t(1) << (a.T + a.nb)));
-    const size_t red_bytes = sizeof(double) * 2 * kSumGroup * kThreads;
-    double* red = reinterpret_cast<double*>(sum_smem);          // reused after the last tile
-    int* aE_t = reinterpret_cast<int*>(sum_smem + (tiles > red_bytes ? tiles : red_bytes));
-    int* bF_t = aE_t + (1 << a.na);
-    for (int i = threadIdx.x; i < (1 << a.na); i += kThreads) aE_t[i] = (int)pdep(i, a.aE);
-    for (int i = threadIdx.x; i < (1 << a.nb); i += kThreads) bF_t[i] = (int)pdep(i, a.bF);
-    const int g = blockIdx.x / a.G, part = blockIdx.x % a.G;
-    const int og_n = sum_groups(a);
-    const int rt = kThreads / og_n;                              // threads per result group (>= 1)
-    const int og = threadIdx.x % og_n, rl = threadIdx.x / og_n;
-    const bool active = rl < rt;
-    const int64_t abase = pdep(g, a.gA), bbase = pdep(g, a.gB);
-    double dr[kSumGroup], di[kSumGroup];
-    for (int j = 0; j < kSumGroup; j++) { dr[j] = 0.0; di[j] = 0.0; }
-    for (int64_t t = part; t < a.ntiles; t += a.G) {
-        sum_tile_load<T>(a, abase + pdep(t, a.hiA), bbase + pdep(t, a.hiB), threadIdx.x, kThreads, As, Bs);
-        __syncthreads();                                         // tiles (and tables) in place
-        if (active) {
-            R sr[kSumGroup], si[kSumGroup];
-            for (int j = 0; j < kSumGroup; j++) { sr[j] = R(0); si[j] = R(0); }
-            sum_tile_rows<T>(a, og, rl, rt, As, Bs, aE_t, bF_t, sr, si);
-            for (int j = 0; j < kSumGroup; j++) { dr[j] += (double)sr[j]; di[j] += (double)si[j]; }
-        }
-        __syncthreads();                                         // tiles free for the next loads
-    }
-    for (int j = 0; j < kSumGroup; j++) {
-        red[(2 * j) * kThreads + threadIdx.x] = dr[j];
-        red[(2 * j + 1) * kThreads + threadIdx.x] = di[j];
-    }
+// Lane block of warp `warp`, lane `lane`: first a and b values (a0, b0).
+__host__ __device__ __forceinline__ void lsum_lane_block(const LSumArgs& a, int NA, int NB, int warp, int lane, int* a0,
+                                                         int* b0) {
+    const int CW = a.CA * a.CB, c = warp % CW, S = 32 >> a.LR;
+    *a0 = ((c / a.CB) * S + (lane >> a.LR)) * NA;
+    *b0 = (c % a.CB) * NB;
+}
+
+// Launched with kThreads threads, grid ng x G; dynamic shared memory lsum_smem_bytes.
+template <int NA, int NB>
+__global__ void __launch_bounds__(kThreads) contract_lsum_kernel(const LSumArgs a, double2* partial) {
+    extern __shared__ __align__(16) unsigned char lsum_smem[];
+    const int Na = lsum_na(a, NA), Nb = a.CB * NB;
+    const LSumSmem t = lsum_carve(lsum_smem, Na, Nb);
+    lsum_fill(a, t, Na, Nb, threadIdx.x, kThreads);
     __syncthreads();
-    sum_block_out(a, red, threadIdx.x, kThreads, partial + (int64_t)blockIdx.x * (og_n * kSumGroup));
+    const int g = blockIdx.x / a.G, part = blockIdx.x % a.G;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int CW = a.CA * a.CB, sets = kLSumWarps / CW;      // warp sets dividing the rows
+    int a0, b0;
+    lsum_lane_block(a, NA, NB, warp, lane, &a0, &b0);
+    unsigned long long acc[NA][NB];
+#pragma unroll
+    for (int i = 0; i < NA; i++)
+#pragma unroll
+        for (int j = 0; j < NB; j++) acc[i][j] = 0ull;
+    lsum_walk<NA, NB>(a, t, pdep(g, a.gA), pdep(g, a.gB), (int64_t)part * sets + warp / CW, (int64_t)a.G * sets, lane,
+                      a0, b0, acc);
+    // FP64: butterfly over the lanes of one sub-lane (the low LR lane bits) ...
+    const int S = 32 >> a.LR, R = 1 << a.LR, sub = lane >> a.LR;
+    const int pw = S * NA * NB;                                 // results of one warp
+#pragma unroll
+    for (int i = 0; i < NA; i++)
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            double re = (double)u2f((unsigned)(acc[i][j] & 0xffffffffull));
+            double im = (double)u2f((unsigned)(acc[i][j] >> 32));
+            for (int o = 1; o < R; o <<= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            if ((lane & (R - 1)) == 0) {
+                const int res = (sub * NA + i) * NB + j;
+                t.red[2 * (warp * pw + res)] = re;
+                t.red[2 * (warp * pw + res) + 1] = im;
+            }
+        }
+    __syncthreads();
+    // ... then the warp sets in order, one partial per result (a, b) of the g value
+    for (int o = threadIdx.x; o < Na * Nb; o += kThreads) {
+        const int av = o / Nb, bv = o % Nb;
+        const int ca = av / (S * NA), sub2 = (av % (S * NA)) / NA, i = av % NA;
+        const int cb = bv / NB, j = bv % NB;
+        const int c = ca * a.CB + cb, res = (sub2 * NA + i) * NB + j;
+        double re = 0.0, im = 0.0;
+        for (int st = 0; st < sets; st++) {
+            const int w = st * CW + c;
+            re += t.red[2 * (w * pw + res)];
+            im += t.red[2 * (w * pw + res) + 1];
+        }
+        partial[((int64_t)g * a.G + part) * (Na * Nb) + o] = make_double2(re, im);
+    }
 }
 
-// One result of the reduce: the blocks' partials in block order, scaled.
-template <typename T>
-__host__ __device__ __forceinline__ bool sum_reduce_one(const SumTileArgs& a, const double2* partial, int64_t idx,
-                                                        double scale, T* C, float* mag) {
-    using R = typename Real<T>::type;
-    const int og_n = sum_groups(a), per = og_n * kSumGroup;
-    const int nbv = 1 << a.nb, bgroups = (nbv + kSumGroup - 1) / kSumGroup;
+// One result (idx over g and the per = Na Nb results (a, b) of a g value): the parts in order,
+// scaled, stored at its C offset; returns its magnitude.
+__host__ __device__ __forceinline__ float lsum_reduce_one(const LSumArgs& a, int per, int Nb, const double2* partial,
+                                                          int64_t idx, double scale) {
     const int g = (int)(idx / per), o = (int)(idx % per);
-    const int grp = o / kSumGroup, j = o % kSumGroup;
-    const int av = grp / bgroups, bv = (grp % bgroups) * kSumGroup + j;
-    if (bv >= nbv) return false;
     double r = 0.0, i = 0.0;
     for (int p = 0; p < a.G; p++) {
         const double2 v = partial[((int64_t)g * a.G + p) * per + o];
@@ -608,16 +669,13 @@ __host__ __device__ __forceinline__ bool sum_reduce_one(const SumTileArgs& a, co
         i += v.y;
     }
     r *= scale; i *= scale;
-    *mag = fmaxf(fabsf((float)r), fabsf((float)i));
-    T out; out.x = (R)r; out.y = (R)i;
-    C[pdep(g, a.gC) + pdep(av, a.aC) + pdep(bv, a.bC)] = out;
-    return true;
+    float2* C = static_cast<float2*>(a.C);
+    C[pdep(g, a.gC) + pdep(o / Nb, a.aC) + pdep(o % Nb, a.bC)] = make_float2((float)r, (float)i);
+    return fmaxf(fabsf((float)r), fabsf((float)i));
 }
 
-// Adds the blocks' partials of each result, scales into the result's exponent and stores;
-// raises the result's exponent slot like the other contraction kernels.
-template <typename T, bool SCALED>
-__global__ void sumtile_reduce_kernel(const SumTileArgs a, const double2* partial, int* exps) {
+template <bool SCALED>
+__global__ void lsum_reduce_kernel(const LSumArgs a, int per, int Nb, const double2* partial, int* exps) {
     double scale = 1.0;
     if (SCALED) {
         const int mA = read_m(exps, a.expA), mB = read_m(exps, a.expB);
@@ -625,13 +683,12 @@ __global__ void sumtile_reduce_kernel(const SumTileArgs a, const double2* partia
         if (blockIdx.x == 0 && threadIdx.x == 0)
             exps[2 * a.expC] = exps[2 * a.expA] + exps[2 * a.expB] + mA + mB;
     }
-    const int64_t total = (int64_t)a.ng * sum_groups(a) * kSumGroup;
+    const int64_t total = (int64_t)a.ng * per;
     int emax = kExpUnset;
-    T* __restrict__ C = static_cast<T*>(a.C);
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
-        float mx = 0.f;
-        if (sum_reduce_one<T>(a, partial, idx, scale, C, &mx) && SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
+        const float mx = lsum_reduce_one(a, per, Nb, partial, idx, scale);
+        if (SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
     }
     if (SCALED) {
         for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
@@ -1070,102 +1127,107 @@ bool plan_rows2(const RowArgs& ra, Rows2Args* r2) {
     return true;
 }
 
-// Fill the tiled long sum: at least 2^12 summed terms, at most 2^6 values of each of the a and
-// b bits and kSumMaxOut results per g value.  blocks: the blocks the launch should fill.
-bool plan_sumtiles(const StepArgs& s, int esize, int64_t blocks, SumTileArgs* sa) {
-    if (s.nk < 12 || s.nk > 46) return false;
+// Fill the long sum (FP32): at least 2^12 summed terms, every summed bit in both operands; "a" is
+// the side with more result bits.  Lane blocks of NA x NB results (NB <= 4, NA NB <= kLSumOut),
+// up to 8 sub-lanes, up to 8 warps per row range; at most 2^20 values of the shared result bits.
+// sm_count, blocks_per_sm: the grid fills the GPU once (blocks_per_sm 0: occupancy query).
+bool plan_lsum(const StepArgs& s0, int sm_count, LSumArgs* la, int* NA, int* NB, int blocks_per_sm = 0) {
+    if (s0.nk < 12 || s0.nk > 46) return false;
     auto one = [](const BitMap& m, int bit) {              // destination bit of one index bit, or -1
         const int64_t o = pdep(int64_t(1) << bit, m);
         return o ? __builtin_ctzll((unsigned long long)o) : -1;
     };
     int ncb = 0;
-    while ((int64_t(1) << ncb) < s.nC) ncb++;
-    std::vector<int> ab, bb, gb;                            // result bits by owner
+    while ((int64_t(1) << ncb) < s0.nC) ncb++;
+    std::vector<int> ab, bb, gb;
     for (int p = 0; p < ncb; p++) {
-        const bool ia = one(s.cA, p) >= 0, ib = one(s.cB, p) >= 0;
+        const bool ia = one(s0.cA, p) >= 0, ib = one(s0.cB, p) >= 0;
         if (ia && ib) gb.push_back(p);
         else if (ia) ab.push_back(p);
         else if (ib) bb.push_back(p);
         else return false;
     }
-    const int na = (int)ab.size(), nb = (int)bb.size(), nk = s.nk;
-    if (na > 6 || nb > 6 || (int64_t(1) << (na + nb)) > kSumMaxOut) return false;
-    const int budget = esize == 8 ? kTileSmemTiles : kTileSmemTiles - 1;
-    const int T = std::min({8, nk, budget - na, budget - nb});
-    if (T < 4) return false;
+    for (int j = 0; j < s0.nk; j++)
+        if (one(s0.kA, j) < 0 || one(s0.kB, j) < 0) return false;
+    // the chunked side is the one with more result bits
+    const bool swap = bb.size() > ab.size();
+    const BitMap& cA = swap ? s0.cB : s0.cA;
+    const BitMap& cB = swap ? s0.cA : s0.cB;
+    const BitMap& kA = swap ? s0.kB : s0.kA;
+    const BitMap& kB = swap ? s0.kA : s0.kB;
+    if (swap) std::swap(ab, bb);
+    const int na = (int)ab.size(), nb = (int)bb.size(), nk = s0.nk;
+    if (gb.size() > 20) return false;
+    const int nbv = 1 << nb, nav = 1 << na;
+    const int NBv = std::min(nbv, 4), NAv = std::min(nav, kLSumOut / NBv);
+    const int S = std::min(8, nav / NAv), CA = nav / (S * NAv), CB = nbv / NBv;
+    if (CA * CB > kLSumWarps) return false;
+    int LR = 5;
+    while ((32 >> LR) < S) LR--;
     // summed bits by position in the larger operand
     int amax = 0, bmax = 0;
-    for (int j = 0; j < nk; j++) {
-        if (one(s.kA, j) < 0 || one(s.kB, j) < 0) return false;
-        amax = std::max(amax, one(s.kA, j));
-        bmax = std::max(bmax, one(s.kB, j));
-    }
-    for (int p : ab) amax = std::max(amax, one(s.cA, p));
-    for (int p : bb) bmax = std::max(bmax, one(s.cB, p));
+    for (int j = 0; j < nk; j++) { amax = std::max(amax, one(kA, j)); bmax = std::max(bmax, one(kB, j)); }
+    for (int p : ab) amax = std::max(amax, one(cA, p));
+    for (int p : bb) bmax = std::max(bmax, one(cB, p));
+    for (int p : gb) { amax = std::max(amax, one(cA, p)); bmax = std::max(bmax, one(cB, p)); }
     const bool by_a = amax >= bmax;
     std::vector<int> ks(nk);
     for (int j = 0; j < nk; j++) ks[j] = j;
     std::sort(ks.begin(), ks.end(), [&](int x, int y) {
-        return by_a ? one(s.kA, x) < one(s.kA, y) : one(s.kB, x) < one(s.kB, y);
+        return by_a ? one(kA, x) < one(kA, y) : one(kB, x) < one(kB, y);
     });
-    struct TB { int pos, kind, idx; };
-    std::vector<TB> xe, xf;
-    for (int i = 0; i < T; i++) { xe.push_back({one(s.kA, ks[i]), 0, i}); xf.push_back({one(s.kB, ks[i]), 0, i}); }
-    for (int j = 0; j < na; j++) xe.push_back({one(s.cA, ab[j]), 1, j});
-    for (int j = 0; j < nb; j++) xf.push_back({one(s.cB, bb[j]), 1, j});
-    auto bypos = [](const TB& p, const TB& q) { return p.pos < q.pos; };
-    std::sort(xe.begin(), xe.end(), bypos);
-    std::sort(xf.begin(), xf.end(), bypos);
-    std::vector<std::pair<int, int>> pe, pf, psE(T), psF(T), paE(na), pbF(nb), paC, pbC, phA, phB, pgA, pgB, pgC;
-    for (int i = 0; i < (int)xe.size(); i++) {
-        pe.push_back({i, xe[i].pos});
-        if (xe[i].kind == 0) psE[xe[i].idx] = {xe[i].idx, i};
-        else paE[xe[i].idx] = {xe[i].idx, i};
+    std::vector<std::pair<int, int>> lA, lB, gA_, gB_, pgA, pgB, pgC, paA, paC, pbB, pbC;
+    for (int i = 0; i < nk; i++) {
+        auto& mA = i < LR ? lA : gA_;
+        auto& mB = i < LR ? lB : gB_;
+        const int src = i < LR ? i : i - LR;
+        mA.push_back({src, one(kA, ks[i])});
+        mB.push_back({src, one(kB, ks[i])});
     }
-    for (int i = 0; i < (int)xf.size(); i++) {
-        pf.push_back({i, xf[i].pos});
-        if (xf[i].kind == 0) psF[xf[i].idx] = {xf[i].idx, i};
-        else pbF[xf[i].idx] = {xf[i].idx, i};
-    }
-    for (int j = 0; j < na; j++) paC.push_back({j, ab[j]});
-    for (int j = 0; j < nb; j++) pbC.push_back({j, bb[j]});
-    for (int i = T; i < nk; i++) { phA.push_back({i - T, one(s.kA, ks[i])}); phB.push_back({i - T, one(s.kB, ks[i])}); }
     for (int i = 0; i < (int)gb.size(); i++) {
-        pgA.push_back({i, one(s.cA, gb[i])});
-        pgB.push_back({i, one(s.cB, gb[i])});
+        pgA.push_back({i, one(cA, gb[i])});
+        pgB.push_back({i, one(cB, gb[i])});
         pgC.push_back({i, gb[i]});
     }
-    memset(sa, 0, sizeof(*sa));
-    if (!make_runs(pe, &sa->eA) || !make_runs(pf, &sa->fB) || !make_runs(psE, &sa->sE) || !make_runs(psF, &sa->sF) ||
-        !make_runs(paE, &sa->aE) || !make_runs(pbF, &sa->bF) || !make_runs(paC, &sa->aC) || !make_runs(pbC, &sa->bC) ||
-        !make_runs(phA, &sa->hiA) || !make_runs(phB, &sa->hiB) || !make_runs(pgA, &sa->gA) || !make_runs(pgB, &sa->gB) ||
-        !make_runs(pgC, &sa->gC))
+    for (int j = 0; j < na; j++) { paA.push_back({j, one(cA, ab[j])}); paC.push_back({j, ab[j]}); }
+    for (int j = 0; j < nb; j++) { pbB.push_back({j, one(cB, bb[j])}); pbC.push_back({j, bb[j]}); }
+    memset(la, 0, sizeof(*la));
+    if (!make_runs(lA, &la->laneA) || !make_runs(lB, &la->laneB) || !make_runs(gA_, &la->grpA) ||
+        !make_runs(gB_, &la->grpB) || !make_runs(pgA, &la->gA) || !make_runs(pgB, &la->gB) ||
+        !make_runs(pgC, &la->gC) || !make_runs(paA, &la->aA) || !make_runs(paC, &la->aC) ||
+        !make_runs(pbB, &la->bB) || !make_runs(pbC, &la->bC))
         return false;
-    if (gb.size() > 20) return false;
-    sa->A = s.A;
-    sa->B = s.B;
-    sa->C = s.C;
-    sa->T = T;
-    sa->na = na;
-    sa->nb = nb;
-    sa->ng = 1 << (int)gb.size();
-    sa->ntiles = int64_t(1) << (nk - T);
-    const int64_t want = (blocks + sa->ng - 1) / sa->ng;
-    sa->G = (int)std::max<int64_t>(1, std::min<int64_t>(want, sa->ntiles));
-    sa->conjA = s.conjA;
-    sa->conjB = s.conjB;
-    sa->expA = s.expA;
-    sa->expB = s.expB;
-    sa->expC = s.expC;
+    la->A = swap ? s0.B : s0.A;
+    la->B = swap ? s0.A : s0.B;
+    la->C = s0.C;
+    la->conjA = swap ? s0.conjB : s0.conjA;
+    la->conjB = swap ? s0.conjA : s0.conjB;
+    la->expA = swap ? s0.expB : s0.expA;
+    la->expB = swap ? s0.expA : s0.expB;
+    la->expC = s0.expC;
+    *NB = NBv;
+    *NA = NAv;
+    la->LR = LR;
+    la->CA = CA;
+    la->CB = CB;
+    la->ng = 1 << (int)gb.size();
+    la->ngroups = int64_t(1) << (nk - LR);
+    const int sets = kLSumWarps / (CA * CB);
+    if (blocks_per_sm <= 0) blocks_per_sm = lsum_blocks_per_sm(NAv, NBv, lsum_smem_bytes(nav, nbv, S * NAv * NBv));
+    int64_t G = ((int64_t)sm_count * std::max(blocks_per_sm, 1) + la->ng - 1) / la->ng;
+    // at most kLSumRowsPerLane groups per warp set; at least one
+    G = std::max<int64_t>(G, (la->ngroups + (int64_t)sets * kLSumRowsPerLane - 1) / ((int64_t)sets * kLSumRowsPerLane));
+    G = std::max<int64_t>(1, std::min<int64_t>(G, la->ngroups / sets));
+    if ((int64_t)la->ng * G > (int64_t(1) << 30)) return false;
+    la->G = (int)G;
+    la->apair = *NA > 1 && pdep(1, la->aA) == 1 && (reinterpret_cast<uintptr_t>(la->A) & 15) == 0;
+    la->bpair = *NB > 1 && pdep(1, la->bB) == 1 && (reinterpret_cast<uintptr_t>(la->B) & 15) == 0;
     return true;
 }
 
-size_t sum_partial_bytes(const SumTileArgs& sa) {
-    return (size_t)sa.ng * (size_t)sa.G * (size_t)sum_groups(sa) * kSumGroup * sizeof(double2);
+size_t lsum_partial_bytes(const LSumArgs& la, int NA, int NB) {
+    return (size_t)la.ng * la.G * lsum_na(la, NA) * (la.CB * NB) * sizeof(double2);
 }
-
-// Blocks a tiled long sum aims at: eight per SM.
-int64_t sum_blocks(int sm_count) { return (int64_t)sm_count * 8; }
 
 // Splits of the split-K form: used when the results are few (<= 2^14) and each sums at least
 // 2^14 terms; enough splits of the high K index to give about 8 blocks per SM, at least 2^12
@@ -1247,32 +1309,80 @@ cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_cou
 size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
     RowArgs ra;
     if (plan_rows(a, fp64 ? 16 : 32, &ra)) return 0;
-    SumTileArgs sa;
-    if (plan_sumtiles(a, fp64 ? 16 : 8, sum_blocks(sm_count), &sa)) return sum_partial_bytes(sa);
+    LSumArgs la;
+    int NA = 0, NB = 0;
+    if (!fp64 && plan_lsum(a, sm_count, &la, &NA, &NB)) return lsum_partial_bytes(la, NA, NB);
     const int ns = splitk_count(a, sm_count);
     return ns > 0 ? (size_t)ns * (size_t)a.nC * (fp64 ? 16 : 8) : 0;
 }
 
 bool contract_prefers_cuda_cores(const StepArgs& a, bool fp64, int sm_count) {
-    SumTileArgs sa;
-    return plan_sumtiles(a, fp64 ? 16 : 8, sum_blocks(sm_count), &sa) && sa.na + sa.nb <= 7;
+    LSumArgs la;
+    int NA = 0, NB = 0;
+    return !fp64 && plan_lsum(a, sm_count, &la, &NA, &NB);
 }
 
-template <typename T>
-cudaError_t launch_sumtiles(const SumTileArgs& sa, void* scratch, int* exps, cudaStream_t s) {
-    const size_t smem = sum_smem_bytes<T>(sa);
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(contract_sumtile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+template <int NA, int NB>
+cudaError_t launch_lsum_ab(const LSumArgs& la, void* scratch, int* exps, cudaStream_t s) {
     double2* partial = static_cast<double2*>(scratch);
-    contract_sumtile_kernel<T><<<(unsigned)((int64_t)sa.ng * sa.G), kThreads, smem, s>>>(sa, partial);
-    const int64_t total = (int64_t)sa.ng * sum_groups(sa) * kSumGroup;
-    const int g = grid_for(total, 256, 1024);
-    if (exps && sizeof(T) == 8) sumtile_reduce_kernel<T, true><<<g, 256, 0, s>>>(sa, partial, exps);
-    else sumtile_reduce_kernel<T, false><<<g, 256, 0, s>>>(sa, partial, exps);
+    const int Na = lsum_na(la, NA), Nb = la.CB * NB, S = 32 >> la.LR;
+    const size_t smem = lsum_smem_bytes(Na, Nb, S * NA * NB);
+    contract_lsum_kernel<NA, NB><<<(unsigned)((int64_t)la.ng * la.G), kThreads, smem, s>>>(la, partial);
+    const int per = Na * Nb;
+    const int g = grid_for((int64_t)la.ng * per, 256, 1024);
+    if (exps) lsum_reduce_kernel<true><<<g, 256, 0, s>>>(la, per, Nb, partial, exps);
+    else lsum_reduce_kernel<false><<<g, 256, 0, s>>>(la, per, Nb, partial, exps);
     return cudaGetLastError();
+}
+
+template <int NA, int NB>
+int lsum_occupancy(size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, contract_lsum_kernel<NA, NB>, kThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int lsum_blocks_per_sm(int NA, int NB, size_t smem) {
+    static int cache[5][6][2] = {};                 // [log2 NB][log2 NA][large smem]
+    int lb = 0, la = 0;
+    while ((1 << lb) < NB) lb++;
+    while ((1 << la) < NA) la++;
+    if (lb > 4 || la > 5) return 2;
+    int& c = cache[lb][la][smem > 16384];
+    if (c) return c;
+    int n = 0;
+#define QXG_LSUM_OCC(A_, B_) if (NA == A_ && NB == B_) n = lsum_occupancy<A_, B_>(smem);
+    QXG_LSUM_OCC(1, 1) QXG_LSUM_OCC(2, 1) QXG_LSUM_OCC(4, 1) QXG_LSUM_OCC(8, 1) QXG_LSUM_OCC(16, 1)
+    QXG_LSUM_OCC(1, 2) QXG_LSUM_OCC(2, 2) QXG_LSUM_OCC(4, 2) QXG_LSUM_OCC(8, 2)
+    QXG_LSUM_OCC(1, 4) QXG_LSUM_OCC(2, 4) QXG_LSUM_OCC(4, 4)
+#undef QXG_LSUM_OCC
+    c = n > 0 ? n : 2;
+    return c;
+}
+
+template <int NB>
+cudaError_t launch_lsum_b(const LSumArgs& la, int NA, void* scratch, int* exps, cudaStream_t s) {
+    switch (NA) {
+        case 1: return launch_lsum_ab<1, NB>(la, scratch, exps, s);
+        case 2: if constexpr (2 * NB <= kLSumOut) return launch_lsum_ab<2, NB>(la, scratch, exps, s); break;
+        case 4: if constexpr (4 * NB <= kLSumOut) return launch_lsum_ab<4, NB>(la, scratch, exps, s); break;
+        case 8: if constexpr (8 * NB <= kLSumOut) return launch_lsum_ab<8, NB>(la, scratch, exps, s); break;
+        case 16: if constexpr (16 * NB <= kLSumOut) return launch_lsum_ab<16, NB>(la, scratch, exps, s); break;
+        default: break;
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_lsum(const LSumArgs& la, int NA, int NB, void* scratch, int* exps, cudaStream_t s) {
+    switch (NB) {
+        case 1: return launch_lsum_b<1>(la, NA, scratch, exps, s);
+        case 2: return launch_lsum_b<2>(la, NA, scratch, exps, s);
+        case 4: return launch_lsum_b<4>(la, NA, scratch, exps, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 template <typename T, int CONJ>
@@ -1307,8 +1417,9 @@ const char* contract_form(const StepArgs& a, bool fp64, int sm_count) {
         Rows2Args r2;
         return !fp64 && plan_rows2(ra, &r2) ? "cuda-core compact row-form" : "cuda-core row-form";
     }
-    SumTileArgs sa;
-    if (plan_sumtiles(a, fp64 ? 16 : 8, sum_blocks(sm_count), &sa)) return "cuda-core tiled long-sum";
+    LSumArgs la;
+    int NA = 0, NB = 0;
+    if (!fp64 && plan_lsum(a, sm_count, &la, &NA, &NB)) return "cuda-core long-sum";
     return splitk_count(a, sm_count) > 0 ? "cuda-core split-K" : "cuda-core general";
 }
 
@@ -1317,12 +1428,11 @@ cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_
     if (launches) *launches = 1;
     RowArgs ra;
     if (!plan_rows(a, fp64 ? 16 : 32, &ra)) {
-        SumTileArgs sa;
-        if (plan_sumtiles(a, fp64 ? 16 : 8, sum_blocks(sm_count), &sa)) {
-            if (scratch && scratch_bytes >= sum_partial_bytes(sa)) {
-                if (launches) *launches = 2;
-                return fp64 ? launch_sumtiles<double2>(sa, scratch, exps, s) : launch_sumtiles<float2>(sa, scratch, exps, s);
-            }
+        LSumArgs la;
+        int NA = 0, NB = 0;
+        if (!fp64 && plan_lsum(a, sm_count, &la, &NA, &NB) && scratch && scratch_bytes >= lsum_partial_bytes(la, NA, NB)) {
+            if (launches) *launches = 2;
+            return launch_lsum(la, NA, NB, scratch, exps, s);
         }
         const int ns = splitk_count(a, sm_count);
         if (ns > 0 && scratch && scratch_bytes >= (size_t)ns * (size_t)a.nC * (fp64 ? 16 : 8)) {

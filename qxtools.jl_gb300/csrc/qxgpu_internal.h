@@ -154,7 +154,7 @@ bool contract_uses_rows(const StepArgs& a, bool fp64);
 // The CUDA-core form launch_contract picks for a step (for diagnostics).
 const char* contract_form(const StepArgs& a, bool fp64, int sm_count);
 // Whether a step with few results and a long sum is better served by the tiled long sum on the
-// CUDA cores than by a tensor-core GEMM (at most 2^7 results per value of the batch bits).
+// CUDA cores (every operand element read once) than by a tensor-core GEMM.
 bool contract_prefers_cuda_cores(const StepArgs& a, bool fp64, int sm_count);
 cudaError_t launch_view(const ViewArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_output(const OutputArgs& a, bool fp64, int* exps, cudaStream_t s);
