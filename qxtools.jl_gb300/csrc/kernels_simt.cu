@@ -139,7 +139,6 @@ struct RowArgs {
     BitMap cX, cY;             // result index -> X / Y offset
     BitMap kX, kY;             // k -> X / Y offset
 };
-constexpr int kRowMaxY = 2048;          // elements of Y staged in shared memory
 constexpr int kRowMaxN = 1024;          // result columns per row (tabulated offsets)
 
 template <typename T, bool SCALED, int KMAX>
@@ -245,7 +244,8 @@ struct Rows2Args {
     BitMap kX, kY, nC, nY;         // k -> X / Y offset, n -> C / Y offset
     BitMap bY;                     // batch index -> Y offset
 };
-constexpr int kRows2MaxY = 2048;
+constexpr int kRows2MaxY = 8192;        // elements of Y (a 16-byte quadruple each in shared memory)
+constexpr int kRows2MaxYBits = 13;
 
 __host__ __device__ __forceinline__ unsigned f2u(float x) {
 #ifdef __CUDA_ARCH__
@@ -1023,13 +1023,14 @@ bool make_runs(const std::vector<std::pair<int, int>>& pairs, BitMap* m) {
     return true;
 }
 
-// Fill the row form of a step when its smaller operand fits in shared memory and K <= kmax.
-bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra) {
+// Fill the row form of a step when its smaller operand has at most 2^max_ybits elements (the row
+// kernel stages up to 2^11 in shared memory) and K <= kmax.
+bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra, int max_ybits = 11) {
     if (a.nk > 31 || (int64_t(1) << a.nk) > kmax) return false;
     const int abits = dst_bits(a.cA, a.kA), bbits = dst_bits(a.cB, a.kB);
     const bool x_is_a = abits >= bbits;
     const int ybits = x_is_a ? bbits : abits;
-    if (ybits > 11 || (int64_t(1) << ybits) > kRowMaxY) return false;
+    if (ybits > max_ybits) return false;
     const BitMap& cX = x_is_a ? a.cA : a.cB;
     const BitMap& cY = x_is_a ? a.cB : a.cA;
     int ncb = 0;
@@ -1225,6 +1226,11 @@ bool plan_lsum(const StepArgs& s0, int sm_count, LSumArgs* la, int* NA, int* NB,
     return true;
 }
 
+// The compact row form of a step, when it has one (FP32; Y up to kRows2MaxY elements).
+bool use_rows2(const StepArgs& a, bool fp64, RowArgs* ra, Rows2Args* r2) {
+    return !fp64 && plan_rows(a, 32, ra, kRows2MaxYBits) && plan_rows2(*ra, r2);
+}
+
 size_t lsum_partial_bytes(const LSumArgs& la, int NA, int NB) {
     return (size_t)la.ng * la.G * lsum_na(la, NA) * (la.CB * NB) * sizeof(double2);
 }
@@ -1255,6 +1261,10 @@ template <int K, int N>
 cudaError_t launch_rows2_kn(const Rows2Args& r2, int* exps, cudaStream_t s, int sm_count) {
     const size_t smem = rows2_smem_bytes(r2, K, N);
     auto launch = [&](auto kern) -> cudaError_t {
+        if (smem > 48 * 1024) {
+            const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
         int per_sm = 0;
         const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
         if (e != cudaSuccess) return e;
@@ -1308,7 +1318,8 @@ cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_cou
 
 size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
     RowArgs ra;
-    if (plan_rows(a, fp64 ? 16 : 32, &ra)) return 0;
+    Rows2Args r2;
+    if (use_rows2(a, fp64, &ra, &r2) || plan_rows(a, fp64 ? 16 : 32, &ra)) return 0;
     LSumArgs la;
     int NA = 0, NB = 0;
     if (!fp64 && plan_lsum(a, sm_count, &la, &NA, &NB)) return lsum_partial_bytes(la, NA, NB);
@@ -1408,15 +1419,15 @@ cudaError_t launch_splitk(const StepArgs& a, int ns, void* scratch, int* exps, c
 
 bool contract_uses_rows(const StepArgs& a, bool fp64) {
     RowArgs ra;
-    return plan_rows(a, fp64 ? 16 : 32, &ra);
+    Rows2Args r2;
+    return use_rows2(a, fp64, &ra, &r2) || plan_rows(a, fp64 ? 16 : 32, &ra);
 }
 
 const char* contract_form(const StepArgs& a, bool fp64, int sm_count) {
     RowArgs ra;
-    if (plan_rows(a, fp64 ? 16 : 32, &ra)) {
-        Rows2Args r2;
-        return !fp64 && plan_rows2(ra, &r2) ? "cuda-core compact row-form" : "cuda-core row-form";
-    }
+    Rows2Args r2;
+    if (use_rows2(a, fp64, &ra, &r2)) return "cuda-core compact row-form";
+    if (plan_rows(a, fp64 ? 16 : 32, &ra)) return "cuda-core row-form";
     LSumArgs la;
     int NA = 0, NB = 0;
     if (!fp64 && plan_lsum(a, sm_count, &la, &NA, &NB)) return "cuda-core long-sum";
@@ -1427,6 +1438,8 @@ cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_
                             size_t scratch_bytes, int* launches) {
     if (launches) *launches = 1;
     RowArgs ra;
+    Rows2Args r2;
+    if (use_rows2(a, fp64, &ra, &r2)) return launch_rows2(r2, ra.K, ra.N, exps, s, sm_count);
     if (!plan_rows(a, fp64 ? 16 : 32, &ra)) {
         LSumArgs la;
         int NA = 0, NB = 0;
@@ -1441,8 +1454,6 @@ cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_
         }
     }
     if (plan_rows(a, fp64 ? 16 : 32, &ra)) {
-        Rows2Args r2;
-        if (!fp64 && plan_rows2(ra, &r2)) return launch_rows2(r2, ra.K, ra.N, exps, s, sm_count);
         if (fp64) return ra.K <= 4 ? launch_rows<double2, 4>(ra, exps, s, sm_count)
                                    : launch_rows<double2, 16>(ra, exps, s, sm_count);
         if (ra.K <= 4) return launch_rows<float2, 4>(ra, exps, s, sm_count);
