@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "qxgpu_internal.h"
+#include "simt_common.h"
 
 namespace qxg {
 
@@ -23,37 +24,7 @@ int lsum_blocks_per_sm(int NA, int NB, size_t smem);
 
 namespace {
 
-template <typename T> struct Real;
-template <> struct Real<double2> { using type = double; };
-template <> struct Real<float2> { using type = float; };
-
-constexpr int kThreads = 256;
 constexpr int kTileBits = 10;          // 1024 result elements per tile, 4 per thread
-
-// 2^n as a float for |n| <= 126 by building the IEEE bits directly (exact power of two).
-__device__ __forceinline__ float pow2f(int n) {
-    n = n < -126 ? -126 : (n > 127 ? 127 : n);
-    return __int_as_float((n + 127) << 23);
-}
-__device__ __forceinline__ double pow2d(int n) {
-    n = n < -1022 ? -1022 : (n > 1023 ? 1023 : n);
-    return __longlong_as_double((long long)(n + 1023) << 52);
-}
-// Binary exponent e of |x| with |x| in [2^(e-1), 2^e) for normal floats (frexp convention).
-__host__ __device__ __forceinline__ int exp_of(float x) {
-#ifdef __CUDA_ARCH__
-    const unsigned u = __float_as_uint(x);
-#else
-    unsigned u;
-    std::memcpy(&u, &x, sizeof(u));
-#endif
-    return (int)((u >> 23) & 0xffu) - 126;
-}
-
-__device__ __forceinline__ int read_m(const int* exps, int slot) {
-    int m = exps[2 * slot + 1];
-    return m < -400 ? 0 : m;            // all-zero tensor: no scaling
-}
 
 // CONJ bit 0 / bit 1: use the complex conjugate of A / B (adjoint steps).  A compile-time sign
 // folds into the FMA operands, so the forward path pays nothing for it.
@@ -127,18 +98,6 @@ contract_kernel(const StepArgs a, int* exps) {
 // written once, and Y is read from its shared-memory copy.  Rows enumerate the result's bits
 // other than the n bits (rowmap), consecutive rows are consecutive result bits, so the X loads
 // and C stores of a warp fall on consecutive addresses whenever the layouts allow it.
-struct RowArgs {
-    const void* X;
-    const void* Y;
-    void* C;
-    int64_t nrows;
-    int32_t N, K, ny;          // result columns, summed extent, elements of Y
-    int32_t conjX, conjY;
-    int32_t expX, expY, expC;
-    BitMap rowmap, nmap;       // row index / n index -> result index
-    BitMap cX, cY;             // result index -> X / Y offset
-    BitMap kX, kY;             // k -> X / Y offset
-};
 constexpr int kRowMaxN = 1024;          // result columns per row (tabulated offsets)
 
 template <typename T, bool SCALED, int KMAX>
@@ -215,218 +174,6 @@ __global__ void __launch_bounds__(kThreads) contract_rows_kernel(const RowArgs a
         for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
         if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.expC + 1], emax);
     }
-}
-
-// Row form, compact: the row form with the loop work cut to the arithmetic, for FP32 steps with
-// compile-time K and N.  The row kernel above spends most of its issue slots on index work (bit
-// deposits per row, table reads and address arithmetic per (k, n)); here
-//   * a warp walks a contiguous range of 32-row groups (lanes = the 5 lowest row bits) and moves
-//     from one group to the next by adding per-bit offset deltas (the bits of g+1 that differ
-//     from g are 0..ctz(g+1)), so a row costs a few integer adds instead of three deposits;
-//   * Y is restaged densely as [batch][k][n] of (re, im, im, re) quadruples, so every (k, n)
-//     reads one 16-byte word at a compile-time offset from the row's batch base (batches padded
-//     by one word so lanes of different batches fall in different banks);
-//   * the complex product uses paired FP32 FMAs (fma.rn.f32x2): acc += (xr, xr) * (yr, yi) and
-//     acc += (-xi, xi) * (yi, yr), the same roundings in the same order as four scalar FMAs;
-//   * X pairs (k, k+1) and C pairs (n, n+1) move as 16-byte words when k bit 0 / n bit 0 is the
-//     operand's / result's lowest address bit.
-struct Rows2Args {
-    const void* X;
-    const void* Y;
-    void* C;
-    int64_t ngroups;           // 32-row groups
-    int32_t nbatch;            // Y batches (values of the row bits Y has)
-    int32_t conjX, conjY;
-    int32_t expX, expY, expC;
-    int32_t xpair, cpair;
-    BitMap laneX, laneC, laneB;    // lane -> X offset / C offset / batch index
-    BitMap grpX, grpC, grpB;       // group index -> X / C offset / batch index
-    BitMap kX, kY, nC, nY;         // k -> X / Y offset, n -> C / Y offset
-    BitMap bY;                     // batch index -> Y offset
-};
-constexpr int kRows2MaxY = 8192;        // elements of Y (a 16-byte quadruple each in shared memory)
-constexpr int kRows2MaxYBits = 13;
-
-__host__ __device__ __forceinline__ unsigned f2u(float x) {
-#ifdef __CUDA_ARCH__
-    return __float_as_uint(x);
-#else
-    unsigned u;
-    std::memcpy(&u, &x, sizeof(u));
-    return u;
-#endif
-}
-__host__ __device__ __forceinline__ float u2f(unsigned u) {
-#ifdef __CUDA_ARCH__
-    return __uint_as_float(u);
-#else
-    float x;
-    std::memcpy(&x, &u, sizeof(x));
-    return x;
-#endif
-}
-__host__ __device__ __forceinline__ unsigned long long f2pack(float lo, float hi) {
-    return (unsigned long long)f2u(lo) | ((unsigned long long)f2u(hi) << 32);
-}
-// d += a * b on both FP32 halves, each rounded once (fused).
-__host__ __device__ __forceinline__ void fma2(unsigned long long& d, unsigned long long a, unsigned long long b) {
-#ifdef __CUDA_ARCH__
-    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(d) : "l"(a), "l"(b));
-#else
-    const float lo = std::fmaf(u2f((unsigned)a), u2f((unsigned)b), u2f((unsigned)d));
-    const float hi = std::fmaf(u2f((unsigned)(a >> 32)), u2f((unsigned)(b >> 32)), u2f((unsigned)(d >> 32)));
-    d = f2pack(lo, hi);
-#endif
-}
-
-// Shared tables of the compact row form: Y quadruples [batch][k][n] (batches padded by one),
-// per group-bit deltas of the X / C offsets and batch index, X offsets of k, C offsets of n.
-struct Rows2Smem {
-    float4* Ys;
-    int64_t *dX, *dC, *dB, *kx, *cn;
-};
-template <int K, int N>
-__host__ __device__ __forceinline__ Rows2Smem rows2_carve(const Rows2Args& a, unsigned char* base) {
-    Rows2Smem t;
-    t.Ys = reinterpret_cast<float4*>(base);
-    t.dX = reinterpret_cast<int64_t*>(t.Ys + (size_t)a.nbatch * (K * N + 1));
-    t.dC = t.dX + 48;
-    t.dB = t.dC + 48;
-    t.kx = t.dB + 48;
-    t.cn = t.kx + K;
-    return t;
-}
-
-// Table entries written by thread tid of nthr.
-template <int K, int N>
-__host__ __device__ __forceinline__ void rows2_fill(const Rows2Args& a, const Rows2Smem& t, int tid, int nthr) {
-    constexpr int KN = K * N, BS = K * N + 1;
-    const float* __restrict__ Yg = static_cast<const float*>(a.Y);
-    for (int i = tid; i < a.nbatch * KN; i += nthr) {
-        const int b = i / KN, k = (i % KN) / N, n = i % N;
-        const int64_t yo = pdep(b, a.bY) + pdep(k, a.kY) + pdep(n, a.nY);
-        const float yr = Yg[2 * yo], yi = a.conjY ? -Yg[2 * yo + 1] : Yg[2 * yo + 1];
-        t.Ys[b * BS + k * N + n] = make_float4(yr, yi, yi, yr);
-    }
-    for (int j = tid; j < 46; j += nthr) {
-        const int64_t bit = int64_t(1) << j, low = bit - 1;
-        t.dX[j] = pdep(bit, a.grpX) - pdep(low, a.grpX);
-        t.dC[j] = pdep(bit, a.grpC) - pdep(low, a.grpC);
-        t.dB[j] = pdep(bit, a.grpB) - pdep(low, a.grpB);
-    }
-    for (int k = tid; k < K; k += nthr) t.kx[k] = pdep(k, a.kX);
-    for (int n = tid; n < N; n += nthr) t.cn[n] = pdep(n, a.nC);
-}
-
-// The rows of lane `lane` of warp w (of nwarps): its 32-row groups one after another.
-template <int K, int N, bool SCALED>
-__host__ __device__ __forceinline__ void rows2_walk(const Rows2Args& a, const Rows2Smem& t, int64_t w, int64_t nwarps,
-                                                    int lane, float scale, int& emax) {
-    constexpr int BS = K * N + 1;
-    const int64_t lx = pdep(lane, a.laneX), lc = pdep(lane, a.laneC), lb = pdep(lane, a.laneB);
-    const int64_t g0 = a.ngroups * w / nwarps, g1 = a.ngroups * (w + 1) / nwarps;
-    int64_t ox = pdep(g0, a.grpX), oc = pdep(g0, a.grpC), ob = pdep(g0, a.grpB);
-    const float2* __restrict__ X = static_cast<const float2*>(a.X);
-    float2* __restrict__ C = static_cast<float2*>(a.C);
-    const float sx = a.conjX ? -1.f : 1.f;
-    for (int64_t g = g0; g < g1; g++) {
-        const float2* xrow = X + (lx + ox);
-        const float4* yb = t.Ys + (lb + ob) * BS;
-        float xr[K], xi[K];
-        bool paired = false;
-        if constexpr (K > 1) {
-            if (a.xpair) {                                  // k, k+1 adjacent in X
-                paired = true;
-#pragma unroll
-                for (int k = 0; k < K; k += 2) {
-                    const float4 v = *reinterpret_cast<const float4*>(xrow + t.kx[k]);
-                    xr[k] = v.x; xi[k] = v.y; xr[k + 1] = v.z; xi[k + 1] = v.w;
-                }
-            }
-        }
-        if (!paired) {
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                const float2 v = xrow[t.kx[k]];
-                xr[k] = v.x; xi[k] = v.y;
-            }
-        }
-        unsigned long long acc[N];
-#pragma unroll
-        for (int n = 0; n < N; n++) acc[n] = 0ull;
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            const float xik = sx * xi[k];
-            const unsigned long long xx = f2pack(xr[k], xr[k]), xj = f2pack(-xik, xik);
-#pragma unroll
-            for (int n = 0; n < N; n++) {
-                const float4 y = yb[k * N + n];
-                fma2(acc[n], xx, f2pack(y.x, y.y));
-                fma2(acc[n], xj, f2pack(y.z, y.w));
-            }
-        }
-        float re[N], im[N];
-#pragma unroll
-        for (int n = 0; n < N; n++) {
-            re[n] = u2f((unsigned)(acc[n] & 0xffffffffull));
-            im[n] = u2f((unsigned)(acc[n] >> 32));
-            if (SCALED) {
-                re[n] *= scale; im[n] *= scale;
-                const float mx = fmaxf(fabsf(re[n]), fabsf(im[n]));
-                if (mx > 0.f) emax = emax > exp_of(mx) ? emax : exp_of(mx);
-            }
-        }
-        float2* crow = C + (lc + oc);
-        bool cpaired = false;
-        if constexpr (N > 1) {
-            if (a.cpair) {                                  // n, n+1 adjacent in C
-                cpaired = true;
-#pragma unroll
-                for (int n = 0; n < N; n += 2)
-                    *reinterpret_cast<float4*>(crow + t.cn[n]) = make_float4(re[n], im[n], re[n + 1], im[n + 1]);
-            }
-        }
-        if (!cpaired) {
-#pragma unroll
-            for (int n = 0; n < N; n++) crow[t.cn[n]] = make_float2(re[n], im[n]);
-        }
-        const unsigned long long next = (unsigned long long)(g + 1);
-#ifdef __CUDA_ARCH__
-        const int j = __ffsll((long long)next) - 1;        // bits 0..j of g flip
-#else
-        const int j = __builtin_ctzll(next);
-#endif
-        ox += t.dX[j];
-        oc += t.dC[j];
-        ob += t.dB[j];
-    }
-}
-
-// Launched with kThreads threads; dynamic shared memory: rows2_smem_bytes.
-template <int K, int N, bool SCALED>
-__global__ void __launch_bounds__(kThreads) contract_rows2_kernel(const Rows2Args a, int* exps) {
-    extern __shared__ __align__(16) unsigned char rows2_smem[];
-    const Rows2Smem t = rows2_carve<K, N>(a, rows2_smem);
-    rows2_fill<K, N>(a, t, threadIdx.x, kThreads);
-    __syncthreads();
-    float scale = 1.f;
-    if (SCALED) {
-        const int mX = read_m(exps, a.expX), mY = read_m(exps, a.expY);
-        scale = pow2f(-(mX + mY));
-        if (blockIdx.x == 0 && threadIdx.x == 0)
-            exps[2 * a.expC] = exps[2 * a.expX] + exps[2 * a.expY] + mX + mY;
-    }
-    int emax = kExpUnset;
-    rows2_walk<K, N, SCALED>(a, t, (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5),
-                             (int64_t)gridDim.x * (kThreads / 32), threadIdx.x & 31, scale, emax);
-    if (SCALED) {
-        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.expC + 1], emax);
-    }
-}
-
-size_t rows2_smem_bytes(const Rows2Args& a, int K, int N) {
-    return sizeof(float4) * (size_t)a.nbatch * (size_t)(K * N + 1) + sizeof(int64_t) * (3 * 48 + K + N);
 }
 
 // Long sum with a small result (FP32): C[a, b, g] = sum_r A[a, g, r] B[b, g, r], the summed index
@@ -1008,24 +755,9 @@ int dst_bits(const BitMap& c, const BitMap& k) {
     return __builtin_popcountll(used);
 }
 
-// Consecutive (src, dst) pairs with both sides increasing by one collapse into one run.
-bool make_runs(const std::vector<std::pair<int, int>>& pairs, BitMap* m) {
-    m->n = 0;
-    for (size_t i = 0; i < pairs.size();) {
-        size_t j = i + 1;
-        while (j < pairs.size() && pairs[j].first == pairs[j - 1].first + 1 && pairs[j].second == pairs[j - 1].second + 1)
-            j++;
-        if (m->n >= kMaxRuns) return false;
-        m->r[m->n] = Run{(uint8_t)pairs[i].first, (uint8_t)(j - i), (uint8_t)pairs[i].second, 0};
-        m->n++;
-        i = j;
-    }
-    return true;
-}
-
 // Fill the row form of a step when its smaller operand has at most 2^max_ybits elements (the row
 // kernel stages up to 2^11 in shared memory) and K <= kmax.
-bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra, int max_ybits = 11) {
+bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra, int max_ybits = 11, bool wide_ok = false) {
     if (a.nk > 31 || (int64_t(1) << a.nk) > kmax) return false;
     const int abits = dst_bits(a.cA, a.kA), bbits = dst_bits(a.cB, a.kB);
     const bool x_is_a = abits >= bbits;
@@ -1048,8 +780,8 @@ bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra, int max_ybits = 11) {
         else rows.push_back({(int)rows.size(), p});
     }
     if ((int64_t(1) << cols.size()) > kRowMaxN) return false;
-    // a thread writes its N results one after another: wide rows need many of them
-    if (cols.size() > 5 && rows.size() < 16) return false;
+    // the row kernel's thread writes its N results one after another: wide rows need many rows
+    if (!wide_ok && cols.size() > 5 && rows.size() < 16) return false;
     memset(ra, 0, sizeof(*ra));
     if (!make_runs(rows, &ra->rowmap) || !make_runs(cols, &ra->nmap)) return false;
     ra->X = x_is_a ? a.A : a.B;
@@ -1068,63 +800,6 @@ bool plan_rows(const StepArgs& a, int kmax, RowArgs* ra, int max_ybits = 11) {
     ra->cY = cY;
     ra->kX = x_is_a ? a.kA : a.kB;
     ra->kY = x_is_a ? a.kB : a.kA;
-    return true;
-}
-
-// Fill the compact row form (FP32) from a row form: K <= 32, N <= 16, K N <= 256, >= 32 rows.
-bool plan_rows2(const RowArgs& ra, Rows2Args* r2) {
-    auto lg = [](int64_t v) { int b = 0; while ((int64_t(1) << b) < v) b++; return b; };
-    auto pos_of = [](const BitMap& m, int64_t bit) {
-        const int64_t o = pdep(bit, m);
-        return o ? __builtin_ctzll((unsigned long long)o) : -1;
-    };
-    const int R = lg(ra.nrows);
-    if (R < 5 || ra.K > 32 || ra.N > 16 || ra.K * ra.N > 256) return false;
-    std::vector<std::pair<int, int>> lX, lC, lB, gX, gC, gB, nY, bY;
-    int nb = 0;
-    for (int i = 0; i < R; i++) {
-        const int c = pos_of(ra.rowmap, int64_t(1) << i);
-        const int x = pos_of(ra.cX, int64_t(1) << c), y = pos_of(ra.cY, int64_t(1) << c);
-        if (c < 0 || x < 0) return false;
-        auto& mx = i < 5 ? lX : gX;
-        auto& mc = i < 5 ? lC : gC;
-        auto& mb = i < 5 ? lB : gB;
-        const int src = i < 5 ? i : i - 5;
-        mx.push_back({src, x});
-        mc.push_back({src, c});
-        if (y >= 0) {
-            mb.push_back({src, nb});
-            bY.push_back({nb, y});
-            nb++;
-        }
-    }
-    for (int j = 0; (1 << j) < ra.N; j++) {
-        const int c = pos_of(ra.nmap, int64_t(1) << j);
-        const int y = c < 0 ? -1 : pos_of(ra.cY, int64_t(1) << c);
-        if (y < 0) return false;
-        nY.push_back({j, y});
-    }
-    memset(r2, 0, sizeof(*r2));
-    if (!make_runs(lX, &r2->laneX) || !make_runs(lC, &r2->laneC) || !make_runs(lB, &r2->laneB) ||
-        !make_runs(gX, &r2->grpX) || !make_runs(gC, &r2->grpC) || !make_runs(gB, &r2->grpB) ||
-        !make_runs(nY, &r2->nY) || !make_runs(bY, &r2->bY))
-        return false;
-    r2->kX = ra.kX;
-    r2->kY = ra.kY;
-    r2->nC = ra.nmap;
-    r2->X = ra.X;
-    r2->Y = ra.Y;
-    r2->C = ra.C;
-    r2->ngroups = int64_t(1) << (R - 5);
-    r2->nbatch = 1 << nb;
-    if ((int64_t)r2->nbatch * ra.K * ra.N > kRows2MaxY) return false;
-    r2->conjX = ra.conjX;
-    r2->conjY = ra.conjY;
-    r2->expX = ra.expX;
-    r2->expY = ra.expY;
-    r2->expC = ra.expC;
-    r2->xpair = ra.K > 1 && pdep(1, ra.kX) == 1 && (reinterpret_cast<uintptr_t>(ra.X) & 15) == 0;
-    r2->cpair = ra.N > 1 && pdep(1, ra.nmap) == 1 && (reinterpret_cast<uintptr_t>(ra.C) & 15) == 0;
     return true;
 }
 
@@ -1228,7 +903,7 @@ bool plan_lsum(const StepArgs& s0, int sm_count, LSumArgs* la, int* NA, int* NB,
 
 // The compact row form of a step, when it has one (FP32; Y up to kRows2MaxY elements).
 bool use_rows2(const StepArgs& a, bool fp64, RowArgs* ra, Rows2Args* r2) {
-    return !fp64 && plan_rows(a, 32, ra, kRows2MaxYBits) && plan_rows2(*ra, r2);
+    return !fp64 && plan_rows(a, 32, ra, kRows2MaxYBits, true) && plan_rows2(*ra, r2);
 }
 
 size_t lsum_partial_bytes(const LSumArgs& la, int NA, int NB) {
@@ -1257,51 +932,6 @@ void launch_general(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int
     else contract_kernel<float2, false, CONJ><<<grid, kThreads, 0, s>>>(a, exps);
 }
 
-template <int K, int N>
-cudaError_t launch_rows2_kn(const Rows2Args& r2, int* exps, cudaStream_t s, int sm_count) {
-    const size_t smem = rows2_smem_bytes(r2, K, N);
-    auto launch = [&](auto kern) -> cudaError_t {
-        if (smem > 48 * 1024) {
-            const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-        }
-        int per_sm = 0;
-        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
-        if (e != cudaSuccess) return e;
-        const int64_t cap = (int64_t)sm_count * std::max(per_sm, 1);
-        const int64_t want = (r2.ngroups + kThreads / 32 - 1) / (kThreads / 32);
-        const int grid = (int)std::max<int64_t>(1, std::min(want, cap));
-        kern<<<grid, kThreads, smem, s>>>(r2, exps);
-        return cudaGetLastError();
-    };
-    return exps ? launch(contract_rows2_kernel<K, N, true>) : launch(contract_rows2_kernel<K, N, false>);
-}
-
-template <int K>
-cudaError_t launch_rows2_k(const Rows2Args& r2, int N, int* exps, cudaStream_t s, int sm_count) {
-    switch (N) {
-        case 1: return launch_rows2_kn<K, 1>(r2, exps, s, sm_count);
-        case 2: return launch_rows2_kn<K, 2>(r2, exps, s, sm_count);
-        case 4: return launch_rows2_kn<K, 4>(r2, exps, s, sm_count);
-        case 8: if constexpr (K <= 32) return launch_rows2_kn<K, 8>(r2, exps, s, sm_count); break;
-        case 16: if constexpr (K <= 16) return launch_rows2_kn<K, 16>(r2, exps, s, sm_count); break;
-        default: break;
-    }
-    return cudaErrorInvalidValue;
-}
-
-cudaError_t launch_rows2(const Rows2Args& r2, int K, int N, int* exps, cudaStream_t s, int sm_count) {
-    switch (K) {
-        case 1: return launch_rows2_k<1>(r2, N, exps, s, sm_count);
-        case 2: return launch_rows2_k<2>(r2, N, exps, s, sm_count);
-        case 4: return launch_rows2_k<4>(r2, N, exps, s, sm_count);
-        case 8: return launch_rows2_k<8>(r2, N, exps, s, sm_count);
-        case 16: return launch_rows2_k<16>(r2, N, exps, s, sm_count);
-        case 32: return launch_rows2_k<32>(r2, N, exps, s, sm_count);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
 template <typename T, int KMAX>
 cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_count) {
     const size_t smem = (size_t)ra.ny * sizeof(T) + (size_t)KMAX * 12 + (size_t)ra.N * 12;
@@ -1315,6 +945,21 @@ cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_cou
 }
 
 }  // namespace
+
+// Consecutive (src, dst) pairs with both sides increasing by one collapse into one run.
+bool make_runs(const std::vector<std::pair<int, int>>& pairs, BitMap* m) {
+    m->n = 0;
+    for (size_t i = 0; i < pairs.size();) {
+        size_t j = i + 1;
+        while (j < pairs.size() && pairs[j].first == pairs[j - 1].first + 1 && pairs[j].second == pairs[j - 1].second + 1)
+            j++;
+        if (m->n >= kMaxRuns) return false;
+        m->r[m->n] = Run{(uint8_t)pairs[i].first, (uint8_t)(j - i), (uint8_t)pairs[i].second, 0};
+        m->n++;
+        i = j;
+    }
+    return true;
+}
 
 size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
     RowArgs ra;
@@ -1439,7 +1084,7 @@ cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_
     if (launches) *launches = 1;
     RowArgs ra;
     Rows2Args r2;
-    if (use_rows2(a, fp64, &ra, &r2)) return launch_rows2(r2, ra.K, ra.N, exps, s, sm_count);
+    if (use_rows2(a, fp64, &ra, &r2)) return launch_rows2(r2, ra.K, r2.ncol, exps, s, sm_count);
     if (!plan_rows(a, fp64 ? 16 : 32, &ra)) {
         LSumArgs la;
         int NA = 0, NB = 0;
