@@ -210,6 +210,7 @@ struct LSumArgs {
 constexpr int kLSumOut = 16;            // results per lane (NA x NB)
 constexpr int kLSumRowsPerLane = 512;
 constexpr int kLSumWarps = kThreads / 32;
+constexpr int kLSumAhead = 8;           // groups between a lane's L2 prefetch and its loads
 
 __host__ __device__ __forceinline__ int lsum_na(const LSumArgs& a, int NA) { return a.CA * (32 >> a.LR) * NA; }
 
@@ -300,6 +301,23 @@ __host__ __device__ __forceinline__ void lsum_madd(const float* ar, const float*
     }
 }
 
+// L2 prefetch of one row's A and B values (no data returned, no fault on a valid address).
+template <int NA, int NB>
+__host__ __device__ __forceinline__ void lsum_prefetch(const LSumArgs& a, const float2* arow, const float2* brow,
+                                                       const int64_t* ao, const int64_t* bo) {
+#ifdef __CUDA_ARCH__
+    const int sa = a.apair ? 2 : 1, sb = a.bpair ? 2 : 1;
+#pragma unroll
+    for (int i = 0; i < NA; i++)
+        if (i % sa == 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(arow + ao[i]));
+#pragma unroll
+    for (int i = 0; i < NB; i++)
+        if (i % sb == 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(brow + bo[i]));
+#else
+    (void)a; (void)arow; (void)brow; (void)ao; (void)bo;
+#endif
+}
+
 __host__ __device__ __forceinline__ int lsum_ctz(unsigned long long v) {
 #ifdef __CUDA_ARCH__
     return __ffsll((long long)v) - 1;
@@ -323,8 +341,17 @@ __host__ __device__ __forceinline__ void lsum_walk(const LSumArgs& a, const LSum
     const int64_t* ao = t.ao + a0;
     const int64_t* bo = t.bo + b0;
     const float sa = a.conjA ? -1.f : 1.f, sb = a.conjB ? -1.f : 1.f;
+    // a second walker kLSumAhead groups ahead issues L2 prefetches of the rows to come
+    int64_t gp = g0 + kLSumAhead;
+    int64_t pA = gp < g1 ? pdep(gp, a.grpA) : 0, pB = gp < g1 ? pdep(gp, a.grpB) : 0;
     for (int64_t g = g0; g < g1; g += 2) {
         const bool two = g + 1 < g1;
+        for (int u = 0; u < 2 && gp < g1; u++, gp++) {
+            lsum_prefetch<NA, NB>(a, Ag + pA, Bg + pB, ao, bo);
+            const int jp = lsum_ctz((unsigned long long)(gp + 1));
+            pA += t.dA[jp];
+            pB += t.dB[jp];
+        }
         const int j1 = lsum_ctz((unsigned long long)(g + 1));
         const int64_t oA1 = oA + t.dA[j1], oB1 = oB + t.dB[j1];
         float ar[NA], ai[NA], br[NB], bi[NB], ar1[NA], ai1[NA], br1[NB], bi1[NB];
