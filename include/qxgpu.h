@@ -225,7 +225,9 @@ void qxg_program_destroy(qxg_program* prog);
  * QXTns.contract_pair! semantics).  A, B, C are column-major interleaved complex arrays of
  * the given precision's storage type (QXG_PREC_FP64: double2 with FP64 arithmetic; the other
  * modes: float2 with FP32 arithmetic); `stream` is a cudaStream_t or NULL for the default
- * stream.  Dimensions must be powers of two.  Enqueues one kernel and allocates nothing. */
+ * stream.  Dimensions must be powers of two.  Enqueues one kernel; a float2 contraction with
+ * few results and a sum of 2^12 or more terms enqueues two, with their partial sums in scratch
+ * taken and returned in stream order (cudaMallocAsync / cudaFreeAsync on `stream`). */
 int qxg_ncon(int32_t precision,
              void* C, int32_t nc, const int32_t* c_labels,
              const void* A, int32_t na, const int32_t* a_labels, const int64_t* a_dims,
