@@ -178,11 +178,13 @@ typedef enum qxg_kernel_kind {
     QXG_KERNEL_VIEW = 3,            /* slice-batch view materialisation */
     QXG_KERNEL_OUTPUT = 4,          /* bitstring-batch output vectors */
     QXG_KERNEL_REDUCE = 5,          /* FP64 sum over the slice batch */
-    QXG_KERNEL_TC_PACK = 6          /* gather + hi/lo split of both operands for the tensor cores */
+    QXG_KERNEL_TC_PACK = 6,         /* gather + hi/lo split of both operands for the tensor cores */
+    QXG_KERNEL_CONTRACT_BATCH = 7   /* several small independent CUDA-core contractions, one launch */
 } qxg_kernel_kind;
 
 typedef struct qxg_step_profile {
-    int32_t instr;      /* instruction index of the command (-1: the slice reduction) */
+    int32_t instr;      /* instruction index of the command (-1: the slice reduction, -2: batches
+                           of small contractions, QXG_KERNEL_CONTRACT_BATCH) */
     int32_t kernel;     /* qxg_kernel_kind */
     int64_t launches;
     double ms;          /* summed CUDA-event time of those launches */

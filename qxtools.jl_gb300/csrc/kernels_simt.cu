@@ -470,6 +470,76 @@ __global__ void lsum_reduce_kernel(const LSumArgs a, int per, int Nb, const doub
     }
 }
 
+// Batch of small independent contractions in one launch (the gate absorptions of a pass, whose
+// own launches would cost more than their work).  Block b finds its step by binary search over
+// the steps' first blocks, copies the step's arguments and its K offsets into shared memory and
+// computes up to kBatchResults results, each summing its K <= kBatchMaxK products in order; the
+// step's first block sets the result's base exponent and every block raises its maximum, as the
+// single-step kernels do.  Launched with kThreads threads.
+template <typename T, bool SCALED>
+__global__ void __launch_bounds__(kThreads) contract_batch_kernel(const BatchStep* steps, int n, int* exps) {
+    using R = typename Real<T>::type;
+    __shared__ int sel;
+    __shared__ __align__(16) StepArgs a;
+    __shared__ int64_t tA[kBatchMaxK], tB[kBatchMaxK];
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (steps[mid].first_block <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+        }
+        sel = lo;
+    }
+    __syncthreads();
+    {
+        const int* src = reinterpret_cast<const int*>(&steps[sel].a);
+        int* dst = reinterpret_cast<int*>(&a);
+        for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / sizeof(int)); i += kThreads) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int K = 1 << a.nk;
+    for (int k = threadIdx.x; k < K; k += kThreads) { tA[k] = pdep(k, a.kA); tB[k] = pdep(k, a.kB); }
+    __syncthreads();
+    const int part = (int)blockIdx.x - steps[sel].first_block;
+    R scale = R(1);
+    if (SCALED) {
+        const int mA = read_m(exps, a.expA), mB = read_m(exps, a.expB);
+        scale = (R)pow2f(-(mA + mB));
+        if (part == 0 && threadIdx.x == 0) exps[2 * a.expC] = exps[2 * a.expA] + exps[2 * a.expB] + mA + mB;
+    }
+    const T* __restrict__ A = static_cast<const T*>(a.A);
+    const T* __restrict__ B = static_cast<const T*>(a.B);
+    T* __restrict__ C = static_cast<T*>(a.C);
+    const R ca = a.conjA ? R(-1) : R(1), cb = a.conjB ? R(-1) : R(1);
+    const int64_t c0 = (int64_t)part * kBatchResults;
+    const int64_t c1 = c0 + kBatchResults < a.nC ? c0 + kBatchResults : a.nC;
+    int emax = kExpUnset;
+    for (int64_t c = c0 + threadIdx.x; c < c1; c += kThreads) {
+        const int64_t ao = pdep(c, a.cA), bo = pdep(c, a.cB);
+        R re = R(0), im = R(0);
+        for (int k = 0; k < K; k++) {
+            const T x = A[ao + tA[k]];
+            const T y = B[bo + tB[k]];
+            const R xi = ca * x.y, yi = cb * y.y;
+            re = fma(x.x, y.x, re);
+            re = fma(-xi, yi, re);
+            im = fma(x.x, yi, im);
+            im = fma(xi, y.x, im);
+        }
+        if (SCALED) {
+            re *= scale; im *= scale;
+            const float mx = fmaxf(fabsf((float)re), fabsf((float)im));
+            if (mx > 0.f) emax = max(emax, exp_of(mx));
+        }
+        T out; out.x = re; out.y = im;
+        C[c] = out;
+    }
+    if (SCALED) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * a.expC + 1], emax);
+    }
+}
+
 // Split-K form of a contraction with few results and a long sum (the adjoint steps that end in
 // gate-sized leaf gradients sum over every other index of the network).  Pass 1: block
 // (result tile, split) sums the split's range of the high K index (all 2^nkt low K values) for
@@ -1089,6 +1159,13 @@ cudaError_t launch_splitk(const StepArgs& a, int ns, void* scratch, int* exps, c
     return cudaGetLastError();
 }
 
+bool contract_x_is_b(const StepArgs& a, bool fp64) {
+    RowArgs ra;
+    Rows2Args r2;
+    if (!use_rows2(a, fp64, &ra, &r2) && !plan_rows(a, fp64 ? 16 : 32, &ra)) return false;
+    return dst_bits(a.cA, a.kA) < dst_bits(a.cB, a.kB);      // plan_rows' choice of X
+}
+
 bool contract_uses_rows(const StepArgs& a, bool fp64) {
     RowArgs ra;
     Rows2Args r2;
@@ -1145,6 +1222,14 @@ cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_
         case 2: launch_general<2>(a, fp64, exps, s, grid); break;
         default: launch_general<3>(a, fp64, exps, s, grid); break;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const BatchStep* d_steps, int n, int nblocks, bool fp64, int* exps, cudaStream_t s) {
+    if (n <= 0 || nblocks <= 0) return cudaSuccess;
+    if (fp64) contract_batch_kernel<double2, false><<<nblocks, kThreads, 0, s>>>(d_steps, n, exps);
+    else if (exps) contract_batch_kernel<float2, true><<<nblocks, kThreads, 0, s>>>(d_steps, n, exps);
+    else contract_batch_kernel<float2, false><<<nblocks, kThreads, 0, s>>>(d_steps, n, exps);
     return cudaGetLastError();
 }
 

@@ -75,6 +75,9 @@ struct Tensor {
     int slot = -1;                      // exponent slot
 };
 
+// Tensors of at most this many bytes get arena space of their own (no reuse within a pass).
+constexpr int64_t kSmallTensorBytes = int64_t(256) << 10;
+
 // Backward (adjoint) step kinds of gradient plans.
 constexpr int kBwdNcon = 1, kBwdView = 2, kBwdLeaf = 3;
 
@@ -91,6 +94,7 @@ struct Step {                           // an executable item of a pass
     ViewAdjArgs vaargs;
     LeafGradArgs largs;
     bool use_tc = false;                // tensor-core path (split modes)
+    int batch = -1;                     // batch of small steps it runs in (index in its list's batches)
     bool tc_tuned = false;              // the tile variant has been chosen
     std::string tune_note;              // autotuner: milliseconds per candidate variant
     TcStep tc;                          // tensor-core step description
@@ -113,6 +117,14 @@ struct Plan {
     SeedArgs seed;
     int slot_all_end = 0;               // slots [slot_begin[0], slot_all_end) reset every pass
     double flops_bwd = 0;
+    // small CUDA-core steps run in batches (lists 0-2: the groups' steps, 3: the backward steps):
+    // each list runs as `order` -- (0, step index) or (1, batch index) -- a topological order by
+    // dependency level in which the small steps of one level form one batch
+    struct Batch { std::vector<int> members; int first = 0, nblocks = 0; double flops = 0, bytes = 0; };
+    std::vector<Batch> batches[4];
+    std::vector<std::pair<int, int>> order[4];
+    BatchStep* d_batch = nullptr;       // device copies of the batched steps' arguments
+    ~Plan() { if (d_batch) cudaFree(d_batch); }
 };
 
 }  // namespace
@@ -808,7 +820,11 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
     for (int t = 0; t < ntab; t++) {
         if (pos_of[t] < 0) continue;
         const int64_t bytes = ((int64_t(1) << T[t].layout.size()) * (int64_t)P->esize + 255) & ~int64_t(255);
-        items.push_back({t, pos_of[t], std::max(last[t], pos_of[t]), bytes});
+        // small tensors keep their own bytes for the whole pass: reusing them would order
+        // independent sub-trees one after another (a write after another branch's read) and keep
+        // their small steps out of each other's batches and graph branches
+        if (bytes <= kSmallTensorBytes) items.push_back({t, 0, end_pos, bytes});
+        else items.push_back({t, pos_of[t], std::max(last[t], pos_of[t]), bytes});
     }
     std::vector<int> order(items.size());
     for (size_t i = 0; i < items.size(); i++) order[i] = (int)i;
@@ -904,6 +920,7 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
 
 void drop_graphs(qxg_program* P);
 void drop_grad_graph(qxg_program* P);
+int plan_batches(qxg_program* P, Plan& pl);
 
 // Choose batch sizes whose workspace fits the limit, (re)build the forward plan (grad = false)
 // or the gradient plan (grad = true), grow the shared device buffers and bind pointers.  Both
@@ -1009,7 +1026,7 @@ int ensure_plan(qxg_program* P, int nbits_call, bool grad = false) {
         P->h_exps_init[2 * t.slot] = 0;
         P->h_exps_init[2 * t.slot + 1] = t.kind == QXG_OP_LOAD ? P->data_m[t.data_id] : kExpUnset;
     }
-    return 0;
+    return plan_batches(P, pl);
 }
 
 // Event pair around one launch when profiling; returns the index of the first event.
@@ -1311,15 +1328,115 @@ int launch_fwd_step(qxg_program* P, Plan& pl, Step& st, int* exps, cudaStream_t 
     return prof_end(P, ev, instr, kind, st.flops, st.bytes);
 }
 
-void append_group_works(qxg_program* P, Plan& pl, int g, int* exps, std::vector<Work>& w) {
-    for (auto& st : pl.steps[g]) {
+// A step small enough to share a launch: a CUDA-core contraction (forward or adjoint) with at
+// most kBatchMaxResults results, K <= kBatchMaxK and no scratch.
+bool step_small(const qxg_program* P, const Step& st) {
+    if (st.kind != QXG_OP_NCON || st.use_tc) return false;
+    if (st.bkind != 0 && st.bkind != kBwdNcon) return false;
+    if (st.sargs.nC > kBatchMaxResults || (int64_t(1) << st.sargs.nk) > kBatchMaxK) return false;
+    return contract_scratch_bytes(st.sargs, P->fp64, P->sm_count) == 0;
+}
+
+// Order each step list by dependency level (a step's level is one above the highest level of the
+// earlier steps it conflicts with: it reads what they write, or writes what they touch) and
+// gather the small steps of each level into one batch; upload the batched steps' arguments.
+// Called after the plan's pointers are bound.
+int plan_batches(qxg_program* P, Plan& pl) {
+    std::vector<BatchStep> host;
+    for (int L = 0; L < 4; L++) {
+        std::vector<Step>& steps = L < 3 ? pl.steps[L] : pl.bsteps;
+        pl.batches[L].clear();
+        pl.order[L].clear();
+        const int n = (int)steps.size();
+        std::vector<Work> sp(n);
+        for (int j = 0; j < n; j++) {
+            steps[j].batch = -1;
+            add_step_spans(P, pl, steps[j], sp[j]);
+        }
+        std::vector<int> level(n, 0);
+        int top = 0;
+        for (int j = 0; j < n; j++) {
+            for (int i = 0; i < j; i++)
+                if (level[i] + 1 > level[j] &&
+                    (spans_meet(sp[j].wr, sp[i].rd) || spans_meet(sp[j].wr, sp[i].wr) || spans_meet(sp[j].rd, sp[i].wr)))
+                    level[j] = level[i] + 1;
+            top = std::max(top, level[j]);
+        }
+        std::vector<std::vector<int>> at(top + 1);
+        for (int j = 0; j < n; j++) at[level[j]].push_back(j);
+        for (auto& lv : at) {
+            std::vector<int> small;
+            for (int j : lv)
+                if (step_small(P, steps[j])) small.push_back(j);
+            for (int j : lv)
+                if (small.size() < 2 || !step_small(P, steps[j])) pl.order[L].push_back({0, j});
+            if (small.size() < 2) continue;
+            Plan::Batch b;
+            b.first = (int)host.size();
+            for (int j : small) {
+                BatchStep d;
+                d.a = steps[j].sargs;
+                if (contract_x_is_b(d.a, P->fp64)) {       // same factor order as the step's own kernel
+                    std::swap(d.a.A, d.a.B);
+                    std::swap(d.a.cA, d.a.cB);
+                    std::swap(d.a.kA, d.a.kB);
+                    std::swap(d.a.conjA, d.a.conjB);
+                    std::swap(d.a.expA, d.a.expB);
+                }
+                d.first_block = b.nblocks;
+                d.nblocks = (int)((steps[j].sargs.nC + kBatchResults - 1) / kBatchResults);
+                b.nblocks += d.nblocks;
+                b.flops += steps[j].flops;
+                b.bytes += steps[j].bytes;
+                steps[j].batch = (int)pl.batches[L].size();
+                b.members.push_back(j);
+                host.push_back(d);
+            }
+            pl.order[L].push_back({1, (int)pl.batches[L].size()});
+            pl.batches[L].push_back(std::move(b));
+        }
+    }
+    if (pl.d_batch) cudaFree(pl.d_batch);
+    pl.d_batch = nullptr;
+    if (!host.empty()) {
+        QXG_CUDA(cudaMalloc(&pl.d_batch, sizeof(BatchStep) * host.size()));
+        QXG_CUDA(cudaMemcpy(pl.d_batch, host.data(), sizeof(BatchStep) * host.size(), cudaMemcpyHostToDevice));
+    }
+    return 0;
+}
+
+int launch_batch_work(qxg_program* P, Plan& pl, int L, int b, int* exps, cudaStream_t s) {
+    const Plan::Batch& bt = pl.batches[L][b];
+    size_t ev = 0;
+    if (int r = prof_begin(P, &ev)) return r;
+    QXG_CUDA(launch_batch(pl.d_batch + bt.first, (int)bt.members.size(), bt.nblocks, P->fp64, exps, s));
+    return prof_end(P, ev, -2, QXG_KERNEL_CONTRACT_BATCH, bt.flops, bt.bytes);
+}
+
+// The works of step list L in its batched order; `one` launches a single step of the list.
+void append_list_works(qxg_program* P, Plan& pl, int L, int* exps, std::vector<Work>& w,
+                       const std::function<int(Step&, cudaStream_t)>& one) {
+    std::vector<Step>& steps = L < 3 ? pl.steps[L] : pl.bsteps;
+    for (const auto& it : pl.order[L]) {
         Work x;
-        Step* sp = &st;
-        Plan* pp = &pl;
-        x.launch = [P, pp, sp, exps](cudaStream_t s) { return launch_fwd_step(P, *pp, *sp, exps, s); };
-        add_step_spans(P, pl, st, x);
+        if (it.first == 0) {
+            Step* sp = &steps[it.second];
+            x.launch = [one, sp](cudaStream_t s) { return one(*sp, s); };
+            add_step_spans(P, pl, *sp, x);
+        } else {
+            Plan* pp = &pl;
+            const int b = it.second;
+            x.launch = [P, pp, L, b, exps](cudaStream_t s) { return launch_batch_work(P, *pp, L, b, exps, s); };
+            for (int j : pl.batches[L][b].members) add_step_spans(P, pl, steps[j], x);
+        }
         w.push_back(std::move(x));
     }
+}
+
+void append_group_works(qxg_program* P, Plan& pl, int g, int* exps, std::vector<Work>& w) {
+    Plan* pp = &pl;
+    append_list_works(P, pl, g, exps, w,
+                      [P, pp, exps](Step& st, cudaStream_t s) { return launch_fwd_step(P, *pp, st, exps, s); });
 }
 
 int run_group_eager(qxg_program* P, int g, Plan* plp) {
@@ -1489,13 +1606,7 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
             add_tensor_span(P, pl, n + P->root, x.wr);
             w.push_back(std::move(x));
         }
-        for (auto& st : pl.bsteps) {
-            Work x;
-            Step* sp = &st;
-            x.launch = [&bwd_step, sp](cudaStream_t s) { return bwd_step(*sp, s); };
-            add_step_spans(P, pl, st, x);
-            w.push_back(std::move(x));
-        }
+        append_list_works(P, pl, 3, exps, w, [&bwd_step](Step& st, cudaStream_t s) { return bwd_step(st, s); });
         return launch_works(P, w);
     };
     // with use_graphs (outside profiling) the pass is captured on its second run with the same
@@ -1968,7 +2079,7 @@ std::string describe_step(const qxg_program* P, const Step& st, int group, int i
         for (size_t i = 0; i < at.size(); i++) d += (i ? "," : "") + at[i];
         if (!st.tune_note.empty()) d += " tuned=" + st.tune_note;
     } else {
-        d += contract_form(st.sargs, P->fp64, P->sm_count);
+        d += st.batch >= 0 ? "cuda-core batched small step" : contract_form(st.sargs, P->fp64, P->sm_count);
         int ncb = 0;
         while ((int64_t(1) << ncb) < st.sargs.nC) ncb++;
         d += " c_bits=" + std::to_string(ncb) + " nk=" + std::to_string(st.sargs.nk);

@@ -143,6 +143,16 @@ struct ReduceArgs {
     const PassParams* params;
 };
 
+// A small CUDA-core contraction inside a batch launched at once (contract_batch_kernel): its
+// arguments and its blocks [first_block, first_block + nblocks) of the launch.
+struct BatchStep {
+    StepArgs a;
+    int32_t first_block, nblocks;
+};
+constexpr int kBatchResults = 1024;     // results per block of a batched step
+constexpr int kBatchMaxK = 64;          // summed extent of a batched step
+constexpr int64_t kBatchMaxResults = int64_t(1) << 15;
+
 // Kernel launchers (kernels_simt.cu).  Storage: double2 when fp64 != 0, else float2.
 // scratch (may be null): device memory for the partials of steps with few results and a long
 // sum (contract_scratch_bytes); *launches receives the kernels launched (1 or 2).
@@ -151,11 +161,18 @@ cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_
 size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count);
 // Whether launch_contract runs a step in the row form (smaller operand staged in shared memory).
 bool contract_uses_rows(const StepArgs& a, bool fp64);
+// Whether launch_contract multiplies with B as the first factor of each complex product (the row
+// forms put the larger operand first).  The products of a complex multiply-add are summed in a
+// fixed order, so swapping the factors changes the rounding: kernels that must reproduce
+// launch_contract's results bit for bit follow the same order.
+bool contract_x_is_b(const StepArgs& a, bool fp64);
 // The CUDA-core form launch_contract picks for a step (for diagnostics).
 const char* contract_form(const StepArgs& a, bool fp64, int sm_count);
 // Whether a step with few results and a long sum is better served by the tiled long sum on the
 // CUDA cores (every operand element read once) than by a tensor-core GEMM.
 bool contract_prefers_cuda_cores(const StepArgs& a, bool fp64, int sm_count);
+// Run n batched steps (device array, blocks numbered consecutively, nblocks in all).
+cudaError_t launch_batch(const BatchStep* d_steps, int n, int nblocks, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_view(const ViewArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_output(const OutputArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_reduce(const ReduceArgs& a, bool fp64, const int* exps, cudaStream_t s);

@@ -63,7 +63,7 @@ class qxg_step_profile(ct.Structure):
 
 
 KERNEL_KINDS = {0: "contract_fp64", 1: "contract_fp32", 2: "contract_tc", 3: "view", 4: "output", 5: "reduce",
-                6: "tc_pack"}
+                6: "tc_pack", 7: "contract_batch"}
 
 _lib = None
 
