@@ -371,9 +371,17 @@ def run_ours(args):
     elif dom_name == "contract_tc":
         ach = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
         pk = peaks["bf16_tflops"]
+        # the split form runs three products (hi*hi, hi*lo, lo*hi) per algorithmic FLOP; TF32
+        # operands run at half the BF16 tensor rate
+        op_peak = pk / 2 if args.precision == "split_tf32" else pk
         roof = {"bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s", "frac": ach / pk,
                 "traffic": traffic, "peak_source": f"bf16_tflops of {peak_src}", "kernel": kernel_name,
-                "kernel_share": dom["ms"] / total_ms}
+                "kernel_share": dom["ms"] / total_ms,
+                "tensor_executed_tflops": 3 * ach,
+                "tensor_peak_for_operand_type": op_peak,
+                "tensor_frac": 3 * ach / op_peak,
+                "tensor_note": "executed tensor FLOPs = 3 x algorithmic (three split products); the operand "
+                               "type's peak = measured bf16 peak, halved for TF32 operands"}
     else:
         ach = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
         pk = peaks["hbm_gbs"]

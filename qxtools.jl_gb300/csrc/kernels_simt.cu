@@ -198,6 +198,7 @@ struct LSumArgs {
     int64_t ngroups;           // groups of 2^LR values of r
     int32_t LR;                // r bits per lane group (2..5)
     int32_t CA, CB;            // a / b blocks across the warps of one row range
+    int32_t nrc;               // chunks of the a values over the grid's second dimension
     int32_t G;                 // blocks per g value
     int32_t ng;                // g values
     int32_t apair, bpair;
@@ -212,7 +213,9 @@ constexpr int kLSumRowsPerLane = 512;
 constexpr int kLSumWarps = kThreads / 32;
 constexpr int kLSumAhead = 8;           // groups between a lane's L2 prefetch and its loads
 
+// a values of one chunk (lsum_na) and of the whole result (lsum_na_all)
 __host__ __device__ __forceinline__ int lsum_na(const LSumArgs& a, int NA) { return a.CA * (32 >> a.LR) * NA; }
+__host__ __device__ __forceinline__ int lsum_na_all(const LSumArgs& a, int NA) { return a.nrc * lsum_na(a, NA); }
 
 struct LSumSmem {
     int64_t *dA, *dB, *ao, *bo;
@@ -375,19 +378,20 @@ __host__ __device__ __forceinline__ void lsum_lane_block(const LSumArgs& a, int 
     *b0 = (c % a.CB) * NB;
 }
 
-// Launched with kThreads threads, grid ng x G; dynamic shared memory lsum_smem_bytes.
+// Launched with kThreads threads, grid (ng x G, nrc); dynamic shared memory lsum_smem_bytes.
 template <int NA, int NB>
 __global__ void __launch_bounds__(kThreads) contract_lsum_kernel(const LSumArgs a, double2* partial) {
     extern __shared__ __align__(16) unsigned char lsum_smem[];
-    const int Na = lsum_na(a, NA), Nb = a.CB * NB;
-    const LSumSmem t = lsum_carve(lsum_smem, Na, Nb);
-    lsum_fill(a, t, Na, Nb, threadIdx.x, kThreads);
+    const int Na = lsum_na(a, NA), NaAll = lsum_na_all(a, NA), Nb = a.CB * NB;
+    const LSumSmem t = lsum_carve(lsum_smem, NaAll, Nb);
+    lsum_fill(a, t, NaAll, Nb, threadIdx.x, kThreads);
     __syncthreads();
-    const int g = blockIdx.x / a.G, part = blockIdx.x % a.G;
+    const int g = blockIdx.x / a.G, part = blockIdx.x % a.G, chunk = blockIdx.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int CW = a.CA * a.CB, sets = kLSumWarps / CW;      // warp sets dividing the rows
     int a0, b0;
     lsum_lane_block(a, NA, NB, warp, lane, &a0, &b0);
+    a0 += chunk * Na;
     unsigned long long acc[NA][NB];
 #pragma unroll
     for (int i = 0; i < NA; i++)
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(kThreads) contract_lsum_kernel(const LSumArgs 
             }
         }
     __syncthreads();
-    // ... then the warp sets in order, one partial per result (a, b) of the g value
+    // ... then the warp sets in order, one partial per result (a, b) of the chunk
     for (int o = threadIdx.x; o < Na * Nb; o += kThreads) {
         const int av = o / Nb, bv = o % Nb;
         const int ca = av / (S * NA), sub2 = (av % (S * NA)) / NA, i = av % NA;
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(kThreads) contract_lsum_kernel(const LSumArgs 
             re += t.red[2 * (w * pw + res)];
             im += t.red[2 * (w * pw + res) + 1];
         }
-        partial[((int64_t)g * a.G + part) * (Na * Nb) + o] = make_double2(re, im);
+        partial[((int64_t)g * a.G + part) * (NaAll * Nb) + (int64_t)chunk * Na * Nb + o] = make_double2(re, im);
     }
 }
 
@@ -933,8 +937,11 @@ bool plan_lsum(const StepArgs& s0, int sm_count, LSumArgs* la, int* NA, int* NB,
     if (gb.size() > 20) return false;
     const int nbv = 1 << nb, nav = 1 << na;
     const int NBv = std::min(nbv, 4), NAv = std::min(nav, kLSumOut / NBv);
-    const int S = std::min(8, nav / NAv), CA = nav / (S * NAv), CB = nbv / NBv;
-    if (CA * CB > kLSumWarps) return false;
+    const int S = std::min(8, nav / NAv), CB = nbv / NBv;
+    if (CB > kLSumWarps) return false;
+    int CA = nav / (S * NAv), nrc = 1;                      // more lane blocks than warps: chunks
+    while (CA * CB > kLSumWarps) { CA /= 2; nrc *= 2; }
+    if (nrc > 16) return false;
     int LR = 5;
     while ((32 >> LR) < S) LR--;
     // summed bits by position in the larger operand
@@ -983,11 +990,13 @@ bool plan_lsum(const StepArgs& s0, int sm_count, LSumArgs* la, int* NA, int* NB,
     la->LR = LR;
     la->CA = CA;
     la->CB = CB;
+    la->nrc = nrc;
     la->ng = 1 << (int)gb.size();
     la->ngroups = int64_t(1) << (nk - LR);
     const int sets = kLSumWarps / (CA * CB);
     if (blocks_per_sm <= 0) blocks_per_sm = lsum_blocks_per_sm(NAv, NBv, lsum_smem_bytes(nav, nbv, S * NAv * NBv));
-    int64_t G = ((int64_t)sm_count * std::max(blocks_per_sm, 1) + la->ng - 1) / la->ng;
+    const int64_t slots = (int64_t)la->ng * nrc;
+    int64_t G = ((int64_t)sm_count * std::max(blocks_per_sm, 1) + slots - 1) / slots;
     // at most kLSumRowsPerLane groups per warp set; at least one
     G = std::max<int64_t>(G, (la->ngroups + (int64_t)sets * kLSumRowsPerLane - 1) / ((int64_t)sets * kLSumRowsPerLane));
     G = std::max<int64_t>(1, std::min<int64_t>(G, la->ngroups / sets));
@@ -1004,7 +1013,7 @@ bool use_rows2(const StepArgs& a, bool fp64, RowArgs* ra, Rows2Args* r2) {
 }
 
 size_t lsum_partial_bytes(const LSumArgs& la, int NA, int NB) {
-    return (size_t)la.ng * la.G * lsum_na(la, NA) * (la.CB * NB) * sizeof(double2);
+    return (size_t)la.ng * la.G * lsum_na_all(la, NA) * (la.CB * NB) * sizeof(double2);
 }
 
 // Splits of the split-K form: used when the results are few (<= 2^14) and each sums at least
@@ -1072,15 +1081,16 @@ size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
 bool contract_prefers_cuda_cores(const StepArgs& a, bool fp64, int sm_count) {
     LSumArgs la;
     int NA = 0, NB = 0;
-    return !fp64 && plan_lsum(a, sm_count, &la, &NA, &NB);
+    return !fp64 && plan_lsum(a, sm_count, &la, &NA, &NB) && la.nrc <= 2;
 }
 
 template <int NA, int NB>
 cudaError_t launch_lsum_ab(const LSumArgs& la, void* scratch, int* exps, cudaStream_t s) {
     double2* partial = static_cast<double2*>(scratch);
-    const int Na = lsum_na(la, NA), Nb = la.CB * NB, S = 32 >> la.LR;
+    const int Na = lsum_na_all(la, NA), Nb = la.CB * NB, S = 32 >> la.LR;
     const size_t smem = lsum_smem_bytes(Na, Nb, S * NA * NB);
-    contract_lsum_kernel<NA, NB><<<(unsigned)((int64_t)la.ng * la.G), kThreads, smem, s>>>(la, partial);
+    const dim3 grid((unsigned)((int64_t)la.ng * la.G), (unsigned)la.nrc);
+    contract_lsum_kernel<NA, NB><<<grid, kThreads, smem, s>>>(la, partial);
     const int per = Na * Nb;
     const int g = grid_for((int64_t)la.ng * per, 256, 1024);
     if (exps) lsum_reduce_kernel<true><<<g, 256, 0, s>>>(la, per, Nb, partial, exps);

@@ -273,15 +273,18 @@ def test_gate_steps_random_layouts(q, gpu_lib, precision):
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_long_sums_random_layouts(q, gpu_lib, precision):
     """Contractions with few results and a long sum (2^12..2^14 summed terms; 0..4 bits only in
-    A, 0..4 only in B, 0..2 in both and in the result) under random label orders: the tiled long
-    sum (per-block FP64 partials added in block order) against numpy."""
+    A, 0..4 only in B, 0..2 in both and in the result; four cases with 2^10-2^11 results per
+    batch value) under random label orders: the long sum (per-block FP64 partials added in block
+    order, wide results in chunks) against numpy."""
     import torch
     rng = np.random.default_rng(5)
     cdt = torch.complex128 if precision == "fp64" else torch.complex64
     letters = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
-    for case in range(16):
+    for case in range(20):
         nk, na, nb, ng = (int(rng.integers(12, 15)), int(rng.integers(0, 5)), int(rng.integers(0, 5)),
                           int(rng.integers(0, 3)))
+        if case >= 16:                      # wide results: 2^10..2^11 values per batch value
+            nk, na, nb = 12, 5 + case % 2, 5
         kl = list(range(1, nk + 1))
         al = list(range(100, 100 + na))
         bl = list(range(200, 200 + nb))
