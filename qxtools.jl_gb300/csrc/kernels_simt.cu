@@ -1176,12 +1176,6 @@ bool contract_x_is_b(const StepArgs& a, bool fp64) {
     return dst_bits(a.cA, a.kA) < dst_bits(a.cB, a.kB);      // plan_rows' choice of X
 }
 
-bool contract_uses_rows(const StepArgs& a, bool fp64) {
-    RowArgs ra;
-    Rows2Args r2;
-    return use_rows2(a, fp64, &ra, &r2) || plan_rows(a, fp64 ? 16 : 32, &ra);
-}
-
 const char* contract_form(const StepArgs& a, bool fp64, int sm_count) {
     RowArgs ra;
     Rows2Args r2;

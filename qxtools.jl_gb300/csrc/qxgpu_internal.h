@@ -159,8 +159,6 @@ constexpr int64_t kBatchMaxResults = int64_t(1) << 15;
 cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_t s, int sm_count,
                             void* scratch = nullptr, size_t scratch_bytes = 0, int* launches = nullptr);
 size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count);
-// Whether launch_contract runs a step in the row form (smaller operand staged in shared memory).
-bool contract_uses_rows(const StepArgs& a, bool fp64);
 // Whether launch_contract multiplies with B as the first factor of each complex product (the row
 // forms put the larger operand first).  The products of a complex multiply-add are summed in a
 // fixed order, so swapping the factors changes the rounding: kernels that must reproduce
