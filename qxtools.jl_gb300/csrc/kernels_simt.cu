@@ -1,10 +1,12 @@
-// CUDA-core kernels of the executor: the general pairwise contraction (one `ncon` command,
-// docs/src/users_guide.md:124-146), view materialisation for a batch of slices
-// (users_guide.md:104-122), output vectors for a batch of bitstrings (users_guide.md:149-158)
-// and the FP64 sum over slices (users_guide.md:11-17).
+// CUDA-core kernels of the executor: the pairwise contraction (one `ncon` command,
+// docs/src/users_guide.md:124-146) in its general, row (FP64), long-sum, split-K and batched
+// forms, view materialisation for a batch of slices (users_guide.md:104-122), output vectors for
+// a batch of bitstrings (users_guide.md:149-158), the FP64 sum over slices (users_guide.md:11-17)
+// and the gradient's seed, view-adjoint and leaf-gradient kernels.  The compact row form of the
+// Complex64 gate steps is in kernels_rows.cu; launch_contract picks the form of a step.
 //
-// The contraction kernel is the plain executor's hot loop (ComplexF64 on the FP64 pipe) and
-// the small-K path of the Complex64 executors (FP32 FMA).  A block owns tiles of 2^TB
+// The general kernel is the plain executor's hot loop (ComplexF64 on the FP64 pipe) and the
+// fallback of the Complex64 executors (FP32 FMA).  A block owns tiles of 2^TB
 // consecutive result elements; because a bit permutation is additive over disjoint bits,
 // offset(tile | lo) = offset(tile) + offset(lo), so the low-bit offsets of the result and all
 // K offsets (up to 2^kKTableBits) are tabulated once per block in shared memory and each
