@@ -75,8 +75,10 @@ struct Tensor {
     int slot = -1;                      // exponent slot
 };
 
-// Tensors of at most this many bytes get arena space of their own (no reuse within a pass).
+// Tensors of at most this many bytes get arena space of their own (no reuse within a pass), up
+// to kSmallTensorBudget bytes in all; later small tensors share space like the large ones.
 constexpr int64_t kSmallTensorBytes = int64_t(256) << 10;
+constexpr int64_t kSmallTensorBudget = int64_t(1) << 30;
 
 // Backward (adjoint) step kinds of gradient plans.
 constexpr int kBwdNcon = 1, kBwdView = 2, kBwdLeaf = 3;
@@ -817,14 +819,19 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
     for (auto& st : plan->bsteps) { use(st.reads[0], pos); use(st.reads[1], pos); pos++; }
     if (!grad && pos_of[P->root] >= 0) last[P->root] = end_pos;
     std::vector<Item> items;
+    int64_t small_total = 0;
     for (int t = 0; t < ntab; t++) {
         if (pos_of[t] < 0) continue;
         const int64_t bytes = ((int64_t(1) << T[t].layout.size()) * (int64_t)P->esize + 255) & ~int64_t(255);
         // small tensors keep their own bytes for the whole pass: reusing them would order
         // independent sub-trees one after another (a write after another branch's read) and keep
         // their small steps out of each other's batches and graph branches
-        if (bytes <= kSmallTensorBytes) items.push_back({t, 0, end_pos, bytes});
-        else items.push_back({t, pos_of[t], std::max(last[t], pos_of[t]), bytes});
+        if (bytes <= kSmallTensorBytes && small_total + bytes <= kSmallTensorBudget) {
+            small_total += bytes;
+            items.push_back({t, 0, end_pos, bytes});
+        } else {
+            items.push_back({t, pos_of[t], std::max(last[t], pos_of[t]), bytes});
+        }
     }
     std::vector<int> order(items.size());
     for (size_t i = 0; i < items.size(); i++) order[i] = (int)i;
