@@ -1,0 +1,46 @@
+"""bench.py's reference arm on the host cores: the JSON line it prints and its rank behaviour.
+
+The reference arm times the FP64 CPU restatement of the reference's contraction path (the oracle)
+on a bounded sample of the default workload; it needs no GPU, so its output contract is checked
+here: one JSON line with the metric, value, unit, the cpu_baseline description and an e2e block
+without host-device traffic.  Under several ranks only rank 0 works and prints.
+"""
+import json
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _run(extra_env=None):
+    env = dict(os.environ)
+    env.update(extra_env or {})
+    return subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
+                           "--warmup", "0", "--cpu-seconds", "2"], capture_output=True, text=True, env=env,
+                          cwd=ROOT, timeout=600)
+
+
+def test_reference_arm_prints_the_contract_line():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    r = _run()
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["steps"] == 1 and d["warmup"] == 0
+    assert d["config"]["workload"] == "rqc_5x5_d12_open6"
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    r = _run({"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"})
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert not [x for x in r.stdout.splitlines() if x.startswith("{")]
