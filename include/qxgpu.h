@@ -35,7 +35,7 @@ typedef enum qxg_status {
     QXG_ERR_INVALID = -1,      /* malformed programme, bad label, dimension mismatch, bad argument */
     QXG_ERR_CUDA = -2,         /* a CUDA runtime or driver call failed */
     QXG_ERR_OOM = -3,          /* the workspace does not fit in device memory or the set limit */
-    QXG_ERR_UNSUPPORTED = -4,  /* valid input outside what this build supports */
+    QXG_ERR_UNSUPPORTED = -4,  /* valid input outside what the library supports */
     QXG_ERR_TIMEOUT = -5,      /* a bounded device-side wait gave up */
     QXG_ERR_STATE = -6         /* call made in the wrong order (e.g. data not set) */
 } qxg_status;
