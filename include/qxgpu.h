@@ -260,6 +260,30 @@ int qxg_ncon_tc_static(int32_t precision,
                        const void* B, int32_t nb, const int32_t* b_labels, const int64_t* b_dims,
                        void* stream);
 
+/* Sizes of the arrays qxg_parse_qx fills (capacities on input when it fills them). */
+typedef struct qxg_qx_sizes {
+    int32_t ninstr;       /* commands */
+    int32_t ndata;        /* distinct data keys */
+    int64_t nlabels;      /* ncon labels, concatenated */
+    int64_t ndims;        /* data dimensions, concatenated over the data keys */
+    int64_t key_bytes;    /* bytes of the data keys, each NUL-terminated, one after another */
+    int32_t nqubits;      /* largest output qubit: the bitstring length */
+    int32_t reserved[3];
+} qxg_qx_sizes;
+
+/* Parse `.qx` DSL text (docs/src/users_guide.md:93-165, the file generate_simulation_files
+ * writes, src/simulation.jl:52-77) into qxg_program_create's arguments: one qxg_instr per
+ * command, the concatenated ncon labels, and per data key (numbered in order of first `load`)
+ * its rank and dims and its name (the `data_N` key of the leaf data file).  Replaces the parse
+ * QXContexts performs in `execute` (bin/qxrun.jl:83-87).  Host code only, no device.
+ * With instrs, labels, data_rank, data_dims and data_keys all NULL it only sets *sizes; else
+ * *sizes holds the capacities of those arrays on input (too small: QXG_ERR_INVALID) and the sizes
+ * used on output.  A malformed line, an unknown command, a tensor defined twice or used before
+ * its definition, or a data key loaded with two shapes gives QXG_ERR_INVALID with the line
+ * number in qxg_last_error. */
+int qxg_parse_qx(const char* text, qxg_qx_sizes* sizes, qxg_instr* instrs, int32_t* labels,
+                 int32_t* data_rank, int64_t* data_dims, char* data_keys);
+
 /* Thread-local description of the last error ("" when none). */
 const char* qxg_last_error(void);
 

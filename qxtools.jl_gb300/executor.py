@@ -46,6 +46,11 @@ class qxg_options(ct.Structure):
                 ("tc_plane_budget_mb", ct.c_int32), ("reserved", ct.c_int32 * 5)]
 
 
+class qxg_qx_sizes(ct.Structure):
+    _fields_ = [("ninstr", ct.c_int32), ("ndata", ct.c_int32), ("nlabels", ct.c_int64), ("ndims", ct.c_int64),
+                ("key_bytes", ct.c_int64), ("nqubits", ct.c_int32), ("reserved", ct.c_int32 * 3)]
+
+
 class qxg_program_info(ct.Structure):
     _fields_ = [("num_slices", ct.c_int64), ("output_size", ct.c_int64), ("num_qubits", ct.c_int32),
                 ("num_steps", ct.c_int32), ("bitstring_batch", ct.c_int32), ("slice_batch", ct.c_int32),
@@ -87,6 +92,8 @@ def load_library(path=None):
                                        ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), ct.c_int32, ct.c_int32,
                                        ct.POINTER(qxg_options), ct.POINTER(P)]
     lib.qxg_program_set_data.argtypes = [P, ct.c_int32, ct.POINTER(ct.c_double), ct.c_int64]
+    lib.qxg_parse_qx.argtypes = [ct.c_char_p, ct.POINTER(qxg_qx_sizes), ct.POINTER(qxg_instr),
+                                 ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), ct.c_char_p]
     lib.qxg_amplitudes.argtypes = [P, ct.c_char_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_double)]
     lib.qxg_amplitudes_device.argtypes = [P, P, ct.c_int32, ct.c_int64, ct.c_int64, P]
     lib.qxg_program_synchronize.argtypes = [P]
@@ -208,6 +215,34 @@ class Programme:
         instrs = np.array(rows, dtype=np.int32).reshape(-1, 10)
         return cls(instrs, np.array(labels, dtype=np.int32), dkeys,
                    [np.asarray(data[k], dtype=np.complex128) for k in dkeys], nqubits, ids)
+
+    @classmethod
+    def from_qx_text(cls, text: str, data: "OrderedDict[str, np.ndarray]", lib=None) -> "Programme":
+        """A programme from `.qx` text through the library's own parser (qxg_parse_qx), with the
+        leaf data given by key; the data ids follow the keys' order of first `load`."""
+        lib = lib or load_library()
+        raw = text.encode()
+        sz = qxg_qx_sizes()
+        _check(lib, lib.qxg_parse_qx(raw, ct.byref(sz), None, None, None, None, None))
+        ins = (qxg_instr * max(sz.ninstr, 1))()
+        lab = (ct.c_int32 * max(sz.nlabels, 1))()
+        rank = (ct.c_int32 * max(sz.ndata, 1))()
+        dims = (ct.c_int64 * max(sz.ndims, 1))()
+        keys = ct.create_string_buffer(max(sz.key_bytes, 1))
+        _check(lib, lib.qxg_parse_qx(raw, ct.byref(sz), ins, lab, rank, dims, keys))
+        names = keys.raw[:sz.key_bytes].split(b"\0")[:sz.ndata]
+        dkeys = [n.decode() for n in names]
+        instrs = np.frombuffer(bytes(ins), dtype=np.int32)[:10 * sz.ninstr].reshape(-1, 10).copy()
+        off, leaves = 0, []
+        for i, k in enumerate(dkeys):
+            shape = tuple(int(x) for x in dims[off:off + rank[i]])
+            off += rank[i]
+            if k not in data:
+                raise ValueError(f"no data {k}")
+            if tuple(np.shape(data[k])) != shape:
+                raise ValueError(f"data {k}: shape {np.shape(data[k])}, the .qx loads {shape}")
+            leaves.append(np.asarray(data[k], dtype=np.complex128))
+        return cls(instrs, np.array(lab[:sz.nlabels], dtype=np.int32), dkeys, leaves, sz.nqubits, {})
 
     @classmethod
     def from_graph(cls, graph: ComputeGraph) -> "Programme":
