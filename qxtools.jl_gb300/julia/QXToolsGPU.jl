@@ -11,11 +11,10 @@ or passed in as a Dict{String,Array{ComplexF64}} (e.g. loaded from the reference
 """
 module QXToolsGPU
 
-export QxgProgram, load_qx, amplitudes, single_amplitude
+export QxgProgram, parse_qx, load_qx, amplitudes, single_amplitude
 
 const libqxgpu = joinpath(@__DIR__, "..", "_build", "libqxgpu.so")
 
-const OP_LOAD, OP_VIEW, OP_OUTPUT, OP_NCON, OP_SAVE = Int32(1), Int32(2), Int32(3), Int32(4), Int32(5)
 const PREC = Dict(:fp64 => Int32(0), :split_bf16 => Int32(1), :split_tf32 => Int32(2), :fp32 => Int32(3))
 
 struct QxgInstr            # qxg_instr
@@ -41,43 +40,45 @@ end
 last_error() = unsafe_string(ccall((:qxg_last_error, libqxgpu), Cstring, ()))
 check(rc) = rc == 0 || error("libqxgpu status $rc: $(last_error())")
 
-labels(s) = s == "0" ? Int32[] : parse.(Int32, split(s, ","))
+struct QxgQxSizes          # qxg_qx_sizes
+    ninstr::Int32; ndata::Int32; nlabels::Int64; ndims::Int64; key_bytes::Int64
+    nqubits::Int32; reserved::NTuple{3,Int32}
+end
+
+"""
+    parse_qx(text) -> (instrs, labels, keys, rank, dims, nqubits)
+
+The library's parse of `.qx` text (`qxg_parse_qx`): one `QxgInstr` per command, the concatenated
+ncon labels, and per data key (in order of first `load`) its name, rank and dims.
+"""
+function parse_qx(text::AbstractString)
+    sig = (Cstring, Ref{QxgQxSizes}, Ptr{QxgInstr}, Ptr{Int32}, Ptr{Int32}, Ptr{Int64}, Ptr{UInt8})
+    sz = Ref(QxgQxSizes(0, 0, 0, 0, 0, 0, (0, 0, 0)))
+    check(ccall((:qxg_parse_qx, libqxgpu), Cint, sig, text, sz, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL))
+    s = sz[]
+    instrs = Vector{QxgInstr}(undef, s.ninstr); labs = Vector{Int32}(undef, s.nlabels)
+    rank = Vector{Int32}(undef, s.ndata); dims = Vector{Int64}(undef, s.ndims)
+    kbuf = Vector{UInt8}(undef, s.key_bytes)
+    check(ccall((:qxg_parse_qx, libqxgpu), Cint, sig, text, sz, instrs, labs, rank, dims, kbuf))
+    keys = s.ndata == 0 ? String[] : String.(split(String(kbuf[1:end-1]), '\0'))
+    instrs, labs, keys, rank, dims, Int(s.nqubits)
+end
 
 """
     load_qx(qx_file, data::Dict{String,<:AbstractArray}; precision=:fp64, device=0)
 
-Compile a `.qx` programme (docs/src/users_guide.md:93-165) into a GPU programme.
+Compile a `.qx` programme (docs/src/users_guide.md:93-165) into a GPU programme: the library
+parses the text (`qxg_parse_qx`), `data` supplies each key's leaf tensor, whose length must match
+the dims of its `load` line.
 """
 function load_qx(qx_file::String, data::AbstractDict; precision::Symbol=:fp64, device::Int=0)
-    ids = Dict{String,Int32}(); dkeys = String[]; instrs = QxgInstr[]; labs = Int32[]; nq = 0
-    tid(s) = get!(ids, s, Int32(length(ids)))
-    did(s) = (i = findfirst(==(s), dkeys); i === nothing ? (push!(dkeys, s); Int32(length(dkeys) - 1)) : Int32(i - 1))
-    for line in eachline(qx_file)
-        (isempty(strip(line)) || startswith(line, "#")) && continue
-        t = split(line)
-        if t[1] == "load"
-            push!(instrs, QxgInstr(OP_LOAD, tid(t[2]), did(t[3]), 0, 0, 0, 0, 0, 0, 0))
-        elseif t[1] == "view"
-            src = ids[t[3]]
-            push!(instrs, QxgInstr(OP_VIEW, tid(t[2]), src, parse(Int32, t[4][2:end]) - 1,
-                                   parse(Int32, t[5]) - 1, parse(Int32, t[6]), 0, 0, 0, 0))
-        elseif t[1] == "output"
-            q = parse(Int32, t[3]); nq = max(nq, q)
-            push!(instrs, QxgInstr(OP_OUTPUT, tid(t[2]), q - 1, parse(Int32, t[4]), 0, 0, 0, 0, 0, 0))
-        elseif t[1] == "ncon"
-            lc, la, lb = labels(t[3]), labels(t[5]), labels(t[7])
-            a, b = ids[t[4]], ids[t[6]]
-            off = Int32(length(labs)); append!(labs, lc, la, lb)
-            push!(instrs, QxgInstr(OP_NCON, tid(t[2]), a, b, 0, 0, length(lc), length(la), length(lb), off))
-        elseif t[1] == "save"
-            push!(instrs, QxgInstr(OP_SAVE, 0, ids[t[3]], 0, 0, 0, 0, 0, 0, 0))
-        else
-            error("unknown .qx instruction $(t[1])")
-        end
+    instrs, labs, dkeys, rank, dims, nq = parse_qx(read(qx_file, String))
+    arrays = [ComplexF64.(vec(data[k])) for k in dkeys]
+    off = 0
+    for (i, x) in enumerate(arrays)
+        n = prod(dims[off+1:off+rank[i]]; init=1); off += rank[i]
+        length(x) == n || error("data key $(dkeys[i]) has $(length(x)) elements, its load line wants $n")
     end
-    arrays = [ComplexF64.(data[k]) for k in dkeys]
-    rank = Int32[ndims(x) for x in arrays]
-    dims = Int64[d for x in arrays for d in size(x)]
     opts = Ref(QxgOptions(PREC[precision], device, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 5)))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:qxg_program_create, libqxgpu), Cint,
