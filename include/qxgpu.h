@@ -284,6 +284,39 @@ typedef struct qxg_qx_sizes {
 int qxg_parse_qx(const char* text, qxg_qx_sizes* sizes, qxg_instr* instrs, int32_t* labels,
                  int32_t* data_rank, int64_t* data_dims, char* data_keys);
 
+/* Output methods of a `.yml` parameter file (output_params_dict, src/outputs.jl:47-78). */
+typedef enum qxg_output_method {
+    QXG_OUTPUT_LIST = 0,       /* params.bitstrings, explicit */
+    QXG_OUTPUT_UNIFORM = 1,    /* params.num_samples bitstrings drawn uniformly from params.seed */
+    QXG_OUTPUT_REJECTION = 2   /* rejection sampling with params.M, params.fix_M, params.seed */
+} qxg_output_method;
+
+/* The `output:` block of a `.yml` parameter file. */
+typedef struct qxg_yml_output {
+    int32_t method;        /* qxg_output_method */
+    int32_t num_qubits;    /* List: length of its bitstrings; Uniform, Rejection: params.num_qubits */
+    int64_t num_samples;   /* params.num_samples (List without it: the number of bitstrings) */
+    int64_t nbitstrings;   /* List: bitstrings listed; 0 for the other methods */
+    int64_t seed;          /* params.seed when has_seed */
+    double M;              /* Rejection: params.M (1e-4 when absent) */
+    int32_t has_seed;      /* 0 when the seed is absent or ~ */
+    int32_t fix_M;         /* Rejection: params.fix_M (0 when absent) */
+    int32_t reserved[4];
+} qxg_yml_output;
+
+/* Read the `output:` block of the `.yml` parameter file that generate_parameter_file writes
+ * (src/simulation.jl:149-155; layout docs/src/users_guide.md:22-35), the List bitstrings that
+ * QXContexts' `execute` reads in bin/qxrun.jl:83-87.  The YAML read is the subset those writers
+ * produce: block mappings, block (`- x`) or flow (`[x, y]`) sequences of scalars, plain or quoted
+ * scalars, `~`, `#` comment lines.  Fills *out; for a List with `bitstrings` non-NULL it also
+ * writes the bitstrings packed, nbitstrings x num_qubits characters with no separators (the
+ * layout qxg_amplitudes takes); capacity is that buffer's size in bytes.  Bitstring characters
+ * are `0 1 + -`, all of one length, taken as written (a plain `010` stays "010").  Host code
+ * only, no device.  A missing `output:` block, method or params, an unknown method, a malformed
+ * line, or a bitstring of another length or character gives QXG_ERR_INVALID with the line
+ * number in qxg_last_error. */
+int qxg_parse_yml_output(const char* text, qxg_yml_output* out, char* bitstrings, int64_t capacity);
+
 /* Thread-local description of the last error ("" when none). */
 const char* qxg_last_error(void);
 

@@ -17,7 +17,7 @@ import numpy as np
 from .compute_graph import ComputeGraph, Load, Ncon, Output, Save, View
 
 __all__ = ["QXG_OP", "PRECISION", "QXGError", "Programme", "Executor", "load_library",
-           "library_path", "ncon_device"]
+           "library_path", "ncon_device", "parse_yml_output"]
 
 _HERE = Path(__file__).resolve().parent
 _LIB_PATH = _HERE / "_build" / "libqxgpu.so"
@@ -49,6 +49,15 @@ class qxg_options(ct.Structure):
 class qxg_qx_sizes(ct.Structure):
     _fields_ = [("ninstr", ct.c_int32), ("ndata", ct.c_int32), ("nlabels", ct.c_int64), ("ndims", ct.c_int64),
                 ("key_bytes", ct.c_int64), ("nqubits", ct.c_int32), ("reserved", ct.c_int32 * 3)]
+
+
+class qxg_yml_output(ct.Structure):
+    _fields_ = [("method", ct.c_int32), ("num_qubits", ct.c_int32), ("num_samples", ct.c_int64),
+                ("nbitstrings", ct.c_int64), ("seed", ct.c_int64), ("M", ct.c_double), ("has_seed", ct.c_int32),
+                ("fix_M", ct.c_int32), ("reserved", ct.c_int32 * 4)]
+
+
+OUTPUT_METHODS = ("List", "Uniform", "Rejection")   # qxg_output_method
 
 
 class qxg_program_info(ct.Structure):
@@ -94,6 +103,7 @@ def load_library(path=None):
     lib.qxg_program_set_data.argtypes = [P, ct.c_int32, ct.POINTER(ct.c_double), ct.c_int64]
     lib.qxg_parse_qx.argtypes = [ct.c_char_p, ct.POINTER(qxg_qx_sizes), ct.POINTER(qxg_instr),
                                  ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), ct.c_char_p]
+    lib.qxg_parse_yml_output.argtypes = [ct.c_char_p, ct.POINTER(qxg_yml_output), ct.c_char_p, ct.c_int64]
     lib.qxg_amplitudes.argtypes = [P, ct.c_char_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_double)]
     lib.qxg_amplitudes_device.argtypes = [P, P, ct.c_int32, ct.c_int64, ct.c_int64, P]
     lib.qxg_program_synchronize.argtypes = [P]
@@ -250,6 +260,37 @@ class Programme:
         programme without outputs (open wires only) takes empty bitstrings."""
         nq = max([c.qubit for c in graph.commands if isinstance(c, Output)], default=0)
         return cls.from_commands(graph.commands, graph.data, nq)
+
+
+def parse_yml_output(text: str, lib=None) -> "OrderedDict":
+    """The `output:` block of `.yml` text through the library's reader (qxg_parse_yml_output),
+    as the dict output_params_dict builds (src/outputs.jl:47-78): {"method", "params"} with the
+    params each method writes."""
+    lib = lib or load_library()
+    raw = text.encode()
+    o = qxg_yml_output()
+    _check(lib, lib.qxg_parse_yml_output(raw, ct.byref(o), None, 0))
+    params = OrderedDict()
+    method = OUTPUT_METHODS[o.method]
+    seed = int(o.seed) if o.has_seed else None
+    if method == "List":
+        n = o.nbitstrings * o.num_qubits
+        buf = ct.create_string_buffer(max(n, 1))
+        _check(lib, lib.qxg_parse_yml_output(raw, ct.byref(o), buf, n))
+        packed = buf.raw[:n].decode()
+        params["num_samples"] = int(o.num_samples)
+        params["bitstrings"] = [packed[i * o.num_qubits:(i + 1) * o.num_qubits] for i in range(o.nbitstrings)]
+    elif method == "Uniform":
+        params["num_qubits"] = int(o.num_qubits)
+        params["num_samples"] = int(o.num_samples)
+        params["seed"] = seed
+    else:
+        params["num_qubits"] = int(o.num_qubits)
+        params["M"] = float(o.M)
+        params["fix_M"] = bool(o.fix_M)
+        params["seed"] = seed
+        params["num_samples"] = int(o.num_samples)
+    return OrderedDict([("method", method), ("params", params)])
 
 
 def _bitstring_bytes(bitstrings, nqubits: int) -> bytes:

@@ -11,7 +11,7 @@ or passed in as a Dict{String,Array{ComplexF64}} (e.g. loaded from the reference
 """
 module QXToolsGPU
 
-export QxgProgram, parse_qx, load_qx, amplitudes, single_amplitude
+export QxgProgram, parse_qx, load_qx, read_bitstrings, qxrun, amplitudes, single_amplitude
 
 const libqxgpu = joinpath(@__DIR__, "..", "_build", "libqxgpu.so")
 
@@ -111,6 +111,45 @@ function amplitudes(p::QxgProgram, bitstrings::AbstractVector{<:AbstractString};
     check(ccall((:qxg_amplitudes, libqxgpu), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Int32, Int64, Int64, Ptr{ComplexF64}),
                 p.handle, buf, length(bitstrings), first(slices), last(slices) + 1, out))
     out
+end
+
+struct QxgYmlOutput        # qxg_yml_output
+    method::Int32; num_qubits::Int32; num_samples::Int64; nbitstrings::Int64; seed::Int64
+    M::Float64; has_seed::Int32; fix_M::Int32; reserved::NTuple{4,Int32}
+end
+
+"""
+    read_bitstrings(yml_file) -> Vector{String}
+
+The `List` bitstrings of a `.yml` parameter file (docs/src/users_guide.md:22-35) through the
+library's reader (`qxg_parse_yml_output`).  Other output methods draw their bitstrings on the
+host (QXTools' samplers), so they are an error here.
+"""
+function read_bitstrings(yml_file::String)
+    text = read(yml_file, String)
+    sig = (Cstring, Ref{QxgYmlOutput}, Ptr{UInt8}, Int64)
+    o = Ref(QxgYmlOutput(0, 0, 0, 0, 0, 0.0, 0, 0, (0, 0, 0, 0)))
+    check(ccall((:qxg_parse_yml_output, libqxgpu), Cint, sig, text, o, C_NULL, 0))
+    o[].method == 0 || error("$yml_file: the output method is not List")
+    n, q = Int(o[].nbitstrings), Int(o[].num_qubits)
+    buf = Vector{UInt8}(undef, n * q)
+    check(ccall((:qxg_parse_yml_output, libqxgpu), Cint, sig, text, o, buf, length(buf)))
+    [String(buf[i*q+1:(i+1)*q]) for i in 0:n-1]
+end
+
+"""
+    qxrun(qx_file, data, yml_file; max_slices=nothing, precision=:fp64) -> Dict{String,ComplexF64}
+
+The `.qx` + leaf data + `.yml` run of qxrun (bin/qxrun.jl:83-87) on the GPU: one amplitude per
+List bitstring, summed over the first `max_slices` slices (all when `nothing`).
+"""
+function qxrun(qx_file::String, data::AbstractDict, yml_file::String;
+               max_slices::Union{Int,Nothing}=nothing, precision::Symbol=:fp64)
+    p = load_qx(qx_file, data; precision=precision)
+    bits = read_bitstrings(yml_file)
+    ns = max_slices === nothing ? p.num_slices : min(max_slices, p.num_slices)
+    amps = amplitudes(p, bits; slices=0:ns-1)
+    Dict(b => amps[1, i] for (i, b) in enumerate(bits))
 end
 
 """
