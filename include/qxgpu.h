@@ -317,6 +317,51 @@ typedef struct qxg_yml_output {
  * number in qxg_last_error. */
 int qxg_parse_yml_output(const char* text, qxg_yml_output* out, char* bitstrings, int64_t capacity);
 
+/* Options of qxg_plan_contraction (zero-initialised: the defaults). */
+typedef struct qxg_plan_options {
+    int32_t trials;          /* recursive-bisection trees tried (0: 64) */
+    int32_t greedy_trials;   /* random-greedy trees tried besides them (0: 16; negative: none) */
+    int64_t seed;            /* the search is deterministic for a seed */
+    double max_log2;         /* slice labels until every intermediate has <= 2^max_log2 elements
+                                (<= 0: no width target) */
+    int32_t num_sliced;      /* slice at least this many labels (number_bonds_to_slice; 0: none) */
+    int32_t max_sliced;      /* slice at most this many labels (0: no limit) */
+    double flops_per_s;      /* step model: max(FLOPs / flops_per_s, bytes / bytes_per_s); 0: 1e14 */
+    double bytes_per_s;      /* 0: 5e12 (Complex64 bytes of A, B and C) */
+    const uint8_t* tensor_batched;  /* ntensors flags (NULL: none): the tensors that change with the
+                                       bitstring (the `output` tensors); every step that depends on
+                                       one runs once per bitstring of a batch */
+    double batch_log2;       /* log2 of the bitstrings run together, for the step model */
+    int32_t reserved[6];
+} qxg_plan_options;
+
+typedef struct qxg_plan_stats {
+    double log2_flops;        /* FLOPs of one slice (8 |A u B| per step, complex), log2 */
+    double log2_flops_total;  /* FLOPs of all slices, log2 */
+    double max_log2;          /* elements of the largest intermediate of one slice, log2 */
+    double time;              /* modelled seconds of one slice */
+    double log2_slices;       /* number of slices, log2 */
+    int32_t num_sliced;       /* labels sliced */
+    int32_t trees_tried;
+    int32_t reserved[6];
+} qxg_plan_stats;
+
+/* Contraction tree and sliced labels for a tensor network given as a hypergraph: tensor v holds
+ * labels[label_off[v] .. label_off[v+1]) (ids 0..nlabels-1), label l has dimension
+ * 2^label_log2dim[l] and is kept to the end when label_open[l] (NULL: none open).  A label is
+ * summed by the contraction that encloses all its holders (QXTns contraction_indices, called at
+ * src/compute_graph/compute_graph.jl:65).  Writes ntensors-1 steps to pairs: step k contracts
+ * nodes pairs[2k] and pairs[2k+1] into node ntensors+k (nodes 0..ntensors-1 are the tensors); the
+ * steps in order are an `(A, B, C)` plan (src/contraction_planning.jl:386-448).  label_sliced
+ * (optional, nlabels bytes) marks the labels to slice (contraction_scheme's bond groups,
+ * :219-299).  Replaces FlowCutter (flow_cutter_contraction_plan, :90-113), which QXTools calls
+ * but does not ship, by recursive hypergraph bisection and randomised greedy trees scored by the
+ * executor's step model, then greedy slicing.  Host code only, no device. */
+int qxg_plan_contraction(int32_t ntensors, const int64_t* label_off, const int32_t* labels, int32_t nlabels,
+                         const int32_t* label_log2dim, const uint8_t* label_open,
+                         const qxg_plan_options* opts, int32_t* pairs, uint8_t* label_sliced,
+                         qxg_plan_stats* stats);
+
 /* Thread-local description of the last error ("" when none). */
 const char* qxg_last_error(void);
 

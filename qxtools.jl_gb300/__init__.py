@@ -16,7 +16,8 @@ from .executor import Executor, Programme, QXGError, load_library, ncon_device
 from .planning import (HyperNet, contraction_indices, contraction_scheme, convert_to_graph,
                        convert_to_line_graph, flow_cutter_contraction_plan,
                        greedy_contraction_plan, hyper_network, min_fill,
-                       min_fill_contraction_plan, netcon, order_to_contraction_plan, plan_cost)
+                       min_fill_contraction_plan, native_contraction_scheme, native_plan, netcon,
+                       order_to_contraction_plan, plan_cost)
 from .simulation import (amplitudes_all, amplitudes_uniform, compile_programme, execute,
                          generate_parameter_file, generate_simulation_files, output_params_dict,
                          run_simulation, single_amplitude)

@@ -60,6 +60,19 @@ class qxg_yml_output(ct.Structure):
 OUTPUT_METHODS = ("List", "Uniform", "Rejection")   # qxg_output_method
 
 
+class qxg_plan_options(ct.Structure):
+    _fields_ = [("trials", ct.c_int32), ("greedy_trials", ct.c_int32), ("seed", ct.c_int64), ("max_log2", ct.c_double),
+                ("num_sliced", ct.c_int32), ("max_sliced", ct.c_int32), ("flops_per_s", ct.c_double),
+                ("bytes_per_s", ct.c_double), ("tensor_batched", ct.POINTER(ct.c_uint8)), ("batch_log2", ct.c_double),
+                ("reserved", ct.c_int32 * 6)]
+
+
+class qxg_plan_stats(ct.Structure):
+    _fields_ = [("log2_flops", ct.c_double), ("log2_flops_total", ct.c_double), ("max_log2", ct.c_double),
+                ("time", ct.c_double), ("log2_slices", ct.c_double), ("num_sliced", ct.c_int32),
+                ("trees_tried", ct.c_int32), ("reserved", ct.c_int32 * 6)]
+
+
 class qxg_program_info(ct.Structure):
     _fields_ = [("num_slices", ct.c_int64), ("output_size", ct.c_int64), ("num_qubits", ct.c_int32),
                 ("num_steps", ct.c_int32), ("bitstring_batch", ct.c_int32), ("slice_batch", ct.c_int32),
@@ -104,6 +117,9 @@ def load_library(path=None):
     lib.qxg_parse_qx.argtypes = [ct.c_char_p, ct.POINTER(qxg_qx_sizes), ct.POINTER(qxg_instr),
                                  ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int64), ct.c_char_p]
     lib.qxg_parse_yml_output.argtypes = [ct.c_char_p, ct.POINTER(qxg_yml_output), ct.c_char_p, ct.c_int64]
+    lib.qxg_plan_contraction.argtypes = [ct.c_int32, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int32), ct.c_int32,
+                                         ct.POINTER(ct.c_int32), ct.POINTER(ct.c_uint8), ct.POINTER(qxg_plan_options),
+                                         ct.POINTER(ct.c_int32), ct.POINTER(ct.c_uint8), ct.POINTER(qxg_plan_stats)]
     lib.qxg_amplitudes.argtypes = [P, ct.c_char_p, ct.c_int32, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_double)]
     lib.qxg_amplitudes_device.argtypes = [P, P, ct.c_int32, ct.c_int64, ct.c_int64, P]
     lib.qxg_program_synchronize.argtypes = [P]

@@ -38,6 +38,7 @@ __all__ = [
     "convert_to_graph", "convert_to_line_graph", "min_fill",
     "order_to_contraction_plan", "netcon", "greedy_contraction_plan",
     "flow_cutter_contraction_plan", "min_fill_contraction_plan", "contraction_scheme",
+    "native_plan", "native_contraction_scheme",
 ]
 
 
@@ -663,5 +664,86 @@ def contraction_scheme(tnc, num: int, time: int = 120, seed: int = -1,
         ("Method used", "greedy deletion of the largest intermediate's bonds"),
         ("Edges sliced", len(sliced)), ("Score function used", score_function),
         ("Log2 largest intermediate after slicing consecutive edges", widths),
+    ])
+    return groups, plan, metadata
+
+
+# ---------------------------------------------------------------------------------------
+# the library's planner (qxg_plan_contraction)
+# ---------------------------------------------------------------------------------------
+def native_plan(net: HyperNet, trials: int = 64, greedy_trials: int = 16, seed: int = 0,
+                max_log2: float | None = None, num_sliced: int = 0, max_sliced: int = 0, batched=(),
+                beta: int = 1, lib=None):
+    """Plan (and labels to slice) from the library's planner: recursive hypergraph bisection and
+    random-greedy trees scored by the executor's step model, then greedy slicing until every
+    intermediate has at most 2^max_log2 elements (or `num_sliced` labels are sliced).  Steps that
+    depend on a `batched` tensor (the outputs) run `beta` times in the step model.
+    -> (plan, sliced labels, stats dict).  Intermediates are named `I<k>`."""
+    import ctypes as ct
+    from .executor import _check, load_library, qxg_plan_options, qxg_plan_stats
+    lib = lib or load_library()
+    names = list(net.tensors)
+    labs = sorted({l for ls in net.tensors.values() for l in ls}, key=lambda x: (str(type(x)), str(x)))
+    lid = {l: i for i, l in enumerate(labs)}
+    off, flat = [0], []
+    for n in names:
+        flat += [lid[l] for l in dict.fromkeys(net.tensors[n])]
+        off.append(len(flat))
+    log2dim = [max(0, int(math.ceil(math.log2(net.dims[l])))) for l in labs]
+    opens = [1 if l in net.open else 0 for l in labs]
+    V = len(names)
+    a_off = (ct.c_int64 * (V + 1))(*off)
+    a_lab = (ct.c_int32 * max(1, len(flat)))(*flat)
+    a_w = (ct.c_int32 * max(1, len(labs)))(*log2dim)
+    a_open = (ct.c_uint8 * max(1, len(labs)))(*opens)
+    o = qxg_plan_options(trials=trials, greedy_trials=greedy_trials if greedy_trials else -1, seed=seed,
+                         max_log2=float(max_log2 or 0.0), num_sliced=num_sliced, max_sliced=max_sliced)
+    bset = set(batched)
+    a_batched = (ct.c_uint8 * V)(*[1 if nm in bset else 0 for nm in names])
+    if bset and beta > 1:
+        o.tensor_batched = a_batched
+        o.batch_log2 = math.log2(beta)
+    pairs = (ct.c_int32 * max(1, 2 * (V - 1)))()
+    sl = (ct.c_uint8 * max(1, len(labs)))()
+    st = qxg_plan_stats()
+    _check(lib, lib.qxg_plan_contraction(V, a_off, a_lab, len(labs), a_w, a_open, ct.byref(o), pairs, sl,
+                                         ct.byref(st)))
+    node = list(names)
+    taken = set(names)
+    plan, k = [], 0
+    for s in range(V - 1):
+        k += 1
+        while f"I{k}" in taken:
+            k += 1
+        c = f"I{k}"
+        taken.add(c)
+        plan.append((node[pairs[2 * s]], node[pairs[2 * s + 1]], c))
+        node.append(c)
+    sliced = [labs[i] for i in range(len(labs)) if sl[i]]
+    stats = {f: getattr(st, f) for f, _ in qxg_plan_stats._fields_ if f != "reserved"}
+    return plan, sliced, stats
+
+
+def native_contraction_scheme(tnc, num: int = 0, seed: int = 0, max_log2: float | None = None,
+                              trials: int = 64, greedy_trials: int = 16, batched=(), beta: int = 1, lib=None):
+    """`contraction_scheme` (:219-299) through the library's planner -> (index_groups_to_slice,
+    plan, metadata): `num` bonds sliced (number_bonds_to_slice), or as many as bring every
+    intermediate to at most 2^max_log2 elements; steps that depend on the `batched` tensors run
+    `beta` times in the step model."""
+    tn = getattr(tnc, "tn", tnc)
+    net = hyper_network(tnc)
+    plan, sliced, st = native_plan(net, trials=trials, greedy_trials=greedy_trials, seed=seed, max_log2=max_log2,
+                                   num_sliced=num, batched=batched, beta=beta, lib=lib)
+    groups = [sorted(ix for ix in tn.dims if tn.root(ix) == l and tn.tensors_with_index(ix)) for l in sliced]
+    metadata = OrderedDict()
+    metadata["Determination of contraction plan"] = OrderedDict([
+        ("Method used", "recursive hypergraph bisection and random greedy (qxg_plan_contraction)"),
+        ("Treewidth", int(round(plan_cost(net, plan)["max_log2"]))),
+        ("Trees tried", int(st["trees_tried"])), ("Seed used", seed), ("Hypergraph used", True),
+    ])
+    metadata["Slicing"] = OrderedDict([
+        ("Method used", "greedy: the label of the largest intermediates that minimises modelled time x slices"),
+        ("Edges sliced", len(sliced)), ("Log2 largest intermediate after slicing", st["max_log2"]),
+        ("Log2 FLOPs over all slices", st["log2_flops_total"]),
     ])
     return groups, plan, metadata

@@ -11,10 +11,19 @@ deterministic for (name, seed, time).  Generated programmes are cached under _bu
 (the planner takes seconds to a minute).
 
   rqc_4x4_d10          4x4 grid, 10 cycles, unsliced, 64 bitstrings (the CPU-runnable case)
-  rqc_6x6_d14_s4       6x6 grid, 14 cycles, 4 sliced bonds, 256 bitstrings
+  rqc_6x6_d14_s4       6x6 grid, 14 cycles, 4 sliced bonds, 256 bitstrings (library planner)
   rqc_5x5_d12_open6    5x5 grid, 12 cycles, 6 qubits open (2^6 amplitudes per bitstring),
                        64 bitstrings of the other 19 qubits -> 4096 amplitudes
   rqc_3x4_d8_s3        3x4 grid, 8 cycles, 3 sliced bonds, 64 bitstrings (parity size)
+  rqc_7x7_d10_w22      7x7 grid, 10 cycles, sliced until every intermediate has at most 2^22
+                       elements (8 slices), 1024 bitstrings (library planner): the 7x7 precision
+                       case at a depth one GPU finishes; at 16 cycles every balanced split of the
+                       network cuts all 49 qubit wires and no plan comes near 2^28 elements with
+                       2^10 slices
+
+Workloads marked "library planner" are planned by qxg_plan_contraction (recursive hypergraph
+bisection and random-greedy trees, subtree reconfiguration, greedy slicing; `plan_time` x 8 trees)
+with the bitstring batch in its step model; the others by the Python stand-in for FlowCutter.
 """
 from __future__ import annotations
 
@@ -28,7 +37,7 @@ from . import dsl as _dsl
 from .circuits import create_parametrised_circuit, create_rqc_circuit
 from .compute_graph import build_compute_graph
 from .executor import Programme
-from .planning import contraction_scheme, hyper_network, plan_cost
+from .planning import contraction_scheme, hyper_network, native_contraction_scheme, plan_cost
 from .simulation import amplitudes_uniform
 from .tnc import convert_to_tnc
 
@@ -36,10 +45,11 @@ __all__ = ["WORKLOADS", "build_workload"]
 
 WORKLOADS = {
     "rqc_4x4_d10": dict(rows=4, cols=4, depth=10, nslice=0, open=0, nbits=64),
-    "rqc_6x6_d14_s4": dict(rows=6, cols=6, depth=14, nslice=4, open=0, nbits=256),
+    "rqc_6x6_d14_s4": dict(rows=6, cols=6, depth=14, nslice=4, open=0, nbits=256, planner="native"),
     # plan_seed / plan_time: the fastest of the seed search's best-ranked plans, measured on a GB300
     "rqc_5x5_d12_open6": dict(rows=5, cols=5, depth=12, nslice=0, open=6, nbits=64, plan_time=4, plan_seed=18),
     "rqc_3x4_d8_s3": dict(rows=3, cols=4, depth=8, nslice=3, open=0, nbits=64),
+    "rqc_7x7_d10_w22": dict(rows=7, cols=7, depth=10, nslice=0, max_log2=22, open=0, nbits=1024, planner="native"),
     # parametrised: per layer Rx(t) Rz(t) on every qubit + fSim(t, p) on one coupler pattern;
     # 840 angles; two-qubit gates kept whole so each gate is one differentiable leaf
     "param_5x5_l12": dict(rows=5, cols=5, depth=12, nslice=0, open=0, nbits=256, parametrised=True, plan_time=4,
@@ -89,8 +99,13 @@ def build_workload(name: str, seed: int = 1, time: int | None = None, cache: boo
     else:
         open_q, out_q = [], list(range(1, n + 1))
     tnc.add_output_subset(out_q)
-    groups, plan, meta = contraction_scheme(tnc, spec["nslice"], seed=spec.get("plan_seed", seed), time=time,
-                                            width_cap=WIDTH_CAP, batched=tnc.output_tensors, beta=spec["nbits"])
+    if spec.get("planner") == "native":
+        groups, plan, meta = native_contraction_scheme(tnc, num=spec["nslice"], seed=spec.get("plan_seed", seed),
+                                                       max_log2=spec.get("max_log2"), trials=8 * time,
+                                                       batched=tnc.output_tensors, beta=spec["nbits"])
+    else:
+        groups, plan, meta = contraction_scheme(tnc, spec["nslice"], seed=spec.get("plan_seed", seed), time=time,
+                                                width_cap=WIDTH_CAP, batched=tnc.output_tensors, beta=spec["nbits"])
     graph = build_compute_graph(tnc, plan, groups)
     nq = len(out_q)
     prog = Programme.from_commands(graph.commands, graph.data, nq)

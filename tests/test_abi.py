@@ -39,7 +39,8 @@ def test_struct_layouts(q, tmp_path):
     if cc is None:
         pytest.skip("no C compiler")
     fields = {"qxg_instr": ex.qxg_instr, "qxg_options": ex.qxg_options, "qxg_program_info": ex.qxg_program_info,
-              "qxg_qx_sizes": ex.qxg_qx_sizes, "qxg_yml_output": ex.qxg_yml_output}
+              "qxg_qx_sizes": ex.qxg_qx_sizes, "qxg_yml_output": ex.qxg_yml_output,
+              "qxg_plan_options": ex.qxg_plan_options, "qxg_plan_stats": ex.qxg_plan_stats}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "qxgpu.h"', "int main(void){"]
     for s, cls in fields.items():
         lines.append(f'printf("{s} %zu\\n", sizeof({s}));')

@@ -1,0 +1,193 @@
+"""qxg_plan_contraction, the library's planner (host code, no device needed).
+
+Its plans must be complete `(A, B, C)` plans of the network, its cost report must agree with
+plan_cost (the Python restatement of the executor's step model and of QXTns' label rule), the
+amplitudes of programmes built from its plans (sliced or not) must equal the state vector through
+the CPU oracle, slicing must meet the width target, the search must be deterministic for a seed,
+and on a 6x6, 14-cycle circuit it must beat the Python stand-in for FlowCutter by a wide margin.
+"""
+import ctypes as ct
+import math
+
+import numpy as np
+import pytest
+
+from test_oracle_golden import amp_from_sv, statevector
+
+
+def _plan(q, gpu_lib, tnc, **kw):
+    net = q.hyper_network(tnc)
+    plan, sliced, st = q.native_plan(net, lib=gpu_lib, **kw)
+    return net, plan, sliced, st
+
+
+def _check_complete(net, plan):
+    alive = set(net.tensors)
+    for a, b, c in plan:
+        assert a in alive and b in alive and a != b and c not in alive
+        alive -= {a, b}
+        alive.add(c)
+    assert len(alive) == 1 and len(plan) == len(net.tensors) - 1
+
+
+@pytest.mark.parametrize("shape", [(3, 3, 5, 11), (2, 4, 6, 5), (3, 4, 8, 2)])
+def test_native_plan_is_complete_and_costs_agree(q, gpu_lib, shape):
+    r, c, d, seed = shape
+    tnc = q.convert_to_tnc(q.create_rqc_circuit(r, c, d, seed=seed), decompose=True)
+    net, plan, sliced, st = _plan(q, gpu_lib, tnc, trials=16, greedy_trials=4, seed=3)
+    _check_complete(net, plan)
+    assert sliced == []
+    pc = q.plan_cost(net, plan)
+    assert abs(math.log2(pc["flops"]) - st["log2_flops"]) < 1e-9
+    assert pc["max_log2"] == st["max_log2"]
+    assert abs(pc["time"] - st["time"]) <= 1e-9 * pc["time"]
+
+
+def test_native_plan_amplitudes_match_statevector(q, gpu_lib, oracle):
+    circ = q.create_rqc_circuit(3, 3, 6, seed=7)
+    psi = statevector(circ)
+    tnc = q.convert_to_tnc(circ, decompose=True)
+    bits = list(q.amplitudes_uniform(9, 3, 12))
+    ref = np.array([amp_from_sv(psi, b) for b in bits])
+    groups, plan, meta = q.native_contraction_scheme(tnc, num=3, seed=2, trials=8, greedy_trials=4, lib=gpu_lib)
+    assert len(groups) == 3
+    prog = q.Programme.from_graph(q.build_compute_graph(tnc, plan, groups))
+    assert prog.num_slices >= 8
+    amps = oracle.run_programme(prog, bits, nthreads=4)[:, 0]
+    assert np.max(np.abs(amps - ref)) < 1e-13
+    unsliced = q.Programme.from_graph(q.build_compute_graph(tnc, plan))
+    amps = oracle.run_programme(unsliced, bits, nthreads=4)[:, 0]
+    assert np.max(np.abs(amps - ref)) < 1e-13
+
+
+def test_native_plan_open_outputs(q, gpu_lib, oracle):
+    """Open qubits stay to the end: the saved tensor is the 2^k batch of amplitudes."""
+    circ = q.create_rqc_circuit(2, 3, 5, seed=4)
+    psi = statevector(circ)
+    tnc = q.convert_to_tnc(circ, decompose=True, no_output=True)
+    tnc.add_output_subset([1, 2, 3, 5])            # qubits 4 and 6 open
+    net, plan, sliced, st = _plan(q, gpu_lib, tnc, trials=8, greedy_trials=2, seed=1)
+    _check_complete(net, plan)
+    prog = q.Programme.from_graph(q.build_compute_graph(tnc, plan))
+    out = oracle.run_programme(prog, ["0110"], out_size=4)[0]
+    for k, (b4, b6) in enumerate([(0, 0), (1, 0), (0, 1), (1, 1)]):
+        full = "011" + str(b4) + "0" + str(b6)
+        assert abs(out[k] - amp_from_sv(psi, full)) < 1e-13
+
+
+def test_native_slicing_meets_the_width_target(q, gpu_lib):
+    tnc = q.convert_to_tnc(q.create_rqc_circuit(4, 4, 8, seed=1), decompose=True)
+    net, plan, sliced, st = _plan(q, gpu_lib, tnc, trials=16, greedy_trials=4, seed=1)
+    target = st["max_log2"] - 4
+    net, plan2, sliced2, st2 = _plan(q, gpu_lib, tnc, trials=16, greedy_trials=4, seed=1, max_log2=target)
+    assert st2["max_log2"] <= target and len(sliced2) == st2["num_sliced"] >= 2
+    pc = q.plan_cost(net, plan2, sliced2)
+    assert pc["max_log2"] <= target
+    assert abs(st2["log2_slices"] - sum(math.log2(net.dims[l]) for l in sliced2)) < 1e-9
+    # a number of bonds, like number_bonds_to_slice
+    _, _, sliced3, st3 = _plan(q, gpu_lib, tnc, trials=8, greedy_trials=2, seed=1, num_sliced=3)
+    assert len(sliced3) == 3
+
+
+def test_native_plan_is_deterministic(q, gpu_lib):
+    tnc = q.convert_to_tnc(q.create_rqc_circuit(3, 4, 6, seed=9), decompose=True)
+    a = _plan(q, gpu_lib, tnc, trials=12, greedy_trials=3, seed=5, max_log2=10)
+    b = _plan(q, gpu_lib, tnc, trials=12, greedy_trials=3, seed=5, max_log2=10)
+    assert a[1] == b[1] and a[2] == b[2]
+
+
+def test_native_plan_beats_the_greedy_stand_in(q, gpu_lib):
+    """6x6 grid, 14 cycles (the sliced plain-executor configuration's circuit): the library's
+    trees are far cheaper than the Python random-greedy stand-in for FlowCutter."""
+    tnc = q.convert_to_tnc(q.create_rqc_circuit(6, 6, 14, seed=1), decompose=True)
+    net, plan, _, st = _plan(q, gpu_lib, tnc, trials=24, greedy_trials=4, seed=1)
+    py = q.plan_cost(net, q.flow_cutter_contraction_plan(tnc, time=1, seed=1))
+    assert st["log2_flops"] < 44.0
+    assert st["log2_flops"] < math.log2(py["flops"]) - 5
+    assert st["max_log2"] <= py["max_log2"]
+
+
+def test_native_plan_batch_model(q, gpu_lib):
+    """With 256 bitstrings in the step model the plan's modelled time (outputs batched) is no worse
+    than that of the plan chosen for one bitstring."""
+    circ = q.create_rqc_circuit(4, 4, 8, seed=3)
+    tnc = q.convert_to_tnc(circ, decompose=True, no_output=True)
+    tnc.add_output_subset(list(range(1, 17)))
+    net = q.hyper_network(tnc)
+    p1, _, _ = q.native_plan(net, trials=16, greedy_trials=4, seed=2, lib=gpu_lib)
+    p2, _, st2 = q.native_plan(net, trials=16, greedy_trials=4, seed=2, batched=tnc.output_tensors, beta=256,
+                               lib=gpu_lib)
+    t1 = q.plan_cost(net, p1, (), tnc.output_tensors, 256)["time"]
+    t2 = q.plan_cost(net, p2, (), tnc.output_tensors, 256)["time"]
+    assert abs(t2 - st2["time"]) <= 1e-9 * t2
+    assert t2 <= t1 * (1 + 1e-9)
+
+
+@pytest.mark.parametrize("case,msg", [
+    ("label", "label id out of range"),
+    ("log2", "log2 dimension outside 0..16"),
+    ("offsets", "label offsets decrease"),
+    ("empty", "bad arguments"),
+])
+def test_native_plan_rejects_bad_input(q, gpu_lib, case, msg):
+    from qxtools_gb300 import executor as ex
+    off = (ct.c_int64 * 3)(0, 2, 4)
+    labs = (ct.c_int32 * 4)(0, 1, 1, 0)
+    w = (ct.c_int32 * 2)(1, 1)
+    V, E = 2, 2
+    if case == "label":
+        labs[3] = 5
+    elif case == "log2":
+        w[1] = 17
+    elif case == "offsets":
+        off[1] = 5
+        off[2] = 4
+    elif case == "empty":
+        V = 0
+    pairs = (ct.c_int32 * 2)()
+    st = ex.qxg_plan_stats()
+    rc = gpu_lib.qxg_plan_contraction(V, off, labs, E, w, None, None, pairs, None, ct.byref(st))
+    assert rc == -1 and msg in gpu_lib.qxg_last_error().decode()
+
+
+@pytest.mark.timeout(600)
+def test_planner_under_address_sanitizer(q, tmp_path):
+    """The planner built with AddressSanitizer and UBSan, run on networks with open, batched and
+    sliced labels: no out-of-range access, a complete plan."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    root = Path(__file__).resolve().parent.parent
+    exe = tmp_path / "planner"
+    cmd = [gxx, "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer",
+           "-I", str(root / "include"), "-x", "c++", str(root / "qxtools.jl_gb300" / "csrc" / "planner.cu"),
+           "-x", "c++", str(root / "tests" / "emu" / "planner_driver.cpp"), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    for (rows, cols, depth, nopen), args in [((3, 4, 8, 2), ["12", "3", "1", "8", "0", "6"]),
+                                              ((4, 4, 10, 0), ["16", "4", "2", "0", "3", "0"]),
+                                              ((2, 3, 4, 6), ["6", "2", "3", "0", "0", "0"])]:
+        circ = q.create_rqc_circuit(rows, cols, depth, seed=rows + depth)
+        tnc = q.convert_to_tnc(circ, decompose=True, no_output=True)
+        n = circ.num_qubits
+        tnc.add_output_subset(list(range(1, n + 1 - nopen)))
+        net = q.hyper_network(tnc)
+        names = list(net.tensors)
+        labs = sorted({l for ls in net.tensors.values() for l in ls}, key=str)
+        lid = {l: i for i, l in enumerate(labs)}
+        outs = set(tnc.output_tensors)
+        lines = [f"{len(names)} {len(labs)}",
+                 " ".join(str(int(math.log2(net.dims[l]))) for l in labs),
+                 " ".join("1" if l in net.open else "0" for l in labs),
+                 " ".join("1" if nm in outs else "0" for nm in names)]
+        for nm in names:
+            ids = [lid[l] for l in dict.fromkeys(net.tensors[nm])]
+            lines.append(f"{len(ids)} " + " ".join(map(str, ids)))
+        path = tmp_path / f"net_{rows}{cols}{depth}.txt"
+        path.write_text("\n".join(lines) + "\n")
+        r = subprocess.run([str(exe), str(path)] + args, capture_output=True, text=True, timeout=300,
+                           env={"ASAN_OPTIONS": "detect_leaks=1", "UBSAN_OPTIONS": "halt_on_error=1"})
+        assert r.returncode == 0 and r.stdout.strip().endswith("ok"), (r.stdout[-2000:], r.stderr[-3000:])
