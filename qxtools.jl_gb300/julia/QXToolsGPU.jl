@@ -11,7 +11,8 @@ or passed in as a Dict{String,Array{ComplexF64}} (e.g. loaded from the reference
 """
 module QXToolsGPU
 
-export QxgProgram, parse_qx, load_qx, read_bitstrings, qxrun, amplitudes, single_amplitude
+export QxgProgram, parse_qx, load_qx, read_bitstrings, qxrun, plan_contraction, amplitudes,
+       single_amplitude
 
 const libqxgpu = joinpath(@__DIR__, "..", "_build", "libqxgpu.so")
 
@@ -150,6 +151,56 @@ function qxrun(qx_file::String, data::AbstractDict, yml_file::String;
     ns = max_slices === nothing ? p.num_slices : min(max_slices, p.num_slices)
     amps = amplitudes(p, bits; slices=0:ns-1)
     Dict(b => amps[1, i] for (i, b) in enumerate(bits))
+end
+
+struct QxgPlanOptions      # qxg_plan_options
+    trials::Int32; greedy_trials::Int32; seed::Int64; max_log2::Float64
+    num_sliced::Int32; max_sliced::Int32; flops_per_s::Float64; bytes_per_s::Float64
+    tensor_batched::Ptr{UInt8}; batch_log2::Float64; reserved::NTuple{6,Int32}
+end
+
+struct QxgPlanStats        # qxg_plan_stats
+    log2_flops::Float64; log2_flops_total::Float64; max_log2::Float64; time::Float64
+    log2_slices::Float64; num_sliced::Int32; trees_tried::Int32; reserved::NTuple{6,Int32}
+end
+
+"""
+    plan_contraction(tensor_labels, log2dims; open=nothing, max_log2=0, num_sliced=0,
+                     trials=64, seed=0, batched=nothing, batch=1) -> (steps, sliced, stats)
+
+The library's planner (`qxg_plan_contraction`) in place of FlowCutter
+(flow_cutter_contraction_plan, src/contraction_planning.jl:90-113, and the slicer of
+contraction_scheme, :219-299).  `tensor_labels[i]` lists the label ids (1-based) of tensor i,
+`log2dims[l]` is log2 of label l's dimension, `open[l]` keeps label l to the end.  `steps[k] =
+(a, b)` contracts nodes a and b into node `length(tensor_labels) + k` (nodes 1..n are the
+tensors), so naming node n+k `:I\$k` gives the reference's `(A, B, C)` plan; `sliced` lists the
+labels to slice.  Steps that depend on a tensor with `batched[i]` run `batch` times in the step
+model (the output tensors and the number of bitstrings).
+"""
+function plan_contraction(tensor_labels::AbstractVector, log2dims::AbstractVector{<:Integer};
+                          open=nothing, max_log2::Real=0, num_sliced::Integer=0, trials::Integer=64,
+                          seed::Integer=0, batched=nothing, batch::Integer=1)
+    n, nl = length(tensor_labels), length(log2dims)
+    off = Int64[0]; labs = Int32[]
+    for t in tensor_labels
+        append!(labs, Int32.(t) .- Int32(1)); push!(off, length(labs))
+    end
+    w = Int32.(log2dims)
+    op = open === nothing ? zeros(UInt8, nl) : UInt8.(open)
+    bt = batched === nothing ? zeros(UInt8, n) : UInt8.(batched)
+    pairs = zeros(Int32, max(1, 2 * (n - 1))); sl = zeros(UInt8, max(1, nl))
+    st = Ref(QxgPlanStats(0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 6)))
+    GC.@preserve bt begin
+        o = Ref(QxgPlanOptions(trials, 0, seed, max_log2, num_sliced, 0, 0, 0,
+                               batched === nothing ? C_NULL : pointer(bt), batch > 1 ? log2(batch) : 0,
+                               ntuple(_ -> Int32(0), 6)))
+        check(ccall((:qxg_plan_contraction, libqxgpu), Cint,
+                    (Int32, Ptr{Int64}, Ptr{Int32}, Int32, Ptr{Int32}, Ptr{UInt8}, Ref{QxgPlanOptions},
+                     Ptr{Int32}, Ptr{UInt8}, Ref{QxgPlanStats}),
+                    n, off, labs, nl, w, op, o, pairs, sl, st))
+    end
+    steps = [(Int(pairs[2k-1]) + 1, Int(pairs[2k]) + 1) for k in 1:n-1]
+    steps, findall(!iszero, sl[1:nl]), st[]
 end
 
 """
