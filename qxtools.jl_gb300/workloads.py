@@ -15,6 +15,9 @@ deterministic for (name, seed, time).  Generated programmes are cached under _bu
   rqc_5x5_d12_open6    5x5 grid, 12 cycles, 6 qubits open (2^6 amplitudes per bitstring),
                        64 bitstrings of the other 19 qubits -> 4096 amplitudes
   rqc_3x4_d8_s3        3x4 grid, 8 cycles, 3 sliced bonds, 64 bitstrings (parity size)
+  rqc_6x6_d14_w28      the same circuit sliced until every intermediate has at most 2^28 elements
+                       (8 bonds, 256 slices; 4 GiB per ComplexF64 intermediate instead of the
+                       64 GiB of the 4-bond plan's largest), 256 bitstrings (library planner)
   rqc_7x7_d10_w22      7x7 grid, 10 cycles, sliced until every intermediate has at most 2^22
                        elements (8 slices), 1024 bitstrings (library planner): the 7x7 precision
                        case at a depth one GPU finishes; at 16 cycles every balanced split of the
@@ -49,6 +52,7 @@ WORKLOADS = {
     # plan_seed / plan_time: the fastest of the seed search's best-ranked plans, measured on a GB300
     "rqc_5x5_d12_open6": dict(rows=5, cols=5, depth=12, nslice=0, open=6, nbits=64, plan_time=4, plan_seed=18),
     "rqc_3x4_d8_s3": dict(rows=3, cols=4, depth=8, nslice=3, open=0, nbits=64),
+    "rqc_6x6_d14_w28": dict(rows=6, cols=6, depth=14, nslice=4, max_log2=28, open=0, nbits=256, planner="native"),
     "rqc_7x7_d10_w22": dict(rows=7, cols=7, depth=10, nslice=0, max_log2=22, open=0, nbits=1024, planner="native"),
     # parametrised: per layer Rx(t) Rz(t) on every qubit + fSim(t, p) on one coupler pattern;
     # 840 angles; two-qubit gates kept whole so each gate is one differentiable leaf

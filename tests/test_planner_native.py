@@ -191,3 +191,13 @@ def test_planner_under_address_sanitizer(q, tmp_path):
         r = subprocess.run([str(exe), str(path)] + args, capture_output=True, text=True, timeout=300,
                            env={"ASAN_OPTIONS": "detect_leaks=1", "UBSAN_OPTIONS": "halt_on_error=1"})
         assert r.returncode == 0 and r.stdout.strip().endswith("ok"), (r.stdout[-2000:], r.stderr[-3000:])
+
+
+def test_native_planned_workloads_build(q, gpu_lib):
+    """The 7x7 precision workload: planned by the library within its width target, with the
+    bitstring list and slices the executor runs."""
+    prog, bits, info = q.workloads.build_workload("rqc_7x7_d10_w22", cache=False)
+    assert info["max_log2"] <= 22 and prog.num_slices == 8 and len(bits) == 1024
+    nncon = int((prog.instrs[:, 0] == 4).sum())
+    assert nncon >= info["plan_steps"] > 900
+    assert info["est_seconds_per_pass"] < 1.0
