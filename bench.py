@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--bits-per-step", type=int, default=0, help="bitstrings per step (0: the workload's list)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--plan-seed", type=int, default=None, help="planner seed (default: the workload's pinned one)")
+    ap.add_argument("--planner", default=None, choices=["python", "native"],
+                    help="plan with the Python stand-in or the library's planner (default: the workload's)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--compare-fp64", action="store_true", help="also time the FP64 path and report the error")
@@ -205,7 +207,8 @@ def run_reference(args):
     q = entry.load()
     from oracle import oracle
     oracle.build()
-    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed, plan_seed=args.plan_seed)
+    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed, plan_seed=args.plan_seed,
+                                                  planner=args.planner)
     cores = oracle.max_threads()
     out_size = info["amplitudes_per_bitstring"]
     per = max(2.0, min(args.cpu_seconds, 20.0))
@@ -239,6 +242,7 @@ def workload_config(info, args, ex_info):
            "amplitudes_per_bitstring": info["amplitudes_per_bitstring"], "slices": info["num_slices"],
            "plan_steps": info["plan_steps"], "max_intermediate_log2": info["max_log2"],
            "flops_per_bitstring": info["flops_per_bitstring"], "seed": info["seed"],
+           "planner": info["spec"].get("planner", "python"),
            "precision": args.precision, "cuda_graphs": not args.no_graphs,
            "l2": "intermediates larger than L2 (no flush needed)"}
     if ex_info:
@@ -266,7 +270,8 @@ def run_ours(args):
         entry._load_build_module().build()
     q = entry.load()
     from oracle import oracle
-    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed, plan_seed=args.plan_seed)
+    prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed, plan_seed=args.plan_seed,
+                                                  planner=args.planner)
     # default batch: the whole list for the Complex64 paths, 16 bitstrings for the slower FP64 path
     nb = args.bits_per_step or (min(16, len(bits)) if args.precision == "fp64" else len(bits))
     # weak scaling: rank r takes its own shard of bitstrings (regenerated deterministically)

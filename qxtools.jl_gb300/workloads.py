@@ -73,14 +73,19 @@ def _key(name, spec, seed, time):
 
 
 def build_workload(name: str, seed: int = 1, time: int | None = None, cache: bool = True,
-                   plan_seed: int | None = None):
+                   plan_seed: int | None = None, planner: str | None = None):
     """-> (Programme, bitstrings, info dict).  Deterministic for (name, seed, time, plan seed).
     `seed` draws the circuit and the bitstrings; the planner's seed is `plan_seed`, else the
     workload's pinned "plan_seed" (the best of a seed search under plan_cost's ranking), else
-    `seed`; `time` (8 x time greedy trials) defaults to the workload's "plan_time", else 16."""
+    `seed`; `time` (8 x time greedy trials) defaults to the workload's "plan_time", else 16.
+    `planner` ("python" or "native") overrides the workload's planner."""
     spec = dict(WORKLOADS[name])
     if plan_seed is not None:
         spec["plan_seed"] = int(plan_seed)
+    if planner is not None:
+        if planner not in ("python", "native"):
+            raise ValueError(f"planner {planner!r}: python or native")
+        spec["planner"] = planner
     if time is None:
         time = spec.get("plan_time", 16)
     key = _key(name, spec, seed, time)
