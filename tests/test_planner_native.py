@@ -123,7 +123,23 @@ def test_native_plan_batch_model(q, gpu_lib):
     assert t2 <= t1 * (1 + 1e-9)
 
 
+def test_native_plan_small_and_disconnected(q, gpu_lib):
+    """One tensor: no steps.  Tensors sharing no label: joined as outer products, smallest first."""
+    from qxtools_gb300 import executor as ex
+    st = ex.qxg_plan_stats()
+    off = (ct.c_int64 * 2)(0, 1)
+    labs = (ct.c_int32 * 1)(0)
+    w = (ct.c_int32 * 1)(1)
+    assert gpu_lib.qxg_plan_contraction(1, off, labs, 1, w, None, None, None, None, ct.byref(st)) == 0
+    assert st.log2_flops == 0 and st.max_log2 == 0
+    net = q.HyperNet({"a": ["x"], "b": ["y", "z"], "c": []}, {"x": 2, "y": 2, "z": 4})
+    plan, sliced, st = q.native_plan(net, trials=2, greedy_trials=1, lib=gpu_lib)
+    _check_complete(net, plan)
+    assert st["max_log2"] == 4.0 and sliced == []
+
+
 @pytest.mark.parametrize("case,msg", [
+    ("negative", "negative label offset"),
     ("label", "label id out of range"),
     ("log2", "log2 dimension outside 0..16"),
     ("offsets", "label offsets decrease"),
@@ -135,7 +151,9 @@ def test_native_plan_rejects_bad_input(q, gpu_lib, case, msg):
     labs = (ct.c_int32 * 4)(0, 1, 1, 0)
     w = (ct.c_int32 * 2)(1, 1)
     V, E = 2, 2
-    if case == "label":
+    if case == "negative":
+        off[0] = -1
+    elif case == "label":
         labs[3] = 5
     elif case == "log2":
         w[1] = 17
