@@ -866,11 +866,14 @@ struct Scored {
     double key() const { return cost.time * std::ldexp(1.0, (int)slices_log2); }
 };
 
-void slice_greedy(const Net& n, const Steps& st, const Model& m, double max_log2, int max_sliced, int num, Scored* s) {
+// Adds at most `limit` labels to s->sliced; returns how many it added.
+int slice_greedy(const Net& n, const Steps& st, const Model& m, double max_log2, int max_sliced, int num, Scored* s,
+                 int limit) {
     std::vector<int> w = n.w;
     for (int l : s->sliced) w[l] = 0;
     s->cost = cost_of(n, st, w, m);
-    while (true) {
+    int added = 0;
+    while (added < limit) {
         const bool need_width = max_log2 > 0 && s->cost.max_log2 > max_log2;
         const bool need_num = num > 0 && (int)s->sliced.size() < num;
         if (!need_width && !need_num) break;
@@ -906,7 +909,9 @@ void slice_greedy(const Net& n, const Steps& st, const Model& m, double max_log2
         w[best] = 0;
         s->sliced.push_back(best);
         s->cost = bc;
+        added++;
     }
+    return added;
 }
 
 }  // namespace
@@ -1011,11 +1016,12 @@ extern "C" int qxg_plan_contraction(int32_t ntensors, const int64_t* label_off, 
         for (int i : pick) {
             Scored& s = trees[i];
             refine(s, n.w, 8);
-            if (slicing) {
-                slice_greedy(n, tree_steps(n, s.pairs), m, o.max_log2, o.max_sliced, o.num_sliced, &s);
-                std::vector<int> w = n.w;
-                for (int l : s.sliced) w[l] = 0;
-                refine(s, w, 8);
+            if (slicing) {  // one label at a time, the tree reconfigured under each new slicing
+                while (slice_greedy(n, tree_steps(n, s.pairs), m, o.max_log2, o.max_sliced, o.num_sliced, &s, 1)) {
+                    std::vector<int> w = n.w;
+                    for (int l : s.sliced) w[l] = 0;
+                    refine(s, w, 8);
+                }
             }
             std::vector<int> w = n.w;
             for (int l : s.sliced) w[l] = 0;
