@@ -758,8 +758,9 @@ double node_time(const Tree& t, int x, const std::vector<int>& w, const Model& m
     return step_time(t.lab[t.L[x]], t.dep[t.L[x]], t.lab[t.R[x]], t.dep[t.R[x]], t.lab[x], w, m);
 }
 
-// One sweep over the internal nodes, largest steps first; returns the time saved.
-double reconfigure_pass(const Net& n, Tree& t, const std::vector<int>& w, const Model& m, int k) {
+// One sweep over the internal nodes, largest steps first; returns the time saved.  New
+// intermediates wider than 2^cap elements are not formed.
+double reconfigure_pass(const Net& n, Tree& t, const std::vector<int>& w, const Model& m, int k, int cap) {
     const int N = (int)t.L.size();
     std::vector<std::pair<double, int>> order;
     for (int x = t.V; x < N; x++) order.push_back({-node_time(t, x, w, m), x});
@@ -807,12 +808,17 @@ double reconfigure_pass(const Net& n, Tree& t, const std::vector<int>& w, const 
             const int low = mask & -mask;
             merge_labels(n, sl[low], sl[mask ^ low], &sl[mask], nullptr);
             sdep[mask] = sdep[low] || sdep[mask ^ low];
+            if (mask != full && weight_of(sl[mask], w) > cap) {
+                best[mask] = -1;  // not formed
+                continue;
+            }
             double bt = -1;
             int bs = 0;
             // splits with the lowest member in `sub`, so each unordered pair is seen once
             for (int sub = (mask - 1) & mask; sub; sub = (sub - 1) & mask) {
                 if (!(sub & low)) continue;
                 const int rest = mask ^ sub;
+                if (best[sub] < 0 || best[rest] < 0) continue;
                 const double c = best[sub] + best[rest] + step_time(sl[sub], sdep[sub], sl[rest], sdep[rest], sl[mask], w, m);
                 if (bt < 0 || c < bt) {
                     bt = c;
@@ -822,7 +828,7 @@ double reconfigure_pass(const Net& n, Tree& t, const std::vector<int>& w, const 
             best[mask] = bt;
             split[mask] = bs;
         }
-        if (best[full] >= cur * (1.0 - 1e-9)) continue;
+        if (best[full] < 0 || best[full] >= cur * (1.0 - 1e-9)) continue;
         saved += cur - best[full];
         // rebuild: x stays the subtree's root; the other inner ids are reused
         std::vector<int> free_ids(inner.begin() + 1, inner.end());
@@ -993,6 +999,8 @@ extern "C" int qxg_plan_contraction(int32_t ntensors, const int64_t* label_off, 
             return a < b;
         });
         const bool slicing = o.max_log2 > 0 || o.num_sliced > 0;
+        constexpr int kNoCap = 1 << 30;
+        const int width_cap = o.max_log2 > 0 ? (int)std::floor(o.max_log2) : kNoCap;
         std::vector<int> pick(idx.begin(), idx.begin() + std::min<int>((int)idx.size(), 6));
         if (slicing) {
             std::vector<int> by_width = idx;
@@ -1002,11 +1010,11 @@ extern "C" int qxg_plan_contraction(int32_t ntensors, const int64_t* label_off, 
         }
         std::sort(pick.begin(), pick.end());
         pick.erase(std::unique(pick.begin(), pick.end()), pick.end());
-        auto refine = [&](Scored& s, const std::vector<int>& w, int k) {
+        auto refine = [&](Scored& s, const std::vector<int>& w, int k, int cap) {
             Tree t = tree_of(n, s.pairs);
             double cur = cost_tree(n, t, w, m).time;
             for (int pass = 0; pass < 8; pass++) {
-                const double saved = reconfigure_pass(n, t, w, m, k);
+                const double saved = reconfigure_pass(n, t, w, m, k, cap);
                 cur -= saved;
                 if (saved <= 1e-3 * cur) break;
             }
@@ -1015,12 +1023,12 @@ extern "C" int qxg_plan_contraction(int32_t ntensors, const int64_t* label_off, 
         int best = -1;
         for (int i : pick) {
             Scored& s = trees[i];
-            refine(s, n.w, 8);
+            refine(s, n.w, 8, kNoCap);
             if (slicing) {  // one label at a time, the tree reconfigured under each new slicing
                 while (slice_greedy(n, tree_steps(n, s.pairs), m, o.max_log2, o.max_sliced, o.num_sliced, &s, 1)) {
                     std::vector<int> w = n.w;
                     for (int l : s.sliced) w[l] = 0;
-                    refine(s, w, 8);
+                    refine(s, w, 8, width_cap);
                 }
             }
             std::vector<int> w = n.w;
@@ -1036,7 +1044,7 @@ extern "C" int qxg_plan_contraction(int32_t ntensors, const int64_t* label_off, 
             Scored& s = trees[best];
             std::vector<int> w = n.w;
             for (int l : s.sliced) w[l] = 0;
-            refine(s, w, 10);
+            refine(s, w, 10, width_cap);
             s.cost = cost_of(n, tree_steps(n, s.pairs), w, m);
         }
         const Scored& b = trees[best];
