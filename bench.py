@@ -440,7 +440,7 @@ def run_gradient(args):
     # with the bitstring batch)
     spec = q.workloads.WORKLOADS["param_5x5_l12"]
     plan_opts = dict(seed=args.plan_seed if args.plan_seed is not None else spec["plan_seed"], time=spec["plan_time"],
-                     width_cap=q.workloads.WIDTH_CAP, beta=spec["nbits"])
+                     width_cap=q.workloads.WIDTH_CAP, beta=spec["nbits"], planner=args.planner or "python")
     # forward and gradient passes both replayed from CUDA graphs (unless --no-graphs)
     f = q.gradients.ParametrisedCircuitLoss(circ, precision=args.precision, use_graphs=not args.no_graphs,
                                             **plan_opts)
@@ -468,6 +468,7 @@ def run_gradient(args):
             "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic (seeded angles, bitstrings)",
             "config": {"workload": "param_5x5_l12", "params": circ.num_params, "bitstrings": len(bits),
                        "precision": args.precision, "plan_steps": info["num_steps"],
+                       "planner": args.planner or "python",
                        "flops_per_amplitude": info["flops_per_amplitude"]},
             "forward_s": fwd, "gradient_s": grad, "amplitudes_per_s_forward": len(bits) / fwd,
             "loss": L, "max_abs_err_vs_fp64_8bits": float(np.max(np.abs(gs - g64))),

@@ -17,7 +17,7 @@ import numpy as np
 
 from .compute_graph import build_compute_graph
 from .executor import Executor, Programme
-from .planning import contraction_scheme
+from .planning import contraction_scheme, native_contraction_scheme
 from .tnc import convert_to_tnc
 
 __all__ = ["gate_derivatives", "ParametrisedCircuitLoss"]
@@ -46,15 +46,22 @@ def gate_derivatives(gate) -> list:
 class ParametrisedCircuitLoss:
     """L(theta) = sum over bitstrings of |<x|C(theta)|0>|^2 and dL/dtheta on the GPU.
 
-    The circuit is converted without decomposition, planned (with `nslice` sliced bonds) and
-    compiled once; each evaluation runs one reverse-mode pass per (slice batch, bitstring batch)."""
+    The circuit is converted without decomposition, planned (with `nslice` sliced bonds; by the
+    Python stand-in for FlowCutter, or by the library's planner with planner="native") and compiled
+    once; each evaluation runs one reverse-mode pass per (slice batch, bitstring batch)."""
 
     def __init__(self, circ, nslice: int = 0, seed: int = 1, time: int = 1, precision: str = "fp64",
-                 width_cap: float | None = None, beta: int = 1, **opts):
+                 width_cap: float | None = None, beta: int = 1, planner: str = "python", **opts):
         self.circ = circ
         self.tnc = convert_to_tnc(circ, decompose=False)
-        groups, plan, _ = contraction_scheme(self.tnc, nslice, seed=seed, time=time, width_cap=width_cap,
-                                             batched=self.tnc.output_tensors, beta=beta)
+        if planner == "native":
+            groups, plan, _ = native_contraction_scheme(self.tnc, num=nslice, seed=seed, trials=8 * time,
+                                                        batched=self.tnc.output_tensors, beta=beta)
+        elif planner == "python":
+            groups, plan, _ = contraction_scheme(self.tnc, nslice, seed=seed, time=time, width_cap=width_cap,
+                                                 batched=self.tnc.output_tensors, beta=beta)
+        else:
+            raise ValueError(f"planner {planner!r}: python or native")
         self.graph = build_compute_graph(self.tnc, plan, groups)
         self.programme = Programme.from_graph(self.graph)
         self.executor = Executor(self.programme, precision=precision, **opts)
