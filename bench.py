@@ -14,7 +14,8 @@ point qxg_amplitudes with pinned host buffers (bitstrings copied in, amplitudes 
 every step).  Intermediates exceed L2 (largest intermediate reported in `config`).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32|split_bf16|split_tf32]
-    python bench.py --impl reference ...   # the CPU FP64 oracle on the host cores
+    python bench.py --impl reference ...   # the reference's CPU arithmetic (permute + OpenBLAS
+                                           # zgemm per ncon, oracle/blas_walk.py) on the host cores
 Under torchrun (N > 1) every rank runs its own replica on its own shard of bitstrings (the
 path shards by bitstring with no exchange) and the slowest rank's time is reported.
 """
@@ -183,18 +184,20 @@ def traffic_summary(workload: str, kernel: str, precision: str):
 
 # --------------------------------------------------------------------------------------------
 def cpu_baseline(q, oracle, prog, bits, info, seconds: float):
-    """The oracle (FP64 CPU restatement) on a bounded sample: one bitstring's walk for one slice
-    with every host thread inside the contractions, stopped after `seconds`; the FLOP rate is
-    converted to amplitudes/s with the programme's FLOPs per bitstring."""
-    cores = oracle.max_threads()
+    """The reference's CPU arithmetic restated (oracle/blas_walk.py: permute + OpenBLAS zgemm per
+    ncon, as TensorOperations contracts) on a bounded sample: one bitstring's walk for one slice
+    with BLAS on every host thread, stopped after `seconds`; the FLOP rate is converted to
+    amplitudes/s with the programme's FLOPs per bitstring.  `oracle` is unused (kept for callers)."""
+    from oracle import blas_walk
+    cores = blas_walk.blas_threads()
     out_size = info["amplitudes_per_bitstring"]
-    flops, sec, finished = oracle.run_timed(prog, bits[0], seconds, 0, cores, out_size=out_size)
+    flops, sec, finished = blas_walk.run_timed(prog, bits[0], seconds)
     rate = flops / max(sec, 1e-9)
     amps = rate / info["flops_per_bitstring"] * out_size
-    sample = (f"one FP64 walk of bitstring 0, slice 0 of {info['name']} "
-              f"({'complete' if finished else f'stopped after {sec:.1f} s'}, {flops:.3e} FLOPs in {sec:.1f} s); "
-              f"amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per bitstring x "
-              f"{out_size} amplitudes per bitstring")
+    sample = (f"one FP64 walk (numpy permute + OpenBLAS zgemm per ncon) of bitstring 0, slice 0 of "
+              f"{info['name']} ({'complete' if finished else f'stopped after {sec:.1f} s'}, {flops:.3e} FLOPs "
+              f"in {sec:.1f} s); amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per "
+              f"bitstring x {out_size} amplitudes per bitstring")
     return {"value": amps, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
             "gflops": rate / 1e9}
 
@@ -205,26 +208,28 @@ def run_reference(args):
         return
     import __graft_entry__ as entry
     q = entry.load()
-    from oracle import oracle
-    oracle.build()
+    from oracle import blas_walk
     prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed, plan_seed=args.plan_seed,
                                                   planner=args.planner)
-    cores = oracle.max_threads()
+    cores = blas_walk.blas_threads()
     out_size = info["amplitudes_per_bitstring"]
     per = max(2.0, min(args.cpu_seconds, 20.0))
     for _ in range(args.warmup):
-        oracle.run_timed(prog, bits[0], min(per, 3.0), 0, cores, out_size=out_size)
-    fl_tot, sec_tot = 0.0, 0.0
+        blas_walk.run_timed(prog, bits[0], min(per, 3.0))
+    fl_tot, sec_tot, done = 0.0, 0.0, 0
     t0 = time.perf_counter()
     for k in range(args.steps):
-        fl, sec, _ = oracle.run_timed(prog, bits[k % len(bits)], per, 0, cores, out_size=out_size)
+        fl, sec, fin = blas_walk.run_timed(prog, bits[k % len(bits)], per)
         fl_tot += fl
         sec_tot += sec
+        done += int(fin)
     wall = time.perf_counter() - t0
     rate = fl_tot / sec_tot
     value = rate / info["flops_per_bitstring"] * out_size
-    sample = (f"each step: one FP64 walk (bitstring k, slice 0) stopped after {per:.0f} s; amplitudes/s = "
-              f"FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per bitstring x {out_size} amplitudes")
+    sample = (f"each step: one FP64 walk (bitstring k, slice 0; numpy permute + OpenBLAS zgemm per ncon, "
+              f"as TensorOperations contracts) stopped after {per:.0f} s ({done} of {args.steps} complete); "
+              f"amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per bitstring x "
+              f"{out_size} amplitudes")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",

@@ -363,3 +363,48 @@ int qxo_max_threads(void) {
     return 1;
 #endif
 }
+
+/*
+ * Permute-copy for the BLAS walk (blas_walk.py), the step TensorOperations performs with
+ * Strided.jl's threaded permutedims before each GEMM: dst is written contiguously, last axis
+ * fastest (numpy's C order), dims[0..rank-1]; element i of dst reads src at sum_k idx_k *
+ * strides[k] (complex elements, not bytes).  Contiguous chunks of dst are spread over the
+ * OpenMP threads; each chunk starts its odometer from the digits of its first element.
+ * Returns 0, or -1 for a rank outside 0..QXO_MAX_RANK.
+ */
+int qxo_permute_copy(const double* src, double* dst, int rank, const int64_t* dims,
+                     const int64_t* strides) {
+    if (rank < 0 || rank > QXO_MAX_RANK) return -1;
+    const cplx* s = (const cplx*)src;
+    cplx* d = (cplx*)dst;
+    if (rank == 0) { d[0] = s[0]; return 0; }
+    const int64_t total = prod_dims(rank, dims);
+    if (total <= 0) return 0;
+    const int last = rank - 1;
+    const int64_t inner = dims[last], sin = strides[last];
+    const int64_t rows = total / inner;
+    const int64_t nchunks = rows >= 1024 ? 512 : 1;
+    const int64_t rpc = (rows + nchunks - 1) / nchunks;
+#ifdef _OPENMP
+    #pragma omp parallel for schedule(dynamic, 1) if (nchunks > 1)
+#endif
+    for (int64_t ch = 0; ch < nchunks; ch++) {
+        const int64_t r0 = ch * rpc, r1 = (r0 + rpc < rows) ? r0 + rpc : rows;
+        if (r0 >= r1) continue;
+        int64_t idx[QXO_MAX_RANK];
+        int64_t off = 0;
+        { int64_t rem = r0; for (int k = last - 1; k >= 0; k--) { idx[k] = rem % dims[k]; rem /= dims[k]; off += idx[k] * strides[k]; } }
+        for (int64_t r = r0; r < r1; r++) {
+            cplx* o = d + r * inner;
+            const cplx* p = s + off;
+            if (sin == 1) memcpy(o, p, sizeof(cplx) * (size_t)inner);
+            else for (int64_t i = 0; i < inner; i++) o[i] = p[i * sin];
+            for (int k = last - 1; k >= 0; k--) {   /* odometer over the outer axes */
+                idx[k]++; off += strides[k];
+                if (idx[k] < dims[k]) break;
+                off -= strides[k] * dims[k]; idx[k] = 0;
+            }
+        }
+    }
+    return 0;
+}

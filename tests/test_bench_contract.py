@@ -1,7 +1,8 @@
 """bench.py's reference arm on the host cores: the JSON line it prints and its rank behaviour.
 
-The reference arm times the FP64 CPU restatement of the reference's contraction path (the oracle)
-on a bounded sample of the default workload; it needs no GPU, so its output contract is checked
+The reference arm times the reference's CPU contraction arithmetic restated in FP64 (permute +
+OpenBLAS zgemm per ncon, oracle/blas_walk.py) on a bounded sample of the default workload; it
+needs no GPU, so its output contract is checked
 here: one JSON line with the metric, value, unit, the cpu_baseline description and an e2e block
 without host-device traffic.  Under several ranks only rank 0 works and prints.
 """
@@ -37,6 +38,7 @@ def test_reference_arm_prints_the_contract_line():
     assert d["config"]["workload"] == "rqc_5x5_d12_open6"
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert "zgemm" in cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
