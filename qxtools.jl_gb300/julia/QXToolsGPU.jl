@@ -11,8 +11,11 @@ or passed in as a Dict{String,Array{ComplexF64}} (e.g. loaded from the reference
 """
 module QXToolsGPU
 
+import ChainRulesCore
+using ChainRulesCore: NoTangent, ZeroTangent, AbstractZero, unthunk
+
 export QxgProgram, parse_qx, load_qx, read_bitstrings, qxrun, plan_contraction, amplitudes,
-       single_amplitude
+       single_amplitude, set_leaves!, gradient
 
 const libqxgpu = joinpath(@__DIR__, "..", "_build", "libqxgpu.so")
 
@@ -36,6 +39,9 @@ mutable struct QxgProgram
     nqubits::Int
     output_size::Int
     num_slices::Int
+    keys::Vector{String}            # data keys, numbered by first `load`
+    data_dims::Vector{Vector{Int}}  # dims of each data key's leaf
+    load_data::Vector{Int}          # data key (1-based) of each `load` command, in programme order
 end
 
 last_error() = unsafe_string(ccall((:qxg_last_error, libqxgpu), Cstring, ()))
@@ -75,11 +81,14 @@ the dims of its `load` line.
 function load_qx(qx_file::String, data::AbstractDict; precision::Symbol=:fp64, device::Int=0)
     instrs, labs, dkeys, rank, dims, nq = parse_qx(read(qx_file, String))
     arrays = [ComplexF64.(vec(data[k])) for k in dkeys]
+    ddims = Vector{Int}[]
     off = 0
     for (i, x) in enumerate(arrays)
-        n = prod(dims[off+1:off+rank[i]]; init=1); off += rank[i]
+        push!(ddims, Int.(dims[off+1:off+rank[i]])); off += rank[i]
+        n = prod(ddims[i]; init=1)
         length(x) == n || error("data key $(dkeys[i]) has $(length(x)) elements, its load line wants $n")
     end
+    loads = [Int(I.a) + 1 for I in instrs if I.op == 1]   # QXG_OP_LOAD
     opts = Ref(QxgOptions(PREC[precision], device, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 5)))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:qxg_program_create, libqxgpu), Cint,
@@ -93,7 +102,7 @@ function load_qx(qx_file::String, data::AbstractDict; precision::Symbol=:fp64, d
     info = zeros(UInt8, 128)                  # qxg_program_info: num_slices, output_size first
     check(ccall((:qxg_program_info_get, libqxgpu), Cint, (Ptr{Cvoid}, Ptr{UInt8}), h[], info))
     ns, osz = reinterpret(Int64, info[1:16])
-    p = QxgProgram(h[], nq, osz, ns)
+    p = QxgProgram(h[], nq, osz, ns, dkeys, ddims, loads)
     finalizer(p) do p
         ccall((:qxg_program_destroy, libqxgpu), Cvoid, (Ptr{Cvoid},), p.handle)
     end
@@ -204,11 +213,95 @@ function plan_contraction(tensor_labels::AbstractVector, log2dims::AbstractVecto
 end
 
 """
+    set_leaves!(p, leaves)
+
+Replace the programme's leaf data (`qxg_program_set_data`): `leaves[i]` is the tensor of data key
+`p.keys[i]`, with `prod(p.data_dims[i])` elements (column-major, as Julia stores it).
+"""
+function set_leaves!(p::QxgProgram, leaves::AbstractVector{<:AbstractArray})
+    length(leaves) == length(p.keys) || error("$(length(leaves)) leaves for $(length(p.keys)) data keys")
+    for (i, x) in enumerate(leaves)
+        v = ComplexF64.(vec(x))
+        length(v) == prod(p.data_dims[i]; init=1) ||
+            error("leaf $i ($(p.keys[i])) has $(length(v)) elements, its load line wants $(prod(p.data_dims[i]; init=1))")
+        check(ccall((:qxg_program_set_data, libqxgpu), Cint, (Ptr{Cvoid}, Int32, Ptr{ComplexF64}, Int64),
+                    p.handle, i - 1, v, length(v)))
+    end
+    p
+end
+
+"""
+    gradient(p, bitstrings; amp_bar=nothing, slices=0:p.num_slices-1) -> (amps, leaf_grads)
+
+Reverse-mode pass of the programme (`qxg_gradient`): the amplitudes (output_size x n) and, per
+data key, dL/d conj(leaf) with the leaf's dims, summed over every `load` of that key.
+`amp_bar[:, j]` is dL/d conj(amplitude) for bitstring j; `nothing` means L = sum |amplitude|^2
+(then the slice range must fit one slice batch of the programme).
+"""
+function gradient(p::QxgProgram, bitstrings::AbstractVector{<:AbstractString}; amp_bar=nothing,
+                  slices::UnitRange{Int}=0:p.num_slices-1)
+    n = length(bitstrings)
+    buf = Vector{UInt8}(join(bitstrings))
+    out = Matrix{ComplexF64}(undef, p.output_size, n)
+    sizes = [prod(d; init=1) for d in p.data_dims]
+    grads = Vector{ComplexF64}(undef, max(1, sum((sizes[d] for d in p.load_data); init=0)))
+    ab = amp_bar === nothing ? nothing : Matrix{ComplexF64}(reshape(amp_bar, p.output_size, n))
+    check(ccall((:qxg_gradient, libqxgpu), Cint,
+                (Ptr{Cvoid}, Ptr{UInt8}, Int32, Int64, Int64, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                p.handle, buf, n, first(slices), last(slices) + 1,
+                ab === nothing ? Ptr{ComplexF64}(C_NULL) : ab, out, grads))
+    dleaf = [zeros(ComplexF64, sizes[i]) for i in eachindex(sizes)]
+    off = 0
+    for d in p.load_data                      # one block per `load`, in programme order
+        dleaf[d] .+= view(grads, off+1:off+sizes[d]); off += sizes[d]
+    end
+    out, [reshape(dleaf[i], p.data_dims[i]...) for i in eachindex(dleaf)]
+end
+
+"""
+    amplitudes(p, leaves, bitstrings; slices) -> Matrix{ComplexF64}
+
+The amplitudes with the leaf tensors as an argument (`set_leaves!`, then `amplitudes`), so that
+automatic differentiation reaches them: its `ChainRulesCore.rrule` pulls the amplitudes'
+cotangent back through `qxg_gradient`, and the gate angles of a parametrised circuit get their
+gradients through whatever Julia code builds `leaves` from them.
+"""
+function amplitudes(p::QxgProgram, leaves::AbstractVector{<:AbstractArray},
+                    bitstrings::AbstractVector{<:AbstractString}; slices::UnitRange{Int}=0:p.num_slices-1)
+    set_leaves!(p, leaves)
+    amplitudes(p, bitstrings; slices=slices)
+end
+
+# ChainRules' cotangent of a complex value z is dL/d(re z) + i dL/d(im z) = 2 dL/d conj(z).
+# qxg_gradient maps dL/d conj(amplitude) to dL/d conj(leaf) linearly, so passing the amplitudes'
+# cotangent as amp_bar returns the leaves' cotangent directly (both sides carry the factor 2).
+function ChainRulesCore.rrule(::typeof(amplitudes), p::QxgProgram, leaves::AbstractVector{<:AbstractArray},
+                              bitstrings::AbstractVector{<:AbstractString};
+                              slices::UnitRange{Int}=0:p.num_slices-1)
+    y = amplitudes(p, leaves, bitstrings; slices=slices)
+    function amplitudes_pullback(ȳ)
+        Δ = unthunk(ȳ)
+        Δ isa AbstractZero && return (NoTangent(), NoTangent(), ZeroTangent(), NoTangent())
+        set_leaves!(p, leaves)                # the handle may have run other leaves since
+        _, g = gradient(p, bitstrings; amp_bar=Δ, slices=slices)
+        dl = [eltype(leaves[i]) <: Real ? real.(reshape(g[i], size(leaves[i]))) : reshape(g[i], size(leaves[i]))
+              for i in eachindex(leaves)]
+        (NoTangent(), NoTangent(), dl, NoTangent())
+    end
+    y, amplitudes_pullback
+end
+
+"""
     single_amplitude(p::QxgProgram, amplitude::String) -> ComplexF64
+    single_amplitude(p::QxgProgram, leaves, amplitude::String) -> ComplexF64
 
 GPU counterpart of `single_amplitude(tnc, plan, amplitude)` (src/simulation.jl:86-91) for a
 programme compiled from the same network and plan (`build_compute_graph` + `generate_dsl_files`).
+The second form takes the leaf tensors and is differentiable in them (through the rrule of
+`amplitudes`).
 """
 single_amplitude(p::QxgProgram, amplitude::String) = amplitudes(p, [amplitude])[1, 1]
+single_amplitude(p::QxgProgram, leaves::AbstractVector{<:AbstractArray}, amplitude::String) =
+    amplitudes(p, leaves, [amplitude])[1, 1]
 
 end # module
