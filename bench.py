@@ -194,7 +194,7 @@ def cpu_baseline(q, oracle, prog, bits, info, seconds: float):
     flops, sec, finished = blas_walk.run_timed(prog, bits[0], seconds)
     rate = flops / max(sec, 1e-9)
     amps = rate / info["flops_per_bitstring"] * out_size
-    sample = (f"one FP64 walk (numpy permute + OpenBLAS zgemm per ncon) of bitstring 0, slice 0 of "
+    sample = (f"one FP64 walk (threaded permute + {blas_walk.blas_name()} zgemm per ncon) of bitstring 0, slice 0 of "
               f"{info['name']} ({'complete' if finished else f'stopped after {sec:.1f} s'}, {flops:.3e} FLOPs "
               f"in {sec:.1f} s); amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per "
               f"bitstring x {out_size} amplitudes per bitstring")
@@ -226,7 +226,8 @@ def run_reference(args):
     wall = time.perf_counter() - t0
     rate = fl_tot / sec_tot
     value = rate / info["flops_per_bitstring"] * out_size
-    sample = (f"each step: one FP64 walk (bitstring k, slice 0; numpy permute + OpenBLAS zgemm per ncon, "
+    sample = (f"each step: one FP64 walk (bitstring k, slice 0; threaded permute + {blas_walk.blas_name()} "
+              f"zgemm per ncon, "
               f"as TensorOperations contracts) stopped after {per:.0f} s ({done} of {args.steps} complete); "
               f"amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per bitstring x "
               f"{out_size} amplitudes")

@@ -102,6 +102,15 @@ def _contiguous(x):
     return out
 
 
+def blas_name() -> str:
+    """numpy's BLAS as its build configuration names it (e.g. "scipy-openblas 0.3.x")."""
+    try:
+        d = np.show_config(mode="dicts")["Build Dependencies"]["blas"]
+        return f"{d.get('name', '?')} {d.get('version', '')}".strip()
+    except Exception:   # older numpy without mode="dicts", or a build without the section
+        return "unknown BLAS"
+
+
 def _leaf(flat, offs, dims_list, i):
     dims = dims_list[i]
     n = int(np.prod(dims)) if len(dims) else 1
