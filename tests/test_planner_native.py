@@ -168,10 +168,9 @@ def test_native_plan_rejects_bad_input(q, gpu_lib, case, msg):
     assert rc == -1 and msg in gpu_lib.qxg_last_error().decode()
 
 
-@pytest.mark.timeout(600)
-def test_planner_under_address_sanitizer(q, tmp_path):
-    """The planner built with AddressSanitizer and UBSan, run on networks with open, batched and
-    sliced labels: no out-of-range access, a complete plan."""
+@pytest.fixture(scope="module")
+def planner_asan(tmp_path_factory):
+    """tests/emu/planner_driver.cpp linked with the planner, built with AddressSanitizer and UBSan."""
     import shutil
     import subprocess
     from pathlib import Path
@@ -179,12 +178,29 @@ def test_planner_under_address_sanitizer(q, tmp_path):
     if gxx is None:
         pytest.skip("no g++")
     root = Path(__file__).resolve().parent.parent
-    exe = tmp_path / "planner"
+    exe = tmp_path_factory.mktemp("planner_asan") / "planner"
     cmd = [gxx, "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer",
            "-I", str(root / "include"), "-x", "c++", str(root / "qxtools.jl_gb300" / "csrc" / "planner.cu"),
            "-x", "c++", str(root / "tests" / "emu" / "planner_driver.cpp"), "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+def _run_planner_asan(exe, path, args):
+    import subprocess
+    r = subprocess.run([str(exe), str(path)] + [str(a) for a in args], capture_output=True, text=True,
+                       timeout=300, env={"ASAN_OPTIONS": "detect_leaks=1", "UBSAN_OPTIONS": "halt_on_error=1"})
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), (path.read_text()[:2000], args,
+                                                                 r.stdout[-2000:], r.stderr[-3000:])
+    return r.stdout
+
+
+@pytest.mark.timeout(600)
+def test_planner_under_address_sanitizer(q, tmp_path, planner_asan):
+    """The planner built with AddressSanitizer and UBSan, run on networks with open, batched and
+    sliced labels: no out-of-range access, a complete plan."""
+    exe = planner_asan
     for (rows, cols, depth, nopen), args in [((3, 4, 8, 2), ["12", "3", "1", "8", "0", "6"]),
                                               ((4, 4, 10, 0), ["16", "4", "2", "0", "3", "0"]),
                                               ((2, 3, 4, 6), ["6", "2", "3", "0", "0", "0"])]:
@@ -206,9 +222,35 @@ def test_planner_under_address_sanitizer(q, tmp_path):
             lines.append(f"{len(ids)} " + " ".join(map(str, ids)))
         path = tmp_path / f"net_{rows}{cols}{depth}.txt"
         path.write_text("\n".join(lines) + "\n")
-        r = subprocess.run([str(exe), str(path)] + args, capture_output=True, text=True, timeout=300,
-                           env={"ASAN_OPTIONS": "detect_leaks=1", "UBSAN_OPTIONS": "halt_on_error=1"})
-        assert r.returncode == 0 and r.stdout.strip().endswith("ok"), (r.stdout[-2000:], r.stderr[-3000:])
+        _run_planner_asan(exe, path, args)
+
+
+@pytest.mark.timeout(600)
+def test_planner_random_networks_under_address_sanitizer(tmp_path, planner_asan):
+    """Seeded random hypergraphs through the sanitizer build: 1-40 tensors, labels held by one
+    to four tensors (hyper-indices), dimensions 2 and 4, open and batched flags, width targets
+    that force slicing, and disconnected parts.  Every plan must be complete and in range."""
+    rng = np.random.default_rng(7)
+    for case in range(40):
+        V = int(rng.integers(1, 41))
+        E = int(rng.integers(1, 2 * V + 3))
+        pins = [set() for _ in range(V)]
+        for l in range(E):
+            for v in rng.choice(V, size=min(V, int(rng.integers(1, 5))), replace=False):
+                pins[int(v)].add(l)
+        w = rng.choice([1, 1, 1, 2], size=E)
+        open_ = (rng.random(E) < 0.1).astype(int)
+        batched = (rng.random(V) < 0.2).astype(int)
+        lines = [f"{V} {E}", " ".join(map(str, w)), " ".join(map(str, open_)), " ".join(map(str, batched))]
+        for v in range(V):
+            ls = sorted(pins[v])
+            lines.append(f"{len(ls)} " + " ".join(map(str, ls)))
+        path = tmp_path / f"rand_{case}.txt"
+        path.write_text("\n".join(lines) + "\n")
+        max_log2 = [0, 6, 10][case % 3]
+        args = [int(rng.integers(1, 9)), int(rng.integers(-1, 5)), case, max_log2, case % 4 // 3,
+                [0, 6][case % 2]]
+        _run_planner_asan(planner_asan, path, args)
 
 
 def test_native_planned_workloads_build(q, gpu_lib):
