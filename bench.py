@@ -183,11 +183,11 @@ def traffic_summary(workload: str, kernel: str, precision: str):
 
 
 # --------------------------------------------------------------------------------------------
-def cpu_baseline(q, oracle, prog, bits, info, seconds: float):
+def cpu_baseline(prog, bits, info, seconds: float):
     """The reference's CPU arithmetic restated (oracle/blas_walk.py: permute + OpenBLAS zgemm per
     ncon, as TensorOperations contracts) on a bounded sample: one bitstring's walk for one slice
     with BLAS on every host thread, stopped after `seconds`; the FLOP rate is converted to
-    amplitudes/s with the programme's FLOPs per bitstring.  `oracle` is unused (kept for callers)."""
+    amplitudes/s with the programme's FLOPs per bitstring."""
     from oracle import blas_walk
     cores = blas_walk.blas_threads()
     out_size = info["amplitudes_per_bitstring"]
@@ -275,7 +275,6 @@ def run_ours(args):
     if not lib_path.exists():
         entry._load_build_module().build()
     q = entry.load()
-    from oracle import oracle
     prog, bits, info = q.workloads.build_workload(args.workload, seed=args.seed, plan_seed=args.plan_seed,
                                                   planner=args.planner)
     # default batch: the whole list for the Complex64 paths, 16 bitstrings for the slower FP64 path
@@ -422,7 +421,7 @@ def run_ours(args):
         line["max_rel_err_vs_fp64"] = float(abs(got - ref64).max() / abs(ref64).max())
         ex64.close()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(q, oracle, prog, bits, info, args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(prog, bits, info, args.cpu_seconds)
     ex.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

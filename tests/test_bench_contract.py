@@ -46,3 +46,15 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = _run({"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"})
     assert r.returncode == 0, r.stderr[-2000:]
     assert not [x for x in r.stdout.splitlines() if x.startswith("{")]
+
+
+def test_cpu_baseline_leg_of_the_gpu_arm(q):
+    """The `cpu_baseline` object the GPU arm adds to its line (rank 0, one GPU), computed on the
+    host alone for a small sliced workload: a complete walk, a positive rate, the BLAS named."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    prog, bits, info = q.workloads.build_workload("rqc_3x4_d8_s3")
+    cb = bench.cpu_baseline(prog, bits, info, 30.0)
+    assert cb["kind"] == "port" and cb["unit"] == bench.UNIT and cb["cores"] >= 1
+    assert cb["value"] > 0 and cb["gflops"] > 0
+    assert "complete" in cb["sample"] and "zgemm" in cb["sample"]
