@@ -75,7 +75,8 @@ def _oracle_lib():
 
 def _contiguous(x):
     """x (any strided complex128 view) copied into C order by the threaded gather.  Axes of size
-    1 are dropped and neighbours that are already contiguous in x are merged first."""
+    1 are dropped, neighbours that are already contiguous in x are merged, and merged runs longer
+    than 64 elements are split into pieces of 64 first."""
     if x.flags.c_contiguous:
         return x
     if x.size < _GATHER_MIN:
@@ -91,6 +92,19 @@ def _contiguous(x):
         else:
             dims.append(n)
             strides.append(st)
+    # long runs are split into pieces of 64 so that the gather's tiles stay small and many
+    sd, ss = [], []
+    for n, st in zip(dims, strides):
+        parts = []
+        while n > 64 and n % 64 == 0:
+            parts.append((64, st))
+            n //= 64
+            st *= 64
+        parts.append((n, st))
+        for n2, st2 in reversed(parts):
+            sd.append(n2)
+            ss.append(st2)
+    dims, strides = sd, ss
     out = np.empty(x.shape, dtype=np.complex128)
     d = np.array(dims, dtype=np.int64)
     s = np.array(strides, dtype=np.int64)

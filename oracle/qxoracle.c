@@ -368,10 +368,14 @@ int qxo_max_threads(void) {
  * Permute-copy for the BLAS walk (blas_walk.py), the step TensorOperations performs with
  * Strided.jl's threaded permutedims before each GEMM: dst is written contiguously, last axis
  * fastest (numpy's C order), dims[0..rank-1]; element i of dst reads src at sum_k idx_k *
- * strides[k] (complex elements, not bytes).  Contiguous chunks of dst are spread over the
- * OpenMP threads; each chunk starts its odometer from the digits of its first element.
+ * strides[k] (complex elements, not bytes).
+ * Cache blocking, as blocked tensor transposes do: the last dst axes (up to QXO_TILE elements,
+ * contiguous in dst) and the smallest-stride src axes among the others (up to QXO_TILE elements,
+ * near-contiguous in src) form a tile that stays in L1 while it is read along src and written
+ * along dst.  The remaining axes enumerate the tiles, which are spread over the OpenMP threads.
  * Returns 0, or -1 for a rank outside 0..QXO_MAX_RANK.
  */
+#define QXO_TILE 32
 int qxo_permute_copy(const double* src, double* dst, int rank, const int64_t* dims,
                      const int64_t* strides) {
     if (rank < 0 || rank > QXO_MAX_RANK) return -1;
@@ -380,31 +384,55 @@ int qxo_permute_copy(const double* src, double* dst, int rank, const int64_t* di
     if (rank == 0) { d[0] = s[0]; return 0; }
     const int64_t total = prod_dims(rank, dims);
     if (total <= 0) return 0;
-    const int last = rank - 1;
-    const int64_t inner = dims[last], sin = strides[last];
-    const int64_t rows = total / inner;
-    const int64_t nchunks = rows >= 1024 ? 512 : 1;
-    const int64_t rpc = (rows + nchunks - 1) / nchunks;
+    int64_t dstr[QXO_MAX_RANK];            /* dst strides of the C-order layout */
+    { int64_t st = 1; for (int k = rank - 1; k >= 0; k--) { dstr[k] = st; st *= dims[k]; } }
+    /* D: trailing dst axes; S: smallest-stride src axes among the rest; O: the others */
+    char role[QXO_MAX_RANK];               /* 'D', 'S' or 'O' */
+    int64_t PD = 1, PS = 1;
+    for (int k = 0; k < rank; k++) role[k] = 'O';
+    for (int k = rank - 1; k >= 0 && PD * dims[k] <= QXO_TILE; k--) { role[k] = 'D'; PD *= dims[k]; }
+    if (PD == 1) { role[rank - 1] = 'D'; PD = dims[rank - 1]; }   /* a long last axis is a tile row */
+    for (;;) {
+        int best = -1;
+        for (int k = 0; k < rank; k++)
+            if (role[k] == 'O' && PS * dims[k] <= QXO_TILE && (best < 0 || strides[k] < strides[best])) best = k;
+        if (best < 0) break;
+        role[best] = 'S'; PS *= dims[best];
+    }
+    int od[QXO_MAX_RANK], no = 0, sd[QXO_MAX_RANK], ns = 0, dd[QXO_MAX_RANK], nd = 0;
+    for (int k = 0; k < rank; k++) {
+        if (role[k] == 'O') od[no++] = k;
+        else if (role[k] == 'S') sd[ns++] = k;
+        else dd[nd++] = k;
+    }
+    /* offsets of the tile's S combinations (src and dst) and D combinations (src; dst is 0..PD-1) */
+    int64_t* sofS = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * PS + PD));
+    if (!sofS) return -2;
+    int64_t* dofS = sofS + PS;
+    int64_t* sofD = dofS + PS;
+    for (int64_t i = 0; i < PS; i++) {
+        int64_t rem = i, so = 0, doff = 0;
+        for (int j = ns - 1; j >= 0; j--) { const int k = sd[j]; const int64_t x = rem % dims[k]; rem /= dims[k]; so += x * strides[k]; doff += x * dstr[k]; }
+        sofS[i] = so; dofS[i] = doff;
+    }
+    for (int64_t i = 0; i < PD; i++) {
+        int64_t rem = i, so = 0;
+        for (int j = nd - 1; j >= 0; j--) { const int k = dd[j]; so += (rem % dims[k]) * strides[k]; rem /= dims[k]; }
+        sofD[i] = so;
+    }
+    const int64_t ntiles = total / (PS * PD);
 #ifdef _OPENMP
-    #pragma omp parallel for schedule(dynamic, 1) if (nchunks > 1)
+    #pragma omp parallel for schedule(static) if (ntiles >= 64)
 #endif
-    for (int64_t ch = 0; ch < nchunks; ch++) {
-        const int64_t r0 = ch * rpc, r1 = (r0 + rpc < rows) ? r0 + rpc : rows;
-        if (r0 >= r1) continue;
-        int64_t idx[QXO_MAX_RANK];
-        int64_t off = 0;
-        { int64_t rem = r0; for (int k = last - 1; k >= 0; k--) { idx[k] = rem % dims[k]; rem /= dims[k]; off += idx[k] * strides[k]; } }
-        for (int64_t r = r0; r < r1; r++) {
-            cplx* o = d + r * inner;
-            const cplx* p = s + off;
-            if (sin == 1) memcpy(o, p, sizeof(cplx) * (size_t)inner);
-            else for (int64_t i = 0; i < inner; i++) o[i] = p[i * sin];
-            for (int k = last - 1; k >= 0; k--) {   /* odometer over the outer axes */
-                idx[k]++; off += strides[k];
-                if (idx[k] < dims[k]) break;
-                off -= strides[k] * dims[k]; idx[k] = 0;
-            }
+    for (int64_t t = 0; t < ntiles; t++) {
+        int64_t rem = t, sb = 0, db = 0;
+        for (int j = no - 1; j >= 0; j--) { const int k = od[j]; const int64_t x = rem % dims[k]; rem /= dims[k]; sb += x * strides[k]; db += x * dstr[k]; }
+        for (int64_t i = 0; i < PS; i++) {
+            const cplx* p = s + sb + sofS[i];
+            cplx* o = d + db + dofS[i];
+            for (int64_t j = 0; j < PD; j++) o[j] = p[sofD[j]];
         }
     }
+    free(sofS);
     return 0;
 }
