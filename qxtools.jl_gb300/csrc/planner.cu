@@ -939,8 +939,11 @@ extern "C" int qxg_plan_contraction(int32_t ntensors, const int64_t* label_off, 
         for (int l = 0; l < n.E; l++)
             if (n.w[l] < 0 || n.w[l] > 16) return qxg::ncon_fail(QXG_ERR_INVALID, "qxg_plan_contraction: label log2 dimension outside 0..16");
         if (label_off[0] < 0) return qxg::ncon_fail(QXG_ERR_INVALID, "qxg_plan_contraction: negative label offset");
-        for (int v = 0; v < n.V; v++) {
+        // every offset first: labels are then read only within [label_off[0], label_off[V]),
+        // the extent the caller declares for its array
+        for (int v = 0; v < n.V; v++)
             if (label_off[v + 1] < label_off[v]) return qxg::ncon_fail(QXG_ERR_INVALID, "qxg_plan_contraction: label offsets decrease");
+        for (int v = 0; v < n.V; v++) {
             for (int64_t p = label_off[v]; p < label_off[v + 1]; p++) {
                 const int l = labels[p];
                 if (l < 0 || l >= n.E) return qxg::ncon_fail(QXG_ERR_INVALID, "qxg_plan_contraction: label id out of range");
