@@ -88,7 +88,13 @@ typedef struct qxg_options {
                                      N tile; then narrower tiles, then the X-planes variants) */
     int32_t tc_plane_budget_mb;   /* packed planes of a tensor-core step's smaller operand beyond which
                                      its free columns are processed in blocks; 0 = 4096 MiB */
-    int32_t reserved[5];
+    int32_t tc_wait_limit;        /* polls before a tensor-core kernel's bounded wait gives up (0: 2^20).
+                                     A wait that gives up ends the call with QXG_ERR_TIMEOUT; the waits
+                                     for copies and MMAs already in flight keep the full limit */
+    int32_t tc_stall_test;        /* test hook, leave 0: nonzero makes the first CTA of every
+                                     tensor-core GEMM issue no operand copies, so its waits run out and
+                                     the call returns QXG_ERR_TIMEOUT (exercises the timeout path) */
+    int32_t reserved[3];
 } qxg_options;
 
 typedef struct qxg_program qxg_program;

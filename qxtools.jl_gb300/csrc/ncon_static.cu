@@ -3,11 +3,13 @@
 // Some callers cannot call cudaMalloc: code that runs while a CUDA graph is being captured,
 // hosts whose device allocator belongs to another runtime, allocation-free real-time loops.  For
 // them this entry point keeps its scratch -- the packed hi/lo operand planes and three exponent
-// slots -- in one file-scope device array of QXG_TC_STATIC_SCRATCH_BYTES.  Host code may not use
-// the array's name as a device address; the address is looked up once per device with
-// cudaGetSymbolAddress (on the first call made with that device current).  Shapes whose planes
-// do not fit are rejected.  All calls on a device share the array; it keeps the last call's
-// contents, and calls that overlap on one GPU race.
+// slots and a timeout word -- in one file-scope device array of QXG_TC_STATIC_SCRATCH_BYTES.
+// Host code may not use the array's name as a device address; the address is looked up once per
+// device with cudaGetSymbolAddress (on the first call made with that device current).  Shapes
+// whose planes do not fit are rejected.  All calls on a device share the array; it keeps the last
+// call's contents, and calls that overlap on one GPU race.  The GEMM's bounded waits report to the
+// timeout word in the array's header (not to the word programme walks read), so a call outside
+// stream capture waits for its stream and returns QXG_ERR_TIMEOUT when a wait gave up.
 #include <mutex>
 #include <string>
 
@@ -24,7 +26,8 @@ int ncon_build_args(StepArgs* s, int32_t nc, const int32_t* lc, int32_t na, cons
 namespace {
 
 constexpr size_t kStaticBytes = (size_t)QXG_TC_STATIC_SCRATCH_BYTES;
-constexpr size_t kExpBytes = 256;   // exponent slots (A, B, C) at the start of the array
+constexpr size_t kExpBytes = 256;   // header: exponent slots (A, B, C) and the timeout word
+constexpr size_t kErrWord = 32;     // int index of the timeout word in the header (byte 128)
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
@@ -76,8 +79,10 @@ extern "C" int qxg_ncon_tc_static(int32_t precision, void* C, int32_t nc, const 
     int cbits = 0;
     while ((int64_t(1) << cbits) < s.nC) cbits++;
     TcStep t;
+    // the Y planes are cut into outer column blocks before they outgrow the array (partial sums
+    // of a split K come on top; the size check below has the final word)
     if (!tc_plan_step(s, (size_t)bits_of(a_dims, na), (size_t)bits_of(b_dims, nb), (size_t)cbits,
-                      precision == QXG_PREC_SPLIT_TF32, &t))
+                      precision == QXG_PREC_SPLIT_TF32, &t, (double)((kStaticBytes - kExpBytes) / 4)))
         return ncon_fail(QXG_ERR_UNSUPPORTED,
                          "qxg_ncon_tc_static: shape not served by the tensor cores (needs >= 128 free rows on the "
                          "larger operand, or >= 16 with a summed extent above 1024, a summed extent >= 8 and "
@@ -96,10 +101,28 @@ extern "C" int qxg_ncon_tc_static(int32_t precision, void* C, int32_t nc, const 
     if (int r = static_scratch(dev, &base)) return r;
     int* exps = static_cast<int*>(base);
     void* planes = static_cast<unsigned char*>(base) + kExpBytes;
+    t.err_word = exps + kErrWord;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // exponent slots start at zero: operands enter unscaled and the result is stored as is
+    // the header starts at zero: exponent slots at 0 (operands enter unscaled, the result is
+    // stored as is) and no timeout
     e = cudaMemsetAsync(exps, 0, kExpBytes, st);
     if (e == cudaSuccess) e = tc_run_step(t, s, exps, planes, st, sms, nullptr);
     if (e != cudaSuccess) return ncon_fail(QXG_ERR_CUDA, cudaGetErrorString(e));
+    // outside stream capture, wait for the call and report a wait that gave up; under capture
+    // nothing can be read back, and a replay that timed out leaves its code in the header
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+        cudaGetLastError();             // a query refused during another stream's capture
+        return QXG_OK;
+    }
+    if (cap != cudaStreamCaptureStatusNone) return QXG_OK;
+    int code = 0;
+    e = cudaMemcpyAsync(&code, t.err_word, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return ncon_fail(QXG_ERR_CUDA, cudaGetErrorString(e));
+    if (code) {
+        std::string m = "qxg_ncon_tc_static: a tensor-core wait gave up (code " + std::to_string(code) + ")";
+        return ncon_fail(QXG_ERR_TIMEOUT, m.c_str());
+    }
     return QXG_OK;
 }

@@ -163,6 +163,7 @@ struct qxg_program {
     size_t scratch_cap = 0;
     int* d_exps = nullptr;
     int nslots = 0;
+    int* d_tc_err = nullptr;            // code of a tensor-core wait that gave up (0: none)
     PassParams* d_params = nullptr;
     PassParams* h_params = nullptr;     // pinned, one per pass
     size_t h_params_cap = 0;
@@ -472,6 +473,10 @@ std::vector<int64_t> leaf_offsets(const qxg_program* P, int64_t* total) {
 // tc_tuning = k >= 1: candidate k-1 of every tensor-core step (the last one where a step has
 // fewer), chosen at plan time; 0 leaves the choice to the autotuner.
 void tc_fix_variant(const qxg_program* P, Step& st) {
+    // the programme's own timeout word, and the options' test hooks for the bounded waits
+    st.tc.err_word = P->d_tc_err;
+    st.tc.wait_limit = P->opts.tc_wait_limit > 0 ? (uint32_t)P->opts.tc_wait_limit : 0;
+    st.tc.stall_first_cta = P->opts.tc_stall_test != 0;
     if (P->opts.tc_tuning <= 0) return;
     TcVariant cand[kTcMaxVariants];
     const int nc = tc_variants(st.tc, cand);
@@ -1688,7 +1693,7 @@ int check_tc_plan(qxg_program* P, const Plan* pl) {
     for (auto& st : pl->bsteps) any = any || st.use_tc;
     if (!any) return 0;
     int code = 0;
-    QXG_CUDA(tc_read_error(&code, P->stream));
+    QXG_CUDA(tc_read_error(&code, P->d_tc_err, P->stream));
     if (code) return fail(QXG_ERR_TIMEOUT, "a tensor-core kernel gave up waiting (code " + std::to_string(code) + ")");
     return 0;
 }
@@ -1766,6 +1771,8 @@ int qxg_program_create(const qxg_instr* instrs, int32_t ninstr, const int32_t* l
     QXG_CUDA(cudaDeviceGetAttribute(&P->sm_count, cudaDevAttrMultiProcessorCount, P->device));
     QXG_CUDA(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
     QXG_CUDA(cudaMalloc(&P->d_params, sizeof(PassParams)));
+    QXG_CUDA(cudaMalloc(&P->d_tc_err, sizeof(int)));
+    QXG_CUDA(cudaMemset(P->d_tc_err, 0, sizeof(int)));
     P->d_data.assign(ndata, nullptr);
     P->data_m.assign(ndata, 0);
     P->data_set.assign(ndata, false);
@@ -2109,6 +2116,7 @@ void qxg_program_destroy(qxg_program* P) {
         if (e) cudaEventDestroy(e);
     if (P->d_scratch) cudaFree(P->d_scratch);
     if (P->d_exps) cudaFree(P->d_exps);
+    if (P->d_tc_err) cudaFree(P->d_tc_err);
     if (P->d_params) cudaFree(P->d_params);
     if (P->h_params) cudaFreeHost(P->h_params);
     if (P->d_bits) cudaFree(P->d_bits);

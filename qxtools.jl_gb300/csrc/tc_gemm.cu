@@ -94,6 +94,9 @@ struct GemmArgs {
     uint32_t idesc;
     int exp_c;
     int* exps;
+    uint32_t wait_limit;    // mbarrier polls before a wait gives up
+    int stall;              // test hook: CTA 0's operand producer issues nothing (its waits run out)
+    int* err;               // word a wait that gives up writes its code to (nullptr: g_tc_error)
 };
 
 __device__ __forceinline__ int read_m(const int* exps, int slot) {
@@ -242,8 +245,8 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 // Bounded wait for the phase with the given parity; false when it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; i++)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
+    for (uint32_t i = 0; i < limit; i++)
         if (mbar_try(bar, parity)) return true;
     return false;
 }
@@ -427,6 +430,8 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
     constexpr bool SEGS = MODE == kModeBulk || MODE == kModeTma;     // loader warp 6 + split warps 7-10
     constexpr int KC = TF32 ? 8 : 16;            // complex k per 64-byte chunk
     constexpr int SPLIT0 = SEGS ? 224 : 192;   // first thread of the split warps
+    int* const errw = g.err ? g.err : &g_tc_error;
+    const uint32_t wl = g.wait_limit ? g.wait_limit : kWaitLimit;
     extern __shared__ uint8_t smem_raw[];
     // fullB[NS] (bulk bytes of a stage), fullA[NS] (fused: the four split warps), empty[NS],
     // accf[2], acce[2], drain (the MMA thread's last commit)
@@ -515,14 +520,16 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         int s = 0;                          // stage and its phase parity, advanced per chunk
         uint32_t ph = 0;
         int64_t issued = 0;
-        for (int64_t i = 0; i < ntl; i++) {
+        // test hook: CTA 0 issues no copies, so the MMA issuer's first wait runs out
+        const bool stall = g.stall != 0 && blockIdx.x == 0;
+        for (int64_t i = 0; i < (stall ? 0 : ntl); i++) {
             int64_t b, mt, nt;
             tile_of(i, b, mt, nt);
             const int64_t a_tile0 = (b * g.mtiles + mt) * g.kchunks;
             const int64_t b_tile0 = (b * g.ntiles + nt) * g.kchunks;
             bool stop = false;
             for (int64_t c = 0; c < g.kchunks; c++) {
-                if (!mbar_wait(&empty[s], ph ^ 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 1); stop = true; break; }
+                if (!mbar_wait(&empty[s], ph ^ 1u, wl)) { atomicExch(&abort_flag, 1); atomicExch(errw, 1); stop = true; break; }
                 if (*(volatile int*)&abort_flag) { stop = true; break; }
                 uint8_t* st = smem + s * stage_bytes;
                 mbar_expect_tx(&fullB[s], FUSED ? 2u * g.b_tile_bytes : stage_bytes);
@@ -541,7 +548,7 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         }
         // copies still in flight (only after an abort) must land before the CTA leaves
         for (int64_t q = issued - 1; q >= 0 && q >= issued - NS; q--)
-            mbar_wait(&fullB[q % NS], (uint32_t)((q / NS) & 1));
+            mbar_wait(&fullB[q % NS], (uint32_t)((q / NS) & 1));   // full limit: copies must land
     } else if (warp == 1 && lane == 0) {
         // MMA issuer: per tile, into accumulator buffer i & 1 once the epilogue has drained it
         int s = 0;
@@ -549,13 +556,13 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         for (int64_t i = 0; i < ntl; i++) {
             const uint32_t buf = (uint32_t)(i % nbuf);
             const uint32_t use = (uint32_t)(i / nbuf);
-            if (!mbar_wait(&acce[buf], (use & 1u) ^ 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 5); break; }
+            if (!mbar_wait(&acce[buf], (use & 1u) ^ 1u, wl)) { atomicExch(&abort_flag, 1); atomicExch(errw, 5); break; }
             fence_after();
             const uint32_t d = tmem + buf * acc_cols;
             bool stop = false;
             for (int64_t c = 0; c < g.kchunks; c++) {
-                if (!mbar_wait(&fullB[s], ph) || (FUSED && !mbar_wait(&fullA[s], ph))) {
-                    atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 2); stop = true; break;
+                if (!mbar_wait(&fullB[s], ph, wl) || (FUSED && !mbar_wait(&fullA[s], ph, wl))) {
+                    atomicExch(&abort_flag, 1); atomicExch(errw, 2); stop = true; break;
                 }
                 fence_after();
                 const uint32_t st = smem_u32(smem + s * stage_bytes);
@@ -588,7 +595,7 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         }
         // the MMAs must have finished before the tensor memory is freed
         mma_commit(drain);
-        mbar_wait(drain, 0);
+        mbar_wait(drain, 0);                // full limit: the MMAs must finish
     } else if (ROWS && warp >= 6) {
         // X producers: thread r gathers row r of every (tile, chunk) with 8-byte cp.async into a
         // ring of R raw chunks ([R][KC][128 rows], R - 1 chunks in flight ahead of the one being
@@ -599,7 +606,7 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         const int R = g.ring_chunks;
         bool ntl_guard = false;
         if (R != 2 && R != 4 && R != 8) {   // the host guarantees it; never index past the ring
-            if (lane == 0) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 8); }
+            if (lane == 0) { atomicExch(&abort_flag, 1); atomicExch(errw, 8); }
             ntl_guard = true;
         }
         float2* ring = reinterpret_cast<float2*>(smem + NS * stage_bytes);
@@ -650,9 +657,9 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         for (int64_t qq = 0; qq < Q; qq++) {
             issue();
             if (R == 8) cp_async_wait<7>(); else if (R == 4) cp_async_wait<3>(); else cp_async_wait<1>();
-            const bool ok = mbar_wait(&empty[st_i], ph ^ 1u);
+            const bool ok = mbar_wait(&empty[st_i], ph ^ 1u, wl);
             // leave the loop as a whole warp (the __syncwarp below needs every lane)
-            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 4); break; }
+            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(errw, 4); break; }
             if (__any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) break;
             uint8_t* st = smem + st_i * stage_bytes;
             const float2* raw = ring + slot * (KC * kTcTileM) + row;
@@ -701,7 +708,7 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         const int64_t Q = ntl * g.kchunks;
         if (lane == 0) {
             for (int64_t qq = 0; qq < Q; qq++) {
-                if (!mbar_wait(&rempty[slot], ph ^ 1u)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 6); break; }
+                if (!mbar_wait(&rempty[slot], ph ^ 1u, wl)) { atomicExch(&abort_flag, 1); atomicExch(errw, 6); break; }
                 if (*(volatile int*)&abort_flag) break;
                 int co[5] = {0, 0, 0, 0, 0};
                 co[g.tma_outer] = (int)((tbase + pdep(c * KC, g.xk)) >> g.tma_lead);
@@ -716,7 +723,7 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
             }
             // boxes still in flight (only after an abort) must land before the CTA leaves
             for (int64_t q = issued - 1; q >= 0 && q >= issued - R; q--)
-                mbar_wait(&rfull[q % R], (uint32_t)((q / R) & 1));
+                mbar_wait(&rfull[q % R], (uint32_t)((q / R) & 1));     // full limit: copies must land
         }
     } else if (MODE == kModeBulk && warp == 6) {
         // X loader: per (tile, chunk), once the splitters have released the ring slot, fetch the
@@ -738,8 +745,8 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         int64_t issued = 0;
         const int64_t Q = ntl * g.kchunks;
         for (int64_t qq = 0; qq < Q; qq++) {
-            const bool ok = mbar_wait(&rempty[slot], ph ^ 1u);
-            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 6); break; }
+            const bool ok = mbar_wait(&rempty[slot], ph ^ 1u, wl);
+            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(errw, 6); break; }
             if (__any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) break;
             const float2* src = g.X + tbase + pdep(c * KC, g.xk);
             uint8_t* dst = ring + slot * g.slot_bytes;
@@ -756,7 +763,7 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         }
         // segments still in flight (only after an abort) must land before the CTA leaves
         for (int64_t q = issued - 1; q >= 0 && q >= issued - R; q--)
-            mbar_wait(&rfull[q % R], (uint32_t)((q / R) & 1));
+            mbar_wait(&rfull[q % R], (uint32_t)((q / R) & 1));     // full limit: copies must land
     } else if (SEGS && warp >= 7) {
         // splitters: thread r splits row r of each ring slot into the stage's A tiles (bulk) or
         // its tensor-memory A columns (TMA), then releases the slot to the loader and arrives on
@@ -780,8 +787,8 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         while (c >= g.kchunks) c -= g.kchunks;
         const int64_t Q = ntl * g.kchunks;
         for (int64_t qq = grp; qq < Q; qq += NG) {
-            const bool ok = mbar_wait(&rfull[slot], rph) && mbar_wait(&empty[st_i], ph ^ 1u);
-            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 7); break; }
+            const bool ok = mbar_wait(&rfull[slot], rph, wl) && mbar_wait(&empty[st_i], ph ^ 1u, wl);
+            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(errw, 7); break; }
             if (__any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) break;
             uint8_t* st = smem + st_i * stage_bytes;
             const uint8_t* raw = ring + slot * g.slot_bytes + rb;
@@ -820,9 +827,9 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
         for (int64_t i = 0; i < ntl; i++) {
             const uint32_t buf = (uint32_t)(i % nbuf);
             const uint32_t use = (uint32_t)(i / nbuf);
-            const bool ok = mbar_wait(&accf[buf], use & 1u);
+            const bool ok = mbar_wait(&accf[buf], use & 1u, wl);
             fence_after();
-            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(&g_tc_error, 3); break; }
+            if (!__all_sync(0xffffffffu, ok)) { atomicExch(&abort_flag, 1); atomicExch(errw, 3); break; }
             if (__any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) break;
             int64_t b, mt, nt;
             tile_of(i, b, mt, nt);
@@ -1362,6 +1369,9 @@ cudaError_t tc_launch_gemm(const TcStep& t, const StepArgs& s, int* exps, void* 
     g.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((nmma >> 3) << 17) | ((uint32_t)(kTcTileM >> 4) << 24);
     g.exp_c = t.ks > 0 ? -1 : s.expC;
     g.exps = exps;
+    g.wait_limit = t.wait_limit;
+    g.stall = t.stall_first_cta ? 1 : 0;
+    g.err = t.err_word;
     g.X = static_cast<const float2*>(t.x_is_a ? s.A : s.B);
     g.xb = t.xb; g.xm = t.xm; g.xk = t.xk;
     g.K = t.K;
@@ -1449,11 +1459,15 @@ cudaError_t tc_launch_gemm(const TcStep& t, const StepArgs& s, int* exps, void* 
     return cudaGetLastError();
 }
 
-cudaError_t tc_read_error(int* host_code, cudaStream_t st) {
-    int zero = 0;
-    cudaError_t e = cudaMemcpyFromSymbolAsync(host_code, g_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
+cudaError_t tc_read_error(int* host_code, int* d_word, cudaStream_t st) {
+    cudaError_t e = d_word ? cudaMemcpyAsync(host_code, d_word, sizeof(int), cudaMemcpyDeviceToHost, st)
+                           : cudaMemcpyFromSymbolAsync(host_code, g_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) return e;
-    e = cudaMemcpyToSymbolAsync(g_tc_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess || *host_code == 0) return e;
+    const int zero = 0;
+    e = d_word ? cudaMemcpyAsync(d_word, &zero, sizeof(int), cudaMemcpyHostToDevice, st)
+               : cudaMemcpyToSymbolAsync(g_tc_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(st);
 }

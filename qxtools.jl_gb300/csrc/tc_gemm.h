@@ -55,6 +55,12 @@ struct TcStep {
     size_t a_plane_bytes = 0, b_plane_bytes = 0, partial_bytes = 0;
     size_t scratch_bytes = 0;       // 2 planes of A_op (planes variant) + 2 planes of B_op + partials
     size_t scratch_max = 0;         // the largest scratch of any candidate variant
+    // launch controls, not part of the step's shape
+    uint32_t wait_limit = 0;        // mbarrier polls before a wait gives up (0: 2^20)
+    bool stall_first_cta = false;   // test hook: CTA 0's operand producer issues no copies, so its
+                                    // MMA issuer's wait runs out (exercises the timeout path)
+    int* err_word = nullptr;        // device word a wait that gives up writes its code to
+                                    // (nullptr: the library-wide word tc_read_error reads)
 };
 
 // A tile variant of a tensor-core step: X gathered in the GEMM (fused: by rows or by contiguous
@@ -95,7 +101,8 @@ cudaError_t tc_run_gemm(const TcStep& tc, const StepArgs& s, int* exps, void* sc
 cudaError_t tc_run_step(const TcStep& tc, const StepArgs& s, int* exps, void* scratch, cudaStream_t st,
                         int sm_count, int* launches);
 
-// Device error word set by a tensor-core kernel whose bounded wait gave up (0 = none).
-cudaError_t tc_read_error(int* host_code, cudaStream_t st);
+// Read and clear the error word a tensor-core kernel whose bounded wait gave up has set (0 =
+// none): d_word (a TcStep's err_word), or the library-wide word when d_word is null.  Waits for st.
+cudaError_t tc_read_error(int* host_code, int* d_word, cudaStream_t st);
 
 }  // namespace qxg

@@ -43,7 +43,8 @@ class qxg_options(ct.Structure):
     _fields_ = [("precision", ct.c_int32), ("device", ct.c_int32), ("workspace_limit", ct.c_int64),
                 ("max_bitstring_batch", ct.c_int32), ("max_slice_batch", ct.c_int32),
                 ("use_graphs", ct.c_int32), ("tc_tuning", ct.c_int32),
-                ("tc_plane_budget_mb", ct.c_int32), ("reserved", ct.c_int32 * 5)]
+                ("tc_plane_budget_mb", ct.c_int32), ("tc_wait_limit", ct.c_int32), ("tc_stall_test", ct.c_int32),
+                ("reserved", ct.c_int32 * 3)]
 
 
 class qxg_qx_sizes(ct.Structure):
@@ -325,7 +326,8 @@ class Executor:
 
     def __init__(self, programme: Programme, precision: str = "fp64", device: int = 0,
                  workspace_limit: int = 0, max_bitstring_batch: int = 0, max_slice_batch: int = 0,
-                 use_graphs: bool = False, tc_tuning="auto", tc_plane_budget_mb: int = 0):
+                 use_graphs: bool = False, tc_tuning="auto", tc_plane_budget_mb: int = 0,
+                 tc_wait_limit: int = 0, tc_stall_test: bool = False):
         self.lib = load_library()
         self.programme = programme
         self.precision = precision
@@ -337,6 +339,10 @@ class Executor:
         opts.max_slice_batch = max_slice_batch
         opts.use_graphs = int(use_graphs)
         opts.tc_plane_budget_mb = int(tc_plane_budget_mb)
+        # bounded device waits: polls before giving up (0: the library's 2^20), and the test hook
+        # that makes them run out (qxg_options.tc_stall_test)
+        opts.tc_wait_limit = int(tc_wait_limit)
+        opts.tc_stall_test = int(bool(tc_stall_test))
         # "auto": time each tensor-core step's tile variants once and keep the fastest;
         # "fixed" (= 1) or k >= 1: candidate k of every step
         if tc_tuning == "auto":
