@@ -373,7 +373,7 @@ int qxo_max_threads(void) {
  * contiguous in dst) and the smallest-stride src axes among the others (up to QXO_TILE elements,
  * near-contiguous in src) form a tile that stays in L1 while it is read along src and written
  * along dst.  The remaining axes enumerate the tiles, which are spread over the OpenMP threads.
- * Returns 0, or -1 for a rank outside 0..QXO_MAX_RANK.
+ * Returns 0, -1 for a rank outside 0..QXO_MAX_RANK, or -2 when the offset tables cannot be allocated.
  */
 #define QXO_TILE 32
 int qxo_permute_copy(const double* src, double* dst, int rank, const int64_t* dims,

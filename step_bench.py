@@ -9,7 +9,7 @@ times the adjoint of Y instead (the sum over every row of conj(X) and C: a long 
 small result; qxg_ncon does not conjugate, which changes no data movement).  `drop` removes the
 highest row bits to shrink a case (for profiler captures).
 
-    python qxtools.jl_gb300/step_bench.py rqc_1161,rqc_1159s [--drop 0] [--reps 10]
+    python step_bench.py rqc_1161,rqc_1159s [--drop 0] [--reps 10]
 
 Prints one JSON line per case: milliseconds per call and the algorithmic bandwidth
 8 (|X| + |Y| + |C|) bytes / time.
@@ -85,7 +85,7 @@ def main():
     ap.add_argument("cases", help="comma-separated case names (" + ", ".join(CASES) + "; suffix s: adjoint of Y)")
     ap.add_argument("--drop", type=int, default=0)
     ap.add_argument("--reps", type=int, default=10)
-    ap.add_argument("--lib", default=str(HERE / "_build" / "libqxgpu.so"))
+    ap.add_argument("--lib", default=str(HERE / "qxtools.jl_gb300" / "_build" / "libqxgpu.so"))
     args = ap.parse_args()
     import torch
     lib = ct.CDLL(args.lib)

@@ -333,16 +333,18 @@ def test_graph_replay_matches_eager(q, gpu_lib, oracle, precision):
     ref = oracle.run_programme(prog, bits, nthreads=8)[:, 0]
     tol = FP64_TOL if precision == "fp64" else 1e-5
     with q.Executor(prog, precision=precision, use_graphs=True, max_bitstring_batch=16, max_slice_batch=2) as ex:
+        # FP64 per amplitude (rel_err); Complex64 relative to the largest amplitude
+        err = rel_err if precision == "fp64" else (lambda g, r: np.max(np.abs(g - r)) / np.max(np.abs(r)))
         for _ in range(3):                                   # eager run, capture, replay
             got = ex.amplitudes(bits)[:, 0]
-            assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) <= tol
+            assert err(got, ref) <= tol
         part = ex.amplitudes(bits[:7], slices=(2, 6))[:, 0]   # smaller batch: new plan
         refp = oracle.run_programme(prog, bits[:7], slices=(2, 6), nthreads=8)[:, 0]
-        assert np.max(np.abs(part - refp)) / np.max(np.abs(refp)) <= tol
+        assert err(part, refp) <= tol
         raw = torch.tensor(list("".join(bits).encode()), dtype=torch.uint8, device="cuda")
         out = torch.zeros(2 * len(bits), dtype=torch.float64, device="cuda")
         for _ in range(2):
             ex.amplitudes_device(raw.data_ptr(), len(bits), out.data_ptr())
             ex.synchronize()
             dev = out.cpu().numpy().view(np.complex128)
-            assert np.max(np.abs(dev - ref)) / np.max(np.abs(ref)) <= tol
+            assert err(dev, ref) <= tol
