@@ -2,20 +2,26 @@
     QXToolsGPU
 
 Julia binding of libqxgpu (include/qxgpu.h) through `ccall`: runs the `.qx` programmes that
-QXTools' `generate_simulation_files` writes (src/simulation.jl:52-77) on a GB300, and provides a
-`single_amplitude` with the reference's signature (src/simulation.jl:86-91).
+QXTools' `generate_simulation_files` writes (src/simulation.jl:52-77) on a GB300, and provides
+`single_amplitude(tnc, plan, amplitude)` and `run_simulation(circ; num_amplitudes, seed)` with
+the reference's signatures (src/simulation.jl:86-91 and :103-136).  Those two compile the
+network and plan with QXTools' own `build_compute_graph` and `generate_dsl_files` into a GPU
+programme (cached per network object, plan and precision) and run the bitstrings on it.
 
 Not exercised here (no Julia toolchain in the build or GPU images); the C ABI it binds is
-tested through Python ctypes.  Leaf data is read from the `.npz` written by the Python mirror
-or passed in as a Dict{String,Array{ComplexF64}} (e.g. loaded from the reference's `.jld2`).
+tested through Python ctypes.  Leaf data comes from the `.jld2` that `generate_dsl_files` writes
+(read with JLD2), from the `.npz` written by the Python mirror, or as a
+Dict{String,Array{ComplexF64}}.
 """
 module QXToolsGPU
 
 import ChainRulesCore
 using ChainRulesCore: NoTangent, ZeroTangent, AbstractZero, unthunk
+import QXTools
+import JLD2
 
 export QxgProgram, parse_qx, load_qx, read_bitstrings, qxrun, plan_contraction, amplitudes,
-       single_amplitude, set_leaves!, gradient
+       single_amplitude, run_simulation, set_leaves!, gradient, compile_tnc
 
 const libqxgpu = joinpath(@__DIR__, "..", "_build", "libqxgpu.so")
 
@@ -31,7 +37,9 @@ struct QxgOptions          # qxg_options
     max_bitstring_batch::Int32; max_slice_batch::Int32; use_graphs::Int32
     tc_tuning::Int32        # 0: autotune tensor-core tile variants, 1: fixed default
     tc_plane_budget_mb::Int32   # 0: 4096 MiB of packed planes before blocking the free columns
-    reserved::NTuple{5,Int32}
+    tc_wait_limit::Int32    # 0: 2^20 polls before a tensor-core wait gives up
+    tc_stall_test::Int32    # test hook, leave 0
+    reserved::NTuple{3,Int32}
 end
 
 mutable struct QxgProgram
@@ -89,7 +97,7 @@ function load_qx(qx_file::String, data::AbstractDict; precision::Symbol=:fp64, d
         length(x) == n || error("data key $(dkeys[i]) has $(length(x)) elements, its load line wants $n")
     end
     loads = [Int(I.a) + 1 for I in instrs if I.op == 1]   # QXG_OP_LOAD
-    opts = Ref(QxgOptions(PREC[precision], device, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 5)))
+    opts = Ref(QxgOptions(PREC[precision], device, 0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 3)))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:qxg_program_create, libqxgpu), Cint,
                 (Ptr{QxgInstr}, Int32, Ptr{Int32}, Int64, Ptr{Int32}, Ptr{Int64}, Int32, Int32,
@@ -289,6 +297,83 @@ function ChainRulesCore.rrule(::typeof(amplitudes), p::QxgProgram, leaves::Abstr
         (NoTangent(), NoTangent(), dl, NoTangent())
     end
     y, amplitudes_pullback
+end
+
+# GPU programmes compiled from (network object, plan, precision, device); an entry lives as long
+# as its network object
+const _TNC_PROGRAMS = WeakKeyDict{Any,Dict{Any,QxgProgram}}()
+
+"""
+    compile_tnc(tnc, plan; bond_groups=nothing, precision=:fp64, device=0) -> QxgProgram
+
+A GPU programme for a `TensorNetworkCircuit` and its `(A, B, C)` plan, built as
+`generate_simulation_files` builds its files (src/simulation.jl:52-77): QXTools'
+`build_compute_graph(tnc, plan, bond_groups)` (src/compute_graph/compute_graph.jl:15-98) and
+`generate_dsl_files` write the `.qx` programme and the `.jld2` leaf data into a temporary
+directory, which `load_qx` compiles.  The network's output tensors become the programme's
+`output` commands, so one programme serves every bitstring.
+"""
+function compile_tnc(tnc, plan::AbstractVector; bond_groups=nothing, precision::Symbol=:fp64, device::Int=0)
+    cg = QXTools.build_compute_graph(tnc, plan, bond_groups)
+    mktempdir() do dir
+        prefix = joinpath(dir, "programme")
+        QXTools.generate_dsl_files(cg, prefix; force=true)
+        data = JLD2.load(prefix * ".jld2")
+        load_qx(prefix * ".qx", Dict(string(k) => v for (k, v) in data); precision=precision, device=device)
+    end
+end
+
+function _tnc_programme(tnc, plan, precision::Symbol, device::Int)
+    progs = get!(() -> Dict{Any,QxgProgram}(), _TNC_PROGRAMS, tnc)
+    get!(progs, (hash(plan), precision, device)) do
+        compile_tnc(tnc, plan; precision=precision, device=device)
+    end
+end
+
+"""
+    single_amplitude(tnc::TensorNetworkCircuit, plan::Vector{NTuple{3,Symbol}},
+                     amplitude::Union{String,Nothing}=nothing; precision=:fp64, device=0) -> ComplexF64
+
+The reference's `single_amplitude` (src/simulation.jl:86-91) on the GPU: the amplitude of the
+bitstring `amplitude` (character i = qubit i, `0 1 + -`; `nothing` = all zeros) for the network
+contracted along `plan`.  The first call for a network object and plan compiles a programme
+(`compile_tnc`); later calls with other bitstrings reuse it.  The network is not modified.  A
+network changed in place after its first call needs `empty!(QXToolsGPU._TNC_PROGRAMS)`.
+"""
+function single_amplitude(tnc::QXTools.TensorNetworkCircuit, plan::Array{NTuple{3,Symbol},1},
+                          amplitude::Union{String,Nothing}=nothing; precision::Symbol=:fp64, device::Int=0)
+    p = _tnc_programme(tnc, plan, precision, device)
+    bits = amplitude === nothing ? "0"^p.nqubits : amplitude
+    amplitudes(p, [bits])[1, 1]
+end
+
+"""
+    run_simulation(circ; num_amplitudes=nothing, seed=nothing, precision=:fp64, device=0)
+        -> OrderedDict{String,ComplexF64}
+
+The reference's `run_simulation` (src/simulation.jl:103-136) on the GPU: the circuit is converted
+and planned by QXTools itself (`convert_to_tnc`, `flow_cutter_contraction_plan(tnc;
+hypergraph=true)`), the bitstrings are `amplitudes_all` or `amplitudes_uniform(qubits, seed,
+num_amplitudes)` as there (at most 1000 drawn above 30 qubits when none is given), and the unique
+bitstrings run in one batched call instead of one `single_amplitude` each.
+"""
+function run_simulation(circ; num_amplitudes::Union{Int64,Nothing}=nothing, seed::Union{Int64,Nothing}=nothing,
+                        precision::Symbol=:fp64, device::Int=0)
+    tnc = QXTools.convert_to_tnc(circ)
+    plan = QXTools.flow_cutter_contraction_plan(tnc; hypergraph=true)
+    nq = QXTools.qubits(tnc)
+    if num_amplitudes === nothing && nq > 30
+        num_amplitudes = 1000
+    end
+    bits = num_amplitudes === nothing ? QXTools.amplitudes_all(nq) : QXTools.amplitudes_uniform(nq, seed, num_amplitudes)
+    uniq = unique(collect(bits))
+    p = compile_tnc(tnc, plan; precision=precision, device=device)
+    amps = amplitudes(p, uniq)
+    results = QXTools.OrderedDict{String,ComplexF64}()
+    for (i, b) in enumerate(uniq)
+        results[b] = amps[1, i]
+    end
+    results
 end
 
 """

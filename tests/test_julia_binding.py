@@ -210,3 +210,25 @@ def test_ccall_signatures_match_the_header():
         cret, cargs = protos[name]
         assert ret == cret, f"{name}: returns {ret} in Julia, {cret} in C"
         assert args == cargs, f"{name}: Julia passes {args}, the header declares {cargs}"
+
+
+def test_drop_in_methods_have_the_reference_signatures():
+    """The binding offers QXTools' own entry points for the path with the reference's argument
+    lists: single_amplitude(tnc::TensorNetworkCircuit, plan::Array{NTuple{3, Symbol}, 1},
+    amplitude::Union{String, Nothing}=nothing) (src/simulation.jl:86) and run_simulation(circ;
+    num_amplitudes, seed) (src/simulation.jl:103-105), each with extra keywords only, and both
+    built from QXTools' own build_compute_graph / generate_dsl_files."""
+    text = JL.read_text()
+    sa = re.search(r"^function single_amplitude\(tnc::QXTools\.TensorNetworkCircuit,\s*plan::Array\{NTuple\{3,\s*"
+                   r"Symbol\},\s*1\},\s*amplitude::Union\{String,\s*Nothing\}=nothing;", text, re.M)
+    assert sa, "single_amplitude(tnc, plan, amplitude) with the reference's argument types is missing"
+    rs = re.search(r"^function run_simulation\(circ;\s*num_amplitudes::Union\{Int64,\s*Nothing\}=nothing,\s*"
+                   r"seed::Union\{Int64,\s*Nothing\}=nothing", text, re.M)
+    assert rs, "run_simulation(circ; num_amplitudes, seed) is missing"
+    assert "QXTools.build_compute_graph(tnc, plan, bond_groups)" in text
+    assert "QXTools.generate_dsl_files(cg, prefix; force=true)" in text
+    # every exported name is defined
+    exported = re.search(r"^export (.*?)\n(?=\S)", text, re.M | re.S).group(1)
+    for name in re.findall(r"\w+!?", exported):
+        assert re.search(rf"^(function |const |struct |mutable struct ){re.escape(name)}(?![\w!])|^{re.escape(name)}\(",
+                         text, re.M), f"{name} is exported but not defined"
