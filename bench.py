@@ -1,19 +1,27 @@
 #!/usr/bin/env python3
-"""Benchmark of the GB300 contraction executor (amplitudes/s and TFLOP/s).
+"""Benchmark of the GB300 contraction executor (amplitudes/s and TFLOP/s): the split-precision
+batched executor against the plain ComplexF64 GPU executor on the same programme.
 
-Workload (default `rqc_5x5_d12_open6`): a seeded 5x5-grid random circuit, 12 cycles of
+Workload (default `rqc_7x7_d10_w22`): a seeded 7x7-grid random circuit (49 qubits), 10 cycles of
 {sqrt X, sqrt Y, sqrt W} + fSim(pi/2, pi/6) (pattern ABCDCDAB), two-qubit gates decomposed,
-planned and compiled into a `.qx` programme as generate_simulation_files does, with 6 qubits
-left open (a 2^6-amplitude output tensor per bitstring) and 64 seeded bitstrings of the other
-19 qubits -> 4096 amplitudes per pass.  Synthetic, seeded data.
+planned by the library's planner and sliced until every intermediate has at most 2^22 elements
+(8 slices), compiled into a `.qx` programme as generate_simulation_files does, with 1024 seeded
+bitstrings.  It stands in for the 7x7, 16-cycle precision configuration (<= 2^28 elements with
+about 2^10 slices), for which no contraction tree exists within that budget: every balanced
+split of the 16-cycle network cuts all 49 qubit wires.  Synthetic, seeded data.
 
 A step is one pass of the programme over one batch of bitstrings (`--bits-per-step`, default
-all 64) and all its slices.  `value` times steps with the bitstrings already in HBM (the
-device entry point qxg_amplitudes_device); `e2e` times the same steps through the host entry
-point qxg_amplitudes with pinned host buffers (bitstrings copied in, amplitudes copied out,
-every step).  Intermediates exceed L2 (largest intermediate reported in `config`).
+all 1024) and all its slices.  `value` times steps of the split-precision executor
+(`--precision`, default 3xTF32) with the bitstrings already in HBM (the device entry point
+qxg_amplitudes_device); `e2e` times the same steps through the host entry point qxg_amplitudes
+with pinned host buffers (bitstrings copied in, amplitudes copied out, every step).  The FP64
+arm (`fp64`) runs the plain ComplexF64 executor on the first `--fp64-bits` bitstrings of the
+same list, and the line reports the ratio of the two rates and the error of the split arm's
+amplitudes against the FP64 ones, per amplitude.  Intermediates exceed L2 (largest intermediate
+reported in `config`).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32|split_bf16|split_tf32]
+                    [--workload NAME] [--fp64-bits N] [--fp64-steps K] [--no-fp64]
     python bench.py --impl reference ...   # the reference's CPU arithmetic (permute + OpenBLAS
                                            # zgemm per ncon, oracle/blas_walk.py) on the host cores
 Under torchrun (N > 1) every rank runs its own replica on its own shard of bitstrings (the
@@ -44,7 +52,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="rqc_5x5_d12_open6")
+    ap.add_argument("--workload", default="rqc_7x7_d10_w22")
     ap.add_argument("--precision", default="split_tf32", choices=["fp64", "fp32", "split_bf16", "split_tf32"])
     ap.add_argument("--bits-per-step", type=int, default=0, help="bitstrings per step (0: the workload's list)")
     ap.add_argument("--seed", type=int, default=1)
@@ -53,7 +61,10 @@ def parse():
                     help="plan with the Python stand-in or the library's planner (default: the workload's)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--compare-fp64", action="store_true", help="also time the FP64 path and report the error")
+    ap.add_argument("--fp64-bits", type=int, default=0,
+                    help="bitstrings of the FP64 arm, the first ones of the split arm's list (0: all of them)")
+    ap.add_argument("--fp64-steps", type=int, default=1, help="timed steps of the FP64 arm (after one warm-up)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 arm and the error")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel eagerly (no CUDA graphs)")
     ap.add_argument("--tuning-file", default=None,
                     help="read the autotuner's decisions from this file if it exists, else write them after warm-up "
@@ -183,23 +194,41 @@ def traffic_summary(workload: str, kernel: str, precision: str):
 
 
 # --------------------------------------------------------------------------------------------
+def cpu_sample(prog, bits, info, seconds: float, start: int = 0):
+    """FP64 walks (oracle/blas_walk.py) of (bitstring, slice) pairs in order from bitstring
+    `start`, slice 0, until `seconds` have passed; the last walk may stop at an instruction
+    boundary.  -> (FLOPs of completed contractions, seconds, walks completed, walks started)."""
+    from oracle import blas_walk
+    nsl = max(1, int(info["num_slices"]))
+    flops, sec, done, started, k = 0.0, 0.0, 0, 0, 0
+    while sec < seconds:
+        b, sl = bits[(start + k // nsl) % len(bits)], k % nsl
+        f, t, fin = blas_walk.run_timed(prog, b, seconds - sec, slice_id=sl)
+        flops += f
+        sec += t
+        done += int(fin)
+        started += 1
+        k += 1
+    return flops, sec, done, started
+
+
 def cpu_baseline(prog, bits, info, seconds: float):
     """The reference's CPU arithmetic restated (oracle/blas_walk.py: permute + OpenBLAS zgemm per
-    ncon, as TensorOperations contracts) on a bounded sample: one bitstring's walk for one slice
-    with BLAS on every host thread, stopped after `seconds`; the FLOP rate is converted to
-    amplitudes/s with the programme's FLOPs per bitstring."""
+    ncon, as TensorOperations contracts) on a bounded sample: walks of one bitstring and one slice
+    each, in order, with BLAS on every host thread, for `seconds`; the FLOP rate is converted to
+    amplitudes/s with the programme's FLOPs per bitstring (all slices)."""
     from oracle import blas_walk
     cores = blas_walk.blas_threads()
     out_size = info["amplitudes_per_bitstring"]
-    flops, sec, finished = blas_walk.run_timed(prog, bits[0], seconds)
+    flops, sec, done, started = cpu_sample(prog, bits, info, seconds)
     rate = flops / max(sec, 1e-9)
     amps = rate / info["flops_per_bitstring"] * out_size
-    sample = (f"one FP64 walk (threaded permute + {blas_walk.blas_name()} zgemm per ncon) of bitstring 0, slice 0 of "
-              f"{info['name']} ({'complete' if finished else f'stopped after {sec:.1f} s'}, {flops:.3e} FLOPs "
-              f"in {sec:.1f} s); amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per "
-              f"bitstring x {out_size} amplitudes per bitstring")
+    sample = (f"FP64 walks (threaded permute + {blas_walk.blas_name()} zgemm per ncon) of (bitstring, slice) pairs of "
+              f"{info['name']} in order for {sec:.1f} s ({done} walks complete of {started} started, "
+              f"{flops:.3e} FLOPs); amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per "
+              f"bitstring (all {info['num_slices']} slices) x {out_size} amplitudes per bitstring")
     return {"value": amps, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
-            "gflops": rate / 1e9}
+            "gflops": rate / 1e9, "executed_flops_per_amplitude": info["flops_per_bitstring"] / out_size}
 
 
 def run_reference(args):
@@ -213,28 +242,36 @@ def run_reference(args):
                                                   planner=args.planner)
     cores = blas_walk.blas_threads()
     out_size = info["amplitudes_per_bitstring"]
-    per = max(2.0, min(args.cpu_seconds, 20.0))
-    for _ in range(args.warmup):
-        blas_walk.run_timed(prog, bits[0], min(per, 3.0))
-    fl_tot, sec_tot, done = 0.0, 0.0, 0
+    # each step is a bounded sample (the whole run stays within a few minutes)
+    per = max(1.0, min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup)))
+    for w in range(args.warmup):
+        cpu_sample(prog, bits, info, min(per, 3.0), start=w)
+    fl_tot, sec_tot, done, started = 0.0, 0.0, 0, 0
     t0 = time.perf_counter()
     for k in range(args.steps):
-        fl, sec, fin = blas_walk.run_timed(prog, bits[k % len(bits)], per)
+        fl, sec, d, st = cpu_sample(prog, bits, info, per, start=k * 7)
         fl_tot += fl
         sec_tot += sec
-        done += int(fin)
+        done += d
+        started += st
     wall = time.perf_counter() - t0
     rate = fl_tot / sec_tot
     value = rate / info["flops_per_bitstring"] * out_size
-    sample = (f"each step: one FP64 walk (bitstring k, slice 0; threaded permute + {blas_walk.blas_name()} "
-              f"zgemm per ncon, "
-              f"as TensorOperations contracts) stopped after {per:.0f} s ({done} of {args.steps} complete); "
-              f"amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} FLOPs per bitstring x "
-              f"{out_size} amplitudes")
+    sample = (f"each step: {per:.1f} s of FP64 walks of (bitstring, slice) pairs (threaded permute + "
+              f"{blas_walk.blas_name()} zgemm per ncon, as TensorOperations contracts; {done} walks complete of "
+              f"{started} started over all steps); amplitudes/s = FLOP rate / {info['flops_per_bitstring']:.3e} "
+              f"FLOPs per bitstring (all {info['num_slices']} slices) x {out_size} amplitudes")
+    cfg = workload_config(info, args, None)
+    cfg.update({"precision": "fp64", "executor": "CPU: permute + zgemm per ncon (TensorOperations' algorithm)",
+                "threads": cores})
+    for k in ("cuda_graphs", "tc_tuning"):
+        cfg.pop(k, None)
+    cfg["arm"] = "reference CPU arithmetic, restated (oracle/blas_walk.py)"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": workload_config(info, args, None),
+            "data": "synthetic (seeded)", "config": cfg,
+            "executed_flops_per_amplitude": info["flops_per_bitstring"] / out_size,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "tflops": rate / 1e12}
@@ -250,7 +287,7 @@ def workload_config(info, args, ex_info):
            "flops_per_bitstring": info["flops_per_bitstring"], "seed": info["seed"],
            "planner": info["spec"].get("planner", "python"),
            "precision": args.precision, "cuda_graphs": not args.no_graphs,
-           "l2": "intermediates larger than L2 (no flush needed)"}
+           "l2": "intermediates larger than L2 (no flush needed)", "arm": "split-precision batched executor"}
     if ex_info:
         cfg.update({"bitstring_batch": ex_info["bitstring_batch"], "slice_batch": ex_info["slice_batch"],
                     "workspace_bytes": ex_info["workspace_bytes"],
@@ -258,6 +295,62 @@ def workload_config(info, args, ex_info):
                     "fused_gather_steps": ex_info["num_steps_fused"],
                     "autotuned_steps": ex_info["num_steps_tuned"], "tc_tuning": args.tc_tuning})
     return cfg
+
+
+def error_stats(got, ref, target: float = 1e-5) -> dict:
+    """Error of `got` against the FP64 amplitudes `ref`, per amplitude: |got - ref| / |ref| for
+    every amplitude (random-circuit amplitudes are never 0; an amplitude below 1e-12 of the
+    largest would be compared at that floor), as max / 99th / 90th percentile / median and the
+    share within `target`; and normalised by the largest and by the RMS amplitude."""
+    import numpy as np
+    g, r = np.asarray(got).ravel(), np.asarray(ref).ravel()
+    a = np.abs(r)
+    floor = 1e-12 * a.max()
+    rel = np.abs(g - r) / np.maximum(a, floor)
+    rms = float(np.sqrt(np.mean(a ** 2)))
+    return {"amplitudes": int(r.size), "per_amplitude_max": float(rel.max()),
+            "per_amplitude_p99": float(np.quantile(rel, 0.99)), "per_amplitude_p90": float(np.quantile(rel, 0.90)),
+            "per_amplitude_median": float(np.median(rel)),
+            "share_within_target": float(np.mean(rel <= target)), "target": target,
+            "max_over_largest_amplitude": float(np.abs(g - r).max() / a.max()),
+            "max_over_rms_amplitude": float(np.abs(g - r).max() / rms),
+            "floor": "amplitudes below 1e-12 of the largest compared at that floor (none here)"
+                     if not np.any(a < floor) else "amplitudes below 1e-12 of the largest compared at that floor"}
+
+
+def fp64_arm(q, prog, bits, out_size, local, dev, stream_of, args):
+    """The plain ComplexF64 executor on `bits` of the same programme: one warm-up call, then
+    `--fp64-steps` timed steps (CUDA events on the executor's stream, inputs in HBM).
+    -> (summary dict, its amplitudes as complex128 (n, out_size))."""
+    import numpy as np
+    torch = stream_of
+    n = len(bits)
+    ex = q.Executor(prog, precision="fp64", device=local, use_graphs=not args.no_graphs)
+    stream = torch.cuda.ExternalStream(ex.stream, device=dev)
+    d_bits = torch.tensor(list("".join(bits).encode()), dtype=torch.uint8, device=dev)
+    d_out = torch.zeros(2 * n * out_size, dtype=torch.float64, device=dev)
+    nsl = ex.num_slices
+    run = lambda: ex.amplitudes_device(d_bits.data_ptr(), n, d_out.data_ptr(), slices=(0, nsl))
+    run()
+    ex.synchronize()
+    steps = max(1, args.fp64_steps)
+    torch.cuda.synchronize()
+    s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s_ev.record(stream)
+    for _ in range(steps):
+        run()
+    e_ev.record(stream)
+    ex.synchronize()
+    ms = s_ev.elapsed_time(e_ev)
+    inf = ex.info()
+    amps = d_out.cpu().numpy().view(np.complex128).reshape(n, out_size).copy()
+    ex.close()
+    value = n * out_size * steps / (ms * 1e-3)
+    return ({"value": value, "unit": UNIT, "bitstrings": n, "amplitudes_per_step": n * out_size, "steps": steps,
+             "warmup": 1, "ms_per_step": ms / steps, "dtype": "f64", "precision": "fp64",
+             "bitstring_batch": inf["bitstring_batch"], "slice_batch": inf["slice_batch"],
+             "note": "same programme, the first bitstrings of the split arm's list; FP64 CUDA-core contractions"},
+            amps)
 
 
 def run_ours(args):
@@ -347,8 +440,9 @@ def run_ours(args):
     e2e = {"value": ws * amps_per_step * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(h_bits.numel()), "d2h_bytes_per_step": int(h_out.numel() * 8)}
     # ---- roofline of the dominant kernel: CUDA events on the executor's stream ---------------
+    psteps = max(1, min(args.steps, 3))
     ex.profile(True)
-    for _ in range(args.steps):
+    for _ in range(psteps):
         step_device()
     rows, _ = ex.profile_read()
     ex.profile(False)
@@ -362,9 +456,9 @@ def run_ours(args):
     peaks, peak_src = measured_peaks()
     flops_exec = sum(v["flops"] for v in by_kind.values())
     tflops = flops_exec / (total_ms * 1e-3) / 1e12 if total_ms else 0.0
-    kernel_name = {"contract_fp64": "contract_kernel_fp64", "contract_fp32": "contract_kernel_fp32",
-                   "contract_tc": "tc_contract"}.get(dom_name, dom_name)
-    traffic, tsum = traffic_summary(args.workload, kernel_name, args.precision)
+    kernel_name = dom_name
+    traffic, tsum = traffic_summary(args.workload, {"contract_tc": "tc_contract"}.get(dom_name, dom_name),
+                                    args.precision)
     if tsum and "dram_over_algorithmic" in tsum and dom["launches"]:
         # measured on a smaller case: DRAM bytes per algorithmic byte of this kernel class, applied
         # to this run's algorithmic bytes per launch
@@ -397,11 +491,17 @@ def run_ours(args):
         pk = peaks["hbm_gbs"]
         roof = {"bound": "hbm", "achieved": ach, "peak": pk, "unit": "GB/s", "frac": ach / pk, "traffic": traffic,
                 "peak_source": f"hbm_gbs of {peak_src}", "kernel": kernel_name, "kernel_share": dom["ms"] / total_ms}
+    # per kernel class over the profiled steps; tc_pack moves operands for the tensor cores and
+    # has no algorithmic bytes of its own (its entry counts the bytes it reads and writes)
     roof["kernels"] = {k: {"launches": v["launches"], "ms": round(v["ms"], 3), "share": v["ms"] / total_ms,
-                           "algorithmic_bytes": v["bytes"], "algorithmic_flops": v["flops"]}
+                           ("bytes_moved" if k == "tc_pack" else "algorithmic_bytes"): v["bytes"],
+                           "algorithmic_flops": v["flops"]}
                        for k, v in sorted(by_kind.items(), key=lambda kv: -kv[1]["ms"])}
+    roof["profiled_steps"] = psteps
+    roof["profile_note"] = ("kernel times from CUDA events around every launch of an eager run (no graph "
+                            "replay, no concurrent branches), so their sum exceeds a replayed step")
     top = sorted(rows, key=lambda r: -r["ms"])[:10]
-    roof["top_steps"] = [{"instr": r["instr"], "kernel": r["kernel"], "ms_per_pass": round(r["ms"] / args.steps, 3),
+    roof["top_steps"] = [{"instr": r["instr"], "kernel": r["kernel"], "ms_per_pass": round(r["ms"] / psteps, 3),
                           "gb_s": round(r["bytes"] / (r["ms"] * 1e-3) / 1e9, 1) if r["ms"] else None,
                           "tflop_s": round(r["flops"] / (r["ms"] * 1e-3) / 1e12, 2) if r["ms"] else None}
                          for r in top]
@@ -411,18 +511,19 @@ def run_ours(args):
             "data": "synthetic (seeded random circuit, seeded bitstrings)",
             "config": workload_config(info, args, ex_info) | {"parallelism": f"replicas x{ws} (bitstring shards)"},
             "tflops": tflops, "tflops_note": "executed FLOPs (8 |C| K per contraction) / CUDA-event time of all kernels",
+            "executed_flops_per_amplitude": flops_exec / (psteps * amps_per_step),
             "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches1 - launches0), "roofline": roof,
             "wall_s": wall}
-    # ---- error of this run against the FP64 path and the oracle ------------------------------
     got = d_out.cpu().numpy().view("complex128").reshape(nb, out_size)
-    if args.compare_fp64 and args.precision != "fp64":
-        ex64 = q.Executor(prog, precision="fp64", device=local)
-        ref64 = ex64.amplitudes(all_bits)
-        line["max_rel_err_vs_fp64"] = float(abs(got - ref64).max() / abs(ref64).max())
-        ex64.close()
+    ex.close()
+    # ---- the plain ComplexF64 executor on the same programme and bitstrings, and the error ----
+    if not args.no_fp64 and args.precision != "fp64":
+        n64 = min(args.fp64_bits or nb, nb)
+        line["fp64"], ref64 = fp64_arm(q, prog, all_bits[:n64], out_size, local, dev, stream_of=torch, args=args)
+        line["split_over_fp64"] = value / line["fp64"]["value"]
+        line["err_vs_fp64"] = error_stats(got[:n64], ref64)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(prog, bits, info, args.cpu_seconds)
-    ex.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

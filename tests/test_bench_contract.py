@@ -35,7 +35,10 @@ def test_reference_arm_prints_the_contract_line():
     assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
     assert d["value"] > 0 and d["higher_is_better"] is True
     assert d["steps"] == 1 and d["warmup"] == 0
-    assert d["config"]["workload"] == "rqc_5x5_d12_open6"
+    assert d["config"]["workload"] == "rqc_7x7_d10_w22"
+    # the arm describes itself: FP64 on the host, no GPU options
+    assert d["config"]["precision"] == "fp64" and "cuda_graphs" not in d["config"]
+    assert d["executed_flops_per_amplitude"] > 0
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert "zgemm" in cb["sample"]
@@ -54,7 +57,7 @@ def test_cpu_baseline_leg_of_the_gpu_arm(q):
     sys.path.insert(0, str(ROOT))
     import bench
     prog, bits, info = q.workloads.build_workload("rqc_3x4_d8_s3")
-    cb = bench.cpu_baseline(prog, bits, info, 30.0)
+    cb = bench.cpu_baseline(prog, bits, info, 3.0)
     assert cb["kind"] == "port" and cb["unit"] == bench.UNIT and cb["cores"] >= 1
     assert cb["value"] > 0 and cb["gflops"] > 0
     assert "complete" in cb["sample"] and "zgemm" in cb["sample"]

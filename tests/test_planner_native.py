@@ -261,3 +261,24 @@ def test_native_planned_workloads_build(q, gpu_lib):
     nncon = int((prog.instrs[:, 0] == 4).sum())
     assert nncon >= info["plan_steps"] > 900
     assert info["est_seconds_per_pass"] < 1.0
+
+
+def test_7x7_precision_configuration_widths(q, gpu_lib):
+    """Why the 7x7 precision case runs at 10 cycles: the library planner's trees for the 7x7
+    random circuit (fSim(pi/2, pi/6) in pattern ABCDCDAB, decomposed, 49 closed outputs) need
+    2^8 slices at 12 cycles to keep every intermediate within 2^28 elements, but at 16 cycles the
+    unsliced width jumps past 2^50 and the same target takes more than 2^20 slices (the
+    configuration asks for about 2^10), with more than 2^60 FLOPs per amplitude."""
+    rows = {}
+    for depth in (12, 16):
+        circ = q.create_rqc_circuit(7, 7, depth, seed=1)
+        tnc = q.convert_to_tnc(circ, decompose=True, no_output=True)
+        tnc.add_output_subset(list(range(1, 50)))
+        _, _, _, st0 = _plan(q, gpu_lib, tnc, trials=8, greedy_trials=2, seed=1)
+        _, _, _, st = _plan(q, gpu_lib, tnc, trials=8, greedy_trials=2, seed=1, max_log2=28)
+        assert st["max_log2"] <= 28
+        rows[depth] = (st0["max_log2"], st["log2_slices"], st["log2_flops_total"])
+        print(f"7x7, {depth} cycles: unsliced width 2^{st0['max_log2']:.0f}; at <= 2^28: 2^{st['log2_slices']:.0f} "
+              f"slices, 2^{st['log2_flops_total']:.1f} FLOPs per amplitude")
+    assert rows[12][1] <= 10
+    assert rows[16][0] >= 50 and rows[16][1] >= 20 and rows[16][2] >= 60
