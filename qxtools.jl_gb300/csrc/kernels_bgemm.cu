@@ -1,0 +1,402 @@
+// Batched small GEMM with a long sum on the CUDA cores (Complex64 storage, FP32 products).
+//
+// The last joins of a sliced, bitstring-batched contraction tree contract two large halves of the
+// network into a small result per (slice, bitstring):
+//     C[b, m, n] = sum_k A[b, m, k] B[b, k, n]
+// with M, N <= 64 free values per batch value b, 2^10 to 2^25 summed terms and 2^5 to 2^12 batch
+// values, both operands holding 2^28 to 2^33 elements.  Each operand element is used by M or N
+// results only (16 FLOPs per byte at M = N = 32), so the step is bound by HBM and by the FP32
+// pipe together; the tensor-core path would first have to pack the smaller operand into hi/lo
+// planes four times its size, and the long-sum kernel (built for a few dozen results) re-reads the
+// operands once per block of 16 results.
+//
+// Here one block owns one batch value and one range of K:
+//   * the block's threads tile the M x N result (TM x TN complex results per thread, in
+//     registers);
+//   * the K range is walked in chunks of KC terms.  A chunk's A values (M x KC) and B values
+//     (KC x N) are loaded in the order of the operands' own address bits (so a warp's loads
+//     coalesce when the lowest address bits are result or summed bits), scaled by the operands'
+//     power-of-two exponents and stored in shared memory as (ar, ar, -ai, ai) and (br, bi, bi,
+//     br) quadruples; each complex multiply-add is then two paired FMAs (fma.rn.f32x2) on one
+//     16-byte read of each.  The next chunk's loads are in flight while the current one is
+//     multiplied (two shared-memory buffers, one barrier per chunk);
+//   * every thread sums at most kFlushK terms in FP32 before adding them into FP64
+//     accumulators, so the error does not grow with K (the long-sum kernel's rule);
+//   * with one K range per batch value the block writes C directly; otherwise it writes FP64
+//     partials and bgemm_reduce_kernel adds them in range order (deterministic).
+// Blocks are numbered batch value first, so blocks running side by side read neighbouring batch
+// values: where a batch bit is among an operand's lowest address bits, the sectors one block
+// fetches are read by its neighbour from L2.
+#include <algorithm>
+
+#include "simt_common.h"
+
+namespace qxg {
+
+constexpr int kFlushK = 512;            // FP32 terms per thread before the FP64 accumulation
+constexpr size_t kBGemmMaxSmem = 48 * 1024;
+
+// ---- phases of the kernel, shared with the host emulation of its index work --------------------
+
+// Element j of thread tid in a chunk of A (j < la): its offset from the chunk's base and its
+// shared-memory slot [k][m]; the same for B (j < lb), slot [k][n].
+__host__ __device__ __forceinline__ void bgemm_elem_a(const BGemmArgs& g, int tid, int j, int64_t* off, int* slot) {
+    const int64_t e = tid + (int64_t)j * (g.thr_m * g.thr_n);
+    *off = pdep(e, g.eA);
+    *slot = (int)(pdep(e, g.eAk) * g.M + pdep(e, g.eAm));
+}
+__host__ __device__ __forceinline__ void bgemm_elem_b(const BGemmArgs& g, int tid, int j, int64_t* off, int* slot) {
+    const int64_t e = tid + (int64_t)j * (g.thr_m * g.thr_n);
+    *off = pdep(e, g.eB);
+    *slot = (int)(pdep(e, g.eBk) * g.N + pdep(e, g.eBn));
+}
+// Base offsets of chunk c of K range si for batch value bi.
+__host__ __device__ __forceinline__ int64_t bgemm_base_a(const BGemmArgs& g, int64_t bi, int64_t si, int64_t c) {
+    return pdep(bi, g.bA) + pdep(si * g.nchunks + c, g.hA);
+}
+__host__ __device__ __forceinline__ int64_t bgemm_base_b(const BGemmArgs& g, int64_t bi, int64_t si, int64_t c) {
+    return pdep(bi, g.bB) + pdep(si * g.nchunks + c, g.hB);
+}
+// Shared-memory quadruples: A as (ar, ar, -ai, ai), B as (br, bi, bi, br), scaled (s) with the
+// imaginary part's sign folded in for conjugation (si = -s).
+__host__ __device__ __forceinline__ float4 bgemm_quad_a(float2 v, float s, float si) {
+    const float ar = v.x * s, ai = v.y * si;
+    return make_float4(ar, ar, -ai, ai);
+}
+__host__ __device__ __forceinline__ float4 bgemm_quad_b(float2 v, float s, float si) {
+    const float br = v.x * s, bi = v.y * si;
+    return make_float4(br, bi, bi, br);
+}
+// One chunk's products for thread (tm, tn): rows tm + thr_m i, columns tn + thr_n j.
+template <int TM, int TN>
+__host__ __device__ __forceinline__ void bgemm_chunk(const BGemmArgs& g, const float4* as, const float4* bs, int tm,
+                                                     int tn, unsigned long long (&acc)[TM][TN]) {
+    as += tm;
+    bs += tn;
+    for (int k = 0; k < g.kc; k++) {
+        float4 qa[TM], qb[TN];
+#pragma unroll
+        for (int i = 0; i < TM; i++) qa[i] = as[k * g.M + i * g.thr_m];
+#pragma unroll
+        for (int j = 0; j < TN; j++) qb[j] = bs[k * g.N + j * g.thr_n];
+#pragma unroll
+        for (int i = 0; i < TM; i++) {
+            const unsigned long long a1 = f2pack(qa[i].x, qa[i].y), a2 = f2pack(qa[i].z, qa[i].w);
+#pragma unroll
+            for (int j = 0; j < TN; j++) {
+                fma2(acc[i][j], a1, f2pack(qb[j].x, qb[j].y));
+                fma2(acc[i][j], a2, f2pack(qb[j].z, qb[j].w));
+            }
+        }
+    }
+}
+template <int TM, int TN>
+__host__ __device__ __forceinline__ void bgemm_flush(unsigned long long (&acc)[TM][TN], double2 (&dacc)[TM][TN]) {
+#pragma unroll
+    for (int i = 0; i < TM; i++)
+#pragma unroll
+        for (int j = 0; j < TN; j++) {
+            dacc[i][j].x += (double)u2f((unsigned)acc[i][j]);
+            dacc[i][j].y += (double)u2f((unsigned)(acc[i][j] >> 32));
+            acc[i][j] = 0ull;
+        }
+}
+__host__ __device__ __forceinline__ int64_t bgemm_c_offset(const BGemmArgs& g, int64_t bi, int m, int n) {
+    return pdep(bi, g.bC) + pdep(m, g.mC) + pdep(n, g.nC);
+}
+// Result idx (batch-major, then m, then n) from the K-range partials, summed in range order.
+__host__ __device__ __forceinline__ float2 bgemm_reduce_one(const BGemmArgs& g, const double2* partial, int64_t idx,
+                                                            int64_t* c_off) {
+    const int64_t per = (int64_t)g.M * g.N, total = g.nbatch * per;
+    double re = 0.0, im = 0.0;
+    for (int s = 0; s < g.nsplit; s++) {
+        const double2 v = partial[s * total + idx];
+        re += v.x;
+        im += v.y;
+    }
+    const int64_t r = idx % per;
+    *c_off = bgemm_c_offset(g, idx / per, (int)(r / g.N), (int)(r % g.N));
+    return make_float2((float)re, (float)im);
+}
+
+namespace {
+
+template <int TM, int TN, bool SCALED>
+__global__ void __launch_bounds__(256) contract_bgemm_kernel(const BGemmArgs g, double2* partial, int* exps) {
+    extern __shared__ float4 bg_smem[];
+    const int tid = threadIdx.x;
+    const int tn = tid % g.thr_n, tm = tid / g.thr_n;
+    const int64_t bi = (int64_t)blockIdx.x % g.nbatch;
+    const int64_t si = (int64_t)blockIdx.x / g.nbatch;
+    float4* As = bg_smem;                                  // [2][kc][M]
+    float4* Bs = bg_smem + 2 * g.kc * g.M;                 // [2][kc][N]
+    float sa = 1.f, sb = 1.f;
+    if (SCALED) {
+        sa = pow2f(-read_m(exps, g.expA));
+        sb = pow2f(-read_m(exps, g.expB));
+    }
+    const float sai = g.conjA ? -sa : sa, sbi = g.conjB ? -sb : sb;
+    int64_t offA[kBGemmMaxL], offB[kBGemmMaxL];
+    int slotA[kBGemmMaxL], slotB[kBGemmMaxL];
+#pragma unroll
+    for (int j = 0; j < kBGemmMaxL; j++) {
+        bgemm_elem_a(g, tid, j, &offA[j], &slotA[j]);
+        bgemm_elem_b(g, tid, j, &offB[j], &slotB[j]);
+    }
+    float2 ra[kBGemmMaxL], rb[kBGemmMaxL];
+    auto fetch = [&](int64_t c) {
+        const float2* a = g.A + bgemm_base_a(g, bi, si, c);
+        const float2* b = g.B + bgemm_base_b(g, bi, si, c);
+#pragma unroll
+        for (int j = 0; j < kBGemmMaxL; j++) {
+            if (j < g.la) ra[j] = __ldg(a + offA[j]);
+            if (j < g.lb) rb[j] = __ldg(b + offB[j]);
+        }
+    };
+    auto stage = [&](int buf) {
+        float4* as = As + buf * g.kc * g.M;
+        float4* bs = Bs + buf * g.kc * g.N;
+#pragma unroll
+        for (int j = 0; j < kBGemmMaxL; j++) {
+            if (j < g.la) as[slotA[j]] = bgemm_quad_a(ra[j], sa, sai);
+            if (j < g.lb) bs[slotB[j]] = bgemm_quad_b(rb[j], sb, sbi);
+        }
+    };
+    unsigned long long acc[TM][TN];
+    double2 dacc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; i++)
+#pragma unroll
+        for (int j = 0; j < TN; j++) {
+            acc[i][j] = 0ull;
+            dacc[i][j] = make_double2(0.0, 0.0);
+        }
+    fetch(0);
+    stage(0);
+    __syncthreads();
+    for (int64_t c = 0; c < g.nchunks; c++) {
+        const int buf = (int)(c & 1);
+        if (c + 1 < g.nchunks) fetch(c + 1);
+        bgemm_chunk<TM, TN>(g, As + buf * g.kc * g.M, Bs + buf * g.kc * g.N, tm, tn, acc);
+        if ((c + 1) % g.flush == 0 || c + 1 == g.nchunks) bgemm_flush<TM, TN>(acc, dacc);
+        if (c + 1 < g.nchunks) stage(buf ^ 1);
+        __syncthreads();
+    }
+    if (g.nsplit == 1) {
+        int emax = kExpUnset;
+#pragma unroll
+        for (int i = 0; i < TM; i++)
+#pragma unroll
+            for (int j = 0; j < TN; j++) {
+                const float2 v = make_float2((float)dacc[i][j].x, (float)dacc[i][j].y);
+                g.C[bgemm_c_offset(g, bi, tm + i * g.thr_m, tn + j * g.thr_n)] = v;
+                const float mx = fmaxf(fabsf(v.x), fabsf(v.y));
+                if (SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
+            }
+        if (SCALED) {
+            if (blockIdx.x == 0 && tid == 0)
+                exps[2 * g.expC] = exps[2 * g.expA] + exps[2 * g.expB] + read_m(exps, g.expA) + read_m(exps, g.expB);
+            for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+            if ((tid & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * g.expC + 1], emax);
+        }
+    } else {
+        // partial[si][bi][m][n] in FP64, added in K-range order by bgemm_reduce_kernel
+        double2* p = partial + ((si * g.nbatch + bi) * g.M) * g.N;
+#pragma unroll
+        for (int i = 0; i < TM; i++)
+#pragma unroll
+            for (int j = 0; j < TN; j++)
+                p[(tm + i * g.thr_m) * g.N + tn + j * g.thr_n] = dacc[i][j];
+    }
+}
+
+template <bool SCALED>
+__global__ void bgemm_reduce_kernel(const BGemmArgs g, const double2* partial, int* exps) {
+    const int64_t total = g.nbatch * g.M * g.N;
+    int emax = kExpUnset;
+    if (SCALED && blockIdx.x == 0 && threadIdx.x == 0)
+        exps[2 * g.expC] = exps[2 * g.expA] + exps[2 * g.expB] + read_m(exps, g.expA) + read_m(exps, g.expB);
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        int64_t off;
+        const float2 v = bgemm_reduce_one(g, partial, idx, &off);
+        g.C[off] = v;
+        const float mx = fmaxf(fabsf(v.x), fabsf(v.y));
+        if (SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
+    }
+    if (SCALED) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * g.expC + 1], emax);
+    }
+}
+
+int ilog2(int64_t x) {
+    int b = 0;
+    while ((int64_t(1) << b) < x) b++;
+    return b;
+}
+
+size_t bgemm_smem(const BGemmArgs& g) { return (size_t)2 * g.kc * (g.M + g.N) * sizeof(float4); }
+
+// A run of length one per element bit: the element index's bits go to scattered places.
+bool bit_runs(const std::vector<std::pair<int, int>>& p, BitMap* m) {
+    memset(m, 0, sizeof(*m));
+    for (auto& x : p) {
+        if (m->n >= kMaxRuns) return false;
+        m->r[m->n++] = Run{(uint8_t)x.first, 1, (uint8_t)x.second, 0};
+    }
+    return true;
+}
+
+}  // namespace
+
+// Plan the batched small GEMM form of a step (Complex64 storage only).  Eligible: every result
+// bit in A or B, every summed bit in both; 4 to 64 free values on each side with at least 256
+// results per batch value; at least 2^10 summed terms; both operands of at least 2^20 elements
+// (smaller steps are served by the row forms and the tensor cores; min_log2 lowers that floor for
+// the host emulation of the kernel).
+bool plan_bgemm(const StepArgs& s, int sm_count, BGemmArgs* g, int min_log2) {
+    if (s.nk < 10) return false;
+    auto one = [](const BitMap& m, int bit) {
+        const int64_t o = pdep(int64_t(1) << bit, m);
+        return o ? __builtin_ctzll((unsigned long long)o) : -1;
+    };
+    const int ncb = ilog2(s.nC);
+    std::vector<int> gb, ab, bb;             // result bits: batch, A only, B only
+    for (int p = 0; p < ncb; p++) {
+        const bool ia = one(s.cA, p) >= 0, ib = one(s.cB, p) >= 0;
+        if (ia && ib) gb.push_back(p);
+        else if (ia) ab.push_back(p);
+        else if (ib) bb.push_back(p);
+        else return false;
+    }
+    for (int j = 0; j < s.nk; j++)
+        if (one(s.kA, j) < 0 || one(s.kB, j) < 0) return false;
+    const int na = (int)ab.size(), nb = (int)bb.size(), ng = (int)gb.size();
+    if (na < 2 || nb < 2 || na > 6 || nb > 6 || na + nb < 8 || ng > 30) return false;
+    if (ng + std::min(na, nb) + s.nk < min_log2) return false;
+    BGemmArgs a;
+    memset(&a, 0, sizeof(a));
+    a.M = 1 << na;
+    a.N = 1 << nb;
+    // 64 threads of 4 x 4 results up to 1024 results per batch value, else 256 threads
+    const int nthr = std::max(64, a.M * a.N / 16);
+    int TM = 0, TN = 0;
+    for (int tn_ : {4, 2})
+        for (int tm_ : {4, 2})
+            if (!TM && a.M % tm_ == 0 && a.N % tn_ == 0 && (a.M / tm_) * (a.N / tn_) == nthr) { TM = tm_; TN = tn_; }
+    if (!TM) return false;
+    a.thr_m = a.M / TM;
+    a.thr_n = a.N / TN;
+    // summed values per chunk: every thread loads 1..kBGemmMaxL elements of each operand, and the
+    // two buffers fit kBGemmMaxSmem
+    int kc = 1;
+    while (kc * 2 <= 64 && (int64_t)a.M * kc * 2 <= (int64_t)nthr * kBGemmMaxL &&
+           (int64_t)a.N * kc * 2 <= (int64_t)nthr * kBGemmMaxL && (size_t)2 * kc * 2 * (a.M + a.N) * 16 <= kBGemmMaxSmem)
+        kc *= 2;
+    if ((int64_t)a.M * kc < nthr || (int64_t)a.N * kc < nthr) return false;
+    const int lkc = ilog2(kc);
+    if (lkc > s.nk) return false;
+    a.kc = kc;
+    a.la = (int)((int64_t)a.M * kc / nthr);
+    a.lb = (int)((int64_t)a.N * kc / nthr);
+    // the chunk's summed bits: those at the lowest address positions of either operand
+    std::vector<int> ks(s.nk), posA(s.nk), posB(s.nk);
+    for (int j = 0; j < s.nk; j++) { ks[j] = j; posA[j] = one(s.kA, j); posB[j] = one(s.kB, j); }
+    std::sort(ks.begin(), ks.end(), [&](int x, int y) {
+        const int px = std::min(posA[x], posB[x]), py = std::min(posA[y], posB[y]);
+        return px != py ? px < py : x < y;
+    });
+    // chunk element e: its bits are the chunk's (m, k) bits of A in A's address order (and (n, k)
+    // of B in B's), so consecutive elements are at ascending addresses
+    auto element_maps = [&](const BitMap& cmap, const std::vector<int>& freebits, const BitMap& kmap,
+                            BitMap* e_off, BitMap* e_free, BitMap* e_k) {
+        struct Bit { int pos, kind, idx; };
+        std::vector<Bit> bits;
+        for (int i = 0; i < (int)freebits.size(); i++) bits.push_back({one(cmap, freebits[i]), 0, i});
+        for (int i = 0; i < lkc; i++) bits.push_back({one(kmap, ks[i]), 1, i});
+        std::sort(bits.begin(), bits.end(), [](const Bit& x, const Bit& y) { return x.pos < y.pos; });
+        std::vector<std::pair<int, int>> off, fr, kk;
+        for (int e = 0; e < (int)bits.size(); e++) {
+            off.push_back({e, bits[e].pos});
+            (bits[e].kind == 0 ? fr : kk).push_back({e, bits[e].idx});
+        }
+        return bit_runs(off, e_off) && bit_runs(fr, e_free) && bit_runs(kk, e_k);
+    };
+    if (!element_maps(s.cA, ab, s.kA, &a.eA, &a.eAm, &a.eAk)) return false;
+    if (!element_maps(s.cB, bb, s.kB, &a.eB, &a.eBn, &a.eBk)) return false;
+    std::vector<std::pair<int, int>> bA, bB, bC, mC, nC, hA, hB;
+    for (int i = 0; i < ng; i++) {
+        bA.push_back({i, one(s.cA, gb[i])});
+        bB.push_back({i, one(s.cB, gb[i])});
+        bC.push_back({i, gb[i]});
+    }
+    for (int i = 0; i < na; i++) mC.push_back({i, ab[i]});
+    for (int i = 0; i < nb; i++) nC.push_back({i, bb[i]});
+    for (int i = lkc; i < s.nk; i++) {
+        hA.push_back({i - lkc, posA[ks[i]]});
+        hB.push_back({i - lkc, posB[ks[i]]});
+    }
+    if (!make_runs(bA, &a.bA) || !make_runs(bB, &a.bB) || !make_runs(bC, &a.bC) || !make_runs(mC, &a.mC) ||
+        !make_runs(nC, &a.nC) || !make_runs(hA, &a.hA) || !make_runs(hB, &a.hB))
+        return false;
+    a.nbatch = int64_t(1) << ng;
+    const int64_t chunks = int64_t(1) << (s.nk - lkc);
+    // K ranges: enough blocks for about four per SM, each range at least 2^12 terms
+    int64_t nsplit = 1;
+    while (a.nbatch * nsplit < (int64_t)sm_count * 4 && chunks / (nsplit * 2) * kc >= 4096) nsplit *= 2;
+    if (a.nbatch * nsplit > (int64_t(1) << 31) - 1) return false;
+    a.nsplit = (int)nsplit;
+    a.nchunks = chunks / nsplit;
+    a.flush = std::max(1, kFlushK / kc);
+    a.A = static_cast<const float2*>(s.A);
+    a.B = static_cast<const float2*>(s.B);
+    a.C = static_cast<float2*>(s.C);
+    a.conjA = s.conjA;
+    a.conjB = s.conjB;
+    a.expA = s.expA;
+    a.expB = s.expB;
+    a.expC = s.expC;
+    *g = a;
+    return true;
+}
+
+size_t bgemm_partial_bytes(const BGemmArgs& g) {
+    return g.nsplit > 1 ? (size_t)g.nsplit * (size_t)g.nbatch * g.M * g.N * sizeof(double2) : 0;
+}
+
+namespace {
+template <int TM, int TN>
+cudaError_t launch_bgemm_t(const BGemmArgs& g, void* scratch, int* exps, cudaStream_t s) {
+    const size_t smem = bgemm_smem(g);
+    const unsigned blocks = (unsigned)(g.nbatch * g.nsplit);
+    double2* partial = static_cast<double2*>(scratch);
+    const int nthr = g.thr_m * g.thr_n;
+    if (exps) contract_bgemm_kernel<TM, TN, true><<<blocks, nthr, smem, s>>>(g, partial, exps);
+    else contract_bgemm_kernel<TM, TN, false><<<blocks, nthr, smem, s>>>(g, partial, exps);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_bgemm(const BGemmArgs& g, void* scratch, int* exps, cudaStream_t s, int* launches) {
+    const int TM = g.M / g.thr_m, TN = g.N / g.thr_n;
+    cudaError_t e = cudaErrorInvalidValue;
+    if (g.nsplit > 1 && !scratch) return cudaErrorInvalidValue;
+    if (TM == 4 && TN == 4) e = launch_bgemm_t<4, 4>(g, scratch, exps, s);
+    else if (TM == 4 && TN == 2) e = launch_bgemm_t<4, 2>(g, scratch, exps, s);
+    else if (TM == 2 && TN == 4) e = launch_bgemm_t<2, 4>(g, scratch, exps, s);
+    else if (TM == 2 && TN == 2) e = launch_bgemm_t<2, 2>(g, scratch, exps, s);
+    if (e != cudaSuccess) return e;
+    if (launches) *launches = 1;
+    if (g.nsplit > 1) {
+        const int64_t total = g.nbatch * g.M * g.N;
+        const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
+        if (exps) bgemm_reduce_kernel<true><<<grid, 256, 0, s>>>(g, static_cast<const double2*>(scratch), exps);
+        else bgemm_reduce_kernel<false><<<grid, 256, 0, s>>>(g, static_cast<const double2*>(scratch), exps);
+        if (launches) *launches = 2;
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+}  // namespace qxg

@@ -1073,6 +1073,8 @@ size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
     RowArgs ra;
     Rows2Args r2;
     if (use_rows2(a, fp64, &ra, &r2) || plan_rows(a, fp64 ? 16 : 32, &ra)) return 0;
+    BGemmArgs bg;
+    if (!fp64 && plan_bgemm(a, sm_count, &bg)) return bgemm_partial_bytes(bg);
     LSumArgs la;
     int NA = 0, NB = 0;
     if (!fp64 && plan_lsum(a, sm_count, &la, &NA, &NB)) return lsum_partial_bytes(la, NA, NB);
@@ -1080,10 +1082,21 @@ size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
     return ns > 0 ? (size_t)ns * (size_t)a.nC * (fp64 ? 16 : 8) : 0;
 }
 
+// The CUDA cores serve two kinds of long sums better than a tensor-core GEMM: the batched small
+// GEMM of a final join (both operands large, so the tensor cores' packed planes would be several
+// times the operand), and the long sum of a step with few results (a gate's gradient: tens of
+// results, each a sum over the whole network).  Other steps with many results and a long sum are
+// independent GEMMs that the tensor cores serve at a far higher rate than the long sum, so they
+// are left to the tensor-core planner (it falls back to the CUDA cores when it cannot serve them).
+constexpr int64_t kLSumPreferMaxResults = int64_t(1) << 12;
+
 bool contract_prefers_cuda_cores(const StepArgs& a, bool fp64, int sm_count) {
+    if (fp64) return false;
+    BGemmArgs bg;
+    if (plan_bgemm(a, sm_count, &bg)) return true;
     LSumArgs la;
     int NA = 0, NB = 0;
-    return !fp64 && plan_lsum(a, sm_count, &la, &NA, &NB) && la.nrc <= 2;
+    return a.nC <= kLSumPreferMaxResults && plan_lsum(a, sm_count, &la, &NA, &NB) && la.nrc <= 2;
 }
 
 template <int NA, int NB>
@@ -1183,6 +1196,8 @@ const char* contract_form(const StepArgs& a, bool fp64, int sm_count) {
     Rows2Args r2;
     if (use_rows2(a, fp64, &ra, &r2)) return "cuda-core compact row-form";
     if (plan_rows(a, fp64 ? 16 : 32, &ra)) return "cuda-core row-form";
+    BGemmArgs bg;
+    if (!fp64 && plan_bgemm(a, sm_count, &bg)) return "cuda-core batched-gemm";
     LSumArgs la;
     int NA = 0, NB = 0;
     if (!fp64 && plan_lsum(a, sm_count, &la, &NA, &NB)) return "cuda-core long-sum";
@@ -1196,6 +1211,10 @@ cudaError_t launch_contract(const StepArgs& a, bool fp64, int* exps, cudaStream_
     Rows2Args r2;
     if (use_rows2(a, fp64, &ra, &r2)) return launch_rows2(r2, ra.K, r2.ncol, exps, s, sm_count);
     if (!plan_rows(a, fp64 ? 16 : 32, &ra)) {
+        BGemmArgs bg;
+        if (!fp64 && plan_bgemm(a, sm_count, &bg) &&
+            (bg.nsplit == 1 || (scratch && scratch_bytes >= bgemm_partial_bytes(bg))))
+            return launch_bgemm(bg, scratch, exps, s, launches);
         LSumArgs la;
         int NA = 0, NB = 0;
         if (!fp64 && plan_lsum(a, sm_count, &la, &NA, &NB) && scratch && scratch_bytes >= lsum_partial_bytes(la, NA, NB)) {

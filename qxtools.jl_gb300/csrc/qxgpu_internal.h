@@ -166,9 +166,10 @@ size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count);
 bool contract_x_is_b(const StepArgs& a, bool fp64);
 // The CUDA-core form launch_contract picks for a step (for diagnostics).
 const char* contract_form(const StepArgs& a, bool fp64, int sm_count);
-// Whether a step with few results and a long sum is better served by the long sum on the
-// CUDA cores than by a tensor-core GEMM: the long sum reads every element of the operand with
-// more result bits once and the other at most twice.
+// Whether a step with a long sum is better served on the CUDA cores than by a tensor-core GEMM:
+// the batched small GEMM of a final join (both operands large), or the long sum of a step with few
+// results (it reads every element of the operand with more result bits once and the other at most
+// twice).
 bool contract_prefers_cuda_cores(const StepArgs& a, bool fp64, int sm_count);
 // Run n batched steps (device array, blocks numbered consecutively, nblocks in all).
 cudaError_t launch_batch(const BatchStep* d_steps, int n, int nblocks, bool fp64, int* exps, cudaStream_t s);

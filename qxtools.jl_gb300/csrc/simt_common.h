@@ -123,6 +123,37 @@ struct Rows2Args {
 constexpr int kRows2MaxY = 8192;        // elements of Y (a 16-byte quadruple each in shared memory)
 constexpr int kRows2MaxYBits = 13;
 
+// Batched small GEMM with a long sum (kernels_bgemm.cu): C[b, m, n] = sum_k A[b, m, k] B[b, k, n]
+// with 4..64 free values per side and at least 2^10 summed terms, both operands large -- the
+// final joins of sliced, bitstring-batched trees.
+constexpr int kBGemmMaxL = 8;           // operand elements one thread loads per chunk (per operand)
+struct BGemmArgs {
+    const float2* A;
+    const float2* B;
+    float2* C;
+    int32_t M, N;              // free values of A (rows) and of B (columns) per batch value
+    int32_t thr_m, thr_n;      // thread grid: thread (tm, tn) owns rows tm + thr_m i, columns tn + thr_n j
+    int32_t kc;                // summed values per chunk
+    int32_t la, lb;            // A / B elements one thread loads per chunk
+    int64_t nchunks;           // chunks of one K range
+    int32_t nsplit;            // K ranges per batch value (a power of two)
+    int32_t flush;             // chunks between FP64 accumulations
+    int64_t nbatch;
+    int32_t conjA, conjB, expA, expB, expC;
+    BitMap bA, bB, bC;         // batch index -> A / B / C offset
+    BitMap mC, nC;             // m / n -> C offset
+    BitMap eA, eB;             // chunk element (in address order) -> A / B offset within the chunk
+    BitMap eAm, eAk, eBn, eBk; // chunk element -> m / k-in-chunk (A); n / k-in-chunk (B)
+    BitMap hA, hB;             // chunk index within the whole K -> A / B offset
+};
+// Fill the batched small GEMM form of a step (false: the step does not fit it); both operands
+// need at least 2^min_log2 elements.
+bool plan_bgemm(const StepArgs& s, int sm_count, BGemmArgs* g, int min_log2 = 20);
+// Scratch for the FP64 partials of its K ranges (0 with one range per batch value).
+size_t bgemm_partial_bytes(const BGemmArgs& g);
+// Launch it (and the ordered sum of the K-range partials); *launches receives 1 or 2.
+cudaError_t launch_bgemm(const BGemmArgs& g, void* scratch, int* exps, cudaStream_t s, int* launches);
+
 // Consecutive (src, dst) pairs with both sides increasing by one collapse into one run.
 bool make_runs(const std::vector<std::pair<int, int>>& pairs, BitMap* m);
 // Fill the compact row form from a row form (false: the step does not fit it).

@@ -878,20 +878,22 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
     }
 }
 
-// Split-K sum: C[c] = sum over the K blocks s (in order) of partial[s * nC + c], raising the
-// result's exponent slot (the partials share the result's scale).
+// Split-K sum: C[c] = sum over the K blocks s (in order, in FP64) of partial[s * nC + c], raising
+// the result's exponent slot (the partials share the result's scale).
 __global__ void tc_ksum_kernel(const float2* __restrict__ partial, float2* __restrict__ C, int64_t nC, int nsplit,
                                int* exps, int exp_c) {
     int emax = -2139062144;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nC; c += (int64_t)gridDim.x * blockDim.x) {
-        float re = 0.f, im = 0.f;
+        // FP64 sum of the FP32 block partials: thousands of blocks add no error of their own
+        double re = 0.0, im = 0.0;
         for (int j = 0; j < nsplit; j++) {
             const float2 v = partial[(int64_t)j * nC + c];
-            re += v.x;
-            im += v.y;
+            re += (double)v.x;
+            im += (double)v.y;
         }
-        C[c] = make_float2(re, im);
-        const float mx = fmaxf(fabsf(re), fabsf(im));
+        const float2 r = make_float2((float)re, (float)im);
+        C[c] = r;
+        const float mx = fmaxf(fabsf(r.x), fabsf(r.y));
         if (mx > 0.f) emax = max(emax, exp_of(mx));
     }
     for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));

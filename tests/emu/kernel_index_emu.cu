@@ -5,17 +5,23 @@
 //     rows2_fill / rows2_walk, run for every lane of every warp;
 //   * long sum (kernels_simt.cu): plan_lsum and the phases lsum_fill / lsum_walk /
 //     lsum_lane_block, the FP64 butterfly over lanes and the warp-order sums emulated as the
-//     kernel performs them, and lsum_reduce_one.
+//     kernel performs them, and lsum_reduce_one;
+//   * batched small GEMM (kernels_bgemm.cu): plan_bgemm (with a lower operand-size floor, so
+//     the cases stay small) and the phases bgemm_elem_a/_b, bgemm_base_a/_b, bgemm_quad_a/_b,
+//     bgemm_chunk, bgemm_flush, bgemm_c_offset and bgemm_reduce_one, run for every thread of every
+//     block over exactly sized shared-memory buffers and partials.
 //
 // Paired FP32 FMAs run as two fused multiply-adds on the host.  Inputs are seeded; every layout
 // is a random permutation of operand bits (rows, summed, result columns, batch bits), with and
 // without conjugation.  Exit status 0 when every case agrees within 1e-5 of its largest result.
 #include "../../qxtools.jl_gb300/csrc/kernels_simt.cu"
 #include "../../qxtools.jl_gb300/csrc/kernels_rows.cu"
+#include "../../qxtools.jl_gb300/csrc/kernels_bgemm.cu"
 
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
+#include <array>
 #include <random>
 
 using namespace qxg;
@@ -264,6 +270,118 @@ int lsum_case(std::mt19937& rng, int nk, int na, int nb, int ng, bool cA_, bool 
     return 1;
 }
 
+static int g_bgemm_split = 0;
+
+template <int TM, int TN>
+void emulate_bgemm(const BGemmArgs& g, std::vector<double2>& partial) {
+    const int nthr = g.thr_m * g.thr_n;
+    for (int64_t blk = 0; blk < g.nbatch * g.nsplit; blk++) {
+        const int64_t bi = blk % g.nbatch, si = blk / g.nbatch;
+        std::vector<float4> As((size_t)2 * g.kc * g.M), Bs((size_t)2 * g.kc * g.N);
+        std::vector<std::array<unsigned long long, TM * TN>> acc(nthr);
+        std::vector<std::array<double2, TM * TN>> dacc(nthr);
+        for (int t = 0; t < nthr; t++)
+            for (int q = 0; q < TM * TN; q++) { acc[t][q] = 0ull; dacc[t][q] = make_double2(0, 0); }
+        for (int64_t c = 0; c < g.nchunks; c++) {
+            const int buf = (int)(c & 1);
+            for (int t = 0; t < nthr; t++)
+                for (int j = 0; j < kBGemmMaxL; j++) {
+                    int64_t off;
+                    int slot;
+                    if (j < g.la) {
+                        bgemm_elem_a(g, t, j, &off, &slot);
+                        As.at((size_t)buf * g.kc * g.M + (size_t)slot) =
+                            bgemm_quad_a(g.A[bgemm_base_a(g, bi, si, c) + off], 1.f, g.conjA ? -1.f : 1.f);
+                    }
+                    if (j < g.lb) {
+                        bgemm_elem_b(g, t, j, &off, &slot);
+                        Bs.at((size_t)buf * g.kc * g.N + (size_t)slot) =
+                            bgemm_quad_b(g.B[bgemm_base_b(g, bi, si, c) + off], 1.f, g.conjB ? -1.f : 1.f);
+                    }
+                }
+            for (int t = 0; t < nthr; t++) {
+                unsigned long long a2[TM][TN];
+                double2 d2[TM][TN];
+                for (int i = 0; i < TM; i++)
+                    for (int j = 0; j < TN; j++) { a2[i][j] = acc[t][i * TN + j]; d2[i][j] = dacc[t][i * TN + j]; }
+                bgemm_chunk<TM, TN>(g, As.data() + (size_t)buf * g.kc * g.M, Bs.data() + (size_t)buf * g.kc * g.N,
+                                    t / g.thr_n, t % g.thr_n, a2);
+                if ((c + 1) % g.flush == 0 || c + 1 == g.nchunks) bgemm_flush<TM, TN>(a2, d2);
+                for (int i = 0; i < TM; i++)
+                    for (int j = 0; j < TN; j++) { acc[t][i * TN + j] = a2[i][j]; dacc[t][i * TN + j] = d2[i][j]; }
+            }
+        }
+        for (int t = 0; t < nthr; t++) {
+            const int tm = t / g.thr_n, tn = t % g.thr_n;
+            for (int i = 0; i < TM; i++)
+                for (int j = 0; j < TN; j++) {
+                    const int m = tm + i * g.thr_m, n = tn + j * g.thr_n;
+                    const double2 v = dacc[t][i * TN + j];
+                    if (g.nsplit == 1) g.C[bgemm_c_offset(g, bi, m, n)] = make_float2((float)v.x, (float)v.y);
+                    else partial.at((size_t)((si * g.nbatch + bi) * g.M + m) * g.N + n) = v;
+                }
+        }
+    }
+    if (g.nsplit > 1)
+        for (int64_t idx = 0; idx < g.nbatch * g.M * g.N; idx++) {
+            int64_t off;
+            const float2 v = bgemm_reduce_one(g, partial.data(), idx, &off);
+            g.C[off] = v;
+        }
+}
+
+int bgemm_case(std::mt19937& rng, int nk, int na, int nb, int ng, bool cA_, bool cB_, int* used) {
+    const int abits = na + ng + nk, bbits = nb + ng + nk, cbits = na + nb + ng;
+    std::vector<int> ap(abits), bp(bbits), cp(cbits);
+    for (int i = 0; i < abits; i++) ap[i] = i;
+    for (int i = 0; i < bbits; i++) bp[i] = i;
+    for (int i = 0; i < cbits; i++) cp[i] = i;
+    std::shuffle(ap.begin(), ap.end(), rng);
+    std::shuffle(bp.begin(), bp.end(), rng);
+    std::shuffle(cp.begin(), cp.end(), rng);
+    std::vector<std::pair<int,int>> cA, cB, kA, kB;
+    for (int j = 0; j < na; j++) cA.push_back({cp[j], ap[j]});
+    for (int j = 0; j < nb; j++) cB.push_back({cp[na + j], bp[j]});
+    for (int j = 0; j < ng; j++) { cA.push_back({cp[na + nb + j], ap[na + j]}); cB.push_back({cp[na + nb + j], bp[nb + j]}); }
+    for (int j = 0; j < nk; j++) { kA.push_back({j, ap[na + ng + j]}); kB.push_back({j, bp[nb + ng + j]}); }
+    const int64_t NA_ = int64_t(1) << abits, NB_ = int64_t(1) << bbits, NC = int64_t(1) << cbits;
+    std::vector<float2> A(NA_), B(NB_), C(NC, make_float2(NAN, NAN));
+    std::uniform_real_distribution<double> U(-1, 1);
+    for (int64_t i = 0; i < NA_; i++) A[i] = make_float2(U(rng), U(rng));
+    for (int64_t i = 0; i < NB_; i++) B[i] = make_float2(U(rng), U(rng));
+    StepArgs s; memset(&s, 0, sizeof(s));
+    s.A = A.data(); s.B = B.data(); s.C = C.data(); s.nC = NC; s.nk = nk; s.conjA = cA_; s.conjB = cB_;
+    s.cA = mk(cA); s.cB = mk(cB); s.kA = mk(kA); s.kB = mk(kB);
+    BGemmArgs g;
+    if (!plan_bgemm(s, 1 + rng() % 8, &g, 12)) return 0;
+    (*used)++;
+    if (g.nsplit > 1) g_bgemm_split++;
+    std::vector<double2> partial(bgemm_partial_bytes(g) / sizeof(double2), make_double2(NAN, NAN));
+    const int TM = g.M / g.thr_m, TN = g.N / g.thr_n;
+    if (TM == 4 && TN == 4) emulate_bgemm<4, 4>(g, partial);
+    else if (TM == 4 && TN == 2) emulate_bgemm<4, 2>(g, partial);
+    else if (TM == 2 && TN == 4) emulate_bgemm<2, 4>(g, partial);
+    else if (TM == 2 && TN == 2) emulate_bgemm<2, 2>(g, partial);
+    else { printf("no instance TM=%d TN=%d\n", TM, TN); return -1; }
+    double maxerr = 0, maxv = 0;
+    for (int64_t c = 0; c < NC; c++) {
+        std::complex<double> acc = 0;
+        for (int64_t k = 0; k < (int64_t(1) << nk); k++) {
+            float2 x = A[pdep(c, s.cA) + pdep(k, s.kA)], y = B[pdep(c, s.cB) + pdep(k, s.kB)];
+            acc += std::complex<double>(x.x, cA_ ? -x.y : x.y) * std::complex<double>(y.x, cB_ ? -y.y : y.y);
+        }
+        const double e = std::abs(acc - std::complex<double>(C[c].x, C[c].y));
+        if (!(e <= 1e30)) { maxerr = INFINITY; break; }
+        maxerr = std::max(maxerr, e);
+        maxv = std::max(maxv, std::abs(acc));
+    }
+    if (!(maxerr <= 1e-5 * std::max(1.0, maxv))) {
+        printf("FAIL bgemm nk=%d na=%d nb=%d ng=%d kc=%d thr=%dx%d nsplit=%d err=%g max=%g\n", nk, na, nb, ng, g.kc,
+               g.thr_m, g.thr_n, g.nsplit, maxerr, maxv);
+        return -1;
+    }
+    return 1;
+}
 
 int main(int argc, char** argv) {
     const unsigned seed = argc > 1 ? (unsigned)atoi(argv[1]) : 1u;
@@ -284,7 +402,17 @@ int main(int argc, char** argv) {
         const int na = 5 + rng() % 2, nb = 4 + rng() % 2, ng = rng() % 2;
         if (lsum_case(rng, 12, na, nb, ng, rng() % 2, rng() % 2, &lsum_used) < 0) lsum_fail++;
     }
-    printf("compact row form: %d cases, %d failed; long sum: %d cases (%d in chunks), %d failed\n", rows_used,
-           rows_fail, lsum_used, g_lsum_chunked, lsum_fail);
-    return rows_fail || lsum_fail || rows_used == 0 || lsum_used == 0 ? 1 : 0;
+    int bg_used = 0, bg_fail = 0;
+    for (int it = 0; it < nsums / 2; it++) {        // both operands of 2^12 and more elements
+        const int na = 2 + rng() % 5, nb = 2 + rng() % 5, ng = rng() % 4;
+        if (na + nb < 8 || na + nb > 10) continue;
+        const int nk = std::max(10, 13 - ng) + (int)(rng() % 2);
+        if (bgemm_case(rng, nk, na, nb, ng, rng() % 2, rng() % 2, &bg_used) < 0) bg_fail++;
+    }
+    for (int it = 0; it < 4; it++)                  // one batch value, K cut into ranges
+        if (bgemm_case(rng, 14, 4 + it % 2, 4, 0, rng() % 2, rng() % 2, &bg_used) < 0) bg_fail++;
+    printf("compact row form: %d cases, %d failed; long sum: %d cases (%d in chunks), %d failed; batched gemm: %d "
+           "cases (%d with K ranges), %d failed\n", rows_used, rows_fail, lsum_used, g_lsum_chunked, lsum_fail, bg_used,
+           g_bgemm_split, bg_fail);
+    return rows_fail || lsum_fail || bg_fail || rows_used == 0 || lsum_used == 0 || bg_used == 0 ? 1 : 0;
 }

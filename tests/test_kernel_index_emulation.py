@@ -1,12 +1,14 @@
-"""Index work of the compact row-form and long-sum kernels, emulated on the CPU.
+"""Index work of the compact row-form, long-sum and batched small GEMM kernels, emulated on the CPU.
 
-The two kernels keep their addressing in `__host__ __device__` phase functions (fill, walk,
-per-lane blocks, reduce); `tests/emu/kernel_index_emu.cu` runs those phases for every lane of every
-warp on seeded random bit layouts -- permuted row, summed, column and batch bits, conjugation,
-16-byte pairs, column chunks, short row counts, result chunks across the grid -- and compares each
-result with a direct evaluation of the contraction (within 1e-5 of the largest result).  The host
-build uses AddressSanitizer, so an index that leaves an operand, a shared-memory table or the
-partial buffer fails the test.  Needs nvcc (the harness includes the kernel sources); no GPU.
+The kernels keep their addressing in `__host__ __device__` phase functions (fill, walk, per-lane
+blocks, chunk elements and bases, reduce); `tests/emu/kernel_index_emu.cu` runs those phases for
+every lane of every warp (every thread of every block for the batched GEMM) on seeded random bit
+layouts -- permuted row, summed, column and batch bits, conjugation, 16-byte pairs, column chunks,
+short row counts, result chunks across the grid, K cut into ranges with FP64 partials -- and
+compares each result with a direct evaluation of the contraction (within 1e-5 of the largest
+result).  The host build uses AddressSanitizer, so an index that leaves an operand, a shared-memory
+buffer or table, or the partial buffer fails the test.  Needs nvcc (the harness includes the kernel
+sources); no GPU.
 """
 import os
 import shutil
