@@ -177,3 +177,37 @@ def test_tuning_decisions_carry_over(q, gpu_lib):
     assert np.array_equal(got1, got2)
     with pytest.raises(q.QXGError):
         q.Executor(prog, precision="split_tf32").set_tuning("zz 1 7 0 0 0\n")
+
+
+@pytest.mark.parametrize("precision", ["fp32", "split_tf32"])
+@pytest.mark.parametrize("nk,na,nb,ng", [(12, 5, 5, 3), (15, 5, 5, 0), (13, 6, 4, 3), (11, 6, 6, 4)])
+def test_batched_join_gemm(q, gpu_lib, precision, nk, na, nb, ng):
+    """The final-join shape: both operands large (2^20-2^22 elements), 2^4-2^6 free values on
+    each side, 2^11-2^15 summed terms and 2^0-2^4 batch values, under random label orders.  It
+    runs on the batched small GEMM (the plan's explanation names it), with K cut into ranges whose
+    FP64 partials are added in order when there is one batch value; FP32 products with FP64
+    accumulation every 512 terms stay within 1e-6 of the largest result of einsum, and a second
+    call gives the same bits."""
+    rng = np.random.default_rng(nk * 1000 + na * 100 + nb * 10 + ng)
+    kl = list(range(1, nk + 1))
+    al, bl, gl = list(range(100, 100 + na)), list(range(200, 200 + nb)), list(range(300, 300 + ng))
+    la = [int(v) for v in rng.permutation(al + gl + kl)]
+    lb = [int(v) for v in rng.permutation(bl + gl + kl)]
+    lc = [int(v) for v in rng.permutation(al + bl + gl)]
+    A = rng.standard_normal((2,) * len(la)) + 1j * rng.standard_normal((2,) * len(la))
+    B = rng.standard_normal((2,) * len(lb)) + 1j * rng.standard_normal((2,) * len(lb))
+    cmds = [q.Load("a", "data_1", A.shape), q.Load("b", "data_2", B.shape),
+            q.Ncon("c", tuple(lc), "a", tuple(la), "b", tuple(lb)), q.Save("output", "c")]
+    prog = q.Programme.from_commands(cmds, OrderedDict([("data_1", A), ("data_2", B)]), 0)
+    letters = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
+    idx = {v: letters[i] for i, v in enumerate(sorted(set(la + lb)))}
+    sub = lambda ls: "".join(idx[v] for v in ls)
+    ref = np.einsum(f"{sub(la)},{sub(lb)}->{sub(lc)}", A, B).reshape(-1, order="F")
+    with q.Executor(prog, precision=precision) as ex:
+        got = ex.amplitudes([""])[0]
+        got2 = ex.amplitudes([""])[0]
+        assert "batched-gemm" in ex.explain(2), ex.explain(2)
+        assert ex.info()["num_steps_tensor_core"] == 0
+    err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    assert err <= 1e-6, err
+    assert np.array_equal(got, got2)
