@@ -67,27 +67,35 @@ __host__ __device__ __forceinline__ float4 bgemm_quad_b(float2 v, float s, float
     const float br = v.x * s, bi = v.y * si;
     return make_float4(br, bi, bi, br);
 }
-// One chunk's products for thread (tm, tn): rows tm + thr_m i, columns tn + thr_n j.
+// One chunk's products for thread (tm, tn): rows tm + thr_m i, columns tn + thr_n j.  A
+// quadruple is read as two 64-bit halves -- (ar, ar) and (-ai, ai); (br, bi) and (bi, br) -- which
+// are the paired FMAs' operands as they lie, so no value is repacked; the chunk is walked with
+// pointer increments (kc is a multiple of 8).
 template <int TM, int TN>
 __host__ __device__ __forceinline__ void bgemm_chunk(const BGemmArgs& g, const float4* as, const float4* bs, int tm,
                                                      int tn, unsigned long long (&acc)[TM][TN]) {
-    as += tm;
-    bs += tn;
+    const ulonglong2* pa[TM];
+    const ulonglong2* pb[TN];
+#pragma unroll
+    for (int i = 0; i < TM; i++) pa[i] = reinterpret_cast<const ulonglong2*>(as) + tm + i * g.thr_m;
+#pragma unroll
+    for (int j = 0; j < TN; j++) pb[j] = reinterpret_cast<const ulonglong2*>(bs) + tn + j * g.thr_n;
+    const int M = g.M, N = g.N;
+#pragma unroll 4
     for (int k = 0; k < g.kc; k++) {
-        float4 qa[TM], qb[TN];
+        ulonglong2 qa[TM], qb[TN];
 #pragma unroll
-        for (int i = 0; i < TM; i++) qa[i] = as[k * g.M + i * g.thr_m];
+        for (int i = 0; i < TM; i++) { qa[i] = *pa[i]; pa[i] += M; }
 #pragma unroll
-        for (int j = 0; j < TN; j++) qb[j] = bs[k * g.N + j * g.thr_n];
+        for (int j = 0; j < TN; j++) { qb[j] = *pb[j]; pb[j] += N; }
 #pragma unroll
-        for (int i = 0; i < TM; i++) {
-            const unsigned long long a1 = f2pack(qa[i].x, qa[i].y), a2 = f2pack(qa[i].z, qa[i].w);
+        for (int i = 0; i < TM; i++)
 #pragma unroll
-            for (int j = 0; j < TN; j++) {
-                fma2(acc[i][j], a1, f2pack(qb[j].x, qb[j].y));
-                fma2(acc[i][j], a2, f2pack(qb[j].z, qb[j].w));
-            }
-        }
+            for (int j = 0; j < TN; j++) fma2(acc[i][j], qa[i].x, qb[j].x);
+#pragma unroll
+        for (int i = 0; i < TM; i++)
+#pragma unroll
+            for (int j = 0; j < TN; j++) fma2(acc[i][j], qa[i].y, qb[j].y);
     }
 }
 template <int TM, int TN>
@@ -130,27 +138,28 @@ __global__ void __launch_bounds__(256) contract_bgemm_kernel(const BGemmArgs g, 
     const int64_t si = (int64_t)blockIdx.x / g.nbatch;
     float4* As = bg_smem;                                  // [2][kc][M]
     float4* Bs = bg_smem + 2 * g.kc * g.M;                 // [2][kc][N]
+    const int nthr = g.thr_m * g.thr_n;
+    // per-thread element offsets and slots of a chunk, [j][thread] (kept out of registers)
+    int64_t* toffA = reinterpret_cast<int64_t*>(Bs + 2 * g.kc * g.N);
+    int64_t* toffB = toffA + g.la * nthr;
+    int* tslotA = reinterpret_cast<int*>(toffB + g.lb * nthr);
+    int* tslotB = tslotA + g.la * nthr;
     float sa = 1.f, sb = 1.f;
     if (SCALED) {
         sa = pow2f(-read_m(exps, g.expA));
         sb = pow2f(-read_m(exps, g.expB));
     }
     const float sai = g.conjA ? -sa : sa, sbi = g.conjB ? -sb : sb;
-    int64_t offA[kBGemmMaxL], offB[kBGemmMaxL];
-    int slotA[kBGemmMaxL], slotB[kBGemmMaxL];
-#pragma unroll
-    for (int j = 0; j < kBGemmMaxL; j++) {
-        bgemm_elem_a(g, tid, j, &offA[j], &slotA[j]);
-        bgemm_elem_b(g, tid, j, &offB[j], &slotB[j]);
-    }
+    for (int j = 0; j < g.la; j++) bgemm_elem_a(g, tid, j, &toffA[j * nthr + tid], &tslotA[j * nthr + tid]);
+    for (int j = 0; j < g.lb; j++) bgemm_elem_b(g, tid, j, &toffB[j * nthr + tid], &tslotB[j * nthr + tid]);
     float2 ra[kBGemmMaxL], rb[kBGemmMaxL];
     auto fetch = [&](int64_t c) {
         const float2* a = g.A + bgemm_base_a(g, bi, si, c);
         const float2* b = g.B + bgemm_base_b(g, bi, si, c);
 #pragma unroll
         for (int j = 0; j < kBGemmMaxL; j++) {
-            if (j < g.la) ra[j] = __ldg(a + offA[j]);
-            if (j < g.lb) rb[j] = __ldg(b + offB[j]);
+            if (j < g.la) ra[j] = __ldg(a + toffA[j * nthr + tid]);
+            if (j < g.lb) rb[j] = __ldg(b + toffB[j * nthr + tid]);
         }
     };
     auto stage = [&](int buf) {
@@ -158,8 +167,8 @@ __global__ void __launch_bounds__(256) contract_bgemm_kernel(const BGemmArgs g, 
         float4* bs = Bs + buf * g.kc * g.N;
 #pragma unroll
         for (int j = 0; j < kBGemmMaxL; j++) {
-            if (j < g.la) as[slotA[j]] = bgemm_quad_a(ra[j], sa, sai);
-            if (j < g.lb) bs[slotB[j]] = bgemm_quad_b(rb[j], sb, sbi);
+            if (j < g.la) as[tslotA[j * nthr + tid]] = bgemm_quad_a(ra[j], sa, sai);
+            if (j < g.lb) bs[tslotB[j * nthr + tid]] = bgemm_quad_b(rb[j], sb, sbi);
         }
     };
     unsigned long long acc[TM][TN];
@@ -236,7 +245,10 @@ int ilog2(int64_t x) {
     return b;
 }
 
-size_t bgemm_smem(const BGemmArgs& g) { return (size_t)2 * g.kc * (g.M + g.N) * sizeof(float4); }
+// Two chunk buffers of quadruples, then the per-thread offset (8 bytes) and slot (4 bytes) tables.
+size_t bgemm_smem(const BGemmArgs& g) {
+    return (size_t)2 * g.kc * (g.M + g.N) * sizeof(float4) + (size_t)(g.la + g.lb) * g.thr_m * g.thr_n * 12;
+}
 
 // A run of length one per element bit: the element index's bits go to scattered places.
 bool bit_runs(const std::vector<std::pair<int, int>>& p, BitMap* m) {
@@ -290,11 +302,16 @@ bool plan_bgemm(const StepArgs& s, int sm_count, BGemmArgs* g, int min_log2) {
     a.thr_n = a.N / TN;
     // summed values per chunk: every thread loads 1..kBGemmMaxL elements of each operand, and the
     // two buffers fit kBGemmMaxSmem
-    int kc = 1;
+    auto smem_of = [&](int kc_) {
+        return (size_t)2 * kc_ * (a.M + a.N) * 16 + (size_t)((int64_t)(a.M + a.N) * kc_ / nthr) * nthr * 12;
+    };
+    int kc = 8;
     while (kc * 2 <= 64 && (int64_t)a.M * kc * 2 <= (int64_t)nthr * kBGemmMaxL &&
-           (int64_t)a.N * kc * 2 <= (int64_t)nthr * kBGemmMaxL && (size_t)2 * kc * 2 * (a.M + a.N) * 16 <= kBGemmMaxSmem)
+           (int64_t)a.N * kc * 2 <= (int64_t)nthr * kBGemmMaxL && smem_of(kc * 2) <= kBGemmMaxSmem)
         kc *= 2;
-    if ((int64_t)a.M * kc < nthr || (int64_t)a.N * kc < nthr) return false;
+    if ((int64_t)a.M * kc < nthr || (int64_t)a.N * kc < nthr || (int64_t)a.M * kc > (int64_t)nthr * kBGemmMaxL ||
+        (int64_t)a.N * kc > (int64_t)nthr * kBGemmMaxL || smem_of(kc) > kBGemmMaxSmem)
+        return false;
     const int lkc = ilog2(kc);
     if (lkc > s.nk) return false;
     a.kc = kc;

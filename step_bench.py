@@ -34,6 +34,11 @@ CASES = {
     "rqc_1162": ("kbkrbrrrrrrkbrbbrbkrrrkrrr", "krrrrrrkknnkk", "nbnrbrrrrrrbrbbrbrrrrrr"),
     "param_1521": ("rrrrrrrrrrrrkrrrrrrkrrrrrr", "nnkk", "rrrrrrrrrrrrnrrrrrrnrrrrrr"),
     "param_1534": ("rrrrrrrrrrkrrrrrkkrrrrrrrrrrrrk", "nnkkkk", "rrrrrrrrrrnrrrrrnrrrrrrrrrrrr"),
+    # final joins (the batched small GEMM), with fewer batch / summed bits than the full passes:
+    # 7x7 stand-in: 32 x 32 results per batch value, 2^17 summed, 2^5 batch values (2^11 in a pass)
+    "join_7x7": ("rrrrbkkrbkkkkbkkkbkkkbkkkkk", "nnnnrkknrkkkkrkkkrkkkrkkkkk", "rrrrbnnnnnrbbbb"),
+    # 6x6, 14 cycles: 64 x 16 results per batch value, 2^16 summed (2^22 in a pass), 2^5 batch values
+    "join_6x6": ("kbbbbbrkkkrrrkkrrkkkkkkkkkk", "kkkkknnnnrrrrrkkkkkkkkkkk", "bbbbbrrrrrrnnnn"),
 }
 
 
@@ -126,8 +131,11 @@ def main():
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / args.reps
         nbytes = 8 * (X.numel() + Y.numel() + C.numel())
+        nk = len([v for v in lx if v in ly and v not in lc])
+        flops = 8.0 * C.numel() * 2 ** nk
         print(json.dumps({"case": name, "drop": args.drop, "x_log2": len(lx), "y_log2": len(ly), "c_log2": len(lc),
-                          "ms": round(ms, 4), "gb_s": round(nbytes / ms / 1e6, 1)}), flush=True)
+                          "ms": round(ms, 4), "gb_s": round(nbytes / ms / 1e6, 1),
+                          "tflop_s": round(flops / ms / 1e9, 2)}), flush=True)
         del X, Y, C
 
 
