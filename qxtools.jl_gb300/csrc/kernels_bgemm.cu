@@ -34,21 +34,63 @@
 namespace qxg {
 
 constexpr int kFlushK = 512;            // FP32 terms per thread before the FP64 accumulation
-constexpr size_t kBGemmMaxSmem = 48 * 1024;
+constexpr size_t kBGemmMaxSmem = 96 * 1024;
+
+// ---- tile geometry, fixed at compile time per result shape (M x N per batch value) ----------------
+//   threads    64 up to 1024 results per batch value, else M N / 16;
+//   TM x TN    results per thread (4 or 2 each): thread (tm, tn) owns rows tm TM .. + TM-1 and
+//              columns tn TN .. + TN-1;
+//   KC         summed values per chunk: every thread loads 1..kBGemmMaxL elements of each operand
+//              per chunk and the block's shared memory stays within kBGemmMaxSmem;
+//   layout     a chunk's A quadruples as [k][row group][TM + 1] (one padding quadruple per group
+//              keeps the groups of a warp in different banks), B as [k][column group][TN + 1].
+struct BGemmShape {
+    int M, N, nthr, tm, tn, thr_m, thr_n, kc, la, lb, ra, rb;
+    size_t smem;
+};
+constexpr BGemmShape bgemm_shape(int M, int N) {
+    BGemmShape g{M, N, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    g.nthr = M * N / 16 > 64 ? M * N / 16 : 64;
+    const int cand[4][2] = {{4, 4}, {2, 4}, {4, 2}, {2, 2}};     // (tm, tn)
+    for (int c = 0; c < 4 && !g.tm; c++)
+        if (M % cand[c][0] == 0 && N % cand[c][1] == 0 && (M / cand[c][0]) * (N / cand[c][1]) == g.nthr) {
+            g.tm = cand[c][0];
+            g.tn = cand[c][1];
+        }
+    if (!g.tm) return g;
+    g.thr_m = M / g.tm;
+    g.thr_n = N / g.tn;
+    g.ra = g.thr_m * (g.tm + 1);
+    g.rb = g.thr_n * (g.tn + 1);
+    for (int kc = 8; kc <= 64; kc *= 2) {
+        const size_t smem = (size_t)2 * kc * (g.ra + g.rb) * 16 + (size_t)(M + N) * kc * 12;
+        if (M * kc < g.nthr || N * kc < g.nthr || M * kc > g.nthr * kBGemmMaxL || N * kc > g.nthr * kBGemmMaxL ||
+            smem > kBGemmMaxSmem)
+            continue;
+        g.kc = kc;
+        g.smem = smem;
+    }
+    if (!g.kc) { g.tm = 0; return g; }
+    g.la = M * g.kc / g.nthr;
+    g.lb = N * g.kc / g.nthr;
+    return g;
+}
 
 // ---- phases of the kernel, shared with the host emulation of its index work --------------------
 
 // Element j of thread tid in a chunk of A (j < la): its offset from the chunk's base and its
-// shared-memory slot [k][m]; the same for B (j < lb), slot [k][n].
+// shared-memory slot (in quadruples); the same for B (j < lb).
 __host__ __device__ __forceinline__ void bgemm_elem_a(const BGemmArgs& g, int tid, int j, int64_t* off, int* slot) {
     const int64_t e = tid + (int64_t)j * (g.thr_m * g.thr_n);
     *off = pdep(e, g.eA);
-    *slot = (int)(pdep(e, g.eAk) * g.M + pdep(e, g.eAm));
+    const int m = (int)pdep(e, g.eAm), tm = g.M / g.thr_m;
+    *slot = (int)pdep(e, g.eAk) * g.ra + (m / tm) * (tm + 1) + m % tm;
 }
 __host__ __device__ __forceinline__ void bgemm_elem_b(const BGemmArgs& g, int tid, int j, int64_t* off, int* slot) {
     const int64_t e = tid + (int64_t)j * (g.thr_m * g.thr_n);
     *off = pdep(e, g.eB);
-    *slot = (int)(pdep(e, g.eBk) * g.N + pdep(e, g.eBn));
+    const int n = (int)pdep(e, g.eBn), tn = g.N / g.thr_n;
+    *slot = (int)pdep(e, g.eBk) * g.rb + (n / tn) * (tn + 1) + n % tn;
 }
 // Base offsets of chunk c of K range si for batch value bi.
 __host__ __device__ __forceinline__ int64_t bgemm_base_a(const BGemmArgs& g, int64_t bi, int64_t si, int64_t c) {
@@ -67,35 +109,31 @@ __host__ __device__ __forceinline__ float4 bgemm_quad_b(float2 v, float s, float
     const float br = v.x * s, bi = v.y * si;
     return make_float4(br, bi, bi, br);
 }
-// One chunk's products for thread (tm, tn): rows tm + thr_m i, columns tn + thr_n j.  A
-// quadruple is read as two 64-bit halves -- (ar, ar) and (-ai, ai); (br, bi) and (bi, br) -- which
-// are the paired FMAs' operands as they lie, so no value is repacked; the chunk is walked with
-// pointer increments (kc is a multiple of 8).
-template <int TM, int TN>
-__host__ __device__ __forceinline__ void bgemm_chunk(const BGemmArgs& g, const float4* as, const float4* bs, int tm,
-                                                     int tn, unsigned long long (&acc)[TM][TN]) {
-    const ulonglong2* pa[TM];
-    const ulonglong2* pb[TN];
+// One chunk's products for thread (tm, tn).  A quadruple is read as two 64-bit halves -- (ar, ar)
+// and (-ai, ai); (br, bi) and (bi, br) -- which are the paired FMAs' operands as they lie, and
+// every read is at a compile-time offset from one of two base addresses.
+template <int M, int N>
+__host__ __device__ __forceinline__ void bgemm_chunk(const float4* as, const float4* bs, int tm, int tn,
+                                                     unsigned long long (&acc)[bgemm_shape(M, N).tm]
+                                                                              [bgemm_shape(M, N).tn]) {
+    constexpr BGemmShape S = bgemm_shape(M, N);
+    const ulonglong2* pa = reinterpret_cast<const ulonglong2*>(as) + tm * (S.tm + 1);
+    const ulonglong2* pb = reinterpret_cast<const ulonglong2*>(bs) + tn * (S.tn + 1);
 #pragma unroll
-    for (int i = 0; i < TM; i++) pa[i] = reinterpret_cast<const ulonglong2*>(as) + tm + i * g.thr_m;
+    for (int k = 0; k < S.kc; k++) {
+        ulonglong2 qa[S.tm], qb[S.tn];
 #pragma unroll
-    for (int j = 0; j < TN; j++) pb[j] = reinterpret_cast<const ulonglong2*>(bs) + tn + j * g.thr_n;
-    const int M = g.M, N = g.N;
-#pragma unroll 4
-    for (int k = 0; k < g.kc; k++) {
-        ulonglong2 qa[TM], qb[TN];
+        for (int i = 0; i < S.tm; i++) qa[i] = pa[k * S.ra + i];
 #pragma unroll
-        for (int i = 0; i < TM; i++) { qa[i] = *pa[i]; pa[i] += M; }
+        for (int j = 0; j < S.tn; j++) qb[j] = pb[k * S.rb + j];
 #pragma unroll
-        for (int j = 0; j < TN; j++) { qb[j] = *pb[j]; pb[j] += N; }
+        for (int i = 0; i < S.tm; i++)
 #pragma unroll
-        for (int i = 0; i < TM; i++)
+            for (int j = 0; j < S.tn; j++) fma2(acc[i][j], qa[i].x, qb[j].x);
 #pragma unroll
-            for (int j = 0; j < TN; j++) fma2(acc[i][j], qa[i].x, qb[j].x);
+        for (int i = 0; i < S.tm; i++)
 #pragma unroll
-        for (int i = 0; i < TM; i++)
-#pragma unroll
-            for (int j = 0; j < TN; j++) fma2(acc[i][j], qa[i].y, qb[j].y);
+            for (int j = 0; j < S.tn; j++) fma2(acc[i][j], qa[i].y, qb[j].y);
     }
 }
 template <int TM, int TN>
@@ -127,56 +165,63 @@ __host__ __device__ __forceinline__ float2 bgemm_reduce_one(const BGemmArgs& g, 
     return make_float2((float)re, (float)im);
 }
 
+// The result shapes served (M, N per batch value); F(M, N) is expanded once per shape.
+#define QXG_BGEMM_SHAPES(F)                                                                           \
+    F(8, 32) F(8, 64) F(16, 16) F(16, 32) F(16, 64) F(32, 8) F(32, 16) F(32, 32) F(32, 64) F(64, 8) \
+    F(64, 16) F(64, 32) F(64, 64)
+
 namespace {
 
-template <int TM, int TN, bool SCALED>
-__global__ void __launch_bounds__(256) contract_bgemm_kernel(const BGemmArgs g, double2* partial, int* exps) {
+template <int M, int N, bool SCALED>
+__global__ void __launch_bounds__(bgemm_shape(M, N).nthr)
+    contract_bgemm_kernel(const BGemmArgs g, double2* partial, int* exps) {
+    constexpr BGemmShape S = bgemm_shape(M, N);
+    constexpr int NT = S.nthr;
     extern __shared__ float4 bg_smem[];
     const int tid = threadIdx.x;
-    const int tn = tid % g.thr_n, tm = tid / g.thr_n;
+    const int tn = tid % S.thr_n, tm = tid / S.thr_n;
     const int64_t bi = (int64_t)blockIdx.x % g.nbatch;
     const int64_t si = (int64_t)blockIdx.x / g.nbatch;
-    float4* As = bg_smem;                                  // [2][kc][M]
-    float4* Bs = bg_smem + 2 * g.kc * g.M;                 // [2][kc][N]
-    const int nthr = g.thr_m * g.thr_n;
+    float4* As = bg_smem;                                  // [2][kc][ra]
+    float4* Bs = bg_smem + 2 * S.kc * S.ra;                // [2][kc][rb]
     // per-thread element offsets and slots of a chunk, [j][thread] (kept out of registers)
-    int64_t* toffA = reinterpret_cast<int64_t*>(Bs + 2 * g.kc * g.N);
-    int64_t* toffB = toffA + g.la * nthr;
-    int* tslotA = reinterpret_cast<int*>(toffB + g.lb * nthr);
-    int* tslotB = tslotA + g.la * nthr;
+    int64_t* toffA = reinterpret_cast<int64_t*>(Bs + 2 * S.kc * S.rb);
+    int64_t* toffB = toffA + S.la * NT;
+    int* tslotA = reinterpret_cast<int*>(toffB + S.lb * NT);
+    int* tslotB = tslotA + S.la * NT;
     float sa = 1.f, sb = 1.f;
     if (SCALED) {
         sa = pow2f(-read_m(exps, g.expA));
         sb = pow2f(-read_m(exps, g.expB));
     }
     const float sai = g.conjA ? -sa : sa, sbi = g.conjB ? -sb : sb;
-    for (int j = 0; j < g.la; j++) bgemm_elem_a(g, tid, j, &toffA[j * nthr + tid], &tslotA[j * nthr + tid]);
-    for (int j = 0; j < g.lb; j++) bgemm_elem_b(g, tid, j, &toffB[j * nthr + tid], &tslotB[j * nthr + tid]);
-    float2 ra[kBGemmMaxL], rb[kBGemmMaxL];
+#pragma unroll
+    for (int j = 0; j < S.la; j++) bgemm_elem_a(g, tid, j, &toffA[j * NT + tid], &tslotA[j * NT + tid]);
+#pragma unroll
+    for (int j = 0; j < S.lb; j++) bgemm_elem_b(g, tid, j, &toffB[j * NT + tid], &tslotB[j * NT + tid]);
+    float2 ra[S.la], rb[S.lb];
     auto fetch = [&](int64_t c) {
         const float2* a = g.A + bgemm_base_a(g, bi, si, c);
         const float2* b = g.B + bgemm_base_b(g, bi, si, c);
 #pragma unroll
-        for (int j = 0; j < kBGemmMaxL; j++) {
-            if (j < g.la) ra[j] = __ldg(a + toffA[j * nthr + tid]);
-            if (j < g.lb) rb[j] = __ldg(b + toffB[j * nthr + tid]);
-        }
+        for (int j = 0; j < S.la; j++) ra[j] = __ldg(a + toffA[j * NT + tid]);
+#pragma unroll
+        for (int j = 0; j < S.lb; j++) rb[j] = __ldg(b + toffB[j * NT + tid]);
     };
     auto stage = [&](int buf) {
-        float4* as = As + buf * g.kc * g.M;
-        float4* bs = Bs + buf * g.kc * g.N;
+        float4* as = As + buf * S.kc * S.ra;
+        float4* bs = Bs + buf * S.kc * S.rb;
 #pragma unroll
-        for (int j = 0; j < kBGemmMaxL; j++) {
-            if (j < g.la) as[tslotA[j * nthr + tid]] = bgemm_quad_a(ra[j], sa, sai);
-            if (j < g.lb) bs[tslotB[j * nthr + tid]] = bgemm_quad_b(rb[j], sb, sbi);
-        }
+        for (int j = 0; j < S.la; j++) as[tslotA[j * NT + tid]] = bgemm_quad_a(ra[j], sa, sai);
+#pragma unroll
+        for (int j = 0; j < S.lb; j++) bs[tslotB[j * NT + tid]] = bgemm_quad_b(rb[j], sb, sbi);
     };
-    unsigned long long acc[TM][TN];
-    double2 dacc[TM][TN];
+    unsigned long long acc[S.tm][S.tn];
+    double2 dacc[S.tm][S.tn];
 #pragma unroll
-    for (int i = 0; i < TM; i++)
+    for (int i = 0; i < S.tm; i++)
 #pragma unroll
-        for (int j = 0; j < TN; j++) {
+        for (int j = 0; j < S.tn; j++) {
             acc[i][j] = 0ull;
             dacc[i][j] = make_double2(0.0, 0.0);
         }
@@ -186,19 +231,19 @@ __global__ void __launch_bounds__(256) contract_bgemm_kernel(const BGemmArgs g, 
     for (int64_t c = 0; c < g.nchunks; c++) {
         const int buf = (int)(c & 1);
         if (c + 1 < g.nchunks) fetch(c + 1);
-        bgemm_chunk<TM, TN>(g, As + buf * g.kc * g.M, Bs + buf * g.kc * g.N, tm, tn, acc);
-        if ((c + 1) % g.flush == 0 || c + 1 == g.nchunks) bgemm_flush<TM, TN>(acc, dacc);
+        bgemm_chunk<M, N>(As + buf * S.kc * S.ra, Bs + buf * S.kc * S.rb, tm, tn, acc);
+        if ((c + 1) % g.flush == 0 || c + 1 == g.nchunks) bgemm_flush<S.tm, S.tn>(acc, dacc);
         if (c + 1 < g.nchunks) stage(buf ^ 1);
         __syncthreads();
     }
     if (g.nsplit == 1) {
         int emax = kExpUnset;
 #pragma unroll
-        for (int i = 0; i < TM; i++)
+        for (int i = 0; i < S.tm; i++)
 #pragma unroll
-            for (int j = 0; j < TN; j++) {
+            for (int j = 0; j < S.tn; j++) {
                 const float2 v = make_float2((float)dacc[i][j].x, (float)dacc[i][j].y);
-                g.C[bgemm_c_offset(g, bi, tm + i * g.thr_m, tn + j * g.thr_n)] = v;
+                g.C[bgemm_c_offset(g, bi, tm * S.tm + i, tn * S.tn + j)] = v;
                 const float mx = fmaxf(fabsf(v.x), fabsf(v.y));
                 if (SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
             }
@@ -210,12 +255,11 @@ __global__ void __launch_bounds__(256) contract_bgemm_kernel(const BGemmArgs g, 
         }
     } else {
         // partial[si][bi][m][n] in FP64, added in K-range order by bgemm_reduce_kernel
-        double2* p = partial + ((si * g.nbatch + bi) * g.M) * g.N;
+        double2* p = partial + ((si * g.nbatch + bi) * M) * N;
 #pragma unroll
-        for (int i = 0; i < TM; i++)
+        for (int i = 0; i < S.tm; i++)
 #pragma unroll
-            for (int j = 0; j < TN; j++)
-                p[(tm + i * g.thr_m) * g.N + tn + j * g.thr_n] = dacc[i][j];
+            for (int j = 0; j < S.tn; j++) p[(tm * S.tm + i) * N + tn * S.tn + j] = dacc[i][j];
     }
 }
 
@@ -245,11 +289,6 @@ int ilog2(int64_t x) {
     return b;
 }
 
-// Two chunk buffers of quadruples, then the per-thread offset (8 bytes) and slot (4 bytes) tables.
-size_t bgemm_smem(const BGemmArgs& g) {
-    return (size_t)2 * g.kc * (g.M + g.N) * sizeof(float4) + (size_t)(g.la + g.lb) * g.thr_m * g.thr_n * 12;
-}
-
 // A run of length one per element bit: the element index's bits go to scattered places.
 bool bit_runs(const std::vector<std::pair<int, int>>& p, BitMap* m) {
     memset(m, 0, sizeof(*m));
@@ -263,10 +302,10 @@ bool bit_runs(const std::vector<std::pair<int, int>>& p, BitMap* m) {
 }  // namespace
 
 // Plan the batched small GEMM form of a step (Complex64 storage only).  Eligible: every result
-// bit in A or B, every summed bit in both; 4 to 64 free values on each side with at least 256
-// results per batch value; at least 2^10 summed terms; both operands of at least 2^20 elements
-// (smaller steps are served by the row forms and the tensor cores; min_log2 lowers that floor for
-// the host emulation of the kernel).
+// bit in A or B, every summed bit in both; a result shape of QXG_BGEMM_SHAPES (8 to 64 free values
+// on each side, at least 256 results per batch value); at least 2^10 summed terms; both operands
+// of at least 2^min_log2 elements (smaller steps are served by the row forms and the tensor
+// cores; the host emulation of the kernel lowers the floor).
 bool plan_bgemm(const StepArgs& s, int sm_count, BGemmArgs* g, int min_log2) {
     if (s.nk < 10) return false;
     auto one = [](const BitMap& m, int bit) {
@@ -285,38 +324,28 @@ bool plan_bgemm(const StepArgs& s, int sm_count, BGemmArgs* g, int min_log2) {
     for (int j = 0; j < s.nk; j++)
         if (one(s.kA, j) < 0 || one(s.kB, j) < 0) return false;
     const int na = (int)ab.size(), nb = (int)bb.size(), ng = (int)gb.size();
-    if (na < 2 || nb < 2 || na > 6 || nb > 6 || na + nb < 8 || ng > 30) return false;
+    if (na < 3 || nb < 3 || na > 6 || nb > 6 || na + nb < 8 || ng > 30) return false;
     if (ng + std::min(na, nb) + s.nk < min_log2) return false;
+    const BGemmShape S = bgemm_shape(1 << na, 1 << nb);
+    if (!S.tm) return false;
+    bool served = false;
+#define QXG_BGEMM_IS(M_, N_) served = served || (S.M == M_ && S.N == N_);
+    QXG_BGEMM_SHAPES(QXG_BGEMM_IS)
+#undef QXG_BGEMM_IS
+    if (!served) return false;
     BGemmArgs a;
     memset(&a, 0, sizeof(a));
-    a.M = 1 << na;
-    a.N = 1 << nb;
-    // 64 threads of 4 x 4 results up to 1024 results per batch value, else 256 threads
-    const int nthr = std::max(64, a.M * a.N / 16);
-    int TM = 0, TN = 0;
-    for (int tn_ : {4, 2})
-        for (int tm_ : {4, 2})
-            if (!TM && a.M % tm_ == 0 && a.N % tn_ == 0 && (a.M / tm_) * (a.N / tn_) == nthr) { TM = tm_; TN = tn_; }
-    if (!TM) return false;
-    a.thr_m = a.M / TM;
-    a.thr_n = a.N / TN;
-    // summed values per chunk: every thread loads 1..kBGemmMaxL elements of each operand, and the
-    // two buffers fit kBGemmMaxSmem
-    auto smem_of = [&](int kc_) {
-        return (size_t)2 * kc_ * (a.M + a.N) * 16 + (size_t)((int64_t)(a.M + a.N) * kc_ / nthr) * nthr * 12;
-    };
-    int kc = 8;
-    while (kc * 2 <= 64 && (int64_t)a.M * kc * 2 <= (int64_t)nthr * kBGemmMaxL &&
-           (int64_t)a.N * kc * 2 <= (int64_t)nthr * kBGemmMaxL && smem_of(kc * 2) <= kBGemmMaxSmem)
-        kc *= 2;
-    if ((int64_t)a.M * kc < nthr || (int64_t)a.N * kc < nthr || (int64_t)a.M * kc > (int64_t)nthr * kBGemmMaxL ||
-        (int64_t)a.N * kc > (int64_t)nthr * kBGemmMaxL || smem_of(kc) > kBGemmMaxSmem)
-        return false;
-    const int lkc = ilog2(kc);
+    a.M = S.M;
+    a.N = S.N;
+    a.thr_m = S.thr_m;
+    a.thr_n = S.thr_n;
+    a.kc = S.kc;
+    a.la = S.la;
+    a.lb = S.lb;
+    a.ra = S.ra;
+    a.rb = S.rb;
+    const int lkc = ilog2(S.kc);
     if (lkc > s.nk) return false;
-    a.kc = kc;
-    a.la = (int)((int64_t)a.M * kc / nthr);
-    a.lb = (int)((int64_t)a.N * kc / nthr);
     // the chunk's summed bits: those at the lowest address positions of either operand
     std::vector<int> ks(s.nk), posA(s.nk), posB(s.nk);
     for (int j = 0; j < s.nk; j++) { ks[j] = j; posA[j] = one(s.kA, j); posB[j] = one(s.kB, j); }
@@ -361,11 +390,11 @@ bool plan_bgemm(const StepArgs& s, int sm_count, BGemmArgs* g, int min_log2) {
     const int64_t chunks = int64_t(1) << (s.nk - lkc);
     // K ranges: enough blocks for about four per SM, each range at least 2^12 terms
     int64_t nsplit = 1;
-    while (a.nbatch * nsplit < (int64_t)sm_count * 4 && chunks / (nsplit * 2) * kc >= 4096) nsplit *= 2;
+    while (a.nbatch * nsplit < (int64_t)sm_count * 4 && chunks / (nsplit * 2) * S.kc >= 4096) nsplit *= 2;
     if (a.nbatch * nsplit > (int64_t(1) << 31) - 1) return false;
     a.nsplit = (int)nsplit;
     a.nchunks = chunks / nsplit;
-    a.flush = std::max(1, kFlushK / kc);
+    a.flush = std::max(1, kFlushK / S.kc);
     a.A = static_cast<const float2*>(s.A);
     a.B = static_cast<const float2*>(s.B);
     a.C = static_cast<float2*>(s.C);
@@ -383,33 +412,38 @@ size_t bgemm_partial_bytes(const BGemmArgs& g) {
 }
 
 namespace {
-template <int TM, int TN>
-cudaError_t launch_bgemm_t(const BGemmArgs& g, void* scratch, int* exps, cudaStream_t s) {
-    const size_t smem = bgemm_smem(g);
-    const unsigned blocks = (unsigned)(g.nbatch * g.nsplit);
-    double2* partial = static_cast<double2*>(scratch);
-    const int nthr = g.thr_m * g.thr_n;
-    if (exps) contract_bgemm_kernel<TM, TN, true><<<blocks, nthr, smem, s>>>(g, partial, exps);
-    else contract_bgemm_kernel<TM, TN, false><<<blocks, nthr, smem, s>>>(g, partial, exps);
+template <int M, int N, bool SCALED>
+cudaError_t launch_bgemm_shape(const BGemmArgs& g, double2* partial, int* exps, cudaStream_t s) {
+    constexpr BGemmShape S = bgemm_shape(M, N);
+    static bool attr = false;                   // the kernel's dynamic shared memory limit, once
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(contract_bgemm_kernel<M, N, SCALED>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    contract_bgemm_kernel<M, N, SCALED><<<(unsigned)(g.nbatch * g.nsplit), S.nthr, S.smem, s>>>(g, partial, exps);
     return cudaGetLastError();
 }
 }  // namespace
 
 cudaError_t launch_bgemm(const BGemmArgs& g, void* scratch, int* exps, cudaStream_t s, int* launches) {
-    const int TM = g.M / g.thr_m, TN = g.N / g.thr_n;
-    cudaError_t e = cudaErrorInvalidValue;
     if (g.nsplit > 1 && !scratch) return cudaErrorInvalidValue;
-    if (TM == 4 && TN == 4) e = launch_bgemm_t<4, 4>(g, scratch, exps, s);
-    else if (TM == 4 && TN == 2) e = launch_bgemm_t<4, 2>(g, scratch, exps, s);
-    else if (TM == 2 && TN == 4) e = launch_bgemm_t<2, 4>(g, scratch, exps, s);
-    else if (TM == 2 && TN == 2) e = launch_bgemm_t<2, 2>(g, scratch, exps, s);
+    double2* partial = static_cast<double2*>(scratch);
+    cudaError_t e = cudaErrorInvalidValue;
+#define QXG_BGEMM_LAUNCH(M_, N_)                                                              \
+    if (g.M == M_ && g.N == N_)                                                               \
+        e = exps ? launch_bgemm_shape<M_, N_, true>(g, partial, exps, s)                      \
+                 : launch_bgemm_shape<M_, N_, false>(g, partial, exps, s);
+    QXG_BGEMM_SHAPES(QXG_BGEMM_LAUNCH)
+#undef QXG_BGEMM_LAUNCH
     if (e != cudaSuccess) return e;
     if (launches) *launches = 1;
     if (g.nsplit > 1) {
         const int64_t total = g.nbatch * g.M * g.N;
         const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
-        if (exps) bgemm_reduce_kernel<true><<<grid, 256, 0, s>>>(g, static_cast<const double2*>(scratch), exps);
-        else bgemm_reduce_kernel<false><<<grid, 256, 0, s>>>(g, static_cast<const double2*>(scratch), exps);
+        if (exps) bgemm_reduce_kernel<true><<<grid, 256, 0, s>>>(g, partial, exps);
+        else bgemm_reduce_kernel<false><<<grid, 256, 0, s>>>(g, partial, exps);
         if (launches) *launches = 2;
         e = cudaGetLastError();
     }

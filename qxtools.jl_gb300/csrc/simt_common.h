@@ -132,9 +132,10 @@ struct BGemmArgs {
     const float2* B;
     float2* C;
     int32_t M, N;              // free values of A (rows) and of B (columns) per batch value
-    int32_t thr_m, thr_n;      // thread grid: thread (tm, tn) owns rows tm + thr_m i, columns tn + thr_n j
+    int32_t thr_m, thr_n;      // thread grid: thread (tm, tn) owns rows tm TM + i, columns tn TN + j
     int32_t kc;                // summed values per chunk
     int32_t la, lb;            // A / B elements one thread loads per chunk
+    int32_t ra, rb;            // quadruples per summed value of a chunk in shared memory (A / B)
     int64_t nchunks;           // chunks of one K range
     int32_t nsplit;            // K ranges per batch value (a power of two)
     int32_t flush;             // chunks between FP64 accumulations

@@ -272,53 +272,62 @@ int lsum_case(std::mt19937& rng, int nk, int na, int nb, int ng, bool cA_, bool 
 
 static int g_bgemm_split = 0;
 
-template <int TM, int TN>
+template <int M, int N>
 void emulate_bgemm(const BGemmArgs& g, std::vector<double2>& partial) {
-    const int nthr = g.thr_m * g.thr_n;
+    constexpr BGemmShape S = bgemm_shape(M, N);
+    constexpr int TM = S.tm, TN = S.tn;
+    const int nthr = S.nthr;
+    if (g.M != M || g.N != N || g.thr_m != S.thr_m || g.thr_n != S.thr_n || g.kc != S.kc || g.ra != S.ra ||
+        g.rb != S.rb) { printf("shape mismatch\n"); exit(1); }
     for (int64_t blk = 0; blk < g.nbatch * g.nsplit; blk++) {
         const int64_t bi = blk % g.nbatch, si = blk / g.nbatch;
-        std::vector<float4> As((size_t)2 * g.kc * g.M), Bs((size_t)2 * g.kc * g.N);
+        std::vector<float4> As((size_t)2 * S.kc * S.ra), Bs((size_t)2 * S.kc * S.rb);
         std::vector<std::array<unsigned long long, TM * TN>> acc(nthr);
         std::vector<std::array<double2, TM * TN>> dacc(nthr);
         for (int t = 0; t < nthr; t++)
             for (int q = 0; q < TM * TN; q++) { acc[t][q] = 0ull; dacc[t][q] = make_double2(0, 0); }
         for (int64_t c = 0; c < g.nchunks; c++) {
             const int buf = (int)(c & 1);
-            for (int t = 0; t < nthr; t++)
-                for (int j = 0; j < kBGemmMaxL; j++) {
+            for (int t = 0; t < nthr; t++) {
+                for (int j = 0; j < S.la; j++) {
                     int64_t off;
                     int slot;
-                    if (j < g.la) {
-                        bgemm_elem_a(g, t, j, &off, &slot);
-                        As.at((size_t)buf * g.kc * g.M + (size_t)slot) =
-                            bgemm_quad_a(g.A[bgemm_base_a(g, bi, si, c) + off], 1.f, g.conjA ? -1.f : 1.f);
-                    }
-                    if (j < g.lb) {
-                        bgemm_elem_b(g, t, j, &off, &slot);
-                        Bs.at((size_t)buf * g.kc * g.N + (size_t)slot) =
-                            bgemm_quad_b(g.B[bgemm_base_b(g, bi, si, c) + off], 1.f, g.conjB ? -1.f : 1.f);
-                    }
+                    bgemm_elem_a(g, t, j, &off, &slot);
+                    As.at((size_t)buf * S.kc * S.ra + (size_t)slot) =
+                        bgemm_quad_a(g.A[bgemm_base_a(g, bi, si, c) + off], 1.f, g.conjA ? -1.f : 1.f);
                 }
+                for (int j = 0; j < S.lb; j++) {
+                    int64_t off;
+                    int slot;
+                    bgemm_elem_b(g, t, j, &off, &slot);
+                    Bs.at((size_t)buf * S.kc * S.rb + (size_t)slot) =
+                        bgemm_quad_b(g.B[bgemm_base_b(g, bi, si, c) + off], 1.f, g.conjB ? -1.f : 1.f);
+                }
+            }
             for (int t = 0; t < nthr; t++) {
+                const int tm = t / S.thr_n, tn = t % S.thr_n;
+                // the reads of bgemm_chunk stay inside the buffer (its largest offset)
+                const size_t last_a = (size_t)buf * S.kc * S.ra + tm * (TM + 1) + (S.kc - 1) * S.ra + TM - 1;
+                const size_t last_b = (size_t)buf * S.kc * S.rb + tn * (TN + 1) + (S.kc - 1) * S.rb + TN - 1;
+                if (last_a >= As.size() || last_b >= Bs.size()) { printf("chunk read out of range\n"); exit(1); }
                 unsigned long long a2[TM][TN];
                 double2 d2[TM][TN];
                 for (int i = 0; i < TM; i++)
                     for (int j = 0; j < TN; j++) { a2[i][j] = acc[t][i * TN + j]; d2[i][j] = dacc[t][i * TN + j]; }
-                bgemm_chunk<TM, TN>(g, As.data() + (size_t)buf * g.kc * g.M, Bs.data() + (size_t)buf * g.kc * g.N,
-                                    t / g.thr_n, t % g.thr_n, a2);
+                bgemm_chunk<M, N>(As.data() + (size_t)buf * S.kc * S.ra, Bs.data() + (size_t)buf * S.kc * S.rb, tm, tn, a2);
                 if ((c + 1) % g.flush == 0 || c + 1 == g.nchunks) bgemm_flush<TM, TN>(a2, d2);
                 for (int i = 0; i < TM; i++)
                     for (int j = 0; j < TN; j++) { acc[t][i * TN + j] = a2[i][j]; dacc[t][i * TN + j] = d2[i][j]; }
             }
         }
         for (int t = 0; t < nthr; t++) {
-            const int tm = t / g.thr_n, tn = t % g.thr_n;
+            const int tm = t / S.thr_n, tn = t % S.thr_n;
             for (int i = 0; i < TM; i++)
                 for (int j = 0; j < TN; j++) {
-                    const int m = tm + i * g.thr_m, n = tn + j * g.thr_n;
+                    const int m = tm * TM + i, n = tn * TN + j;
                     const double2 v = dacc[t][i * TN + j];
                     if (g.nsplit == 1) g.C[bgemm_c_offset(g, bi, m, n)] = make_float2((float)v.x, (float)v.y);
-                    else partial.at((size_t)((si * g.nbatch + bi) * g.M + m) * g.N + n) = v;
+                    else partial.at((size_t)((si * g.nbatch + bi) * M + m) * N + n) = v;
                 }
         }
     }
@@ -357,12 +366,11 @@ int bgemm_case(std::mt19937& rng, int nk, int na, int nb, int ng, bool cA_, bool
     (*used)++;
     if (g.nsplit > 1) g_bgemm_split++;
     std::vector<double2> partial(bgemm_partial_bytes(g) / sizeof(double2), make_double2(NAN, NAN));
-    const int TM = g.M / g.thr_m, TN = g.N / g.thr_n;
-    if (TM == 4 && TN == 4) emulate_bgemm<4, 4>(g, partial);
-    else if (TM == 4 && TN == 2) emulate_bgemm<4, 2>(g, partial);
-    else if (TM == 2 && TN == 4) emulate_bgemm<2, 4>(g, partial);
-    else if (TM == 2 && TN == 2) emulate_bgemm<2, 2>(g, partial);
-    else { printf("no instance TM=%d TN=%d\n", TM, TN); return -1; }
+    bool ran = false;
+#define QXG_EMU_BGEMM(M_, N_) if (!ran && g.M == M_ && g.N == N_) { emulate_bgemm<M_, N_>(g, partial); ran = true; }
+    QXG_BGEMM_SHAPES(QXG_EMU_BGEMM)
+#undef QXG_EMU_BGEMM
+    if (!ran) { printf("no instance M=%d N=%d\n", g.M, g.N); return -1; }
     double maxerr = 0, maxv = 0;
     for (int64_t c = 0; c < NC; c++) {
         std::complex<double> acc = 0;
@@ -404,7 +412,7 @@ int main(int argc, char** argv) {
     }
     int bg_used = 0, bg_fail = 0;
     for (int it = 0; it < nsums / 2; it++) {        // both operands of 2^12 and more elements
-        const int na = 2 + rng() % 5, nb = 2 + rng() % 5, ng = rng() % 4;
+        const int na = 3 + rng() % 4, nb = 3 + rng() % 4, ng = rng() % 4;
         if (na + nb < 8 || na + nb > 10) continue;
         const int nk = std::max(10, 13 - ng) + (int)(rng() % 2);
         if (bgemm_case(rng, nk, na, nb, ng, rng() % 2, rng() % 2, &bg_used) < 0) bg_fail++;
