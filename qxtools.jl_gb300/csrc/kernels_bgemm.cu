@@ -13,13 +13,15 @@
 // Here one block owns one batch value and one range of K:
 //   * the block's threads tile the M x N result (TM x TN complex results per thread, in
 //     registers);
-//   * the K range is walked in chunks of KC terms.  A chunk's A values (M x KC) and B values
-//     (KC x N) are loaded in the order of the operands' own address bits (so a warp's loads
-//     coalesce when the lowest address bits are result or summed bits), scaled by the operands'
-//     power-of-two exponents and stored in shared memory as (ar, ar, -ai, ai) and (br, bi, bi,
-//     br) quadruples; each complex multiply-add is then two paired FMAs (fma.rn.f32x2) on one
-//     16-byte read of each.  The next chunk's loads are in flight while the current one is
-//     multiplied (two shared-memory buffers, one barrier per chunk);
+//   * the K range is walked in chunks of 8 terms.  A chunk's A values (M x 8) and B values
+//     (8 x N) are copied with 8-byte cp.async into a ring of raw chunks in shared memory, several
+//     chunks ahead of the one being multiplied, in the order of the operands' own address bits (so
+//     a warp's copies coalesce when the lowest address bits are result or summed bits).  Each
+//     thread then turns its own elements of the current chunk, scaled by the operands'
+//     power-of-two exponents, into (ar, ar, -ai, ai) and (br, bi, bi, br) quadruples, and a
+//     complex multiply-add is two paired FMAs (fma.rn.f32x2) on one 16-byte read of each
+//     (two quadruple buffers, one barrier per chunk).  The ring keeps tens of KB per SM in flight
+//     without holding registers, which the step needs to reach HBM speed;
 //   * every thread sums at most kFlushK terms in FP32 before adding them into FP64
 //     accumulators, so the error does not grow with K (the long-sum kernel's rule);
 //   * with one K range per batch value the block writes C directly; otherwise it writes FP64
@@ -35,21 +37,25 @@ namespace qxg {
 
 constexpr int kFlushK = 512;            // FP32 terms per thread before the FP64 accumulation
 constexpr size_t kBGemmMaxSmem = 96 * 1024;
+constexpr size_t kBGemmRingTarget = 44 * 1024;   // quadruple buffers plus ring, per block
+constexpr int kBGemmKC = 8;             // summed values per chunk
 
 // ---- tile geometry, fixed at compile time per result shape (M x N per batch value) ----------------
 //   threads    64 up to 1024 results per batch value, else M N / 16;
 //   TM x TN    results per thread (4 or 2 each): thread (tm, tn) owns rows tm TM .. + TM-1 and
 //              columns tn TN .. + TN-1;
-//   KC         summed values per chunk: every thread loads 1..kBGemmMaxL elements of each operand
-//              per chunk and the block's shared memory stays within kBGemmMaxSmem;
+//   kc         summed values per chunk (8): every thread copies 1..kBGemmMaxL elements of each
+//              operand per chunk;
 //   layout     a chunk's A quadruples as [k][row group][TM + 1] (one padding quadruple per group
-//              keeps the groups of a warp in different banks), B as [k][column group][TN + 1].
+//              keeps the groups of a warp in different banks), B as [k][column group][TN + 1];
+//   ring       raw chunks in flight, 3..8, as many as fit kBGemmRingTarget with the two
+//              quadruple buffers (each raw chunk [j][thread] float2 for A, then for B).
 struct BGemmShape {
-    int M, N, nthr, tm, tn, thr_m, thr_n, kc, la, lb, ra, rb;
-    size_t smem;
+    int M, N, nthr, tm, tn, thr_m, thr_n, kc, la, lb, ra, rb, ring;
+    size_t quad_bytes, raw_bytes, smem;
 };
 constexpr BGemmShape bgemm_shape(int M, int N) {
-    BGemmShape g{M, N, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    BGemmShape g{M, N, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     g.nthr = M * N / 16 > 64 ? M * N / 16 : 64;
     const int cand[4][2] = {{4, 4}, {2, 4}, {4, 2}, {2, 2}};     // (tm, tn)
     for (int c = 0; c < 4 && !g.tm; c++)
@@ -62,19 +68,30 @@ constexpr BGemmShape bgemm_shape(int M, int N) {
     g.thr_n = N / g.tn;
     g.ra = g.thr_m * (g.tm + 1);
     g.rb = g.thr_n * (g.tn + 1);
-    for (int kc = 8; kc <= 64; kc *= 2) {
-        const size_t smem = (size_t)2 * kc * (g.ra + g.rb) * 16 + (size_t)(M + N) * kc * 12;
-        if (M * kc < g.nthr || N * kc < g.nthr || M * kc > g.nthr * kBGemmMaxL || N * kc > g.nthr * kBGemmMaxL ||
-            smem > kBGemmMaxSmem)
-            continue;
-        g.kc = kc;
-        g.smem = smem;
+    const int kc = kBGemmKC;
+    if (M * kc < g.nthr || N * kc < g.nthr || M * kc > g.nthr * kBGemmMaxL || N * kc > g.nthr * kBGemmMaxL) {
+        g.tm = 0;
+        return g;
     }
-    if (!g.kc) { g.tm = 0; return g; }
-    g.la = M * g.kc / g.nthr;
-    g.lb = N * g.kc / g.nthr;
+    g.kc = kc;
+    g.la = M * kc / g.nthr;
+    g.lb = N * kc / g.nthr;
+    g.quad_bytes = (size_t)2 * kc * (g.ra + g.rb) * 16;
+    g.raw_bytes = (size_t)(M + N) * kc * 8;
+    g.ring = 3;
+    while (g.ring < 8 && g.quad_bytes + (size_t)(g.ring + 1) * g.raw_bytes <= kBGemmRingTarget) g.ring++;
+    g.smem = g.quad_bytes + (size_t)g.ring * g.raw_bytes;
+    if (g.smem > kBGemmMaxSmem) g.tm = 0;
     return g;
 }
+
+__device__ __forceinline__ void bg_cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void bg_cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void bg_cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // ---- phases of the kernel, shared with the host emulation of its index work --------------------
 
@@ -176,7 +193,7 @@ template <int M, int N, bool SCALED>
 __global__ void __launch_bounds__(bgemm_shape(M, N).nthr)
     contract_bgemm_kernel(const BGemmArgs g, double2* partial, int* exps) {
     constexpr BGemmShape S = bgemm_shape(M, N);
-    constexpr int NT = S.nthr;
+    constexpr int NT = S.nthr, R = S.ring;
     extern __shared__ float4 bg_smem[];
     const int tid = threadIdx.x;
     const int tn = tid % S.thr_n, tm = tid / S.thr_n;
@@ -184,37 +201,41 @@ __global__ void __launch_bounds__(bgemm_shape(M, N).nthr)
     const int64_t si = (int64_t)blockIdx.x / g.nbatch;
     float4* As = bg_smem;                                  // [2][kc][ra]
     float4* Bs = bg_smem + 2 * S.kc * S.ra;                // [2][kc][rb]
-    // per-thread element offsets and slots of a chunk, [j][thread] (kept out of registers)
-    int64_t* toffA = reinterpret_cast<int64_t*>(Bs + 2 * S.kc * S.rb);
-    int64_t* toffB = toffA + S.la * NT;
-    int* tslotA = reinterpret_cast<int*>(toffB + S.lb * NT);
-    int* tslotB = tslotA + S.la * NT;
+    float2* raw = reinterpret_cast<float2*>(Bs + 2 * S.kc * S.rb);   // [R][la + lb][NT]
     float sa = 1.f, sb = 1.f;
     if (SCALED) {
         sa = pow2f(-read_m(exps, g.expA));
         sb = pow2f(-read_m(exps, g.expB));
     }
     const float sai = g.conjA ? -sa : sa, sbi = g.conjB ? -sb : sb;
+    int64_t offA[S.la], offB[S.lb];
+    int slotA[S.la], slotB[S.lb];
 #pragma unroll
-    for (int j = 0; j < S.la; j++) bgemm_elem_a(g, tid, j, &toffA[j * NT + tid], &tslotA[j * NT + tid]);
+    for (int j = 0; j < S.la; j++) bgemm_elem_a(g, tid, j, &offA[j], &slotA[j]);
 #pragma unroll
-    for (int j = 0; j < S.lb; j++) bgemm_elem_b(g, tid, j, &toffB[j * NT + tid], &tslotB[j * NT + tid]);
-    float2 ra[S.la], rb[S.lb];
-    auto fetch = [&](int64_t c) {
-        const float2* a = g.A + bgemm_base_a(g, bi, si, c);
-        const float2* b = g.B + bgemm_base_b(g, bi, si, c);
+    for (int j = 0; j < S.lb; j++) bgemm_elem_b(g, tid, j, &offB[j], &slotB[j]);
+    // chunk c's raw elements go to ring slot c % R: [j][tid], A's la rows then B's lb rows; each
+    // thread copies and later reads back only its own elements
+    auto issue = [&](int64_t c) {
+        if (c < g.nchunks) {
+            const float2* a = g.A + bgemm_base_a(g, bi, si, c);
+            const float2* b = g.B + bgemm_base_b(g, bi, si, c);
+            float2* r = raw + (size_t)(c % R) * (S.la + S.lb) * NT + tid;
 #pragma unroll
-        for (int j = 0; j < S.la; j++) ra[j] = __ldg(a + toffA[j * NT + tid]);
+            for (int j = 0; j < S.la; j++) bg_cp_async8(r + j * NT, a + offA[j]);
 #pragma unroll
-        for (int j = 0; j < S.lb; j++) rb[j] = __ldg(b + toffB[j * NT + tid]);
+            for (int j = 0; j < S.lb; j++) bg_cp_async8(r + (S.la + j) * NT, b + offB[j]);
+        }
+        bg_cp_async_commit();               // one group per chunk (empty past the end)
     };
-    auto stage = [&](int buf) {
-        float4* as = As + buf * S.kc * S.ra;
-        float4* bs = Bs + buf * S.kc * S.rb;
+    auto stage = [&](int64_t c) {
+        const float2* r = raw + (size_t)(c % R) * (S.la + S.lb) * NT + tid;
+        float4* as = As + (int)(c & 1) * S.kc * S.ra;
+        float4* bs = Bs + (int)(c & 1) * S.kc * S.rb;
 #pragma unroll
-        for (int j = 0; j < S.la; j++) as[tslotA[j * NT + tid]] = bgemm_quad_a(ra[j], sa, sai);
+        for (int j = 0; j < S.la; j++) as[slotA[j]] = bgemm_quad_a(r[j * NT], sa, sai);
 #pragma unroll
-        for (int j = 0; j < S.lb; j++) bs[tslotB[j * NT + tid]] = bgemm_quad_b(rb[j], sb, sbi);
+        for (int j = 0; j < S.lb; j++) bs[slotB[j]] = bgemm_quad_b(r[(S.la + j) * NT], sb, sbi);
     };
     unsigned long long acc[S.tm][S.tn];
     double2 dacc[S.tm][S.tn];
@@ -225,17 +246,17 @@ __global__ void __launch_bounds__(bgemm_shape(M, N).nthr)
             acc[i][j] = 0ull;
             dacc[i][j] = make_double2(0.0, 0.0);
         }
-    fetch(0);
-    stage(0);
-    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < R - 1; c++) issue(c);
     for (int64_t c = 0; c < g.nchunks; c++) {
-        const int buf = (int)(c & 1);
-        if (c + 1 < g.nchunks) fetch(c + 1);
-        bgemm_chunk<M, N>(As + buf * S.kc * S.ra, Bs + buf * S.kc * S.rb, tm, tn, acc);
+        issue(c + R - 1);
+        bg_cp_async_wait<R - 1>();          // chunk c's own copies have landed
+        stage(c);
+        __syncthreads();                    // chunk c's quadruples are complete
+        bgemm_chunk<M, N>(As + (int)(c & 1) * S.kc * S.ra, Bs + (int)(c & 1) * S.kc * S.rb, tm, tn, acc);
         if ((c + 1) % g.flush == 0 || c + 1 == g.nchunks) bgemm_flush<S.tm, S.tn>(acc, dacc);
-        if (c + 1 < g.nchunks) stage(buf ^ 1);
-        __syncthreads();
     }
+    bg_cp_async_wait<0>();                  // nothing lands after the block has left
     if (g.nsplit == 1) {
         int emax = kExpUnset;
 #pragma unroll
