@@ -37,7 +37,8 @@ namespace qxg {
 
 constexpr int kFlushK = 512;            // FP32 terms per thread before the FP64 accumulation
 constexpr size_t kBGemmMaxSmem = 96 * 1024;
-constexpr size_t kBGemmRingTarget = 44 * 1024;   // quadruple buffers plus ring, per block
+constexpr size_t kBGemmRingTarget = 36 * 1024;   // quadruple buffers plus ring, per block
+constexpr int kBGemmMaxChunkBits = 48;  // delta table entries (bits of the chunk index)
 constexpr int kBGemmKC = 8;             // summed values per chunk
 
 // ---- tile geometry, fixed at compile time per result shape (M x N per batch value) ----------------
@@ -116,6 +117,13 @@ __host__ __device__ __forceinline__ int64_t bgemm_base_a(const BGemmArgs& g, int
 __host__ __device__ __forceinline__ int64_t bgemm_base_b(const BGemmArgs& g, int64_t bi, int64_t si, int64_t c) {
     return pdep(bi, g.bB) + pdep(si * g.nchunks + c, g.hB);
 }
+// Walking chunk indices in order: base(c + 1) = base(c) + delta(t) with t = ctz(c + 1), where
+// delta(t) = pdep(2^t) - pdep(2^t - 1) (bit t set, bits 0..t-1 cleared), so a chunk's base costs
+// one table read and one add instead of a deposit over every run of the map.
+__host__ __device__ __forceinline__ int64_t bgemm_delta(const BitMap& h, int t) {
+    return pdep(int64_t(1) << t, h) - pdep((int64_t(1) << t) - 1, h);
+}
+
 // Shared-memory quadruples: A as (ar, ar, -ai, ai), B as (br, bi, bi, br), scaled (s) with the
 // imaginary part's sign folded in for conjugation (si = -s).
 __host__ __device__ __forceinline__ float4 bgemm_quad_a(float2 v, float s, float si) {
@@ -189,8 +197,9 @@ __host__ __device__ __forceinline__ float2 bgemm_reduce_one(const BGemmArgs& g, 
 
 namespace {
 
+// at least six blocks of 64 threads (12 warps) per SM: the registers are capped to fit them
 template <int M, int N, bool SCALED>
-__global__ void __launch_bounds__(bgemm_shape(M, N).nthr)
+__global__ void __launch_bounds__(bgemm_shape(M, N).nthr, bgemm_shape(M, N).nthr <= 64 ? 6 : 384 / bgemm_shape(M, N).nthr)
     contract_bgemm_kernel(const BGemmArgs g, double2* partial, int* exps) {
     constexpr BGemmShape S = bgemm_shape(M, N);
     constexpr int NT = S.nthr, R = S.ring;
@@ -202,6 +211,11 @@ __global__ void __launch_bounds__(bgemm_shape(M, N).nthr)
     float4* As = bg_smem;                                  // [2][kc][ra]
     float4* Bs = bg_smem + 2 * S.kc * S.ra;                // [2][kc][rb]
     float2* raw = reinterpret_cast<float2*>(Bs + 2 * S.kc * S.rb);   // [R][la + lb][NT]
+    __shared__ int64_t dA[kBGemmMaxChunkBits], dB[kBGemmMaxChunkBits];
+    for (int t = tid; t < kBGemmMaxChunkBits; t += NT) {
+        dA[t] = bgemm_delta(g.hA, t);
+        dB[t] = bgemm_delta(g.hB, t);
+    }
     float sa = 1.f, sb = 1.f;
     if (SCALED) {
         sa = pow2f(-read_m(exps, g.expA));
@@ -215,11 +229,18 @@ __global__ void __launch_bounds__(bgemm_shape(M, N).nthr)
 #pragma unroll
     for (int j = 0; j < S.lb; j++) bgemm_elem_b(g, tid, j, &offB[j], &slotB[j]);
     // chunk c's raw elements go to ring slot c % R: [j][tid], A's la rows then B's lb rows; each
-    // thread copies and later reads back only its own elements
+    // thread copies and later reads back only its own elements.  Chunks are issued in order, so
+    // their bases advance by the delta table (the first from a full deposit).
+    const int64_t c0 = si * g.nchunks;
+    int64_t baseA = bgemm_base_a(g, bi, si, 0), baseB = bgemm_base_b(g, bi, si, 0);
+    __syncthreads();                        // delta tables written
     auto issue = [&](int64_t c) {
         if (c < g.nchunks) {
-            const float2* a = g.A + bgemm_base_a(g, bi, si, c);
-            const float2* b = g.B + bgemm_base_b(g, bi, si, c);
+            const float2* a = g.A + baseA;
+            const float2* b = g.B + baseB;
+            const int t = __ffsll((unsigned long long)(c0 + c + 1)) - 1;
+            baseA += dA[t];
+            baseB += dB[t];
             float2* r = raw + (size_t)(c % R) * (S.la + S.lb) * NT + tid;
 #pragma unroll
             for (int j = 0; j < S.la; j++) bg_cp_async8(r + j * NT, a + offA[j]);
@@ -254,7 +275,7 @@ __global__ void __launch_bounds__(bgemm_shape(M, N).nthr)
         stage(c);
         __syncthreads();                    // chunk c's quadruples are complete
         bgemm_chunk<M, N>(As + (int)(c & 1) * S.kc * S.ra, Bs + (int)(c & 1) * S.kc * S.rb, tm, tn, acc);
-        if ((c + 1) % g.flush == 0 || c + 1 == g.nchunks) bgemm_flush<S.tm, S.tn>(acc, dacc);
+        if (((c + 1) & (g.flush - 1)) == 0 || c + 1 == g.nchunks) bgemm_flush<S.tm, S.tn>(acc, dacc);
     }
     bg_cp_async_wait<0>();                  // nothing lands after the block has left
     if (g.nsplit == 1) {
@@ -415,7 +436,8 @@ bool plan_bgemm(const StepArgs& s, int sm_count, BGemmArgs* g, int min_log2) {
     if (a.nbatch * nsplit > (int64_t(1) << 31) - 1) return false;
     a.nsplit = (int)nsplit;
     a.nchunks = chunks / nsplit;
-    a.flush = std::max(1, kFlushK / S.kc);
+    a.flush = std::max(1, kFlushK / S.kc);  // a power of two
+    if (s.nk - lkc >= kBGemmMaxChunkBits) return false;
     a.A = static_cast<const float2*>(s.A);
     a.B = static_cast<const float2*>(s.B);
     a.C = static_cast<float2*>(s.C);

@@ -286,8 +286,17 @@ void emulate_bgemm(const BGemmArgs& g, std::vector<double2>& partial) {
         std::vector<std::array<double2, TM * TN>> dacc(nthr);
         for (int t = 0; t < nthr; t++)
             for (int q = 0; q < TM * TN; q++) { acc[t][q] = 0ull; dacc[t][q] = make_double2(0, 0); }
+        int64_t wa = bgemm_base_a(g, bi, si, 0), wb = bgemm_base_b(g, bi, si, 0);
         for (int64_t c = 0; c < g.nchunks; c++) {
             const int buf = (int)(c & 1);
+            // the kernel walks chunk bases with the delta table: it must agree with the deposit
+            if (wa != bgemm_base_a(g, bi, si, c) || wb != bgemm_base_b(g, bi, si, c)) {
+                printf("delta walk differs from the deposit at chunk %lld\n", (long long)c);
+                exit(1);
+            }
+            const int tz = __builtin_ctzll((unsigned long long)(si * g.nchunks + c + 1));
+            wa += bgemm_delta(g.hA, tz);
+            wb += bgemm_delta(g.hB, tz);
             for (int t = 0; t < nthr; t++) {
                 for (int j = 0; j < S.la; j++) {
                     int64_t off;
@@ -315,7 +324,7 @@ void emulate_bgemm(const BGemmArgs& g, std::vector<double2>& partial) {
                 for (int i = 0; i < TM; i++)
                     for (int j = 0; j < TN; j++) { a2[i][j] = acc[t][i * TN + j]; d2[i][j] = dacc[t][i * TN + j]; }
                 bgemm_chunk<M, N>(As.data() + (size_t)buf * S.kc * S.ra, Bs.data() + (size_t)buf * S.kc * S.rb, tm, tn, a2);
-                if ((c + 1) % g.flush == 0 || c + 1 == g.nchunks) bgemm_flush<TM, TN>(a2, d2);
+                if (((c + 1) & (g.flush - 1)) == 0 || c + 1 == g.nchunks) bgemm_flush<TM, TN>(a2, d2);
                 for (int i = 0; i < TM; i++)
                     for (int j = 0; j < TN; j++) { acc[t][i * TN + j] = a2[i][j]; dacc[t][i * TN + j] = d2[i][j]; }
             }
