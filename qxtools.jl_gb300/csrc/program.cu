@@ -683,19 +683,33 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
             const int32_t* ly = a_big ? lb : la;
             std::vector<PBit> from_x;
             for (const PBit& b : X.layout) { PBit c = to_c(lx, b); if (c.axis != -3) from_x.push_back(c); }
-            std::vector<PBit> fresh;
+            // C follows X's bit order, and the free bits new from Y take the places of the summed
+            // bits.  The batch bits (slice and bitstring) go on top, X's first: every batch value
+            // of every intermediate is then one contiguous block, which keeps the final joins --
+            // the steps where both operands carry the batch -- reading whole sectors and pages
+            // instead of pieces strided by the batch
+            auto is_batch = [](const PBit& b) { return b.axis == kBeta || b.axis == kSigma; };
+            std::vector<PBit> fresh, fresh_batch, top;
             for (const PBit& b : Y.layout) {
                 PBit c = to_c(ly, b);
                 if (c.axis == -3) continue;
-                if (std::find(from_x.begin(), from_x.end(), c) == from_x.end()) fresh.push_back(c);
+                if (std::find(from_x.begin(), from_x.end(), c) == from_x.end())
+                    (is_batch(c) ? fresh_batch : fresh).push_back(c);
             }
             size_t fi = 0;
             for (const PBit& b : X.layout) {
                 PBit c = to_c(lx, b);
-                if (c.axis != -3) t.layout.push_back(c);
-                else if (fi < fresh.size()) t.layout.push_back(fresh[fi++]);
+                if (c.axis == -3) {
+                    if (fi < fresh.size()) t.layout.push_back(fresh[fi++]);
+                } else if (is_batch(c)) {
+                    top.push_back(c);
+                } else {
+                    t.layout.push_back(c);
+                }
             }
             while (fi < fresh.size()) t.layout.push_back(fresh[fi++]);
+            for (const PBit& b : top) t.layout.push_back(b);
+            for (const PBit& b : fresh_batch) t.layout.push_back(b);
         }
         if (t.layout.size() > 46) return fail(QXG_ERR_UNSUPPORTED, "tensor with more than 2^46 elements");
     }
@@ -2093,10 +2107,48 @@ std::string describe_step(const qxg_program* P, const Step& st, int group, int i
         for (size_t i = 0; i < at.size(); i++) d += (i ? "," : "") + at[i];
         if (!st.tune_note.empty()) d += " tuned=" + st.tune_note;
     } else {
-        d += st.batch >= 0 ? "cuda-core batched small step" : contract_form(st.sargs, P->fp64, P->sm_count);
+        const std::string form = st.batch >= 0 ? "cuda-core batched small step"
+                                               : contract_form(st.sargs, P->fp64, P->sm_count);
+        d += form;
         int ncb = 0;
         while ((int64_t(1) << ncb) < st.sargs.nC) ncb++;
         d += " c_bits=" + std::to_string(ncb) + " nk=" + std::to_string(st.sargs.nk);
+        if (form.find("batched-gemm") != std::string::npos || form.find("long-sum") != std::string::npos) {
+            // which index bit lies at each address bit of A and of B (b: in A, B and C; m: A and C;
+            // n: B and C; k: summed), from the lowest
+            const StepArgs& s = st.sargs;
+            auto one = [](const BitMap& m, int bit) {
+                const int64_t o = pdep(int64_t(1) << bit, m);
+                return o ? __builtin_ctzll((unsigned long long)o) : -1;
+            };
+            std::vector<std::string> aat, bat;
+            auto put = [](std::vector<std::string>& at, int pos, const std::string& v) {
+                if (pos < 0) return;
+                if ((int)at.size() <= pos) at.resize(pos + 1, "-");
+                at[pos] = v;
+            };
+            int nbat = 0, nm = 0, nn = 0;
+            for (int p = 0; p < ncb; p++) {
+                const int ia = one(s.cA, p), ib = one(s.cB, p);
+                if (ia >= 0 && ib >= 0) {
+                    const std::string v = "b" + std::to_string(nbat++);
+                    put(aat, ia, v);
+                    put(bat, ib, v);
+                } else if (ia >= 0) {
+                    put(aat, ia, "m" + std::to_string(nm++));
+                } else {
+                    put(bat, ib, "n" + std::to_string(nn++));
+                }
+            }
+            for (int j = 0; j < s.nk; j++) {
+                put(aat, one(s.kA, j), "k" + std::to_string(j));
+                put(bat, one(s.kB, j), "k" + std::to_string(j));
+            }
+            d += " a_bits=";
+            for (size_t i = 0; i < aat.size(); i++) d += (i ? "," : "") + aat[i];
+            d += " b_bits=";
+            for (size_t i = 0; i < bat.size(); i++) d += (i ? "," : "") + bat[i];
+        }
     }
     return d;
 }
