@@ -72,7 +72,10 @@ def parse():
     ap.add_argument("--tc-tuning", default="auto",
                     help="tensor-core tile variants: 'auto' (timed per step) or candidate number k >= 1")
     ap.add_argument("--gradient", action="store_true",
-                    help="time the reverse-mode gradient against the forward pass (parametrised 5x5 circuit)")
+                    help="only the reverse-mode gradient against the forward pass (parametrised 5x5 circuit)")
+    ap.add_argument("--no-gradient", action="store_true",
+                    help="leave out the gradient leg of the default line (gradient / forward on the parametrised "
+                         "5x5 circuit, with its error against FP64)")
     return ap.parse_args()
 
 
@@ -522,6 +525,8 @@ def run_ours(args):
         line["fp64"], ref64 = fp64_arm(q, prog, all_bits[:n64], out_size, local, dev, stream_of=torch, args=args)
         line["split_over_fp64"] = value / line["fp64"]["value"]
         line["err_vs_fp64"] = error_stats(got[:n64], ref64)
+    if rank == 0 and ws == 1 and not args.no_gradient and args.precision != "fp64":
+        line["gradient"] = gradient_leg(q, args, max(1, min(args.steps, 3)), 2)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(prog, bits, info, args.cpu_seconds)
     if rank == 0:
@@ -531,37 +536,34 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_gradient(args):
+def gradient_leg(q, args, steps: int, warmup: int) -> dict:
     """Forward vs reverse-mode gradient on the parametrised 5x5, 12-layer circuit (840 angles,
-    256 bitstrings, L = sum |amplitude|^2): seconds per evaluation through the host API, the
-    ratio, and the angle gradient's error against the FP64 gradient on the first 8 bitstrings."""
+    256 bitstrings, L = sum |amplitude|^2): seconds per evaluation through the host API (each
+    replayed from CUDA graphs unless --no-graphs), the ratio, and the angle gradient's error
+    against the FP64 gradient on the first 8 bitstrings."""
     import numpy as np
     import torch
-    import __graft_entry__ as entry
-    q = entry.load()
-    torch.cuda.set_device(0)
     circ = q.create_parametrised_circuit(5, 5, 12, seed=args.seed)
     bits = list(q.amplitudes_uniform(25, args.seed, 256))
-    # planned like the param_5x5_l12 workload (its pinned plan seed and trials, ranked by plan_cost
+    # planned like the param_5x5_l12 workload (its pinned plan seed, trials and planner, ranked
     # with the bitstring batch)
     spec = q.workloads.WORKLOADS["param_5x5_l12"]
     plan_opts = dict(seed=args.plan_seed if args.plan_seed is not None else spec["plan_seed"], time=spec["plan_time"],
-                     width_cap=q.workloads.WIDTH_CAP, beta=spec["nbits"], planner=args.planner or "python")
-    # forward and gradient passes both replayed from CUDA graphs (unless --no-graphs)
+                     width_cap=q.workloads.WIDTH_CAP, beta=spec["nbits"], planner=args.planner or spec.get("planner", "python"))
     f = q.gradients.ParametrisedCircuitLoss(circ, precision=args.precision, use_graphs=not args.no_graphs,
                                             **plan_opts)
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         f.executor.amplitudes(bits)
         f.loss_and_grad(bits)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         f.executor.amplitudes(bits)
-    fwd = (time.perf_counter() - t0) / args.steps
+    fwd = (time.perf_counter() - t0) / steps
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         L, g, _ = f.loss_and_grad(bits)
-    grad = (time.perf_counter() - t0) / args.steps
+    grad = (time.perf_counter() - t0) / steps
     sub = bits[:8]
     ref = q.gradients.ParametrisedCircuitLoss(circ, precision="fp64", **plan_opts)
     _, g64, _ = ref.loss_and_grad(sub)
@@ -569,16 +571,29 @@ def run_gradient(args):
     ref.close()
     info = f.executor.info()
     f.close()
-    line = {"metric": "gradient seconds / forward seconds (reverse-mode adjoint)", "value": grad / fwd,
+    return {"workload": "param_5x5_l12", "params": circ.num_params, "bitstrings": len(bits),
+            "precision": args.precision, "plan_steps": info["num_steps"], "planner": plan_opts["planner"],
+            "flops_per_amplitude": info["flops_per_amplitude"], "steps": steps, "warmup": max(1, warmup),
+            "forward_s": fwd, "gradient_s": grad, "gradient_over_forward": grad / fwd,
+            "amplitudes_per_s_forward": len(bits) / fwd, "loss": L,
+            "max_abs_err_vs_fp64_8bits": float(np.max(np.abs(gs - g64))),
+            "max_rel_err_vs_fp64_8bits": float(np.max(np.abs(gs - g64)) / np.max(np.abs(g64)))}
+
+
+def run_gradient(args):
+    """The gradient leg alone, as its own JSON line (metric: gradient seconds / forward seconds)."""
+    import torch
+    import __graft_entry__ as entry
+    q = entry.load()
+    torch.cuda.set_device(0)
+    g = gradient_leg(q, args, args.steps, args.warmup)
+    line = {"metric": "gradient seconds / forward seconds (reverse-mode adjoint)", "value": g["gradient_over_forward"],
             "unit": "ratio", "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic (seeded angles, bitstrings)",
-            "config": {"workload": "param_5x5_l12", "params": circ.num_params, "bitstrings": len(bits),
-                       "precision": args.precision, "plan_steps": info["num_steps"],
-                       "planner": args.planner or "python",
-                       "flops_per_amplitude": info["flops_per_amplitude"]},
-            "forward_s": fwd, "gradient_s": grad, "amplitudes_per_s_forward": len(bits) / fwd,
-            "loss": L, "max_abs_err_vs_fp64_8bits": float(np.max(np.abs(gs - g64))),
-            "max_rel_err_vs_fp64_8bits": float(np.max(np.abs(gs - g64)) / np.max(np.abs(g64)))}
+            "config": {k: g[k] for k in ("workload", "params", "bitstrings", "precision", "plan_steps", "planner",
+                                         "flops_per_amplitude")}}
+    line.update({k: g[k] for k in ("forward_s", "gradient_s", "amplitudes_per_s_forward", "loss",
+                                   "max_abs_err_vs_fp64_8bits", "max_rel_err_vs_fp64_8bits")})
     print(json.dumps(line), flush=True)
 
 

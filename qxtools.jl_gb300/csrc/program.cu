@@ -684,11 +684,14 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
             std::vector<PBit> from_x;
             for (const PBit& b : X.layout) { PBit c = to_c(lx, b); if (c.axis != -3) from_x.push_back(c); }
             // C follows X's bit order, and the free bits new from Y take the places of the summed
-            // bits.  The batch bits (slice and bitstring) go on top, X's first: every batch value
-            // of every intermediate is then one contiguous block, which keeps the final joins --
-            // the steps where both operands carry the batch -- reading whole sectors and pages
-            // instead of pieces strided by the batch
-            auto is_batch = [](const PBit& b) { return b.axis == kBeta || b.axis == kSigma; };
+            // bits.  In the Complex64 modes the batch bits (slice and bitstring) go on top, X's
+            // first: every batch value of every intermediate is then one contiguous block, which
+            // keeps the final joins -- the steps where both operands carry the batch -- reading
+            // whole sectors and pages instead of pieces strided by the batch.  The FP64 kernels
+            // (compute-bound on the FP64 pipe) run faster with the batch bits where the summed bits
+            // were, so FP64 programmes keep them there.
+            const bool fp64 = P->fp64;
+            auto is_batch = [fp64](const PBit& b) { return !fp64 && (b.axis == kBeta || b.axis == kSigma); };
             std::vector<PBit> fresh, fresh_batch, top;
             for (const PBit& b : Y.layout) {
                 PBit c = to_c(ly, b);

@@ -13,7 +13,7 @@ deterministic for (name, seed, time).  Generated programmes are cached under _bu
   rqc_4x4_d10          4x4 grid, 10 cycles, unsliced, 64 bitstrings (the CPU-runnable case)
   rqc_6x6_d14_s4       6x6 grid, 14 cycles, 4 sliced bonds, 256 bitstrings (library planner)
   rqc_5x5_d12_open6    5x5 grid, 12 cycles, 6 qubits open (2^6 amplitudes per bitstring),
-                       64 bitstrings of the other 19 qubits -> 4096 amplitudes
+                       64 bitstrings of the other 19 qubits -> 4096 amplitudes (library planner)
   rqc_3x4_d8_s3        3x4 grid, 8 cycles, 3 sliced bonds, 64 bitstrings (parity size)
   rqc_6x6_d14_w28      the same circuit sliced until every intermediate has at most 2^28 elements
                        (8 bonds, 256 slices; 4 GiB per ComplexF64 intermediate instead of the
@@ -49,15 +49,19 @@ __all__ = ["WORKLOADS", "build_workload"]
 WORKLOADS = {
     "rqc_4x4_d10": dict(rows=4, cols=4, depth=10, nslice=0, open=0, nbits=64),
     "rqc_6x6_d14_s4": dict(rows=6, cols=6, depth=14, nslice=4, open=0, nbits=256, planner="native"),
-    # plan_seed / plan_time: the fastest of the seed search's best-ranked plans, measured on a GB300
-    "rqc_5x5_d12_open6": dict(rows=5, cols=5, depth=12, nslice=0, open=6, nbits=64, plan_time=4, plan_seed=18),
+    # library planner, plan seed 18, 32 trees: 675k amplitudes/s on a GB300 against 524k for the
+    # fastest plan of a seed search with the Python stand-in
+    "rqc_5x5_d12_open6": dict(rows=5, cols=5, depth=12, nslice=0, open=6, nbits=64, plan_time=4, plan_seed=18,
+                              planner="native"),
     "rqc_3x4_d8_s3": dict(rows=3, cols=4, depth=8, nslice=3, open=0, nbits=64),
     "rqc_6x6_d14_w28": dict(rows=6, cols=6, depth=14, nslice=4, max_log2=28, open=0, nbits=256, planner="native"),
     "rqc_7x7_d10_w22": dict(rows=7, cols=7, depth=10, nslice=0, max_log2=22, open=0, nbits=1024, planner="native"),
     # parametrised: per layer Rx(t) Rz(t) on every qubit + fSim(t, p) on one coupler pattern;
     # 840 angles; two-qubit gates kept whole so each gate is one differentiable leaf
+    # library planner (2^34.9 FLOPs per bitstring against 2^37.1 for the stand-in's plan): the
+    # gradient takes 3.5x the forward time against 4.5x
     "param_5x5_l12": dict(rows=5, cols=5, depth=12, nslice=0, open=0, nbits=256, parametrised=True, plan_time=4,
-                          plan_seed=14),
+                          plan_seed=14, planner="native"),
 }
 
 _CACHE = Path(__file__).resolve().parent / "_build" / "workloads"
