@@ -48,7 +48,7 @@ constexpr int kBGemmKC = 8;             // summed values per chunk
 //   kc         summed values per chunk (8): every thread copies 1..kBGemmMaxL elements of each
 //              operand per chunk;
 //   layout     a chunk's A quadruples as [k][row group][TM + 1] (one padding quadruple per group
-//              keeps the groups of a warp in different banks), B as [k][column group][TN + 1];
+//              keeps the groups of a warp in different banks) plus one per k, B likewise;
 //   ring       raw chunks in flight, 3..8, as many as fit kBGemmRingTarget with the two
 //              quadruple buffers (each raw chunk [j][thread] float2 for A, then for B).
 struct BGemmShape {
@@ -67,8 +67,10 @@ constexpr BGemmShape bgemm_shape(int M, int N) {
     if (!g.tm) return g;
     g.thr_m = M / g.tm;
     g.thr_n = N / g.tn;
-    g.ra = g.thr_m * (g.tm + 1);
-    g.rb = g.thr_n * (g.tn + 1);
+    // one more padding quadruple per summed value: lanes that hold consecutive k of a chunk (the
+    // summed bits are often an operand's lowest address bits) store into different banks
+    g.ra = g.thr_m * (g.tm + 1) + 1;
+    g.rb = g.thr_n * (g.tn + 1) + 1;
     const int kc = kBGemmKC;
     if (M * kc < g.nthr || N * kc < g.nthr || M * kc > g.nthr * kBGemmMaxL || N * kc > g.nthr * kBGemmMaxL) {
         g.tm = 0;
@@ -430,9 +432,9 @@ bool plan_bgemm(const StepArgs& s, int sm_count, BGemmArgs* g, int min_log2) {
         return false;
     a.nbatch = int64_t(1) << ng;
     const int64_t chunks = int64_t(1) << (s.nk - lkc);
-    // K ranges: enough blocks for about four per SM, each range at least 2^12 terms
+    // K ranges: enough blocks for about four per SM, each range at least 2^9 terms
     int64_t nsplit = 1;
-    while (a.nbatch * nsplit < (int64_t)sm_count * 4 && chunks / (nsplit * 2) * S.kc >= 4096) nsplit *= 2;
+    while (a.nbatch * nsplit < (int64_t)sm_count * 4 && chunks / (nsplit * 2) * S.kc >= 512) nsplit *= 2;
     if (a.nbatch * nsplit > (int64_t(1) << 31) - 1) return false;
     a.nsplit = (int)nsplit;
     a.nchunks = chunks / nsplit;

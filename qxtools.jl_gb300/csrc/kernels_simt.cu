@@ -1019,15 +1019,16 @@ size_t lsum_partial_bytes(const LSumArgs& la, int NA, int NB) {
 }
 
 // Splits of the split-K form: used when the results are few (<= 2^14) and each sums at least
-// 2^14 terms; enough splits of the high K index to give about 8 blocks per SM, at least 2^12
-// terms per split, and at most 2^22 partials in all.
+// 2^8 terms (with fewer results than SMs the general form would leave most of the GPU idle);
+// enough splits of the high K index to give about 8 blocks per SM, at least 2^12 terms per split
+// (2^6 below 2^14 summed terms), and at most 2^22 partials in all.
 int splitk_count(const StepArgs& a, int sm_count) {
-    if (a.nC > (int64_t(1) << 14) || a.nk < 14) return 0;
+    if (a.nC > (int64_t(1) << 14) || a.nk < 8) return 0;
     const int nkt = a.nk < kKTableBits ? a.nk : kKTableBits;
     const int64_t KO = int64_t(1) << (a.nk - nkt);
     const int64_t ntile = (a.nC + kSplitTile - 1) / kSplitTile;
     int64_t want = std::max<int64_t>(1, (int64_t)sm_count * 8 / ntile);
-    want = std::min<int64_t>(want, std::max<int64_t>(1, (int64_t(1) << a.nk) >> 12));
+    want = std::min<int64_t>(want, std::max<int64_t>(1, (int64_t(1) << a.nk) >> (a.nk < 14 ? 6 : 12)));
     want = std::min<int64_t>(want, KO);
     want = std::min<int64_t>(want, std::max<int64_t>(1, (int64_t(1) << 22) / a.nC));
     return (int)want;
