@@ -460,7 +460,10 @@ def run_ours(args):
     flops_exec = sum(v["flops"] for v in by_kind.values())
     tflops = flops_exec / (total_ms * 1e-3) / 1e12 if total_ms else 0.0
     kernel_name = dom_name
-    traffic, tsum = traffic_summary(args.workload, {"contract_tc": "tc_contract"}.get(dom_name, dom_name),
+    # the committed DRAM summaries are named for the kernel class: tc_contract (tensor-core GEMMs),
+    # contract_kernel_fp32 (CUDA-core contractions)
+    traffic, tsum = traffic_summary(args.workload, {"contract_tc": "tc_contract", "contract_fp32": "contract_kernel_fp32",
+                                                    "contract_fp64": "contract_kernel_fp64"}.get(dom_name, dom_name),
                                     args.precision)
     if tsum and "dram_over_algorithmic" in tsum and dom["launches"]:
         # measured on a smaller case: DRAM bytes per algorithmic byte of this kernel class, applied
