@@ -291,6 +291,10 @@ def workload_config(info, args, ex_info):
            "planner": info["spec"].get("planner", "python"),
            "precision": args.precision, "cuda_graphs": not args.no_graphs,
            "l2": "intermediates larger than L2 (no flush needed)", "arm": "split-precision batched executor"}
+    if info["name"] == "rqc_7x7_d10_w22":
+        cfg["stands_in_for"] = ("7x7 grid, 16 cycles, every intermediate <= 2^28 elements with about 2^10 slices, 1024 "
+                                "amplitudes: at 16 cycles that width target takes more than 2^20 slices and 2^60 FLOPs "
+                                "per amplitude, so the 7x7 circuit runs at 10 cycles (<= 2^22 elements, 8 slices)")
     if ex_info:
         cfg.update({"bitstring_batch": ex_info["bitstring_batch"], "slice_batch": ex_info["slice_batch"],
                     "workspace_bytes": ex_info["workspace_bytes"],
