@@ -94,7 +94,11 @@ typedef struct qxg_options {
     int32_t tc_stall_test;        /* test hook, leave 0: nonzero makes the first CTA of every
                                      tensor-core GEMM issue no operand copies, so its waits run out and
                                      the call returns QXG_ERR_TIMEOUT (exercises the timeout path) */
-    int32_t reserved[3];
+    int32_t tc_joins;             /* 1: the final joins of split-TF32 programmes (32 x 8..32 results
+                                     per batch value, long sums) run on the tensor-core join (3xTF32,
+                                     operands split in the kernel); 0 = the CUDA cores' batched small
+                                     GEMM (default: it runs the benchmark's 32 x 32 joins as fast) */
+    int32_t reserved[2];
 } qxg_options;
 
 typedef struct qxg_program qxg_program;

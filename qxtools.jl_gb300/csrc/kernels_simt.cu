@@ -1055,21 +1055,6 @@ cudaError_t launch_rows(const RowArgs& ra, int* exps, cudaStream_t s, int sm_cou
 
 }  // namespace
 
-// Consecutive (src, dst) pairs with both sides increasing by one collapse into one run.
-bool make_runs(const std::vector<std::pair<int, int>>& pairs, BitMap* m) {
-    m->n = 0;
-    for (size_t i = 0; i < pairs.size();) {
-        size_t j = i + 1;
-        while (j < pairs.size() && pairs[j].first == pairs[j - 1].first + 1 && pairs[j].second == pairs[j - 1].second + 1)
-            j++;
-        if (m->n >= kMaxRuns) return false;
-        m->r[m->n] = Run{(uint8_t)pairs[i].first, (uint8_t)(j - i), (uint8_t)pairs[i].second, 0};
-        m->n++;
-        i = j;
-    }
-    return true;
-}
-
 size_t contract_scratch_bytes(const StepArgs& a, bool fp64, int sm_count) {
     RowArgs ra;
     Rows2Args r2;

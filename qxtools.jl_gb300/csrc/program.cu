@@ -96,6 +96,8 @@ struct Step {                           // an executable item of a pass
     ViewAdjArgs vaargs;
     LeafGradArgs largs;
     bool use_tc = false;                // tensor-core path (split modes)
+    bool use_join = false;              // tensor-core final join (split TF32; tc_join.cu)
+    TcJoinArgs join{};                  // its plan (operand pointers bound at launch)
     int batch = -1;                     // batch of small steps it runs in (index in its list's batches)
     bool tc_tuned = false;              // the tile variant has been chosen
     std::string tune_note;              // autotuner: milliseconds per candidate variant
@@ -472,6 +474,27 @@ std::vector<int64_t> leaf_offsets(const qxg_program* P, int64_t* total) {
 // gradient.  Adjoint tensors are table entries ntensors + t with the forward tensor's layout.
 // tc_tuning = k >= 1: candidate k-1 of every tensor-core step (the last one where a step has
 // fewer), chosen at plan time; 0 leaves the choice to the autotuner.
+// The final joins of a split-TF32 programme go to the tensor-core join when the options ask for
+// it and the step fits it.
+bool join_eligible(const qxg_program* P, Step& st) {
+    if (P->fp64 || P->opts.precision != QXG_PREC_SPLIT_TF32 || !P->opts.tc_joins) return false;
+    return tc_join_plan(st.sargs, P->sm_count, &st.join);
+}
+
+// Launch a tensor-core join with the step's current operand pointers and the programme's
+// error word and wait controls.
+cudaError_t launch_join(const qxg_program* P, const Step& st, int* exps, cudaStream_t s, int* launches) {
+    TcJoinArgs g = st.join;
+    g.P = static_cast<const float2*>(g.p_is_a ? st.sargs.A : st.sargs.B);
+    g.Q = static_cast<const float2*>(g.p_is_a ? st.sargs.B : st.sargs.A);
+    g.C = static_cast<float2*>(st.sargs.C);
+    g.err = P->d_tc_err;
+    g.wait_limit = P->opts.tc_wait_limit > 0 ? (uint32_t)P->opts.tc_wait_limit : 0;
+    g.stall = P->opts.tc_stall_test != 0 ? 1 : 0;
+    if (g.nsplit > 1 && P->scratch_cap < tc_join_partial_bytes(g)) return cudaErrorInvalidValue;
+    return tc_join_launch(g, exps, P->d_scratch, s, launches);
+}
+
 void tc_fix_variant(const qxg_program* P, Step& st) {
     // the programme's own timeout word, and the options' test hooks for the bounded waits
     st.tc.err_word = P->d_tc_err;
@@ -532,12 +555,13 @@ int build_backward(qxg_program* P, Plan& pl, int* err) {
         st.sargs.expC = T[res].slot;
         st.flops = 8.0 * (double)st.sargs.nC * (double)(int64_t(1) << st.sargs.nk);
         st.bytes = es * (sz(x) + sz(y) + sz(res));
-        if (!P->fp64 && P->opts.precision != QXG_PREC_FP32 &&
+        st.use_join = join_eligible(P, st);
+        if (!st.use_join && !P->fp64 && P->opts.precision != QXG_PREC_FP32 &&
             !contract_prefers_cuda_cores(st.sargs, P->fp64, P->sm_count))
             st.use_tc = tc_plan_step(st.sargs, T[x].layout.size(), T[y].layout.size(), T[res].layout.size(),
                                      P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc,
                                      (double)P->opts.tc_plane_budget_mb * (1 << 20));
-            if (st.use_tc) tc_fix_variant(P, st);
+        if (st.use_tc) tc_fix_variant(P, st);
         pl.flops_bwd += st.flops;
         pl.bsteps.push_back(st);
         return 0;
@@ -790,12 +814,13 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
             st.flops = 8.0 * (double)st.sargs.nC * (double)(int64_t(1) << kbit);
             st.bytes = s * ((double)(int64_t(1) << A.layout.size()) + (double)(int64_t(1) << B.layout.size()) +
                             (double)st.sargs.nC);
-            if (!P->fp64 && P->opts.precision != QXG_PREC_FP32 &&
+            st.use_join = join_eligible(P, st);
+            if (!st.use_join && !P->fp64 && P->opts.precision != QXG_PREC_FP32 &&
                 !contract_prefers_cuda_cores(st.sargs, P->fp64, P->sm_count))
                 st.use_tc = tc_plan_step(st.sargs, A.layout.size(), B.layout.size(), t.layout.size(),
                                          P->opts.precision == QXG_PREC_SPLIT_TF32, &st.tc,
-                                     (double)P->opts.tc_plane_budget_mb * (1 << 20));
-                if (st.use_tc) tc_fix_variant(P, st);
+                                         (double)P->opts.tc_plane_budget_mb * (1 << 20));
+            if (st.use_tc) tc_fix_variant(P, st);
         }
         if (err) return fail(QXG_ERR_UNSUPPORTED, "bit map needs more than the supported number of runs");
         plan->flops_pass[t.group] += st.flops;
@@ -884,13 +909,17 @@ int build_plan(qxg_program* P, int bc, int sc, std::unique_ptr<Plan>& out, bool 
     for (int g = 0; g < 3; g++)
         for (auto& st : plan->steps[g]) if (st.use_tc) scratch = std::max(scratch, tc_scratch_need(P, st));
     for (auto& st : plan->bsteps) if (st.use_tc) scratch = std::max(scratch, tc_scratch_need(P, st));
+    // FP64 partials of tensor-core joins with several K ranges per batch value
+    for (int g = 0; g < 3; g++)
+        for (auto& st : plan->steps[g]) if (st.use_join) scratch = std::max(scratch, tc_join_partial_bytes(st.join));
+    for (auto& st : plan->bsteps) if (st.use_join) scratch = std::max(scratch, tc_join_partial_bytes(st.join));
     // split-K partials of CUDA-core steps with few results and a long sum share the scratch
     for (int g = 0; g < 3; g++)
         for (auto& st : plan->steps[g])
-            if (st.kind == QXG_OP_NCON && !st.use_tc)
+            if (st.kind == QXG_OP_NCON && !st.use_tc && !st.use_join)
                 scratch = std::max(scratch, contract_scratch_bytes(st.sargs, P->fp64, P->sm_count));
     for (auto& st : plan->bsteps)
-        if (st.bkind == kBwdNcon && !st.use_tc)
+        if (st.bkind == kBwdNcon && !st.use_tc && !st.use_join)
             scratch = std::max(scratch, contract_scratch_bytes(st.sargs, P->fp64, P->sm_count));
     plan->tc_scratch_bytes = scratch;
     // reduction of the root
@@ -1223,6 +1252,7 @@ void add_tensor_span(const qxg_program* P, const Plan& pl, int t, std::vector<Sp
 
 bool step_uses_scratch(const qxg_program* P, const Step& st) {
     if (st.kind != QXG_OP_NCON) return false;
+    if (st.use_join) return tc_join_partial_bytes(st.join) > 0;
     return st.use_tc || contract_scratch_bytes(st.sargs, P->fp64, P->sm_count) > 0;
 }
 
@@ -1340,6 +1370,11 @@ int launch_fwd_step(qxg_program* P, Plan& pl, Step& st, int* exps, cudaStream_t 
             kind = QXG_KERNEL_CONTRACT_TC;
             QXG_CUDA(tc_run_gemm(st.tc, st.sargs, exps, P->d_scratch, s, P->sm_count));
             if (st.tc.ks > 0) P->launches++;            // the split-K sum
+        } else if (st.use_join) {
+            kind = QXG_KERNEL_CONTRACT_TC;
+            int nl = 1;
+            QXG_CUDA(launch_join(P, st, exps, s, &nl));
+            P->launches += nl - 1;
         } else {
             kind = P->fp64 ? QXG_KERNEL_CONTRACT_FP64 : QXG_KERNEL_CONTRACT_FP32;
             int nl = 1;
@@ -1360,7 +1395,7 @@ int launch_fwd_step(qxg_program* P, Plan& pl, Step& st, int* exps, cudaStream_t 
 // A step small enough to share a launch: a CUDA-core contraction (forward or adjoint) with at
 // most kBatchMaxResults results, K <= kBatchMaxK and no scratch.
 bool step_small(const qxg_program* P, const Step& st) {
-    if (st.kind != QXG_OP_NCON || st.use_tc) return false;
+    if (st.kind != QXG_OP_NCON || st.use_tc || st.use_join) return false;
     if (st.bkind != 0 && st.bkind != kBwdNcon) return false;
     if (st.sargs.nC > kBatchMaxResults || (int64_t(1) << st.sargs.nk) > kBatchMaxK) return false;
     return contract_scratch_bytes(st.sargs, P->fp64, P->sm_count) == 0;
@@ -1588,6 +1623,11 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
                 QXG_CUDA(tc_run_step(st.tc, st.sargs, exps, P->d_scratch, s, P->sm_count, &nl));
                 P->launches += nl - 1;
                 kind = QXG_KERNEL_CONTRACT_TC;
+            } else if (st.use_join) {
+                int nl = 1;
+                QXG_CUDA(launch_join(P, st, exps, s, &nl));
+                P->launches += nl - 1;
+                kind = QXG_KERNEL_CONTRACT_TC;
             } else {
                 int nl = 1;
                 QXG_CUDA(launch_contract(st.sargs, P->fp64, exps, s, P->sm_count, P->d_scratch, P->scratch_cap, &nl));
@@ -1706,8 +1746,8 @@ int ensure_bits(qxg_program* P, size_t nb) {
 int check_tc_plan(qxg_program* P, const Plan* pl) {
     if (!pl) return 0;
     bool any = false;
-    for (int g = 0; g < 3; g++) for (auto& st : pl->steps[g]) any = any || st.use_tc;
-    for (auto& st : pl->bsteps) any = any || st.use_tc;
+    for (int g = 0; g < 3; g++) for (auto& st : pl->steps[g]) any = any || st.use_tc || st.use_join;
+    for (auto& st : pl->bsteps) any = any || st.use_tc || st.use_join;
     if (!any) return 0;
     int code = 0;
     QXG_CUDA(tc_read_error(&code, P->d_tc_err, P->stream));
@@ -1964,7 +2004,7 @@ int qxg_program_info_get(const qxg_program* P, qxg_program_info* info) {
         for (int g = 0; g < 3; g++)
             for (auto& st : pl.steps[g]) {
                 if (st.kind == QXG_OP_NCON) c[g]++;
-                if (st.use_tc) ntc++;
+                if (st.use_tc || st.use_join) ntc++;
             }
         info->num_steps_tensor_core = ntc;
         int nf = 0;
@@ -2093,7 +2133,7 @@ std::string describe_step(const qxg_program* P, const Step& st, int group, int i
                 at[dst] = std::string(1, cls) + std::to_string(m.r[i].src + j);
             }
     };
-    if (st.use_tc) {
+    if (st.use_tc && !st.use_join) {
         const TcStep& t = st.tc;
         if (t.ks > 0) d += "split-K=" + std::to_string(1 << t.ks) + " ";
         if (t.nouter > 0) d += "n-blocks=" + std::to_string(1 << t.nouter) + " ";
@@ -2110,13 +2150,15 @@ std::string describe_step(const qxg_program* P, const Step& st, int group, int i
         for (size_t i = 0; i < at.size(); i++) d += (i ? "," : "") + at[i];
         if (!st.tune_note.empty()) d += " tuned=" + st.tune_note;
     } else {
-        const std::string form = st.batch >= 0 ? "cuda-core batched small step"
-                                               : contract_form(st.sargs, P->fp64, P->sm_count);
+        const std::string form = st.use_join ? tc_join_describe(st.join)
+                                 : st.batch >= 0 ? "cuda-core batched small step"
+                                                 : contract_form(st.sargs, P->fp64, P->sm_count);
         d += form;
         int ncb = 0;
         while ((int64_t(1) << ncb) < st.sargs.nC) ncb++;
         d += " c_bits=" + std::to_string(ncb) + " nk=" + std::to_string(st.sargs.nk);
-        if (form.find("batched-gemm") != std::string::npos || form.find("long-sum") != std::string::npos) {
+        if (st.use_join || form.find("batched-gemm") != std::string::npos ||
+            form.find("long-sum") != std::string::npos) {
             // which index bit lies at each address bit of A and of B (b: in A, B and C; m: A and C;
             // n: B and C; k: summed), from the lowest
             const StepArgs& s = st.sargs;

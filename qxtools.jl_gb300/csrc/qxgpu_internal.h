@@ -8,6 +8,8 @@
 #pragma once
 
 #include <cstdint>
+#include <utility>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace qxg {
@@ -31,6 +33,21 @@ __host__ __device__ inline int64_t pdep(int64_t x, const BitMap& m) {
         o |= ((x >> q.src) & ((int64_t(1) << q.len) - 1)) << q.dst;
     }
     return o;
+}
+
+// Consecutive (src, dst) pairs with both sides increasing by one collapse into one run (host).
+inline bool make_runs(const std::vector<std::pair<int, int>>& pairs, BitMap* m) {
+    m->n = 0;
+    for (size_t i = 0; i < pairs.size();) {
+        size_t j = i + 1;
+        while (j < pairs.size() && pairs[j].first == pairs[j - 1].first + 1 && pairs[j].second == pairs[j - 1].second + 1)
+            j++;
+        if (m->n >= kMaxRuns) return false;
+        m->r[m->n] = Run{(uint8_t)pairs[i].first, (uint8_t)(j - i), (uint8_t)pairs[i].second, 0};
+        m->n++;
+        i = j;
+    }
+    return true;
 }
 
 // Per-pass parameters read by kernels from device memory, so a captured pass can be replayed

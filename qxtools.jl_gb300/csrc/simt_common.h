@@ -155,8 +155,6 @@ size_t bgemm_partial_bytes(const BGemmArgs& g);
 // Launch it (and the ordered sum of the K-range partials); *launches receives 1 or 2.
 cudaError_t launch_bgemm(const BGemmArgs& g, void* scratch, int* exps, cudaStream_t s, int* launches);
 
-// Consecutive (src, dst) pairs with both sides increasing by one collapse into one run.
-bool make_runs(const std::vector<std::pair<int, int>>& pairs, BitMap* m);
 // Fill the compact row form from a row form (false: the step does not fit it).
 bool plan_rows2(const RowArgs& ra, Rows2Args* r2);
 // Launch the compact row form with K summed values and N result columns per chunk.

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "tc_gemm.h"
+#include "tc_ptx.h"
 
 #include <cuda.h>
 
@@ -44,11 +45,8 @@ constexpr int threads_of(int mode) {
 constexpr int kATmemCols = 32;    // tensor-memory columns of one A stage (hi and lo, 16 each)
 constexpr int kMaxRing = 8;                              // raw X chunks in a gather ring
 constexpr int kMaxStages = 6;                            // operand stages in shared memory
-constexpr int kCols16 = kTcChunkBytes / 16;              // 16-byte core-matrix columns per chunk (4)
-constexpr int kSbo = kCols16 * 128;                      // bytes between 8-row groups (512)
 constexpr int kATileBytes = kTcTileM * kTcChunkBytes;    // 8 KB
 constexpr int kKSteps = kTcChunkBytes / 32;              // MMA K steps (32 bytes each) per chunk
-constexpr uint32_t kWaitLimit = 1u << 20;                // try_wait polls before giving up
 constexpr int kKTable = 4096;                            // k offsets tabulated by the pack kernel
 
 struct PackArgs {
@@ -98,53 +96,6 @@ struct GemmArgs {
     int stall;              // test hook: CTA 0's operand producer issues nothing (its waits run out)
     int* err;               // word a wait that gives up writes its code to (nullptr: g_tc_error)
 };
-
-__device__ __forceinline__ int read_m(const int* exps, int slot) {
-    const int m = exps[2 * slot + 1];
-    return m < -400 ? 0 : m;
-}
-__device__ __forceinline__ float pow2f(int n) {
-    n = n < -126 ? -126 : (n > 127 ? 127 : n);
-    return __int_as_float((n + 127) << 23);
-}
-__device__ __forceinline__ int exp_of(float x) { return (int)((__float_as_uint(x) >> 23) & 0xffu) - 126; }
-
-__device__ __forceinline__ uint32_t to_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
-
-// hi/lo split of one value into the element type's bit pattern
-template <bool TF32> struct Split;
-template <> struct Split<false> {
-    using E = unsigned short;
-    __device__ static void go(float v, E& hi, E& lo) {
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-        hi = __bfloat16_as_ushort(h);
-        lo = __bfloat16_as_ushort(l);
-    }
-};
-template <> struct Split<true> {
-    using E = uint32_t;
-    __device__ static void go(float v, E& hi, E& lo) {
-        hi = to_tf32(v);
-        lo = to_tf32(v - __uint_as_float(hi));
-    }
-};
-
-// Byte offset of (row, 16-byte column) inside a K-major no-swizzle tile of 64-byte rows.
-__device__ __forceinline__ int64_t core_off(int row, int col16) {
-    return (int64_t)(row >> 3) * kSbo + col16 * 128 + (row & 7) * 16;
-}
-
-template <typename E, int NE>
-__device__ __forceinline__ void st16(uint8_t* dst, const E (&v)[NE]) {
-    uint4 w;
-    memcpy(&w, v, 16);
-    *reinterpret_cast<uint4*>(dst) = w;
-}
 
 // One thread: one row, one 16-byte group g (0..1) of one K chunk: NE complex values of k, whose
 // real parts go to column g and imaginary parts to column 2 + g.
@@ -224,110 +175,6 @@ __global__ void pack_kernel(const PackArgs p, int* exps) {
 }
 
 // ---- PTX wrappers ------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait for the phase with the given parity; false when it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
-    for (uint32_t i = 0; i < limit; i++)
-        if (mbar_try(bar, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
-// 5-D tiled TMA load of one box into shared memory, completing on an mbarrier's transaction count.
-__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, const int (&c)[5], uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
-        "[%7];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(smem_u32(bar))
-        : "memory");
-}
-// Shared-memory matrix descriptor: K-major, no swizzle; LBO = 128 B between core matrices along
-// K, SBO = 512 B between 8-row groups; descriptor version 1.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
-    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(kSbo >> 4) << 32) |
-           (1ull << 46);
-}
-template <bool TF32>
-__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    if (TF32) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-            "l"(a), "l"(b), "r"(idesc), "r"(acc)
-            : "memory");
-    } else {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-            "l"(a), "l"(b), "r"(idesc), "r"(acc)
-            : "memory");
-    }
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
-        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
-        "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
-        : "memory");
-}
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
-// MMA with the A operand in tensor memory (kModeTmem).
-template <bool TF32>
-__device__ __forceinline__ void mma_ts(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t acc) {
-    if (TF32) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
-            "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
-            : "memory");
-    } else {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
-            "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
-            : "memory");
-    }
-}
-
 // 8-byte asynchronous global -> shared copies (the fused X gather keeps several K chunks in flight
 // without holding registers for them).
 __device__ __forceinline__ void cp_async8(void* dst, const void* src) {

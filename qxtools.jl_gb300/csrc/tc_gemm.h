@@ -106,3 +106,59 @@ cudaError_t tc_run_step(const TcStep& tc, const StepArgs& s, int* exps, void* sc
 cudaError_t tc_read_error(int* host_code, int* d_word, cudaStream_t st);
 
 }  // namespace qxg
+
+namespace qxg {
+
+// ---- Final joins on the tensor cores (tc_join.cu) ----------------------------------------------
+// C[b, i, j] = sum_k P[b, k, i] Q[b, k, j] with 32 free values i of one operand (P), 8-32 of the
+// other (Q), 2^10+ summed terms per batch value b and both operands large.  The MMA's A operand
+// (128 rows, in tensor memory) stacks P four times -- (Re P | -Im P) and (Im P | Re P), each as
+// tf32 hi and lo parts -- and its B operand (2 NQ rows, in shared memory) stacks Q's hi and lo
+// parts as (Re Q | Im Q), so one M = 128 MMA per 8 summed terms yields all four hi/lo products of
+// the complex product (see tc_join.cu).
+constexpr int kJoinKR = 64;         // summed terms per raw chunk (its 6 summed bits are planned)
+constexpr int kJoinMaxSeg = 256;    // contiguous segments per operand in a raw chunk
+
+struct TcJoinArgs {
+    const float2* P;
+    const float2* Q;
+    float2* C;
+    int32_t nq;                     // free values of Q (8, 16 or 32)
+    int32_t p_is_a;                 // P is the step's A operand
+    int32_t conjP, conjQ, expP, expQ, expC;
+    int64_t nbatch;
+    int32_t nsplit;                 // K ranges per batch value (FP64 partials when > 1)
+    int64_t nchunks;                // raw chunks of one K range
+    int32_t flush;                  // MMA stages (16 terms) between accumulator drains (power of two)
+    int32_t ring;                   // raw chunks in the ring
+    BitMap bP, bQ, bC;              // batch index -> P / Q / C offset
+    BitMap iC, jC;                  // free index of P / Q -> C offset
+    BitMap hP, hQ;                  // chunk index within the whole K -> P / Q offset
+    // a raw chunk of P: its tile (32 free values x 64 summed terms) in P's address order, as
+    // nsegP segments of 2^sbP contiguous elements; segment s starts at P offset pdep(s << sbP, eP)
+    // from the chunk's base and lands at byte s * segP_stride of the ring slot
+    BitMap eP, tPi, tPk;            // tile element -> P offset; i / summed index -> tile element
+    int32_t sbP, nsegP, segP_stride;
+    BitMap eQ, tQj, tQk;            // the same for Q (after P in the slot)
+    int32_t sbQ, nsegQ, segQ_stride;
+    int32_t slotP_bytes, slot_bytes;
+    uint32_t idesc;
+    uint32_t wait_limit;            // mbarrier polls before a wait gives up (0: 2^20)
+    int32_t stall;                  // test hook: CTA 0's loader issues no copies
+    int* err;                       // word a wait that gives up writes its code to
+    int32_t chunk_k[6];             // the chunk's summed bits (step k indices), for describe
+    int32_t run_p, run_q;           // contiguous elements per segment (2^sbP, 2^sbQ)
+};
+
+// Plan a step as a tensor-core join (false: it does not fit); operands of at least 2^min_log2
+// elements.
+bool tc_join_plan(const StepArgs& s, int sm_count, TcJoinArgs* g, int min_log2 = 20);
+// Scratch for the FP64 partials of the K ranges (0 with one range per batch value).
+size_t tc_join_partial_bytes(const TcJoinArgs& g);
+// Launch it (and the ordered sum of the K-range partials); *launches receives 1 or 2.
+// err_word / wait_limit / stall as in TcStep.
+cudaError_t tc_join_launch(const TcJoinArgs& g, int* exps, void* scratch, cudaStream_t st, int* launches);
+// One line for the programme's explain output.
+std::string tc_join_describe(const TcJoinArgs& g);
+
+}  // namespace qxg

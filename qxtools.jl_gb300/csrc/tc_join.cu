@@ -1,0 +1,686 @@
+// Final joins of a sliced, bitstring-batched contraction tree on the tensor cores (3xTF32).
+//
+//     C[b, i, j] = sum_k P[b, k, i] Q[b, k, j]
+// with 32 free values i of one operand (P), NQ = 8..32 free values j of the other (Q), 2^10 to
+// 2^25 summed terms per batch value b, and both operands of 2^28 to 2^33 elements.  Every operand
+// element is used by 32 or NQ results only, so the step streams both operands once; the CUDA
+// cores run out of FP32 issue before HBM does, and the tensor-core GEMM would first pack the
+// smaller operand into planes four times its size.  Here the operands are split on the fly:
+//
+//   A (MMA M = 128 rows, tensor memory): row (role, i) of P's stack
+//       role 0: hi(Re P | -Im P)   role 1: hi(Im P | Re P)   role 2 / 3: the lo parts of 0 / 1
+//   B (MMA N = 2 NQ rows, shared memory): row j = hi(Re Q | Im Q), row NQ + j = lo(Re Q | Im Q)
+//   D[(role, i), (h, j)] = sum over the chunk's terms of A . B          (FP32, tensor memory)
+// so Re C[i, j] = sum over h of D[(0, i), (h, j)] + D[(2, i), (h, j)] and Im C from roles 1 and
+// 3: the four hi/lo products of each complex product (lo*lo included) come from one M = 128,
+// N = 2 NQ, K = 8 MMA per 8 summed terms, each in its own accumulator entry.  (hi, lo): tf32
+// round-to-nearest of x and of x - hi.  The row of role r for free value i sits at tensor-memory
+// lane 32 q + 8 r + (i mod 8) with q = i / 8, so the warp that owns lanes 32 q .. 32 q + 31 holds
+// all four roles of eight free values.
+//
+// One CTA (12 warps) per (batch value, K range):
+//   warp 1         loader: per raw chunk of 64 summed terms, the chunk's P tile (32 x 64) and Q
+//                  tile (NQ x 64), each a few contiguous segments of the operand, are copied with
+//                  cp.async.bulk into a ring slot (an mbarrier counts the bytes).  The chunk's six
+//                  summed bits are planned so both tiles are runs of >= 8 elements;
+//   warps 4-11     P splitters, two groups on alternate MMA stages (16 summed terms each): warp
+//                  4 + 4 g + q reads the stage's terms for its eight free values from the slot,
+//                  splits them into the four roles and stores 32 columns of its lanes with
+//                  tcgen05.st.  Group 0 also drains: every `flush` stages (512 terms) the MMA
+//                  issuer commits one accumulator and switches to the other; group 0 adds each
+//                  committed accumulator (h = hi and lo summed in FP32) into FP64 registers
+//                  before the stage that reuses it, so the FP32 sums never run over more than 512
+//                  terms, and at the end combines the four roles with shuffles and writes C (or
+//                  its FP64 partial, added in K-range order by tc_join_reduce_kernel);
+//   warps 2-3      Q splitters: rows j and NQ + j of the stage's two B tiles (K-major core
+//                  matrices, 64-byte rows: real parts in core columns 0-1, imaginary in 2-3);
+//   warp 0 lane 0  MMA issuer: four tcgen05.mma (kind::tf32, A from tensor memory) per stage.
+// Waiting warps sleep in their barrier polls (a suspend-time hint), so they leave the issue slots
+// to the splitters.
+// Every wait is bounded; a wait that gives up writes its code to the programme's error word, the
+// CTA skips its remaining work, frees its tensor memory and returns.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tc_gemm.h"
+#include "tc_ptx.h"
+
+namespace qxg {
+namespace {
+
+constexpr int kJoinSub = 16;                        // summed terms per MMA stage
+constexpr int kJoinSubs = kJoinKR / kJoinSub;       // MMA stages per raw chunk (4)
+constexpr int kJoinStages = 4;                      // MMA stages in flight
+constexpr int kJoinMaxRing = 4;                     // raw chunks in the ring
+constexpr int kJoinPGroups = 2;                     // P splitter groups (alternate stages)
+constexpr int kJoinThreads = 32 * (4 + 4 * kJoinPGroups);
+constexpr uint32_t kJoinSleepNs = 2000;             // suspend hint of a barrier poll
+constexpr int kJoinStageCols = 2 * kJoinSub;        // tensor-memory columns of one A stage (32)
+constexpr int kJoinFlushTerms = 512;                // summed terms per FP32 accumulator
+constexpr int kJoinChunkBits = 48;                  // delta-table entries (chunk index bits)
+constexpr size_t kJoinSmemCap = 200 * 1024;         // ring + B stages (one CTA per SM)
+constexpr int kJoinPadBytes = 16;                   // padding after each segment of a slot
+
+// Byte of tile element e inside a slot: segment e >> sb, element e mod 2^sb.
+__host__ __device__ __forceinline__ int join_slot_byte(int64_t e, int sb, int stride) {
+    return (int)((e >> sb) * stride + (e & ((int64_t(1) << sb) - 1)) * 8);
+}
+// ---- index work of the kernel, shared with its host emulation -----------------------------------
+// Chunk bases walk in order: base(c + 1) = base(c) + delta(ctz(c + 1)).
+__host__ __device__ __forceinline__ int64_t join_delta(const BitMap& h, int t) {
+    return pdep(int64_t(1) << t, h) - pdep((int64_t(1) << t) - 1, h);
+}
+// Offsets of chunk c of K range si for batch value bi (the walk's first base and its check).
+__host__ __device__ __forceinline__ int64_t join_base_p(const TcJoinArgs& g, int64_t bi, int64_t si, int64_t c) {
+    return pdep(bi, g.bP) + pdep(si * g.nchunks + c, g.hP);
+}
+__host__ __device__ __forceinline__ int64_t join_base_q(const TcJoinArgs& g, int64_t bi, int64_t si, int64_t c) {
+    return pdep(bi, g.bQ) + pdep(si * g.nchunks + c, g.hQ);
+}
+// Operand offset (from the chunk's base) of a raw chunk's segment sg.
+__host__ __device__ __forceinline__ int64_t join_seg_p(const TcJoinArgs& g, int sg) {
+    return pdep((int64_t)sg << g.sbP, g.eP);
+}
+__host__ __device__ __forceinline__ int64_t join_seg_q(const TcJoinArgs& g, int sg) {
+    return pdep((int64_t)sg << g.sbQ, g.eQ);
+}
+// Slot bytes of P's free value i and summed index kl (they add), and of Q's j and kl.
+__host__ __device__ __forceinline__ int join_prow(const TcJoinArgs& g, int i) {
+    return join_slot_byte(pdep(i, g.tPi), g.sbP, g.segP_stride);
+}
+__host__ __device__ __forceinline__ int join_pcol(const TcJoinArgs& g, int kl) {
+    return join_slot_byte(pdep(kl, g.tPk), g.sbP, g.segP_stride);
+}
+__host__ __device__ __forceinline__ int join_qrow(const TcJoinArgs& g, int j) {
+    return g.slotP_bytes + join_slot_byte(pdep(j, g.tQj), g.sbQ, g.segQ_stride);
+}
+__host__ __device__ __forceinline__ int join_qcol(const TcJoinArgs& g, int kl) {
+    return join_slot_byte(pdep(kl, g.tQk), g.sbQ, g.segQ_stride);
+}
+__host__ __device__ __forceinline__ int64_t join_c_offset(const TcJoinArgs& g, int64_t bi, int i, int j) {
+    return pdep(bi, g.bC) + pdep(i, g.iC) + pdep(j, g.jC);
+}
+
+template <int NQ>
+struct JoinShape {
+    static constexpr int kQTile = 2 * NQ * kTcChunkBytes;      // B tile of 8 summed terms
+    static constexpr int kQStage = 2 * kQTile;                 // B operand of one MMA stage
+    static constexpr uint32_t kAccCols = 2 * NQ;               // columns of one accumulator
+    static constexpr uint32_t kACol0 = 2 * kAccCols;           // first A stage column
+    static constexpr uint32_t kNeed = kACol0 + kJoinStages * kJoinStageCols;
+    static constexpr uint32_t kCols = kNeed <= 128 ? 128 : (kNeed <= 256 ? 256 : 512);
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int NQ, bool SCALED>
+__global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinArgs g, double2* partial, int* exps) {
+    using S = JoinShape<NQ>;
+    extern __shared__ uint8_t join_smem_raw[];
+    // rfull / rempty per ring slot, fullA / empty per MMA stage, accf / acce per accumulator, drain
+    __shared__ uint64_t bars[2 * kJoinMaxRing + 2 * kJoinStages + 5];
+    __shared__ int32_t prow[32], pcol[kJoinKR], qrow[NQ], qcol[kJoinKR];
+    __shared__ int64_t psegoff[kJoinMaxSeg], qsegoff[kJoinMaxSeg];
+    __shared__ int64_t dP[kJoinChunkBits], dQ[kJoinChunkBits];
+    __shared__ uint32_t tmem_holder;
+    __shared__ int abort_flag;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(join_smem_raw) + 127) & ~uintptr_t(127));
+    uint64_t* rfull = bars;
+    uint64_t* rempty = bars + kJoinMaxRing;
+    uint64_t* fullA = bars + 2 * kJoinMaxRing;
+    uint64_t* empty = fullA + kJoinStages;
+    uint64_t* accf = empty + kJoinStages;
+    uint64_t* acce = accf + 2;
+    uint64_t* drain = acce + 2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int* const errw = g.err;
+    const uint32_t wl = g.wait_limit ? g.wait_limit : kWaitLimit;
+    const int64_t bi = (int64_t)blockIdx.x % g.nbatch;
+    const int64_t si = (int64_t)blockIdx.x / g.nbatch;
+    // the host guarantees these; never index past the ring or the segment tables
+    const bool bad = g.ring < 2 || g.ring > kJoinMaxRing || g.nsegP > kJoinMaxSeg || g.nsegQ > kJoinMaxSeg ||
+                     g.flush < 1 || (g.flush & (g.flush - 1)) != 0 || g.flush % kJoinPGroups != 0 || g.nq != NQ;
+    const int R = g.ring;
+    uint8_t* ring = smem;
+    uint8_t* qst = smem + (size_t)R * g.slot_bytes;
+    const int64_t nchunks = bad ? 0 : g.nchunks;
+    const int64_t U = nchunks * kJoinSubs;                      // MMA stages of this CTA
+    const int64_t V = bad ? 0 : (U + g.flush - 1) / g.flush;   // accumulator drains
+
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < kJoinMaxRing; r++) { mbar_init(&rfull[r], 1u); mbar_init(&rempty[r], 2u + 4u * kJoinPGroups); }
+        for (int s = 0; s < kJoinStages; s++) { mbar_init(&fullA[s], 6u); mbar_init(&empty[s], 1u); }
+        for (int j = 0; j < 2; j++) { mbar_init(&accf[j], 1u); mbar_init(&acce[j], 4u); }
+        mbar_init(drain, 1u);
+        abort_flag = 0;
+        if (bad) atomicExch(errw, 10);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
+                     "r"(S::kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (!bad) {
+        for (int t = threadIdx.x; t < kJoinKR; t += kJoinThreads) {
+            pcol[t] = join_pcol(g, t);
+            qcol[t] = join_qcol(g, t);
+        }
+        for (int t = threadIdx.x; t < 32; t += kJoinThreads) prow[t] = join_prow(g, t);
+        for (int t = threadIdx.x; t < NQ; t += kJoinThreads) qrow[t] = join_qrow(g, t);
+        for (int t = threadIdx.x; t < g.nsegP; t += kJoinThreads) psegoff[t] = join_seg_p(g, t);
+        for (int t = threadIdx.x; t < g.nsegQ; t += kJoinThreads) qsegoff[t] = join_seg_q(g, t);
+        for (int t = threadIdx.x; t < kJoinChunkBits; t += kJoinThreads) {
+            dP[t] = join_delta(g.hP, t);
+            dQ[t] = join_delta(g.hQ, t);
+        }
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_holder;
+
+    auto wait = [&](uint64_t* bar, uint32_t parity) { return mbar_wait_sleep(bar, parity, wl, kJoinSleepNs); };
+    auto give_up = [&](int code) { atomicExch(&abort_flag, 1); atomicExch(errw, code); };
+    auto aborted = [&]() { return __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0); };
+    if (warp == 1) {
+        // loader: chunk c into slot c mod R once the splitters have released it
+        const bool stall = g.stall != 0 && blockIdx.x == 0;   // test hook: its waits run out
+        const int64_t c0 = si * nchunks;
+        int64_t baseP = join_base_p(g, bi, si, 0), baseQ = join_base_q(g, bi, si, 0);
+        const uint32_t segP = 8u << g.sbP, segQ = 8u << g.sbQ;
+        const uint32_t tx = (uint32_t)g.nsegP * segP + (uint32_t)g.nsegQ * segQ;
+        int slot = 0;
+        uint32_t ph = 0;
+        int64_t issued = 0;
+        for (int64_t c = 0; c < (stall ? 0 : nchunks); c++) {
+            const bool ok = wait(&rempty[slot], ph ^ 1u);
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) give_up(11);
+                break;
+            }
+            if (aborted()) break;
+            uint8_t* dst = ring + (size_t)slot * g.slot_bytes;
+            if (lane == 0) mbar_expect_tx(&rfull[slot], tx);
+            __syncwarp();
+            for (int sg = lane; sg < g.nsegP; sg += 32)
+                bulk_copy(dst + sg * g.segP_stride, g.P + baseP + psegoff[sg], segP, &rfull[slot]);
+            for (int sg = lane; sg < g.nsegQ; sg += 32)
+                bulk_copy(dst + g.slotP_bytes + sg * g.segQ_stride, g.Q + baseQ + qsegoff[sg], segQ, &rfull[slot]);
+            issued++;
+            const int t = __ffsll((unsigned long long)(c0 + c + 1)) - 1;
+            if (c + 1 < nchunks) {
+                baseP += dP[t];
+                baseQ += dQ[t];
+            }
+            if (++slot == R) { slot = 0; ph ^= 1u; }
+        }
+        // copies still in flight (only after an abort) must land before the CTA leaves
+        if (lane == 0)
+            for (int64_t q = issued - 1; q >= 0 && q >= issued - R; q--)
+                mbar_wait(&rfull[q % R], (uint32_t)((q / R) & 1));     // full limit: copies must land
+    } else if (warp == 2 || warp == 3) {
+        // Q splitters: task (j, 8-term group) per thread, every stage
+        const int tq = (warp - 2) * 32 + lane;
+        const bool live = tq < 2 * NQ;
+        const int jq = tq % NQ, gq = (tq / NQ) & 1;
+        float s = 1.f;
+        if (SCALED) s = pow2f(-read_m(exps, g.expQ));
+        const float si_ = g.conjQ ? -s : s;
+        const int rb = live ? qrow[jq] : 0;
+        int qc[8];                          // slot bytes of the task's terms within a stage
+#pragma unroll
+        for (int t = 0; t < 8; t++) qc[t] = qcol[gq * 8 + t];
+        for (int64_t u = 0; u < U; u++) {
+            const int64_t c = u / kJoinSubs;
+            const int sub = (int)(u % kJoinSubs), slot = (int)(c % R), st = (int)(u % kJoinStages);
+            bool ok = sub != 0 || wait(&rfull[slot], (uint32_t)((c / R) & 1));
+            ok = ok && wait(&empty[st], (uint32_t)((u / kJoinStages) & 1) ^ 1u);
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) give_up(12);
+                break;
+            }
+            if (aborted()) break;
+            if (live) {
+                const uint8_t* raw = ring + (size_t)slot * g.slot_bytes + rb + qcol[sub * kJoinSub];
+                uint32_t hr[8], lr[8], hm[8], lm[8];
+#pragma unroll
+                for (int t = 0; t < 8; t++) {
+                    const float2 v = *reinterpret_cast<const float2*>(raw + qc[t]);
+                    Split<true>::go(v.x * s, hr[t], lr[t]);
+                    Split<true>::go(v.y * si_, hm[t], lm[t]);
+                }
+                uint8_t* tile = qst + (size_t)st * S::kQStage + gq * S::kQTile;
+                st16(tile + core_off(jq, 0), *reinterpret_cast<const uint32_t(*)[4]>(hr));
+                st16(tile + core_off(jq, 1), *reinterpret_cast<const uint32_t(*)[4]>(hr + 4));
+                st16(tile + core_off(jq, 2), *reinterpret_cast<const uint32_t(*)[4]>(hm));
+                st16(tile + core_off(jq, 3), *reinterpret_cast<const uint32_t(*)[4]>(hm + 4));
+                st16(tile + core_off(NQ + jq, 0), *reinterpret_cast<const uint32_t(*)[4]>(lr));
+                st16(tile + core_off(NQ + jq, 1), *reinterpret_cast<const uint32_t(*)[4]>(lr + 4));
+                st16(tile + core_off(NQ + jq, 2), *reinterpret_cast<const uint32_t(*)[4]>(lm));
+                st16(tile + core_off(NQ + jq, 3), *reinterpret_cast<const uint32_t(*)[4]>(lm + 4));
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&fullA[st]);
+            if (sub == kJoinSubs - 1) {
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&rempty[slot]);
+            }
+        }
+    } else if (warp >= 4 && warp < 4 + 4 * kJoinPGroups) {
+        // P splitters: group pg takes the stages u = pg mod kJoinPGroups; warp 4 pg + q stores the
+        // tensor-memory lanes 32 q .. 32 q + 31 (roles 0-3 of free values 8 q .. 8 q + 7).  Group 0
+        // also drains: accumulator v is added into FP64 registers just before the stage that
+        // starts interval v + 2 (which reuses it) is written -- its MMAs finished several stages
+        // earlier -- and the last two at the end.
+        const int pg = (warp - 4) >> 2, q4 = warp & 3, role = lane >> 3;
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * q4) << 16);
+        float s = 1.f;
+        if (SCALED) s = pow2f(-read_m(exps, g.expP));
+        const float si_ = g.conjP ? -s : s;
+        // (x0, x1) = (re, -im) for roles 0 and 2, (im, re) for roles 1 and 3; lo parts for 2 and 3
+        const float a0 = (role & 1) ? 0.f : s, b0 = (role & 1) ? si_ : 0.f;
+        const float a1 = (role & 1) ? s : 0.f, b1 = (role & 1) ? 0.f : -si_;
+        const bool lo = role >= 2;
+        const int rb = prow[q4 * 8 + (lane & 7)];
+        int pc[kJoinSub];                   // slot bytes of the terms within a stage
+#pragma unroll
+        for (int t = 0; t < kJoinSub; t++) pc[t] = pcol[t];
+        double acc[NQ];
+#pragma unroll
+        for (int j = 0; j < NQ; j++) acc[j] = 0.0;
+        int64_t drained = 0;
+        auto drain_acc = [&](int64_t v) -> bool {
+            const uint32_t buf = (uint32_t)(v & 1);
+            const bool ok = wait(&accf[buf], (uint32_t)((v >> 1) & 1));
+            fence_after();
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) give_up(16);
+                return false;
+            }
+            const uint32_t d0 = lane_base + buf * S::kAccCols;
+            if constexpr (NQ >= 16) {
+#pragma unroll
+                for (int j0 = 0; j0 < NQ; j0 += 16) {
+                    uint32_t hi[16], lo16[16];
+                    tmem_ld16(d0 + j0, hi);
+                    tmem_ld16(d0 + NQ + j0, lo16);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        if (j0 + j < NQ) acc[j0 + j] += (double)(__uint_as_float(hi[j]) + __uint_as_float(lo16[j]));
+                }
+            } else {
+                uint32_t w[16];             // hi columns 0 .. NQ-1, lo columns NQ .. 2NQ-1
+                tmem_ld16(d0, w);
+                tmem_wait_ld();
+#pragma unroll
+                for (int j = 0; j < NQ; j++) acc[j] += (double)(__uint_as_float(w[j]) + __uint_as_float(w[NQ + j]));
+            }
+            // the accumulator may be overwritten once all four warps' loads have completed
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[buf]);
+            return true;
+        };
+        bool ok_all = true;
+        for (int64_t u = pg; u < U; u += kJoinPGroups) {
+            const int64_t c = u / kJoinSubs;
+            const int sub = (int)(u % kJoinSubs), slot = (int)(c % R), st = (int)(u % kJoinStages);
+            if (pg == 0 && u % g.flush == 0 && u / g.flush >= 2) {
+                if (!drain_acc(drained)) { ok_all = false; break; }
+                drained++;
+            }
+            bool ok = sub != pg || wait(&rfull[slot], (uint32_t)((c / R) & 1));
+            ok = ok && wait(&empty[st], (uint32_t)((u / kJoinStages) & 1) ^ 1u);
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) give_up(13);
+                ok_all = false;
+                break;
+            }
+            if (aborted()) { ok_all = false; break; }
+            fence_after();                  // the MMAs that read this A stage have completed
+            const uint8_t* raw = ring + (size_t)slot * g.slot_bytes + rb + pcol[sub * kJoinSub];
+            uint32_t w0[16], w1[16];
+#pragma unroll
+            for (int t = 0; t < kJoinSub; t++) {
+                const float2 v = *reinterpret_cast<const float2*>(raw + pc[t]);
+                const float x0 = fmaf(v.x, a0, v.y * b0), x1 = fmaf(v.x, a1, v.y * b1);
+                uint32_t h0 = to_tf32(x0), h1 = to_tf32(x1);
+                const uint32_t l0 = to_tf32(x0 - __uint_as_float(h0)), l1 = to_tf32(x1 - __uint_as_float(h1));
+                h0 = lo ? l0 : h0;
+                h1 = lo ? l1 : h1;
+                if (t < 8) { w0[t] = h0; w0[8 + t] = h1; }
+                else { w1[t - 8] = h0; w1[t] = h1; }
+            }
+            const uint32_t ta = lane_base + S::kACol0 + (uint32_t)st * kJoinStageCols;
+            tmem_st16(ta, w0);
+            tmem_st16(ta + 16, w1);
+            tmem_wait_st();
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&fullA[st]);
+            if (sub + kJoinPGroups >= kJoinSubs) {      // this group's last stage of the chunk
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&rempty[slot]);
+            }
+        }
+        if (pg == 0) {
+            for (; ok_all && drained < V; drained++) {
+                if (aborted() || !drain_acc(drained)) break;
+            }
+            // roles 0 + 2 give Re C, 1 + 3 Im C; lanes 0-7 write free values 8 q .. 8 q + 7
+            const int i = q4 * 8 + (lane & 7);
+            int emax = kExpUnset;
+#pragma unroll
+            for (int j = 0; j < NQ; j++) {
+                double x = acc[j];
+                x += __shfl_xor_sync(0xffffffffu, x, 16);
+                const double im = __shfl_down_sync(0xffffffffu, x, 8);
+                if (lane < 8) {
+                    if (g.nsplit == 1) {
+                        const float2 r = make_float2((float)x, (float)im);
+                        g.C[join_c_offset(g, bi, i, j)] = r;
+                        const float mx = fmaxf(fabsf(r.x), fabsf(r.y));
+                        if (SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
+                    } else {
+                        partial[((si * g.nbatch + bi) * 32 + i) * NQ + j] = make_double2(x, im);
+                    }
+                }
+            }
+            if (SCALED && g.nsplit == 1) {
+                if (blockIdx.x == 0 && warp == 4 && lane == 0)
+                    exps[2 * g.expC] = exps[2 * g.expP] + exps[2 * g.expQ] + read_m(exps, g.expP) + read_m(exps, g.expQ);
+                for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+                if (lane == 0 && emax != kExpUnset) atomicMax(&exps[2 * g.expC + 1], emax);
+            }
+        }
+    } else if (warp == 0 && lane == 0) {
+        // MMA issuer
+        const int64_t fm = g.flush - 1;
+        for (int64_t u = 0; u < U; u++) {
+            const int64_t v = u / g.flush;
+            const uint32_t buf = (uint32_t)(v & 1);
+            const int st = (int)(u % kJoinStages);
+            const bool first = (u & fm) == 0;
+            if (first) {
+                if (!wait(&acce[buf], (uint32_t)((v >> 1) & 1) ^ 1u)) { give_up(14); break; }
+                fence_after();
+            }
+            if (!wait(&fullA[st], (uint32_t)((u / kJoinStages) & 1))) { give_up(15); break; }
+            fence_after();
+            const uint32_t d = tmem + buf * S::kAccCols;
+            const uint32_t ta = tmem + S::kACol0 + (uint32_t)st * kJoinStageCols;
+            const uint32_t qb = smem_u32(qst + (size_t)st * S::kQStage);
+#pragma unroll
+            for (int ks = 0; ks < kJoinSub / 4; ks++) {
+                const uint64_t db = smem_desc(qb + (ks >> 1) * S::kQTile + (ks & 1) * 256);
+                mma_ts<true>(d, ta + ks * 8, db, g.idesc, (first && ks == 0) ? 0u : 1u);
+            }
+            mma_commit(&empty[st]);
+            if ((u & fm) == fm || u + 1 == U) mma_commit(&accf[buf]);
+        }
+        // the MMAs must have finished before the tensor memory is freed
+        mma_commit(drain);
+        mbar_wait(drain, 0);                // full limit: the MMAs must finish
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::kCols) : "memory");
+    }
+}
+
+// C from the K-range partials, summed in range order (deterministic).
+template <int NQ, bool SCALED>
+__global__ void tc_join_reduce_kernel(const TcJoinArgs g, const double2* partial, int* exps) {
+    const int64_t per = 32 * NQ, total = g.nbatch * per;
+    int emax = kExpUnset;
+    if (SCALED && blockIdx.x == 0 && threadIdx.x == 0)
+        exps[2 * g.expC] = exps[2 * g.expP] + exps[2 * g.expQ] + read_m(exps, g.expP) + read_m(exps, g.expQ);
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        double re = 0.0, im = 0.0;
+        for (int s = 0; s < g.nsplit; s++) {
+            const double2 v = partial[s * total + idx];
+            re += v.x;
+            im += v.y;
+        }
+        const int64_t b = idx / per, r = idx % per;
+        const float2 c = make_float2((float)re, (float)im);
+        g.C[join_c_offset(g, b, (int)(r / NQ), (int)(r % NQ))] = c;
+        const float mx = fmaxf(fabsf(c.x), fabsf(c.y));
+        if (SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
+    }
+    if (SCALED) {
+        for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if ((threadIdx.x & 31) == 0 && emax != kExpUnset) atomicMax(&exps[2 * g.expC + 1], emax);
+    }
+}
+
+int join_ilog2(int64_t x) {
+    int b = 0;
+    while ((int64_t(1) << b) < x) b++;
+    return b;
+}
+
+size_t join_smem_bytes(const TcJoinArgs& g) {
+    return (size_t)g.ring * g.slot_bytes + (size_t)kJoinStages * 2 * (2 * g.nq * kTcChunkBytes) + 128;
+}
+
+template <int NQ, bool SCALED>
+cudaError_t launch_join_shape(const TcJoinArgs& g, double2* partial, int* exps, cudaStream_t st) {
+    static bool attr = false;               // the kernel's dynamic shared memory limit, once
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(tc_join_kernel<NQ, SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)(kJoinSmemCap + 128));
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    tc_join_kernel<NQ, SCALED><<<(unsigned)(g.nbatch * g.nsplit), kJoinThreads, join_smem_bytes(g), st>>>(g, partial, exps);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || g.nsplit == 1) return e;
+    const int64_t total = g.nbatch * 32 * NQ;
+    const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
+    tc_join_reduce_kernel<NQ, SCALED><<<grid, 256, 0, st>>>(g, partial, exps);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Plan: every result bit in P or Q or both (batch), every summed bit in both; 32 free values on
+// the P side (the step's B when both sides have 32) and 8-32 on the Q side; at least 2^10 summed
+// terms.  The chunk's six summed bits are chosen one at a time for whichever operand's run of
+// contiguous tile bits (free bits and chosen summed bits from address bit 0 up) is shorter, so
+// both tiles are copied as segments of 2^sb >= 8 elements.
+bool tc_join_plan(const StepArgs& s, int sm_count, TcJoinArgs* out, int min_log2) {
+    if (s.nk < 10 || s.nk - 6 >= kJoinChunkBits) return false;
+    auto one = [](const BitMap& m, int bit) {
+        const int64_t o = pdep(int64_t(1) << bit, m);
+        return o ? __builtin_ctzll((unsigned long long)o) : -1;
+    };
+    const int ncb = join_ilog2(s.nC);
+    std::vector<int> gb, ab, bb;             // result bits: batch, A only, B only
+    for (int p = 0; p < ncb; p++) {
+        const bool ia = one(s.cA, p) >= 0, ib = one(s.cB, p) >= 0;
+        if (ia && ib) gb.push_back(p);
+        else if (ia) ab.push_back(p);
+        else if (ib) bb.push_back(p);
+        else return false;
+    }
+    for (int j = 0; j < s.nk; j++)
+        if (one(s.kA, j) < 0 || one(s.kB, j) < 0) return false;
+    const int na = (int)ab.size(), nb = (int)bb.size(), ng = (int)gb.size();
+    bool p_is_a;
+    if (nb == 5 && na >= 3 && na <= 5) p_is_a = false;
+    else if (na == 5 && nb >= 3 && nb <= 4) p_is_a = true;
+    else return false;
+    if (ng > 30) return false;
+    const int nqb = p_is_a ? nb : na;
+    if (ng + 5 + s.nk < min_log2 || ng + nqb + s.nk < min_log2) return false;
+    const BitMap& cP = p_is_a ? s.cA : s.cB;
+    const BitMap& cQ = p_is_a ? s.cB : s.cA;
+    const BitMap& kP = p_is_a ? s.kA : s.kB;
+    const BitMap& kQ = p_is_a ? s.kB : s.kA;
+    const std::vector<int>& fP = p_is_a ? ab : bb;
+    const std::vector<int>& fQ = p_is_a ? bb : ab;
+    std::vector<char> freeP(64, 0), freeQ(64, 0);
+    std::vector<int> kAtP(64, -1), kAtQ(64, -1), posP(s.nk), posQ(s.nk);
+    for (int b : fP) freeP[one(cP, b)] = 1;
+    for (int b : fQ) freeQ[one(cQ, b)] = 1;
+    for (int k = 0; k < s.nk; k++) {
+        posP[k] = one(kP, k);
+        posQ[k] = one(kQ, k);
+        kAtP[posP[k]] = k;
+        kAtQ[posQ[k]] = k;
+    }
+    std::vector<char> chosen(s.nk, 0);
+    auto run = [&](const std::vector<char>& fr, const std::vector<int>& kat) {
+        int r = 0;
+        while (r < 64 && (fr[r] || (kat[r] >= 0 && chosen[kat[r]]))) r++;
+        return r;
+    };
+    std::vector<int> ks;
+    for (int step = 0; step < 6; step++) {
+        const int rp = run(freeP, kAtP), rq = run(freeQ, kAtQ);
+        const int kp = rp < 64 ? kAtP[rp] : -1, kq = rq < 64 ? kAtQ[rq] : -1;
+        int pick = -1;
+        if (rp <= rq && kp >= 0) pick = kp;
+        else if (kq >= 0) pick = kq;
+        else if (kp >= 0) pick = kp;
+        else
+            for (int k = 0; k < s.nk; k++)
+                if (!chosen[k] && (pick < 0 || std::min(posP[k], posQ[k]) < std::min(posP[pick], posQ[pick]))) pick = k;
+        chosen[pick] = 1;
+        ks.push_back(pick);
+    }
+    std::sort(ks.begin(), ks.end(), [&](int x, int y) { return posP[x] < posP[y]; });
+    const int sbP = run(freeP, kAtP), sbQ = run(freeQ, kAtQ);
+    const int tbP = 5 + 6, tbQ = nqb + 6;     // tile bits
+    if (sbP < 3 || sbQ < 3 || tbP - sbP > 8 || tbQ - sbQ > 8) return false;
+    TcJoinArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nq = 1 << nqb;
+    a.p_is_a = p_is_a ? 1 : 0;
+    a.sbP = sbP;
+    a.sbQ = sbQ;
+    a.nsegP = 1 << (tbP - sbP);
+    a.nsegQ = 1 << (tbQ - sbQ);
+    a.segP_stride = (8 << sbP) + kJoinPadBytes;
+    a.segQ_stride = (8 << sbQ) + kJoinPadBytes;
+    a.slotP_bytes = (a.nsegP * a.segP_stride + 127) / 128 * 128;
+    a.slot_bytes = a.slotP_bytes + (a.nsegQ * a.segQ_stride + 127) / 128 * 128;
+    a.run_p = 1 << sbP;
+    a.run_q = 1 << sbQ;
+    for (int t = 0; t < 6; t++) a.chunk_k[t] = ks[t];
+    // tile element maps: the tile's bits in the operand's address order
+    auto tile_maps = [&](const BitMap& cm, const std::vector<int>& fr, const std::vector<int>& pos, BitMap* e,
+                         BitMap* ti, BitMap* tk) {
+        struct Bit { int pos, kind, idx; };
+        std::vector<Bit> bits;
+        for (int i = 0; i < (int)fr.size(); i++) bits.push_back({one(cm, fr[i]), 0, i});
+        for (int t = 0; t < 6; t++) bits.push_back({pos[ks[t]], 1, t});
+        std::sort(bits.begin(), bits.end(), [](const Bit& x, const Bit& y) { return x.pos < y.pos; });
+        std::vector<std::pair<int, int>> pe, pi, pk;
+        for (int t = 0; t < (int)bits.size(); t++) {
+            pe.push_back({t, bits[t].pos});
+            (bits[t].kind == 0 ? pi : pk).push_back({bits[t].idx, t});
+        }
+        std::sort(pi.begin(), pi.end());
+        std::sort(pk.begin(), pk.end());
+        return make_runs(pe, e) && make_runs(pi, ti) && make_runs(pk, tk);
+    };
+    if (!tile_maps(cP, fP, posP, &a.eP, &a.tPi, &a.tPk)) return false;
+    if (!tile_maps(cQ, fQ, posQ, &a.eQ, &a.tQj, &a.tQk)) return false;
+    std::vector<std::pair<int, int>> bP, bQ, bC, iC, jC, hP, hQ;
+    for (int i = 0; i < ng; i++) {
+        bP.push_back({i, one(cP, gb[i])});
+        bQ.push_back({i, one(cQ, gb[i])});
+        bC.push_back({i, gb[i]});
+    }
+    for (int i = 0; i < 5; i++) iC.push_back({i, fP[i]});
+    for (int j = 0; j < nqb; j++) jC.push_back({j, fQ[j]});
+    // the chunk index walks the other summed bits, lowest operand address first
+    std::vector<int> rest;
+    for (int k = 0; k < s.nk; k++)
+        if (!chosen[k]) rest.push_back(k);
+    std::sort(rest.begin(), rest.end(), [&](int x, int y) {
+        const int px = std::min(posP[x], posQ[x]), py = std::min(posP[y], posQ[y]);
+        return px != py ? px < py : x < y;
+    });
+    for (int t = 0; t < (int)rest.size(); t++) {
+        hP.push_back({t, posP[rest[t]]});
+        hQ.push_back({t, posQ[rest[t]]});
+    }
+    if (!make_runs(bP, &a.bP) || !make_runs(bQ, &a.bQ) || !make_runs(bC, &a.bC) || !make_runs(iC, &a.iC) ||
+        !make_runs(jC, &a.jC) || !make_runs(hP, &a.hP) || !make_runs(hQ, &a.hQ))
+        return false;
+    a.nbatch = int64_t(1) << ng;
+    const int64_t chunks = int64_t(1) << (s.nk - 6);
+    // K ranges: two CTAs' worth per SM at least, each range at least 16 chunks (1,024 terms)
+    int64_t nsplit = 1;
+    while (a.nbatch * nsplit < (int64_t)sm_count * 2 && chunks / (nsplit * 2) >= 16) nsplit *= 2;
+    if (a.nbatch * nsplit > (int64_t(1) << 31) - 1) return false;
+    a.nsplit = (int)nsplit;
+    a.nchunks = chunks / nsplit;
+    a.flush = kJoinFlushTerms / kJoinSub;
+    // ring: as many raw chunks (2..4) as fit beside the MMA stages
+    const size_t stages = (size_t)kJoinStages * 2 * (2 * a.nq * kTcChunkBytes);
+    a.ring = 0;
+    for (int r = kJoinMaxRing; r >= 2 && !a.ring; r--)
+        if ((size_t)r * a.slot_bytes + stages <= kJoinSmemCap) a.ring = r;
+    if (!a.ring) return false;
+    const uint32_t nmma = (uint32_t)(2 * a.nq);
+    a.idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((nmma >> 3) << 17) | ((uint32_t)(kTcTileM >> 4) << 24);
+    a.P = static_cast<const float2*>(p_is_a ? s.A : s.B);
+    a.Q = static_cast<const float2*>(p_is_a ? s.B : s.A);
+    a.C = static_cast<float2*>(s.C);
+    a.conjP = p_is_a ? s.conjA : s.conjB;
+    a.conjQ = p_is_a ? s.conjB : s.conjA;
+    a.expP = p_is_a ? s.expA : s.expB;
+    a.expQ = p_is_a ? s.expB : s.expA;
+    a.expC = s.expC;
+    *out = a;
+    return true;
+}
+
+size_t tc_join_partial_bytes(const TcJoinArgs& g) {
+    return g.nsplit > 1 ? (size_t)g.nsplit * (size_t)g.nbatch * 32 * g.nq * sizeof(double2) : 0;
+}
+
+cudaError_t tc_join_launch(const TcJoinArgs& g, int* exps, void* scratch, cudaStream_t st, int* launches) {
+    if (!g.err) return cudaErrorInvalidValue;
+    if (g.nsplit > 1 && !scratch) return cudaErrorInvalidValue;
+    // cp.async.bulk needs 16-byte aligned sources
+    if ((reinterpret_cast<uintptr_t>(g.P) & 15) != 0 || (reinterpret_cast<uintptr_t>(g.Q) & 15) != 0)
+        return cudaErrorInvalidValue;
+    double2* partial = static_cast<double2*>(scratch);
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (g.nq) {
+        case 8: e = exps ? launch_join_shape<8, true>(g, partial, exps, st) : launch_join_shape<8, false>(g, partial, exps, st); break;
+        case 16: e = exps ? launch_join_shape<16, true>(g, partial, exps, st) : launch_join_shape<16, false>(g, partial, exps, st); break;
+        case 32: e = exps ? launch_join_shape<32, true>(g, partial, exps, st) : launch_join_shape<32, false>(g, partial, exps, st); break;
+        default: break;
+    }
+    if (launches) *launches = g.nsplit > 1 ? 2 : 1;
+    return e;
+}
+
+std::string tc_join_describe(const TcJoinArgs& g) {
+    std::string d = "tensor-core join 3xTF32 P=" + std::string(g.p_is_a ? "A" : "B") + " nq=" + std::to_string(g.nq) +
+                    " batch=" + std::to_string(g.nbatch) + " ranges=" + std::to_string(g.nsplit) +
+                    " chunks=" + std::to_string(g.nchunks) + " ring=" + std::to_string(g.ring) + " chunk_k=";
+    for (int t = 0; t < 6; t++) d += (t ? "," : "") + std::string("k") + std::to_string(g.chunk_k[t]);
+    d += " runs=" + std::to_string(g.run_p) + "/" + std::to_string(g.run_q) + " segments=" + std::to_string(g.nsegP) +
+         "/" + std::to_string(g.nsegQ);
+    return d;
+}
+
+}  // namespace qxg

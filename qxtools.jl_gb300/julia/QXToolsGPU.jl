@@ -39,7 +39,8 @@ struct QxgOptions          # qxg_options
     tc_plane_budget_mb::Int32   # 0: 4096 MiB of packed planes before blocking the free columns
     tc_wait_limit::Int32    # 0: 2^20 polls before a tensor-core wait gives up
     tc_stall_test::Int32    # test hook, leave 0
-    reserved::NTuple{3,Int32}
+    tc_joins::Int32         # 1: final joins on the tensor-core join instead of the CUDA cores
+    reserved::NTuple{2,Int32}
 end
 
 mutable struct QxgProgram
@@ -97,7 +98,7 @@ function load_qx(qx_file::String, data::AbstractDict; precision::Symbol=:fp64, d
         length(x) == n || error("data key $(dkeys[i]) has $(length(x)) elements, its load line wants $n")
     end
     loads = [Int(I.a) + 1 for I in instrs if I.op == 1]   # QXG_OP_LOAD
-    opts = Ref(QxgOptions(PREC[precision], device, 0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 3)))
+    opts = Ref(QxgOptions(PREC[precision], device, 0, 0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 2)))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:qxg_program_create, libqxgpu), Cint,
                 (Ptr{QxgInstr}, Int32, Ptr{Int32}, Int64, Ptr{Int32}, Ptr{Int64}, Int32, Int32,

@@ -211,3 +211,57 @@ def test_batched_join_gemm(q, gpu_lib, precision, nk, na, nb, ng):
     err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
     assert err <= 1e-6, err
     assert np.array_equal(got, got2)
+
+
+def join_programme(q, nk, na, nb, ng, seed, batch_on_top=True):
+    """One ncon of the final-join shape; the batch labels last in both operands (the highest
+    address bits, as the programme's layout rule places them in intermediates), the others in a
+    seeded random order.  Returns the programme and the einsum result."""
+    rng = np.random.default_rng(seed)
+    kl = list(range(1, nk + 1))
+    al, bl, gl = list(range(100, 100 + na)), list(range(200, 200 + nb)), list(range(300, 300 + ng))
+    if batch_on_top:
+        la = [int(v) for v in rng.permutation(al + kl)] + [int(v) for v in rng.permutation(gl)]
+        lb = [int(v) for v in rng.permutation(bl + kl)] + [int(v) for v in rng.permutation(gl)]
+    else:
+        la = [int(v) for v in rng.permutation(al + gl + kl)]
+        lb = [int(v) for v in rng.permutation(bl + gl + kl)]
+    lc = [int(v) for v in rng.permutation(al + bl + gl)]
+    A = rng.standard_normal((2,) * len(la)) + 1j * rng.standard_normal((2,) * len(la))
+    B = rng.standard_normal((2,) * len(lb)) + 1j * rng.standard_normal((2,) * len(lb))
+    cmds = [q.Load("a", "data_1", A.shape), q.Load("b", "data_2", B.shape),
+            q.Ncon("c", tuple(lc), "a", tuple(la), "b", tuple(lb)), q.Save("output", "c")]
+    prog = q.Programme.from_commands(cmds, OrderedDict([("data_1", A), ("data_2", B)]), 0)
+    letters = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
+    idx = {v: letters[i] for i, v in enumerate(sorted(set(la + lb)))}
+    sub = lambda ls: "".join(idx[v] for v in ls)
+    ref = np.einsum(f"{sub(la)},{sub(lb)}->{sub(lc)}", A, B).reshape(-1, order="F")
+    return prog, ref
+
+
+# (summed bits, free bits of A, free bits of B, batch bits): P = the side with 32 free values (B
+# when both have), Q with 8, 16 or 32; one batch value cuts K into ranges (FP64 partials)
+JOIN_CASES = [(12, 5, 5, 3), (15, 5, 5, 0), (15, 5, 3, 2), (12, 4, 5, 4), (15, 5, 4, 1)]
+
+
+@pytest.mark.parametrize("nk,na,nb,ng", JOIN_CASES)
+def test_tensor_core_join(q, gpu_lib, nk, na, nb, ng):
+    """The tensor-core join (3xTF32, operands split on the fly, FP64 drains every 512 terms):
+    within the split-TF32 tolerance of einsum, equal to the CUDA-core batched GEMM within it, and
+    the same bits on a second call."""
+    prog, ref = join_programme(q, nk, na, nb, ng, seed=nk * 1000 + na * 100 + nb * 10 + ng)
+    with q.Executor(prog, precision="split_tf32", tc_joins=True) as ex:
+        got = ex.amplitudes([""])[0]
+        got2 = ex.amplitudes([""])[0]
+        desc = ex.explain(2)
+        assert "tensor-core join" in desc, desc
+        assert ex.info()["num_steps_tensor_core"] == 1
+    with q.Executor(prog, precision="split_tf32") as ex:
+        cc = ex.amplitudes([""])[0]
+        assert "batched-gemm" in ex.explain(2)
+    scale = np.max(np.abs(ref))
+    err = np.max(np.abs(got - ref)) / scale
+    print(f"tensor-core join {nk},{na},{nb},{ng}: {err:.2e} of the largest result; {desc.split('join ')[1][:90]}")
+    assert err <= TOL["split_tf32"], err
+    assert np.max(np.abs(got - cc)) / scale <= TOL["split_tf32"]
+    assert np.array_equal(got, got2)

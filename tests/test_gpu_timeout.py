@@ -1,8 +1,9 @@
 """The tensor-core kernels' bounded waits: a wait that runs out ends the call with QXG_ERR_TIMEOUT
 and leaves the GPU usable.
 
-The test hook qxg_options.tc_stall_test makes the first CTA of every tensor-core GEMM issue no
-operand copies, so its MMA issuer waits on a barrier that nothing completes; with a short poll
+The test hook qxg_options.tc_stall_test makes the first CTA of every tensor-core GEMM (and of
+every tensor-core join) issue no operand copies, so its MMA issuer (the join's splitters) waits on
+a barrier that nothing completes; with a short poll
 limit (qxg_options.tc_wait_limit) the wait gives up, the CTA's other warps give up or see the
 abort, and the kernel frees its tensor memory and returns.  No copy is left in flight (the
 stalled producer issued none; the waits for copies in flight keep the full limit), no fault or
@@ -56,5 +57,23 @@ def test_short_wait_limit_alone_does_not_fail_good_calls(q, gpu_lib):
     stall still returns the right result (its waits complete long before the limit)."""
     prog, ref = _tc_programme(q, seed=4)
     with q.Executor(prog, precision="split_tf32", tc_tuning=1, tc_wait_limit=1 << 18) as ex:
+        got = ex.amplitudes([""])[0]
+    assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) <= 5e-6
+
+
+def test_expired_join_wait_reports_timeout_and_gpu_stays_usable(q, gpu_lib):
+    """The tensor-core join's waits: with the stall hook its first CTA's loader issues nothing, the
+    splitters' waits give up, the MMA issuer and the drain warps give up in turn; the call returns
+    QXG_ERR_TIMEOUT twice, and a fresh programme returns the right result."""
+    from test_gpu_split import join_programme
+    prog, ref = join_programme(q, 12, 5, 5, 3, seed=77)
+    with q.Executor(prog, precision="split_tf32", tc_joins=True, tc_wait_limit=1 << 14,
+                    tc_stall_test=True) as ex:
+        for _ in range(2):
+            with pytest.raises(q.QXGError) as e:
+                ex.amplitudes([""])
+            assert e.value.code == -5, str(e.value)
+        assert "tensor-core join" in ex.explain(2)
+    with q.Executor(prog, precision="split_tf32", tc_joins=True) as ex:
         got = ex.amplitudes([""])[0]
     assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) <= 5e-6

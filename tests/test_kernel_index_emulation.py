@@ -48,3 +48,32 @@ def test_row_form_and_long_sum_index_work(tmp_path):
     r = subprocess.run([str(exe), "7", "300", "60"], capture_output=True, text=True, env=env, timeout=800)
     assert r.returncode == 0, (r.stdout[-3000:], r.stderr[-3000:])
     assert "failed" in r.stdout
+
+
+JOIN_SRC = ROOT / "tests" / "emu" / "tc_join_emu.cu"
+
+
+@pytest.mark.timeout(600)
+def test_tensor_core_join_index_work(tmp_path):
+    """The tensor-core join (tc_join.cu): its planner on seeded random layouts (batch bits on top or
+    anywhere, P = A or B, 8-32 free values of Q, K ranges), then per block the delta walk of the
+    chunk bases, the segment copies into a slot of the planned size (each byte once, 16-byte
+    aligned) and the splitters' slot reads, summed in FP64 against the direct contraction."""
+    nvcc = _nvcc()
+    if nvcc is None:
+        pytest.skip("nvcc not found")
+    obj, exe = tmp_path / "join.o", tmp_path / "join"
+    cmd = [nvcc, "-std=c++17", "-O1", "-gencode", "arch=compute_103a,code=sm_103a", "--expt-relaxed-constexpr",
+           "-I", str(ROOT / "include"), "-Xcompiler=-fsanitize=address,-fno-omit-frame-pointer", "-c",
+           str(JOIN_SRC), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    cuda_lib = Path(nvcc).resolve().parent.parent / "lib64"
+    r = subprocess.run(["g++", str(obj), "-o", str(exe), "-fsanitize=address", f"-L{cuda_lib}", "-lcudart"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
+    env["LD_LIBRARY_PATH"] = f"{cuda_lib}:{env.get('LD_LIBRARY_PATH', '')}"
+    r = subprocess.run([str(exe), "5", "80"], capture_output=True, text=True, env=env, timeout=500)
+    assert r.returncode == 0, (r.stdout[-3000:], r.stderr[-3000:])
+    assert "0 failed" in r.stdout
