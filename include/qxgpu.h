@@ -94,10 +94,9 @@ typedef struct qxg_options {
     int32_t tc_stall_test;        /* test hook, leave 0: nonzero makes the first CTA of every
                                      tensor-core GEMM issue no operand copies, so its waits run out and
                                      the call returns QXG_ERR_TIMEOUT (exercises the timeout path) */
-    int32_t tc_joins;             /* 1: the final joins of split-TF32 programmes (32 x 8..32 results
-                                     per batch value, long sums) run on the tensor-core join (3xTF32,
-                                     operands split in the kernel); 0 = the CUDA cores' batched small
-                                     GEMM (default: it runs the benchmark's 32 x 32 joins as fast) */
+    int32_t cuda_core_joins;      /* 1: keep the final joins of split-TF32 programmes (32 x 8..32
+                                     results per batch value, long sums) on the CUDA cores' batched
+                                     small GEMM; 0 = the tensor-core join (default) */
     int32_t reserved[2];
 } qxg_options;
 

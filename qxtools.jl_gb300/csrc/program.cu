@@ -474,10 +474,10 @@ std::vector<int64_t> leaf_offsets(const qxg_program* P, int64_t* total) {
 // gradient.  Adjoint tensors are table entries ntensors + t with the forward tensor's layout.
 // tc_tuning = k >= 1: candidate k-1 of every tensor-core step (the last one where a step has
 // fewer), chosen at plan time; 0 leaves the choice to the autotuner.
-// The final joins of a split-TF32 programme go to the tensor-core join when the options ask for
-// it and the step fits it.
+// The final joins of a split-TF32 programme go to the tensor-core join when they fit it (and the
+// options do not keep them on the CUDA cores).
 bool join_eligible(const qxg_program* P, Step& st) {
-    if (P->fp64 || P->opts.precision != QXG_PREC_SPLIT_TF32 || !P->opts.tc_joins) return false;
+    if (P->fp64 || P->opts.precision != QXG_PREC_SPLIT_TF32 || P->opts.cuda_core_joins) return false;
     return tc_join_plan(st.sargs, P->sm_count, &st.join);
 }
 

@@ -291,7 +291,9 @@ __global__ void __launch_bounds__(threads_of(MODE), MODE == kModeTma ? 1 : 2)
     __shared__ int32_t ktab[SEGS ? KC : 1];      // bulk / TMA: slot bytes of k index j
     __shared__ uint32_t tmem_holder;
     __shared__ int abort_flag;
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    // aligned by pointer arithmetic on the shared array (not through an integer), so the compiler
+    // keeps the shared address space: shared loads and stores, not generic ones
+    uint8_t* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
     const int NS = g.stages;
     const uint32_t a_stage = A_TMEM ? 0u : 2u * kATileBytes;    // A tiles' bytes in a stage
     const uint32_t stage_bytes = a_stage + 2u * g.b_tile_bytes;
@@ -1104,23 +1106,6 @@ cudaError_t tc_run_pack(const TcStep& t, const StepArgs& s, int* exps, void* scr
 // extent 1 up to rank 5.  Every block's base offset is a multiple of 2^tma_lead (its lower
 // address bits all belong to the block), so the copy of a block is the box at coordinate
 // base >> tma_lead of that dimension.  False when the driver rejects the map.
-// cuTensorMapEncodeTiled is a driver function: look it up through the runtime, so the library
-// does not link the driver (and loads on machines without one).
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn encode_tiled() {
-    static EncodeTiledFn fn = [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            return static_cast<EncodeTiledFn>(nullptr);
-        return reinterpret_cast<EncodeTiledFn>(p);
-    }();
-    return fn;
-}
-
 bool make_x_map(const TcStep& t, const void* X, CUtensorMap* map, GemmArgs* g) {
     const EncodeTiledFn encode = encode_tiled();
     if (!encode) return false;

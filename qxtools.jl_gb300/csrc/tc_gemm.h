@@ -119,6 +119,16 @@ namespace qxg {
 constexpr int kJoinKR = 64;         // summed terms per raw chunk (its 6 summed bits are planned)
 constexpr int kJoinMaxSeg = 256;    // contiguous segments per operand in a raw chunk
 
+// One operand's raw tile as a TMA tensor box: dimension 0 is contiguous with extent 2^H (H the
+// operand's lowest batch bit), so its coordinate carries the chunk's offset; the tile's other
+// runs of address bits follow (coordinate 0, box = extent); the batch bits are dimension tb (box 1,
+// coordinate = batch index).  The box lands in shared memory in the tile's address order.
+struct JoinBox {
+    int32_t td, tb;                 // dimensions used (<= 5); the batch dimension (-1: none)
+    int64_t dim[5], stride[5];      // extents and strides, in elements (stride[0] = 1)
+    int32_t box[5];
+};
+
 struct TcJoinArgs {
     const float2* P;
     const float2* Q;
@@ -148,6 +158,9 @@ struct TcJoinArgs {
     int* err;                       // word a wait that gives up writes its code to
     int32_t chunk_k[6];             // the chunk's summed bits (step k indices), for describe
     int32_t run_p, run_q;           // contiguous elements per segment (2^sbP, 2^sbQ)
+    int32_t tma;                    // 1: one TMA tensor copy per operand and chunk (boxP, boxQ);
+                                    // 0: the segments by cp.async.bulk
+    JoinBox boxP, boxQ;
 };
 
 // Plan a step as a tensor-core join (false: it does not fit); operands of at least 2^min_log2

@@ -14,15 +14,17 @@
 // so Re C[i, j] = sum over h of D[(0, i), (h, j)] + D[(2, i), (h, j)] and Im C from roles 1 and
 // 3: the four hi/lo products of each complex product (lo*lo included) come from one M = 128,
 // N = 2 NQ, K = 8 MMA per 8 summed terms, each in its own accumulator entry.  (hi, lo): tf32
-// round-to-nearest of x and of x - hi.  The row of role r for free value i sits at tensor-memory
-// lane 32 q + 8 r + (i mod 8) with q = i / 8, so the warp that owns lanes 32 q .. 32 q + 31 holds
-// all four roles of eight free values.
+// round-to-nearest (ties away) of x and of x - hi.  The row of role r for free value i sits at
+// tensor-memory lane 32 q + 8 r + (i mod 8) with q = i / 8, so the warp that owns lanes
+// 32 q .. 32 q + 31 holds all four roles of eight free values.
 //
 // One CTA (12 warps) per (batch value, K range):
 //   warp 1         loader: per raw chunk of 64 summed terms, the chunk's P tile (32 x 64) and Q
-//                  tile (NQ x 64), each a few contiguous segments of the operand, are copied with
-//                  cp.async.bulk into a ring slot (an mbarrier counts the bytes).  The chunk's six
-//                  summed bits are planned so both tiles are runs of >= 8 elements;
+//                  tile (NQ x 64) land in a ring slot in each operand's address order: one TMA
+//                  tensor copy per operand (the tile's runs of address bits as box dimensions),
+//                  or, where the layout does not fit a box, its contiguous segments by
+//                  cp.async.bulk.  The chunk's six summed bits are planned so both tiles are runs
+//                  of >= 8 elements;
 //   warps 4-11     P splitters, two groups on alternate MMA stages (16 summed terms each): warp
 //                  4 + 4 g + q reads the stage's terms for its eight free values from the slot,
 //                  splits them into the four roles and stores 32 columns of its lanes with
@@ -32,8 +34,11 @@
 //                  before the stage that reuses it, so the FP32 sums never run over more than 512
 //                  terms, and at the end combines the four roles with shuffles and writes C (or
 //                  its FP64 partial, added in K-range order by tc_join_reduce_kernel);
-//   warps 2-3      Q splitters: rows j and NQ + j of the stage's two B tiles (K-major core
-//                  matrices, 64-byte rows: real parts in core columns 0-1, imaginary in 2-3);
+//   warps 2-3      Q splitters: a whole raw chunk at a time, each thread reading elements in the
+//                  slot's order (consecutive threads, consecutive elements) and storing their
+//                  four split words into the chunk's eight B tiles (K-major core matrices, 64-byte
+//                  rows: real parts in core columns 0-1, imaginary in 2-3; the tiles 16 bytes
+//                  apart in bank position), two chunks of B stages in flight;
 //   warp 0 lane 0  MMA issuer: four tcgen05.mma (kind::tf32, A from tensor memory) per stage.
 // Waiting warps sleep in their barrier polls (a suspend-time hint), so they leave the issue slots
 // to the splitters.
@@ -52,7 +57,8 @@ namespace {
 
 constexpr int kJoinSub = 16;                        // summed terms per MMA stage
 constexpr int kJoinSubs = kJoinKR / kJoinSub;       // MMA stages per raw chunk (4)
-constexpr int kJoinStages = 4;                      // MMA stages in flight
+constexpr int kJoinStages = 4;                      // A stages in tensor memory
+constexpr int kJoinQBufs = 2 * kJoinSubs;           // B stages in shared memory (two raw chunks)
 constexpr int kJoinMaxRing = 4;                     // raw chunks in the ring
 constexpr int kJoinPGroups = 2;                     // P splitter groups (alternate stages)
 constexpr int kJoinThreads = 32 * (4 + 4 * kJoinPGroups);
@@ -61,7 +67,7 @@ constexpr int kJoinStageCols = 2 * kJoinSub;        // tensor-memory columns of 
 constexpr int kJoinFlushTerms = 512;                // summed terms per FP32 accumulator
 constexpr int kJoinChunkBits = 48;                  // delta-table entries (chunk index bits)
 constexpr size_t kJoinSmemCap = 200 * 1024;         // ring + B stages (one CTA per SM)
-constexpr int kJoinPadBytes = 16;                   // padding after each segment of a slot
+constexpr int kJoinPadBytes = 16;                   // padding after each bulk segment and each B tile
 
 // Byte of tile element e inside a slot: segment e >> sb, element e mod 2^sb.
 __host__ __device__ __forceinline__ int join_slot_byte(int64_t e, int sb, int stride) {
@@ -93,11 +99,28 @@ __host__ __device__ __forceinline__ int join_prow(const TcJoinArgs& g, int i) {
 __host__ __device__ __forceinline__ int join_pcol(const TcJoinArgs& g, int kl) {
     return join_slot_byte(pdep(kl, g.tPk), g.sbP, g.segP_stride);
 }
-__host__ __device__ __forceinline__ int join_qrow(const TcJoinArgs& g, int j) {
-    return g.slotP_bytes + join_slot_byte(pdep(j, g.tQj), g.sbQ, g.segQ_stride);
+// Inverse of pdep: the index bits that the map deposits at x's bits.
+__host__ __device__ __forceinline__ int64_t join_pext(int64_t x, const BitMap& m) {
+    int64_t o = 0;
+    for (int i = 0; i < m.n; i++) {
+        const Run r = m.r[i];
+        o |= ((x >> r.dst) & ((int64_t(1) << r.len) - 1)) << r.src;
+    }
+    return o;
 }
-__host__ __device__ __forceinline__ int join_qcol(const TcJoinArgs& g, int kl) {
-    return join_slot_byte(pdep(kl, g.tQk), g.sbQ, g.segQ_stride);
+// B tiles: 2 NQ rows of 64 bytes (one 8-term group), 16 bytes of padding after each.
+__host__ __device__ __forceinline__ int join_qtile_bytes(int nq) { return 2 * nq * kTcChunkBytes + kJoinPadBytes; }
+// Q's tile element e (in Q's address order): its slot byte (from the start of Q's part), and the
+// byte of its hi real word in the chunk's eight B tiles -- tile 2 (kl / 16) + (kl / 8 mod 2),
+// row j, core column (kl mod 8) / 4, word kl mod 4 (the imaginary word is 256 bytes further, the
+// lo row NQ + j is NQ / 8 row groups further).  Both add over disjoint bits of e.
+__host__ __device__ __forceinline__ int join_qsrc(const TcJoinArgs& g, int64_t e) {
+    return join_slot_byte(e, g.sbQ, g.segQ_stride);
+}
+__host__ __device__ __forceinline__ int join_qdst(const TcJoinArgs& g, int64_t e) {
+    const int j = (int)join_pext(e, g.tQj), kl = (int)join_pext(e, g.tQk);
+    const int t = kl & 7;
+    return (kl >> 3) * join_qtile_bytes(g.nq) + (j >> 3) * 512 + (t >> 2) * 128 + (j & 7) * 16 + (t & 3) * 4;
 }
 __host__ __device__ __forceinline__ int64_t join_c_offset(const TcJoinArgs& g, int64_t bi, int i, int j) {
     return pdep(bi, g.bC) + pdep(i, g.iC) + pdep(j, g.jC);
@@ -105,8 +128,9 @@ __host__ __device__ __forceinline__ int64_t join_c_offset(const TcJoinArgs& g, i
 
 template <int NQ>
 struct JoinShape {
-    static constexpr int kQTile = 2 * NQ * kTcChunkBytes;      // B tile of 8 summed terms
+    static constexpr int kQTile = 2 * NQ * kTcChunkBytes + kJoinPadBytes;   // B tile of 8 summed terms
     static constexpr int kQStage = 2 * kQTile;                 // B operand of one MMA stage
+    static constexpr int kQLo = (NQ / 8) * 512;                // lo rows NQ + j: NQ / 8 row groups on
     static constexpr uint32_t kAccCols = 2 * NQ;               // columns of one accumulator
     static constexpr uint32_t kACol0 = 2 * kAccCols;           // first A stage column
     static constexpr uint32_t kNeed = kACol0 + kJoinStages * kJoinStageCols;
@@ -116,24 +140,35 @@ struct JoinShape {
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
+// tf32 round to nearest, ties away from zero, on the binary32 bit pattern (finite x): add half a
+// unit in the last place of the 10-bit mantissa (bit 12) and clear the 13 bits below it -- two
+// integer operations.
+__device__ __forceinline__ uint32_t tf32_bits(float x) { return (__float_as_uint(x) + 0x1000u) & 0xffffe000u; }
 
 template <int NQ, bool SCALED>
-__global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinArgs g, double2* partial, int* exps) {
+__global__ void __launch_bounds__(kJoinThreads, 1)
+    tc_join_kernel(const TcJoinArgs g, double2* partial, int* exps, const __grid_constant__ CUtensorMap mapP,
+                   const __grid_constant__ CUtensorMap mapQ) {
     using S = JoinShape<NQ>;
     extern __shared__ uint8_t join_smem_raw[];
-    // rfull / rempty per ring slot, fullA / empty per MMA stage, accf / acce per accumulator, drain
-    __shared__ uint64_t bars[2 * kJoinMaxRing + 2 * kJoinStages + 5];
-    __shared__ int32_t prow[32], pcol[kJoinKR], qrow[NQ], qcol[kJoinKR];
+    // rfull / rempty per ring slot, fullA / empty per A stage, qfull / qempty per B stage, accf /
+    // acce per accumulator, drain
+    __shared__ uint64_t bars[2 * kJoinMaxRing + 2 * kJoinStages + 2 * kJoinQBufs + 5];
+    __shared__ int32_t prow[32], pcol[kJoinKR], qsrc_hi[NQ], qdst_hi[NQ];
     __shared__ int64_t psegoff[kJoinMaxSeg], qsegoff[kJoinMaxSeg];
     __shared__ int64_t dP[kJoinChunkBits], dQ[kJoinChunkBits];
     __shared__ uint32_t tmem_holder;
     __shared__ int abort_flag;
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(join_smem_raw) + 127) & ~uintptr_t(127));
+    // aligned by pointer arithmetic on the shared array (not through an integer), so the compiler
+    // keeps the shared address space: shared loads and stores, not generic ones
+    uint8_t* smem = join_smem_raw + ((128u - (smem_u32(join_smem_raw) & 127u)) & 127u);
     uint64_t* rfull = bars;
     uint64_t* rempty = bars + kJoinMaxRing;
     uint64_t* fullA = bars + 2 * kJoinMaxRing;
     uint64_t* empty = fullA + kJoinStages;
-    uint64_t* accf = empty + kJoinStages;
+    uint64_t* qfull = empty + kJoinStages;
+    uint64_t* qempty = qfull + kJoinQBufs;
+    uint64_t* accf = qempty + kJoinQBufs;
     uint64_t* acce = accf + 2;
     uint64_t* drain = acce + 2;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -153,7 +188,8 @@ __global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinAr
 
     if (threadIdx.x == 0) {
         for (int r = 0; r < kJoinMaxRing; r++) { mbar_init(&rfull[r], 1u); mbar_init(&rempty[r], 2u + 4u * kJoinPGroups); }
-        for (int s = 0; s < kJoinStages; s++) { mbar_init(&fullA[s], 6u); mbar_init(&empty[s], 1u); }
+        for (int s = 0; s < kJoinStages; s++) { mbar_init(&fullA[s], 4u); mbar_init(&empty[s], 1u); }
+        for (int s = 0; s < kJoinQBufs; s++) { mbar_init(&qfull[s], 2u); mbar_init(&qempty[s], 1u); }
         for (int j = 0; j < 2; j++) { mbar_init(&accf[j], 1u); mbar_init(&acce[j], 4u); }
         mbar_init(drain, 1u);
         abort_flag = 0;
@@ -167,12 +203,12 @@ __global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinAr
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (!bad) {
-        for (int t = threadIdx.x; t < kJoinKR; t += kJoinThreads) {
-            pcol[t] = join_pcol(g, t);
-            qcol[t] = join_qcol(g, t);
-        }
+        for (int t = threadIdx.x; t < kJoinKR; t += kJoinThreads) pcol[t] = join_pcol(g, t);
         for (int t = threadIdx.x; t < 32; t += kJoinThreads) prow[t] = join_prow(g, t);
-        for (int t = threadIdx.x; t < NQ; t += kJoinThreads) qrow[t] = join_qrow(g, t);
+        for (int t = threadIdx.x; t < NQ; t += kJoinThreads) {
+            qsrc_hi[t] = join_qsrc(g, (int64_t)t * 64);
+            qdst_hi[t] = join_qdst(g, (int64_t)t * 64);
+        }
         for (int t = threadIdx.x; t < g.nsegP; t += kJoinThreads) psegoff[t] = join_seg_p(g, t);
         for (int t = threadIdx.x; t < g.nsegQ; t += kJoinThreads) qsegoff[t] = join_seg_q(g, t);
         for (int t = threadIdx.x; t < kJoinChunkBits; t += kJoinThreads) {
@@ -192,7 +228,10 @@ __global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinAr
         // loader: chunk c into slot c mod R once the splitters have released it
         const bool stall = g.stall != 0 && blockIdx.x == 0;   // test hook: its waits run out
         const int64_t c0 = si * nchunks;
-        int64_t baseP = join_base_p(g, bi, si, 0), baseQ = join_base_q(g, bi, si, 0);
+        // the chunk's offset below the batch bits (a TMA box's dimension-0 coordinate) and the
+        // batch value's offset
+        const int64_t bP0 = pdep(bi, g.bP), bQ0 = pdep(bi, g.bQ);
+        int64_t chP = join_base_p(g, bi, si, 0) - bP0, chQ = join_base_q(g, bi, si, 0) - bQ0;
         const uint32_t segP = 8u << g.sbP, segQ = 8u << g.sbQ;
         const uint32_t tx = (uint32_t)g.nsegP * segP + (uint32_t)g.nsegQ * segQ;
         int slot = 0;
@@ -208,15 +247,27 @@ __global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinAr
             uint8_t* dst = ring + (size_t)slot * g.slot_bytes;
             if (lane == 0) mbar_expect_tx(&rfull[slot], tx);
             __syncwarp();
-            for (int sg = lane; sg < g.nsegP; sg += 32)
-                bulk_copy(dst + sg * g.segP_stride, g.P + baseP + psegoff[sg], segP, &rfull[slot]);
-            for (int sg = lane; sg < g.nsegQ; sg += 32)
-                bulk_copy(dst + g.slotP_bytes + sg * g.segQ_stride, g.Q + baseQ + qsegoff[sg], segQ, &rfull[slot]);
+            if (g.tma) {
+                if (lane == 0) {
+                    int co[5] = {(int)chP, 0, 0, 0, 0};
+                    if (g.boxP.tb >= 0) co[g.boxP.tb] = (int)bi;
+                    tma_load_5d(dst, &mapP, co, &rfull[slot]);
+                    int cq[5] = {(int)chQ, 0, 0, 0, 0};
+                    if (g.boxQ.tb >= 0) cq[g.boxQ.tb] = (int)bi;
+                    tma_load_5d(dst + g.slotP_bytes, &mapQ, cq, &rfull[slot]);
+                }
+            } else {
+                for (int sg = lane; sg < g.nsegP; sg += 32)
+                    bulk_copy(dst + sg * g.segP_stride, g.P + bP0 + chP + psegoff[sg], segP, &rfull[slot]);
+                for (int sg = lane; sg < g.nsegQ; sg += 32)
+                    bulk_copy(dst + g.slotP_bytes + sg * g.segQ_stride, g.Q + bQ0 + chQ + qsegoff[sg], segQ,
+                              &rfull[slot]);
+            }
             issued++;
             const int t = __ffsll((unsigned long long)(c0 + c + 1)) - 1;
             if (c + 1 < nchunks) {
-                baseP += dP[t];
-                baseQ += dQ[t];
+                chP += dP[t];
+                chQ += dQ[t];
             }
             if (++slot == R) { slot = 0; ph ^= 1u; }
         }
@@ -225,52 +276,56 @@ __global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinAr
             for (int64_t q = issued - 1; q >= 0 && q >= issued - R; q--)
                 mbar_wait(&rfull[q % R], (uint32_t)((q / R) & 1));     // full limit: copies must land
     } else if (warp == 2 || warp == 3) {
-        // Q splitters: task (j, 8-term group) per thread, every stage
+        // Q splitters: a raw chunk at a time; thread tq takes the chunk's elements tq + 64 m (in
+        // the slot's order) and stores their split words into the chunk's B stages 4 (c mod 2) ..
         const int tq = (warp - 2) * 32 + lane;
-        const bool live = tq < 2 * NQ;
-        const int jq = tq % NQ, gq = (tq / NQ) & 1;
         float s = 1.f;
         if (SCALED) s = pow2f(-read_m(exps, g.expQ));
         const float si_ = g.conjQ ? -s : s;
-        const int rb = live ? qrow[jq] : 0;
-        int qc[8];                          // slot bytes of the task's terms within a stage
-#pragma unroll
-        for (int t = 0; t < 8; t++) qc[t] = qcol[gq * 8 + t];
-        for (int64_t u = 0; u < U; u++) {
-            const int64_t c = u / kJoinSubs;
-            const int sub = (int)(u % kJoinSubs), slot = (int)(c % R), st = (int)(u % kJoinStages);
-            bool ok = sub != 0 || wait(&rfull[slot], (uint32_t)((c / R) & 1));
-            ok = ok && wait(&empty[st], (uint32_t)((u / kJoinStages) & 1) ^ 1u);
+        const int src0 = g.slotP_bytes + join_qsrc(g, tq), dst0 = join_qdst(g, tq);
+        for (int64_t c = 0; c < nchunks; c++) {
+            const int slot = (int)(c % R);
+            bool ok = wait(&rfull[slot], (uint32_t)((c / R) & 1));
+            // the chunk's B stages are free once the MMAs of the stages two chunks back are done
+            for (int sb = 0; sb < kJoinSubs && ok; sb++) {
+                const int64_t u = c * kJoinSubs + sb;
+                ok = wait(&qempty[u % kJoinQBufs], (uint32_t)((u / kJoinQBufs) & 1) ^ 1u);
+            }
             if (!__all_sync(0xffffffffu, ok)) {
                 if (lane == 0) give_up(12);
                 break;
             }
             if (aborted()) break;
-            if (live) {
-                const uint8_t* raw = ring + (size_t)slot * g.slot_bytes + rb + qcol[sub * kJoinSub];
-                uint32_t hr[8], lr[8], hm[8], lm[8];
+            const uint8_t* raw = ring + (size_t)slot * g.slot_bytes + src0;
+            uint8_t* qb = qst + (size_t)(c & 1) * (2 * kJoinSubs) * S::kQTile + dst0;
+            // eight elements' loads before their stores (the stores could alias later loads)
+            constexpr int kQB = NQ < 8 ? NQ : 8;
+#pragma unroll 1
+            for (int m0 = 0; m0 < NQ; m0 += kQB) {
+                float2 v[kQB];
+                int dd[kQB];
 #pragma unroll
-                for (int t = 0; t < 8; t++) {
-                    const float2 v = *reinterpret_cast<const float2*>(raw + qc[t]);
-                    Split<true>::go(v.x * s, hr[t], lr[t]);
-                    Split<true>::go(v.y * si_, hm[t], lm[t]);
+                for (int r = 0; r < kQB; r++) {
+                    v[r] = *reinterpret_cast<const float2*>(raw + qsrc_hi[m0 + r]);
+                    dd[r] = qdst_hi[m0 + r];
                 }
-                uint8_t* tile = qst + (size_t)st * S::kQStage + gq * S::kQTile;
-                st16(tile + core_off(jq, 0), *reinterpret_cast<const uint32_t(*)[4]>(hr));
-                st16(tile + core_off(jq, 1), *reinterpret_cast<const uint32_t(*)[4]>(hr + 4));
-                st16(tile + core_off(jq, 2), *reinterpret_cast<const uint32_t(*)[4]>(hm));
-                st16(tile + core_off(jq, 3), *reinterpret_cast<const uint32_t(*)[4]>(hm + 4));
-                st16(tile + core_off(NQ + jq, 0), *reinterpret_cast<const uint32_t(*)[4]>(lr));
-                st16(tile + core_off(NQ + jq, 1), *reinterpret_cast<const uint32_t(*)[4]>(lr + 4));
-                st16(tile + core_off(NQ + jq, 2), *reinterpret_cast<const uint32_t(*)[4]>(lm));
-                st16(tile + core_off(NQ + jq, 3), *reinterpret_cast<const uint32_t(*)[4]>(lm + 4));
+#pragma unroll
+                for (int r = 0; r < kQB; r++) {
+                    const float re = v[r].x * s, im = v[r].y * si_;
+                    const uint32_t hr = tf32_bits(re), hm = tf32_bits(im);
+                    const uint32_t lr = tf32_bits(re - __uint_as_float(hr)), lm = tf32_bits(im - __uint_as_float(hm));
+                    uint8_t* d = qb + dd[r];
+                    *reinterpret_cast<uint32_t*>(d) = hr;
+                    *reinterpret_cast<uint32_t*>(d + 256) = hm;
+                    *reinterpret_cast<uint32_t*>(d + S::kQLo) = lr;
+                    *reinterpret_cast<uint32_t*>(d + S::kQLo + 256) = lm;
+                }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
-            if (lane == 0) mbar_arrive(&fullA[st]);
-            if (sub == kJoinSubs - 1) {
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&rempty[slot]);
+            if (lane == 0) {
+                for (int sb = 0; sb < kJoinSubs; sb++) mbar_arrive(&qfull[(c * kJoinSubs + sb) % kJoinQBufs]);
+                mbar_arrive(&rempty[slot]);
             }
         }
     } else if (warp >= 4 && warp < 4 + 4 * kJoinPGroups) {
@@ -352,8 +407,8 @@ __global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinAr
             for (int t = 0; t < kJoinSub; t++) {
                 const float2 v = *reinterpret_cast<const float2*>(raw + pc[t]);
                 const float x0 = fmaf(v.x, a0, v.y * b0), x1 = fmaf(v.x, a1, v.y * b1);
-                uint32_t h0 = to_tf32(x0), h1 = to_tf32(x1);
-                const uint32_t l0 = to_tf32(x0 - __uint_as_float(h0)), l1 = to_tf32(x1 - __uint_as_float(h1));
+                uint32_t h0 = tf32_bits(x0), h1 = tf32_bits(x1);
+                const uint32_t l0 = tf32_bits(x0 - __uint_as_float(h0)), l1 = tf32_bits(x1 - __uint_as_float(h1));
                 h0 = lo ? l0 : h0;
                 h1 = lo ? l1 : h1;
                 if (t < 8) { w0[t] = h0; w0[8 + t] = h1; }
@@ -413,17 +468,22 @@ __global__ void __launch_bounds__(kJoinThreads, 1) tc_join_kernel(const TcJoinAr
                 if (!wait(&acce[buf], (uint32_t)((v >> 1) & 1) ^ 1u)) { give_up(14); break; }
                 fence_after();
             }
-            if (!wait(&fullA[st], (uint32_t)((u / kJoinStages) & 1))) { give_up(15); break; }
+            if (!wait(&fullA[st], (uint32_t)((u / kJoinStages) & 1)) ||
+                !wait(&qfull[u % kJoinQBufs], (uint32_t)((u / kJoinQBufs) & 1))) {
+                give_up(15);
+                break;
+            }
             fence_after();
             const uint32_t d = tmem + buf * S::kAccCols;
             const uint32_t ta = tmem + S::kACol0 + (uint32_t)st * kJoinStageCols;
-            const uint32_t qb = smem_u32(qst + (size_t)st * S::kQStage);
+            const uint32_t qb = smem_u32(qst + (size_t)(u % kJoinQBufs) * S::kQStage);
 #pragma unroll
             for (int ks = 0; ks < kJoinSub / 4; ks++) {
                 const uint64_t db = smem_desc(qb + (ks >> 1) * S::kQTile + (ks & 1) * 256);
                 mma_ts<true>(d, ta + ks * 8, db, g.idesc, (first && ks == 0) ? 0u : 1u);
             }
             mma_commit(&empty[st]);
+            mma_commit(&qempty[u % kJoinQBufs]);
             if ((u & fm) == fm || u + 1 == U) mma_commit(&accf[buf]);
         }
         // the MMAs must have finished before the tensor memory is freed
@@ -472,11 +532,91 @@ int join_ilog2(int64_t x) {
 }
 
 size_t join_smem_bytes(const TcJoinArgs& g) {
-    return (size_t)g.ring * g.slot_bytes + (size_t)kJoinStages * 2 * (2 * g.nq * kTcChunkBytes) + 128;
+    return (size_t)g.ring * g.slot_bytes + (size_t)kJoinQBufs * 2 * join_qtile_bytes(g.nq) + 128;
+}
+
+// Slot layout for the copy mode: TMA boxes land densely, bulk segments with 16 bytes of padding
+// each (they spread the splitters' reads over the banks); the ring takes as many raw chunks
+// (2..4) as fit beside the B stages.
+bool join_layout(TcJoinArgs& a, bool tma) {
+    a.tma = tma ? 1 : 0;
+    const int pad = tma ? 0 : kJoinPadBytes;
+    a.segP_stride = (8 << a.sbP) + pad;
+    a.segQ_stride = (8 << a.sbQ) + pad;
+    a.slotP_bytes = (a.nsegP * a.segP_stride + 127) / 128 * 128;
+    a.slot_bytes = a.slotP_bytes + (a.nsegQ * a.segQ_stride + 127) / 128 * 128;
+    const size_t stages = (size_t)kJoinQBufs * 2 * join_qtile_bytes(a.nq);
+    a.ring = 0;
+    for (int r = kJoinMaxRing; r >= 2 && !a.ring; r--)
+        if ((size_t)r * a.slot_bytes + stages <= kJoinSmemCap) a.ring = r;
+    return a.ring != 0;
+}
+
+// One operand's tile (address positions `tile`, ascending, the lowest run starting at bit 0) as a
+// TMA box, when its batch bits (positions `batch`, in batch-index order) are contiguous above every
+// other bit of the operand (maxnb: the highest non-batch position) and five dimensions suffice.
+bool join_box(const std::vector<int>& tile, const std::vector<int>& batch, int maxnb, JoinBox* b) {
+    memset(b, 0, sizeof(*b));
+    const int H = batch.empty() ? maxnb + 1 : batch[0];
+    for (size_t i = 0; i < batch.size(); i++)
+        if (batch[i] != H + (int)i) return false;
+    if (maxnb >= H || H > 31) return false;
+    std::vector<std::pair<int, int>> runs;  // (position, length)
+    for (int p : tile) {
+        if (!runs.empty() && runs.back().first + runs.back().second == p) runs.back().second++;
+        else runs.push_back({p, 1});
+    }
+    if (runs.empty() || runs[0].first != 0) return false;
+    int nd = 0;
+    auto add = [&](int64_t dim, int64_t stride, int box) {
+        if (nd >= 5) return false;
+        b->dim[nd] = dim;
+        b->stride[nd] = stride;
+        b->box[nd] = box;
+        nd++;
+        return true;
+    };
+    // dimension 0: the leading run (up to 8 bits of it), extent 2^H for the chunk's offset
+    const int l0 = std::min(runs[0].second, 8);
+    if (!add(int64_t(1) << H, 1, 1 << l0)) return false;
+    std::vector<std::pair<int, int>> rest;
+    if (runs[0].second > l0) rest.push_back({l0, runs[0].second - l0});
+    for (size_t r = 1; r < runs.size(); r++) rest.push_back(runs[r]);
+    for (const auto& pr : rest)
+        for (int pos = pr.first, len = pr.second; len > 0;) {
+            const int l = std::min(len, 8);
+            if (!add(int64_t(1) << l, int64_t(1) << pos, 1 << l)) return false;
+            pos += l;
+            len -= l;
+        }
+    b->tb = -1;
+    if (!batch.empty()) {
+        b->tb = nd;
+        if (!add(int64_t(1) << batch.size(), int64_t(1) << H, 1)) return false;
+    }
+    b->td = nd;
+    return true;
+}
+
+// The box's tensor map over the operand at `base` (8-byte elements; unused dimensions of extent 1).
+bool join_map(const JoinBox& b, const void* base, CUtensorMap* map) {
+    const EncodeTiledFn encode = encode_tiled();
+    if (!encode) return false;
+    cuuint64_t dims[5], strides[4];
+    cuuint32_t box[5], estr[5] = {1, 1, 1, 1, 1};
+    for (int d = 0; d < 5; d++) {
+        dims[d] = d < b.td ? (cuuint64_t)b.dim[d] : 1;
+        box[d] = d < b.td ? (cuuint32_t)b.box[d] : 1;
+        if (d > 0) strides[d - 1] = d < b.td ? (cuuint64_t)(8 * b.stride[d]) : (cuuint64_t)(8ll << 36);
+    }
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 5, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <int NQ, bool SCALED>
-cudaError_t launch_join_shape(const TcJoinArgs& g, double2* partial, int* exps, cudaStream_t st) {
+cudaError_t launch_join_shape(const TcJoinArgs& g, double2* partial, int* exps, cudaStream_t st,
+                              const CUtensorMap& mp, const CUtensorMap& mq) {
     static bool attr = false;               // the kernel's dynamic shared memory limit, once
     if (!attr) {
         const cudaError_t e = cudaFuncSetAttribute(tc_join_kernel<NQ, SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -484,7 +624,8 @@ cudaError_t launch_join_shape(const TcJoinArgs& g, double2* partial, int* exps, 
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    tc_join_kernel<NQ, SCALED><<<(unsigned)(g.nbatch * g.nsplit), kJoinThreads, join_smem_bytes(g), st>>>(g, partial, exps);
+    tc_join_kernel<NQ, SCALED>
+        <<<(unsigned)(g.nbatch * g.nsplit), kJoinThreads, join_smem_bytes(g), st>>>(g, partial, exps, mp, mq);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || g.nsplit == 1) return e;
     const int64_t total = g.nbatch * 32 * NQ;
@@ -573,10 +714,24 @@ bool tc_join_plan(const StepArgs& s, int sm_count, TcJoinArgs* out, int min_log2
     a.sbQ = sbQ;
     a.nsegP = 1 << (tbP - sbP);
     a.nsegQ = 1 << (tbQ - sbQ);
-    a.segP_stride = (8 << sbP) + kJoinPadBytes;
-    a.segQ_stride = (8 << sbQ) + kJoinPadBytes;
-    a.slotP_bytes = (a.nsegP * a.segP_stride + 127) / 128 * 128;
-    a.slot_bytes = a.slotP_bytes + (a.nsegQ * a.segQ_stride + 127) / 128 * 128;
+    // one TMA box per operand and chunk where the layouts allow it
+    {
+        auto box_of = [&](const BitMap& cm, const std::vector<int>& fr, const std::vector<int>& pos, JoinBox* b) {
+            std::vector<int> tile, batch;
+            int maxnb = 0;
+            for (int f : fr) {
+                tile.push_back(one(cm, f));
+                maxnb = std::max(maxnb, one(cm, f));
+            }
+            for (int k = 0; k < s.nk; k++) maxnb = std::max(maxnb, pos[k]);
+            for (int k : ks) tile.push_back(pos[k]);
+            std::sort(tile.begin(), tile.end());
+            for (int b2 : gb) batch.push_back(one(cm, b2));
+            return join_box(tile, batch, maxnb, b);
+        };
+        const bool tma = box_of(cP, fP, posP, &a.boxP) && box_of(cQ, fQ, posQ, &a.boxQ);
+        if (!join_layout(a, tma)) return false;
+    }
     a.run_p = 1 << sbP;
     a.run_q = 1 << sbQ;
     for (int t = 0; t < 6; t++) a.chunk_k[t] = ks[t];
@@ -631,12 +786,6 @@ bool tc_join_plan(const StepArgs& s, int sm_count, TcJoinArgs* out, int min_log2
     a.nsplit = (int)nsplit;
     a.nchunks = chunks / nsplit;
     a.flush = kJoinFlushTerms / kJoinSub;
-    // ring: as many raw chunks (2..4) as fit beside the MMA stages
-    const size_t stages = (size_t)kJoinStages * 2 * (2 * a.nq * kTcChunkBytes);
-    a.ring = 0;
-    for (int r = kJoinMaxRing; r >= 2 && !a.ring; r--)
-        if ((size_t)r * a.slot_bytes + stages <= kJoinSmemCap) a.ring = r;
-    if (!a.ring) return false;
     const uint32_t nmma = (uint32_t)(2 * a.nq);
     a.idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((nmma >> 3) << 17) | ((uint32_t)(kTcTileM >> 4) << 24);
     a.P = static_cast<const float2*>(p_is_a ? s.A : s.B);
@@ -655,18 +804,34 @@ size_t tc_join_partial_bytes(const TcJoinArgs& g) {
     return g.nsplit > 1 ? (size_t)g.nsplit * (size_t)g.nbatch * 32 * g.nq * sizeof(double2) : 0;
 }
 
-cudaError_t tc_join_launch(const TcJoinArgs& g, int* exps, void* scratch, cudaStream_t st, int* launches) {
+cudaError_t tc_join_launch(const TcJoinArgs& g0, int* exps, void* scratch, cudaStream_t st, int* launches) {
+    TcJoinArgs g = g0;
     if (!g.err) return cudaErrorInvalidValue;
     if (g.nsplit > 1 && !scratch) return cudaErrorInvalidValue;
-    // cp.async.bulk needs 16-byte aligned sources
+    // cp.async.bulk and TMA need 16-byte aligned sources
     if ((reinterpret_cast<uintptr_t>(g.P) & 15) != 0 || (reinterpret_cast<uintptr_t>(g.Q) & 15) != 0)
+        return cudaErrorInvalidValue;
+    alignas(64) CUtensorMap mp, mq;
+    memset(&mp, 0, sizeof(mp));
+    memset(&mq, 0, sizeof(mq));
+    // the segments by cp.async.bulk where the driver rejects a box
+    if (g.tma && !(join_map(g.boxP, g.P, &mp) && join_map(g.boxQ, g.Q, &mq)) && !join_layout(g, false))
         return cudaErrorInvalidValue;
     double2* partial = static_cast<double2*>(scratch);
     cudaError_t e = cudaErrorInvalidValue;
     switch (g.nq) {
-        case 8: e = exps ? launch_join_shape<8, true>(g, partial, exps, st) : launch_join_shape<8, false>(g, partial, exps, st); break;
-        case 16: e = exps ? launch_join_shape<16, true>(g, partial, exps, st) : launch_join_shape<16, false>(g, partial, exps, st); break;
-        case 32: e = exps ? launch_join_shape<32, true>(g, partial, exps, st) : launch_join_shape<32, false>(g, partial, exps, st); break;
+        case 8:
+            e = exps ? launch_join_shape<8, true>(g, partial, exps, st, mp, mq)
+                     : launch_join_shape<8, false>(g, partial, exps, st, mp, mq);
+            break;
+        case 16:
+            e = exps ? launch_join_shape<16, true>(g, partial, exps, st, mp, mq)
+                     : launch_join_shape<16, false>(g, partial, exps, st, mp, mq);
+            break;
+        case 32:
+            e = exps ? launch_join_shape<32, true>(g, partial, exps, st, mp, mq)
+                     : launch_join_shape<32, false>(g, partial, exps, st, mp, mq);
+            break;
         default: break;
     }
     if (launches) *launches = g.nsplit > 1 ? 2 : 1;
@@ -679,7 +844,7 @@ std::string tc_join_describe(const TcJoinArgs& g) {
                     " chunks=" + std::to_string(g.nchunks) + " ring=" + std::to_string(g.ring) + " chunk_k=";
     for (int t = 0; t < 6; t++) d += (t ? "," : "") + std::string("k") + std::to_string(g.chunk_k[t]);
     d += " runs=" + std::to_string(g.run_p) + "/" + std::to_string(g.run_q) + " segments=" + std::to_string(g.nsegP) +
-         "/" + std::to_string(g.nsegQ);
+         "/" + std::to_string(g.nsegQ) + (g.tma ? " copies=tma" : " copies=bulk");
     return d;
 }
 

@@ -44,7 +44,7 @@ class qxg_options(ct.Structure):
                 ("max_bitstring_batch", ct.c_int32), ("max_slice_batch", ct.c_int32),
                 ("use_graphs", ct.c_int32), ("tc_tuning", ct.c_int32),
                 ("tc_plane_budget_mb", ct.c_int32), ("tc_wait_limit", ct.c_int32), ("tc_stall_test", ct.c_int32),
-                ("tc_joins", ct.c_int32), ("reserved", ct.c_int32 * 2)]
+                ("cuda_core_joins", ct.c_int32), ("reserved", ct.c_int32 * 2)]
 
 
 class qxg_qx_sizes(ct.Structure):
@@ -327,7 +327,7 @@ class Executor:
     def __init__(self, programme: Programme, precision: str = "fp64", device: int = 0,
                  workspace_limit: int = 0, max_bitstring_batch: int = 0, max_slice_batch: int = 0,
                  use_graphs: bool = False, tc_tuning="auto", tc_plane_budget_mb: int = 0,
-                 tc_wait_limit: int = 0, tc_stall_test: bool = False, tc_joins: bool = False):
+                 tc_wait_limit: int = 0, tc_stall_test: bool = False, cuda_core_joins: bool = False):
         self.lib = load_library()
         self.programme = programme
         self.precision = precision
@@ -343,9 +343,9 @@ class Executor:
         # that makes them run out (qxg_options.tc_stall_test)
         opts.tc_wait_limit = int(tc_wait_limit)
         opts.tc_stall_test = int(bool(tc_stall_test))
-        # final joins of split-TF32 programmes: the CUDA cores' batched small GEMM (default) or the
-        # tensor-core join
-        opts.tc_joins = int(bool(tc_joins))
+        # final joins of split-TF32 programmes: the tensor-core join (default) or the CUDA cores'
+        # batched small GEMM
+        opts.cuda_core_joins = int(bool(cuda_core_joins))
         # "auto": time each tensor-core step's tile variants once and keep the fastest;
         # "fixed" (= 1) or k >= 1: candidate k of every step
         if tc_tuning == "auto":

@@ -39,7 +39,7 @@ struct QxgOptions          # qxg_options
     tc_plane_budget_mb::Int32   # 0: 4096 MiB of packed planes before blocking the free columns
     tc_wait_limit::Int32    # 0: 2^20 polls before a tensor-core wait gives up
     tc_stall_test::Int32    # test hook, leave 0
-    tc_joins::Int32         # 1: final joins on the tensor-core join instead of the CUDA cores
+    cuda_core_joins::Int32  # 1: final joins on the CUDA cores instead of the tensor-core join
     reserved::NTuple{2,Int32}
 end
 

@@ -24,37 +24,71 @@ static BitMap mk(std::vector<std::pair<int, int>> v) {
     return m;
 }
 
-static int g_split = 0;
+static int g_split = 0, g_tma = 0;
 
 // One block's sums: acc[i * nq + j] over the block's K range.
 static bool emulate_block(const TcJoinArgs& g, int64_t bi, int64_t si, std::vector<std::complex<double>>& acc) {
     std::vector<uint8_t> slot((size_t)g.slot_bytes);
     std::vector<uint8_t> written((size_t)g.slot_bytes);
+    const int tileB = join_qtile_bytes(g.nq);
+    std::vector<uint8_t> btiles((size_t)2 * kJoinSubs * tileB);
+    std::vector<uint8_t> bwritten(btiles.size());
+    const int64_t bP0 = pdep(bi, g.bP), bQ0 = pdep(bi, g.bQ);
     int64_t wp = join_base_p(g, bi, si, 0), wq = join_base_q(g, bi, si, 0);
+    auto mark = [&](std::vector<uint8_t>& w, size_t at, size_t n) {
+        for (size_t b = 0; b < n; b++) {
+            if (w.at(at + b)) { printf("byte %zu written twice\n", at + b); return false; }
+            w.at(at + b) = 1;
+        }
+        return true;
+    };
     for (int64_t c = 0; c < g.nchunks; c++) {
         if (wp != join_base_p(g, bi, si, c) || wq != join_base_q(g, bi, si, c)) {
             printf("delta walk differs from the deposit at chunk %lld\n", (long long)c);
             return false;
         }
         std::fill(written.begin(), written.end(), 0);
-        auto copy = [&](const float2* src, int nseg, int sb, int stride, int base_byte, bool p) {
+        // the loader: segments by cp.async.bulk, or one TMA box per operand
+        auto copy_segments = [&](const float2* src, int64_t base, bool p) {
+            const int nseg = p ? g.nsegP : g.nsegQ, sb = p ? g.sbP : g.sbQ;
+            const int stride = p ? g.segP_stride : g.segQ_stride, base_byte = p ? 0 : g.slotP_bytes;
             for (int sg = 0; sg < nseg; sg++) {
-                const int64_t off = (p ? wp : wq) + (p ? join_seg_p(g, sg) : join_seg_q(g, sg));
+                const int64_t off = base + (p ? join_seg_p(g, sg) : join_seg_q(g, sg));
                 const int bytes = 8 << sb;
                 const int dst = base_byte + sg * stride;
                 if (dst % 16 != 0 || (off * 8) % 16 != 0) { printf("unaligned segment\n"); return false; }
                 if (dst + bytes > g.slot_bytes) { printf("segment outside the slot\n"); return false; }
-                for (int b = 0; b < bytes; b++) {
-                    if (written.at((size_t)dst + b)) { printf("slot byte written twice\n"); return false; }
-                    written.at((size_t)dst + b) = 1;
-                }
+                if (!mark(written, (size_t)dst, (size_t)bytes)) return false;
                 memcpy(&slot.at((size_t)dst), src + off, (size_t)bytes);
             }
             return true;
         };
-        if (!copy(g.P, g.nsegP, g.sbP, g.segP_stride, 0, true)) return false;
-        if (!copy(g.Q, g.nsegQ, g.sbQ, g.segQ_stride, g.slotP_bytes, false)) return false;
-        if (g.nsegP * g.segP_stride > g.slotP_bytes) { printf("P segments overrun Q's part\n"); return false; }
+        auto copy_box = [&](const float2* src, const JoinBox& bx, int64_t chunk_off, bool p) {
+            int co[5] = {(int)chunk_off, 0, 0, 0, 0};
+            if (bx.tb >= 0) co[bx.tb] = (int)bi;
+            if ((co[0] * 8) % 16 != 0) { printf("TMA x coordinate not 16-byte aligned\n"); return false; }
+            int64_t n = 1;
+            for (int d = 0; d < bx.td; d++) n *= bx.box[d];
+            const int base_byte = p ? 0 : g.slotP_bytes;
+            if (base_byte % 128 != 0 || base_byte + n * 8 > g.slot_bytes) { printf("box outside the slot\n"); return false; }
+            for (int64_t e = 0; e < n; e++) {
+                int64_t rem = e, off = 0;
+                for (int d = 0; d < bx.td; d++) {
+                    const int64_t i = rem % bx.box[d];
+                    rem /= bx.box[d];
+                    if (co[d] + i >= bx.dim[d]) { printf("box coordinate outside dimension %d\n", d); return false; }
+                    off += (co[d] + i) * bx.stride[d];
+                }
+                if (!mark(written, (size_t)(base_byte + e * 8), 8)) return false;
+                memcpy(&slot.at((size_t)(base_byte + e * 8)), src + off, 8);
+            }
+            return true;
+        };
+        if (g.tma) {
+            if (!copy_box(g.P, g.boxP, wp - bP0, true) || !copy_box(g.Q, g.boxQ, wq - bQ0, false)) return false;
+        } else {
+            if (!copy_segments(g.P, wp, true) || !copy_segments(g.Q, wq, false)) return false;
+        }
         const int t = __builtin_ctzll((unsigned long long)(si * g.nchunks + c + 1));
         wp += join_delta(g.hP, t);
         wq += join_delta(g.hQ, t);
@@ -67,15 +101,49 @@ static bool emulate_block(const TcJoinArgs& g, int64_t bi, int64_t si, std::vect
             memcpy(&v, &slot.at((size_t)byte), 8);
             return v;
         };
-        for (int kl = 0; kl < kJoinKR; kl++)
+        // the Q splitters: thread tq takes elements tq + 64 m, stores (re, im) words into the B tiles
+        std::fill(bwritten.begin(), bwritten.end(), 0);
+        for (int tq = 0; tq < 64; tq++)
+            for (int m = 0; m < g.nq; m++) {
+                const int64_t e = tq + 64 * m;
+                const int src = g.slotP_bytes + join_qsrc(g, tq) + join_qsrc(g, 64 * m);
+                const int dst = join_qdst(g, tq) + join_qdst(g, 64 * m);
+                if (src != g.slotP_bytes + join_qsrc(g, e) || dst != join_qdst(g, e)) {
+                    printf("Q tables do not add\n");
+                    return false;
+                }
+                const float2 v = at(src);
+                const int lo = (g.nq / 8) * 512;
+                const int words[4] = {dst, dst + 256, dst + lo, dst + lo + 256};
+                const float vals[4] = {v.x, v.y, v.x, v.y};
+                for (int w = 0; w < 4; w++) {
+                    if (words[w] < 0 || words[w] + 4 > (int)btiles.size() || words[w] % tileB + 4 > tileB - kJoinPadBytes) {
+                        printf("B word outside its tile\n");
+                        return false;
+                    }
+                    if (!mark(bwritten, (size_t)words[w], 4)) return false;
+                    memcpy(&btiles[(size_t)words[w]], &vals[w], 4);
+                }
+            }
+        // the MMA's view: stage sub, group gg -> tile 2 sub + gg, row j, core column cc, word w
+        auto bword = [&](int tile, int row, int cc, int w) {
+            float x;
+            memcpy(&x, &btiles.at((size_t)tile * tileB + (row >> 3) * 512 + cc * 128 + (row & 7) * 16 + w * 4), 4);
+            return x;
+        };
+        for (int kl = 0; kl < kJoinKR; kl++) {
+            const int tile = kl >> 3, tt = kl & 7;
             for (int i = 0; i < 32; i++) {
                 const float2 p = at(join_prow(g, i) + join_pcol(g, kl));
                 const std::complex<double> pv(p.x, g.conjP ? -p.y : p.y);
                 for (int j = 0; j < g.nq; j++) {
-                    const float2 q = at(join_qrow(g, j) + join_qcol(g, kl));
-                    acc[(size_t)i * g.nq + j] += pv * std::complex<double>(q.x, g.conjQ ? -q.y : q.y);
+                    const float qr = bword(tile, j, tt >> 2, tt & 3), qi = bword(tile, j, 2 + (tt >> 2), tt & 3);
+                    const float lr = bword(tile, g.nq + j, tt >> 2, tt & 3), li = bword(tile, g.nq + j, 2 + (tt >> 2), tt & 3);
+                    if (qr != lr || qi != li) { printf("hi and lo rows disagree\n"); return false; }
+                    acc[(size_t)i * g.nq + j] += pv * std::complex<double>(qr, g.conjQ ? -qi : qi);
                 }
             }
+        }
     }
     return true;
 }
@@ -125,8 +193,9 @@ int join_case(std::mt19937& rng, int nk, int nq_bits, int ng, bool p_is_b, bool 
     if (!tc_join_plan(s, min_nsplit_sm, &g, 12)) return 0;
     (*used)++;
     if (g.nsplit > 1) g_split++;
+    if (g.tma) g_tma++;
     if (g.nq != (1 << nq_bits) || g.ring < 2 || g.ring > kJoinMaxRing || g.nsegP > kJoinMaxSeg ||
-        g.nsegQ > kJoinMaxSeg || (size_t)g.ring * g.slot_bytes + (size_t)kJoinStages * 2 * (2 * g.nq * 64) > kJoinSmemCap) {
+        g.nsegQ > kJoinMaxSeg || join_smem_bytes(g) > kJoinSmemCap + 128) {
         printf("plan outside the kernel's limits\n");
         return -1;
     }
@@ -189,6 +258,7 @@ int main(int argc, char** argv) {
         const int sms = (rng() % 3 == 0) ? 8 : 1;
         if (join_case(rng, nk, nq_bits, ng, p_is_b, rng() % 4 != 0, sms, &used) < 0) fail++;
     }
-    printf("tensor-core join: %d layouts tried, %d planned (%d with K ranges), %d failed\n", tried, used, g_split, fail);
-    return fail || used < 10 || g_split == 0 ? 1 : 0;
+    printf("tensor-core join: %d layouts tried, %d planned (%d with K ranges, %d with TMA boxes), %d failed\n", tried,
+           used, g_split, g_tma, fail);
+    return fail || used < 10 || g_split == 0 || g_tma == 0 ? 1 : 0;
 }

@@ -203,7 +203,8 @@ def test_batched_join_gemm(q, gpu_lib, precision, nk, na, nb, ng):
     idx = {v: letters[i] for i, v in enumerate(sorted(set(la + lb)))}
     sub = lambda ls: "".join(idx[v] for v in ls)
     ref = np.einsum(f"{sub(la)},{sub(lb)}->{sub(lc)}", A, B).reshape(-1, order="F")
-    with q.Executor(prog, precision=precision) as ex:
+    # split-TF32 programmes send the joins that fit it to the tensor-core join unless told otherwise
+    with q.Executor(prog, precision=precision, cuda_core_joins=True) as ex:
         got = ex.amplitudes([""])[0]
         got2 = ex.amplitudes([""])[0]
         assert "batched-gemm" in ex.explain(2), ex.explain(2)
@@ -250,13 +251,13 @@ def test_tensor_core_join(q, gpu_lib, nk, na, nb, ng):
     within the split-TF32 tolerance of einsum, equal to the CUDA-core batched GEMM within it, and
     the same bits on a second call."""
     prog, ref = join_programme(q, nk, na, nb, ng, seed=nk * 1000 + na * 100 + nb * 10 + ng)
-    with q.Executor(prog, precision="split_tf32", tc_joins=True) as ex:
+    with q.Executor(prog, precision="split_tf32") as ex:
         got = ex.amplitudes([""])[0]
         got2 = ex.amplitudes([""])[0]
         desc = ex.explain(2)
         assert "tensor-core join" in desc, desc
         assert ex.info()["num_steps_tensor_core"] == 1
-    with q.Executor(prog, precision="split_tf32") as ex:
+    with q.Executor(prog, precision="split_tf32", cuda_core_joins=True) as ex:
         cc = ex.amplitudes([""])[0]
         assert "batched-gemm" in ex.explain(2)
     scale = np.max(np.abs(ref))

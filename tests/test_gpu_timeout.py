@@ -67,13 +67,12 @@ def test_expired_join_wait_reports_timeout_and_gpu_stays_usable(q, gpu_lib):
     QXG_ERR_TIMEOUT twice, and a fresh programme returns the right result."""
     from test_gpu_split import join_programme
     prog, ref = join_programme(q, 12, 5, 5, 3, seed=77)
-    with q.Executor(prog, precision="split_tf32", tc_joins=True, tc_wait_limit=1 << 14,
-                    tc_stall_test=True) as ex:
+    with q.Executor(prog, precision="split_tf32", tc_wait_limit=1 << 14, tc_stall_test=True) as ex:
         for _ in range(2):
             with pytest.raises(q.QXGError) as e:
                 ex.amplitudes([""])
             assert e.value.code == -5, str(e.value)
         assert "tensor-core join" in ex.explain(2)
-    with q.Executor(prog, precision="split_tf32", tc_joins=True) as ex:
+    with q.Executor(prog, precision="split_tf32") as ex:
         got = ex.amplitudes([""])[0]
     assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) <= 5e-6
