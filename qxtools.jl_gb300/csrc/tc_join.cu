@@ -28,10 +28,10 @@
 //   warps 4-11     P splitters, two groups on alternate MMA stages (16 summed terms each): warp
 //                  4 + 4 g + q reads the stage's terms for its eight free values from the slot,
 //                  splits them into the four roles and stores 32 columns of its lanes with
-//                  tcgen05.st.  Group 0 also drains: every `flush` stages (512 terms) the MMA
+//                  tcgen05.st.  Group 0 also drains: every `flush` stages (128 terms) the MMA
 //                  issuer commits one accumulator and switches to the other; group 0 adds each
-//                  committed accumulator (h = hi and lo summed in FP32) into FP64 registers
-//                  before the stage that reuses it, so the FP32 sums never run over more than 512
+//                  committed accumulator (h = hi and lo summed in FP32) into FP32 register pairs
+//                  before the stage that reuses it, so the FP32 sums never run over more than 128
 //                  terms, and at the end combines the four roles with shuffles and writes C (or
 //                  its FP64 partial, added in K-range order by tc_join_reduce_kernel);
 //   warps 2-3      Q splitters: a whole raw chunk at a time, each thread reading elements in the
@@ -64,7 +64,7 @@ constexpr int kJoinPGroups = 2;                     // P splitter groups (altern
 constexpr int kJoinThreads = 32 * (4 + 4 * kJoinPGroups);
 constexpr uint32_t kJoinSleepNs = 2000;             // suspend hint of a barrier poll
 constexpr int kJoinStageCols = 2 * kJoinSub;        // tensor-memory columns of one A stage (32)
-constexpr int kJoinFlushTerms = 512;                // summed terms per FP32 accumulator
+constexpr int kJoinFlushTerms = 128;                // summed terms per FP32 accumulator
 constexpr int kJoinChunkBits = 48;                  // delta-table entries (chunk index bits)
 constexpr size_t kJoinSmemCap = 200 * 1024;         // ring + B stages (one CTA per SM)
 constexpr int kJoinPadBytes = 16;                   // padding after each bulk segment and each B tile
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
     } else if (warp >= 4 && warp < 4 + 4 * kJoinPGroups) {
         // P splitters: group pg takes the stages u = pg mod kJoinPGroups; warp 4 pg + q stores the
         // tensor-memory lanes 32 q .. 32 q + 31 (roles 0-3 of free values 8 q .. 8 q + 7).  Group 0
-        // also drains: accumulator v is added into FP64 registers just before the stage that
+        // also drains: accumulator v is added into FP32 register pairs just before the stage that
         // starts interval v + 2 (which reuses it) is written -- its MMAs finished several stages
         // earlier -- and the last two at the end.
         const int pg = (warp - 4) >> 2, q4 = warp & 3, role = lane >> 3;
@@ -347,9 +347,16 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
         int pc[kJoinSub];                   // slot bytes of the terms within a stage
 #pragma unroll
         for (int t = 0; t < kJoinSub; t++) pc[t] = pcol[t];
-        double acc[NQ];
+        // the drained sums as unevaluated FP32 pairs (ah + al), added with Knuth's TwoSum: about 48
+        // bits of precision without the FP64 pipe, which GB300 runs at a small fraction of FP32
+        float ah[NQ], al[NQ];
 #pragma unroll
-        for (int j = 0; j < NQ; j++) acc[j] = 0.0;
+        for (int j = 0; j < NQ; j++) { ah[j] = 0.f; al[j] = 0.f; }
+        auto two_sum = [](float& h, float& l, float x) {
+            const float t = h + x, bp = t - h;
+            l += (h - (t - bp)) + (x - bp);
+            h = t;
+        };
         int64_t drained = 0;
         auto drain_acc = [&](int64_t v) -> bool {
             const uint32_t buf = (uint32_t)(v & 1);
@@ -369,14 +376,14 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
                     tmem_wait_ld();
 #pragma unroll
                     for (int j = 0; j < 16; j++)
-                        if (j0 + j < NQ) acc[j0 + j] += (double)(__uint_as_float(hi[j]) + __uint_as_float(lo16[j]));
+                        if (j0 + j < NQ) two_sum(ah[j0 + j], al[j0 + j], __uint_as_float(hi[j]) + __uint_as_float(lo16[j]));
                 }
             } else {
                 uint32_t w[16];             // hi columns 0 .. NQ-1, lo columns NQ .. 2NQ-1
                 tmem_ld16(d0, w);
                 tmem_wait_ld();
 #pragma unroll
-                for (int j = 0; j < NQ; j++) acc[j] += (double)(__uint_as_float(w[j]) + __uint_as_float(w[NQ + j]));
+                for (int j = 0; j < NQ; j++) two_sum(ah[j], al[j], __uint_as_float(w[j]) + __uint_as_float(w[NQ + j]));
             }
             // the accumulator may be overwritten once all four warps' loads have completed
             fence_before();
@@ -435,7 +442,7 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
             int emax = kExpUnset;
 #pragma unroll
             for (int j = 0; j < NQ; j++) {
-                double x = acc[j];
+                double x = (double)ah[j] + (double)al[j];
                 x += __shfl_xor_sync(0xffffffffu, x, 16);
                 const double im = __shfl_down_sync(0xffffffffu, x, 8);
                 if (lane < 8) {

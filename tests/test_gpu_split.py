@@ -247,7 +247,7 @@ JOIN_CASES = [(12, 5, 5, 3), (15, 5, 5, 0), (15, 5, 3, 2), (12, 4, 5, 4), (15, 5
 
 @pytest.mark.parametrize("nk,na,nb,ng", JOIN_CASES)
 def test_tensor_core_join(q, gpu_lib, nk, na, nb, ng):
-    """The tensor-core join (3xTF32, operands split on the fly, FP64 drains every 512 terms):
+    """The tensor-core join (3xTF32, operands split on the fly, FP64 drains every 128 terms):
     within the split-TF32 tolerance of einsum, equal to the CUDA-core batched GEMM within it, and
     the same bits on a second call."""
     prog, ref = join_programme(q, nk, na, nb, ng, seed=nk * 1000 + na * 100 + nb * 10 + ng)
