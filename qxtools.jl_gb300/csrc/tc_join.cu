@@ -18,7 +18,7 @@
 // tensor-memory lane 32 q + 8 r + (i mod 8) with q = i / 8, so the warp that owns lanes
 // 32 q .. 32 q + 31 holds all four roles of eight free values.
 //
-// One CTA (12 warps) per (batch value, K range):
+// One CTA (14 warps) per (batch value, K range):
 //   warp 1         loader: per raw chunk of 64 summed terms, the chunk's P tile (32 x 64) and Q
 //                  tile (NQ x 64) land in a ring slot in each operand's address order: one TMA
 //                  tensor copy per operand (the tile's runs of address bits as box dimensions),
@@ -34,12 +34,13 @@
 //                  before the stage that reuses it, so the FP32 sums never run over more than 128
 //                  terms, and at the end combines the four roles with shuffles and writes C (or
 //                  its FP64 partial, added in K-range order by tc_join_reduce_kernel);
-//   warps 2-3      Q splitters: a whole raw chunk at a time, each thread reading elements in the
+//   warps 2-3, 12-13  Q splitters: a whole raw chunk at a time, each thread reading elements in the
 //                  slot's order (consecutive threads, consecutive elements) and storing their
 //                  four split words into the chunk's eight B tiles (K-major core matrices, 64-byte
 //                  rows: real parts in core columns 0-1, imaginary in 2-3; the tiles 16 bytes
 //                  apart in bank position), two chunks of B stages in flight;
-//   warp 0 lane 0  MMA issuer: four tcgen05.mma (kind::tf32, A from tensor memory) per stage.
+//   warp 0 lane 0  MMA issuer: four tcgen05.mma (kind::tf32, A from tensor memory) per stage and
+//                  one commit, whose barrier frees the stage's B buffer and, four stages on, its A stage.
 // Waiting warps sleep in their barrier polls (a suspend-time hint), so they leave the issue slots
 // to the splitters.
 // Every wait is bounded; a wait that gives up writes its code to the programme's error word, the
@@ -59,9 +60,13 @@ constexpr int kJoinSub = 16;                        // summed terms per MMA stag
 constexpr int kJoinSubs = kJoinKR / kJoinSub;       // MMA stages per raw chunk (4)
 constexpr int kJoinStages = 4;                      // A stages in tensor memory
 constexpr int kJoinQBufs = 2 * kJoinSubs;           // B stages in shared memory (two raw chunks)
+static_assert(kJoinSubs == 4 && kJoinStages == 4 && kJoinQBufs == 8,
+              "the kernel's loops index stages with shifts by 2 (4 per chunk, 4 A stages) and 3 (8 B stages)");
 constexpr int kJoinMaxRing = 4;                     // raw chunks in the ring
 constexpr int kJoinPGroups = 2;                     // P splitter groups (alternate stages)
-constexpr int kJoinThreads = 32 * (4 + 4 * kJoinPGroups);
+constexpr int kJoinQWarps = 4;                      // Q splitter warps (2, 3 and the last two)
+constexpr int kJoinQThreads = 32 * kJoinQWarps;
+constexpr int kJoinThreads = 32 * (2 + kJoinQWarps + 4 * kJoinPGroups);
 constexpr uint32_t kJoinSleepNs = 2000;             // suspend hint of a barrier poll
 constexpr int kJoinStageCols = 2 * kJoinSub;        // tensor-memory columns of one A stage (32)
 constexpr int kJoinFlushTerms = 128;                // summed terms per FP32 accumulator
@@ -151,10 +156,12 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
                    const __grid_constant__ CUtensorMap mapQ) {
     using S = JoinShape<NQ>;
     extern __shared__ uint8_t join_smem_raw[];
-    // rfull / rempty per ring slot, fullA / empty per A stage, qfull / qempty per B stage, accf /
-    // acce per accumulator, drain
-    __shared__ uint64_t bars[2 * kJoinMaxRing + 2 * kJoinStages + 2 * kJoinQBufs + 5];
-    __shared__ int32_t prow[32], pcol[kJoinKR], qsrc_hi[NQ], qdst_hi[NQ];
+    // rfull / rempty per ring slot, fullA per A stage, qfull per B stage, sdone per B stage (the
+    // MMAs of stage u done: u's B stage and, four stages on, its A stage are free), accf / acce per
+    // accumulator, drain
+    __shared__ uint64_t bars[2 * kJoinMaxRing + kJoinStages + 2 * kJoinQBufs + 5];
+    constexpr int kQPer = NQ * kJoinKR / kJoinQThreads;        // Q elements per splitter thread
+    __shared__ int32_t prow[32], pcol[kJoinKR], qsrc_hi[kQPer], qdst_hi[kQPer];
     __shared__ int64_t psegoff[kJoinMaxSeg], qsegoff[kJoinMaxSeg];
     __shared__ int64_t dP[kJoinChunkBits], dQ[kJoinChunkBits];
     __shared__ uint32_t tmem_holder;
@@ -165,10 +172,9 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
     uint64_t* rfull = bars;
     uint64_t* rempty = bars + kJoinMaxRing;
     uint64_t* fullA = bars + 2 * kJoinMaxRing;
-    uint64_t* empty = fullA + kJoinStages;
-    uint64_t* qfull = empty + kJoinStages;
-    uint64_t* qempty = qfull + kJoinQBufs;
-    uint64_t* accf = qempty + kJoinQBufs;
+    uint64_t* qfull = fullA + kJoinStages;
+    uint64_t* sdone = qfull + kJoinQBufs;
+    uint64_t* accf = sdone + kJoinQBufs;
     uint64_t* acce = accf + 2;
     uint64_t* drain = acce + 2;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -184,12 +190,18 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
     uint8_t* qst = smem + (size_t)R * g.slot_bytes;
     const int64_t nchunks = bad ? 0 : g.nchunks;
     const int64_t U = nchunks * kJoinSubs;                      // MMA stages of this CTA
-    const int64_t V = bad ? 0 : (U + g.flush - 1) / g.flush;   // accumulator drains
+    // flush is a power of two: shifts and masks, no 64-bit divisions in the loops
+    const int fsh = bad ? 0 : __ffs(g.flush) - 1;
+    const int64_t fmask = (int64_t(1) << fsh) - 1;
+    const int64_t V = bad ? 0 : (U + fmask) >> fsh;             // accumulator drains
 
     if (threadIdx.x == 0) {
-        for (int r = 0; r < kJoinMaxRing; r++) { mbar_init(&rfull[r], 1u); mbar_init(&rempty[r], 2u + 4u * kJoinPGroups); }
-        for (int s = 0; s < kJoinStages; s++) { mbar_init(&fullA[s], 4u); mbar_init(&empty[s], 1u); }
-        for (int s = 0; s < kJoinQBufs; s++) { mbar_init(&qfull[s], 2u); mbar_init(&qempty[s], 1u); }
+        for (int r = 0; r < kJoinMaxRing; r++) {
+            mbar_init(&rfull[r], 1u);
+            mbar_init(&rempty[r], (uint32_t)(kJoinQWarps + 4 * kJoinPGroups));
+        }
+        for (int s = 0; s < kJoinStages; s++) mbar_init(&fullA[s], 4u);
+        for (int s = 0; s < kJoinQBufs; s++) { mbar_init(&qfull[s], (uint32_t)kJoinQWarps); mbar_init(&sdone[s], 1u); }
         for (int j = 0; j < 2; j++) { mbar_init(&accf[j], 1u); mbar_init(&acce[j], 4u); }
         mbar_init(drain, 1u);
         abort_flag = 0;
@@ -205,9 +217,9 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
     if (!bad) {
         for (int t = threadIdx.x; t < kJoinKR; t += kJoinThreads) pcol[t] = join_pcol(g, t);
         for (int t = threadIdx.x; t < 32; t += kJoinThreads) prow[t] = join_prow(g, t);
-        for (int t = threadIdx.x; t < NQ; t += kJoinThreads) {
-            qsrc_hi[t] = join_qsrc(g, (int64_t)t * 64);
-            qdst_hi[t] = join_qdst(g, (int64_t)t * 64);
+        for (int t = threadIdx.x; t < kQPer; t += kJoinThreads) {
+            qsrc_hi[t] = join_qsrc(g, (int64_t)t * kJoinQThreads);
+            qdst_hi[t] = join_qdst(g, (int64_t)t * kJoinQThreads);
         }
         for (int t = threadIdx.x; t < g.nsegP; t += kJoinThreads) psegoff[t] = join_seg_p(g, t);
         for (int t = threadIdx.x; t < g.nsegQ; t += kJoinThreads) qsegoff[t] = join_seg_q(g, t);
@@ -275,21 +287,22 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
         if (lane == 0)
             for (int64_t q = issued - 1; q >= 0 && q >= issued - R; q--)
                 mbar_wait(&rfull[q % R], (uint32_t)((q / R) & 1));     // full limit: copies must land
-    } else if (warp == 2 || warp == 3) {
-        // Q splitters: a raw chunk at a time; thread tq takes the chunk's elements tq + 64 m (in
+    } else if (warp == 2 || warp == 3 || warp >= 4 + 4 * kJoinPGroups) {
+        // Q splitters: a raw chunk at a time; thread tq takes the chunk's elements tq + 128 m (in
         // the slot's order) and stores their split words into the chunk's B stages 4 (c mod 2) ..
-        const int tq = (warp - 2) * 32 + lane;
+        const int tq = (warp < 4 ? warp - 2 : warp - 2 - 4 * kJoinPGroups) * 32 + lane;
         float s = 1.f;
         if (SCALED) s = pow2f(-read_m(exps, g.expQ));
         const float si_ = g.conjQ ? -s : s;
         const int src0 = g.slotP_bytes + join_qsrc(g, tq), dst0 = join_qdst(g, tq);
+        int slot = 0;                       // ring slot of chunk c and its phase
+        uint32_t rph = 0;
         for (int64_t c = 0; c < nchunks; c++) {
-            const int slot = (int)(c % R);
-            bool ok = wait(&rfull[slot], (uint32_t)((c / R) & 1));
+            bool ok = wait(&rfull[slot], rph);
             // the chunk's B stages are free once the MMAs of the stages two chunks back are done
             for (int sb = 0; sb < kJoinSubs && ok; sb++) {
                 const int64_t u = c * kJoinSubs + sb;
-                ok = wait(&qempty[u % kJoinQBufs], (uint32_t)((u / kJoinQBufs) & 1) ^ 1u);
+                if (u >= kJoinQBufs) ok = wait(&sdone[u & (kJoinQBufs - 1)], (uint32_t)(((u - kJoinQBufs) >> 3) & 1));
             }
             if (!__all_sync(0xffffffffu, ok)) {
                 if (lane == 0) give_up(12);
@@ -299,9 +312,9 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
             const uint8_t* raw = ring + (size_t)slot * g.slot_bytes + src0;
             uint8_t* qb = qst + (size_t)(c & 1) * (2 * kJoinSubs) * S::kQTile + dst0;
             // eight elements' loads before their stores (the stores could alias later loads)
-            constexpr int kQB = NQ < 8 ? NQ : 8;
+            constexpr int kQB = kQPer < 8 ? kQPer : 8;
 #pragma unroll 1
-            for (int m0 = 0; m0 < NQ; m0 += kQB) {
+            for (int m0 = 0; m0 < kQPer; m0 += kQB) {
                 float2 v[kQB];
                 int dd[kQB];
 #pragma unroll
@@ -324,9 +337,10 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             if (lane == 0) {
-                for (int sb = 0; sb < kJoinSubs; sb++) mbar_arrive(&qfull[(c * kJoinSubs + sb) % kJoinQBufs]);
+                for (int sb = 0; sb < kJoinSubs; sb++) mbar_arrive(&qfull[(c * kJoinSubs + sb) & (kJoinQBufs - 1)]);
                 mbar_arrive(&rempty[slot]);
             }
+            if (++slot == R) { slot = 0; rph ^= 1u; }
         }
     } else if (warp >= 4 && warp < 4 + 4 * kJoinPGroups) {
         // P splitters: group pg takes the stages u = pg mod kJoinPGroups; warp 4 pg + q stores the
@@ -347,15 +361,17 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
         int pc[kJoinSub];                   // slot bytes of the terms within a stage
 #pragma unroll
         for (int t = 0; t < kJoinSub; t++) pc[t] = pcol[t];
-        // the drained sums as unevaluated FP32 pairs (ah + al), added with Knuth's TwoSum: about 48
-        // bits of precision without the FP64 pipe, which GB300 runs at a small fraction of FP32
-        float ah[NQ], al[NQ];
-#pragma unroll
-        for (int j = 0; j < NQ; j++) { ah[j] = 0.f; al[j] = 0.f; }
-        auto two_sum = [](float& h, float& l, float x) {
-            const float t = h + x, bp = t - h;
-            l += (h - (t - bp)) + (x - bp);
-            h = t;
+        // the drained sums as unevaluated FP32 pairs (hi + lo), added with Knuth's TwoSum: about 48
+        // bits of precision without the FP64 pipe, which GB300 runs at a small fraction of FP32.
+        // They live in shared memory ([quadrant][j][lane]: a warp's lanes on consecutive words), so
+        // the splitters keep their registers for loads in flight.
+        float2* accs = reinterpret_cast<float2*>(qst + (size_t)kJoinQBufs * S::kQStage) + q4 * NQ * 32 + lane;
+        if (pg == 0)
+            for (int j = 0; j < NQ; j++) accs[j * 32] = make_float2(0.f, 0.f);
+        auto two_sum = [](float2& a, float x) {
+            const float t = a.x + x, bp = t - a.x;
+            a.y += (a.x - (t - bp)) + (x - bp);
+            a.x = t;
         };
         int64_t drained = 0;
         auto drain_acc = [&](int64_t v) -> bool {
@@ -376,14 +392,22 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
                     tmem_wait_ld();
 #pragma unroll
                     for (int j = 0; j < 16; j++)
-                        if (j0 + j < NQ) two_sum(ah[j0 + j], al[j0 + j], __uint_as_float(hi[j]) + __uint_as_float(lo16[j]));
+                        if (j0 + j < NQ) {
+                            float2 a = accs[(j0 + j) * 32];
+                            two_sum(a, __uint_as_float(hi[j]) + __uint_as_float(lo16[j]));
+                            accs[(j0 + j) * 32] = a;
+                        }
                 }
             } else {
                 uint32_t w[16];             // hi columns 0 .. NQ-1, lo columns NQ .. 2NQ-1
                 tmem_ld16(d0, w);
                 tmem_wait_ld();
 #pragma unroll
-                for (int j = 0; j < NQ; j++) two_sum(ah[j], al[j], __uint_as_float(w[j]) + __uint_as_float(w[NQ + j]));
+                for (int j = 0; j < NQ; j++) {
+                    float2 a = accs[j * 32];
+                    two_sum(a, __uint_as_float(w[j]) + __uint_as_float(w[NQ + j]));
+                    accs[j * 32] = a;
+                }
             }
             // the accumulator may be overwritten once all four warps' loads have completed
             fence_before();
@@ -392,15 +416,17 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
             return true;
         };
         bool ok_all = true;
+        int slot = 0;                       // ring slot of the current chunk and its phase
+        uint32_t rph = 0;
         for (int64_t u = pg; u < U; u += kJoinPGroups) {
-            const int64_t c = u / kJoinSubs;
-            const int sub = (int)(u % kJoinSubs), slot = (int)(c % R), st = (int)(u % kJoinStages);
-            if (pg == 0 && u % g.flush == 0 && u / g.flush >= 2) {
+            const int sub = (int)(u & (kJoinSubs - 1)), st = (int)(u & (kJoinStages - 1));
+            if (pg == 0 && (u & fmask) == 0 && (u >> fsh) >= 2) {
                 if (!drain_acc(drained)) { ok_all = false; break; }
                 drained++;
             }
-            bool ok = sub != pg || wait(&rfull[slot], (uint32_t)((c / R) & 1));
-            ok = ok && wait(&empty[st], (uint32_t)((u / kJoinStages) & 1) ^ 1u);
+            bool ok = sub != pg || wait(&rfull[slot], rph);
+            // the A stage is free once the MMAs of stage u - 4 are done
+            if (u >= kJoinStages) ok = ok && wait(&sdone[(u - kJoinStages) & (kJoinQBufs - 1)], (uint32_t)(((u - kJoinStages) >> 3) & 1));
             if (!__all_sync(0xffffffffu, ok)) {
                 if (lane == 0) give_up(13);
                 ok_all = false;
@@ -409,21 +435,25 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
             if (aborted()) { ok_all = false; break; }
             fence_after();                  // the MMAs that read this A stage have completed
             const uint8_t* raw = ring + (size_t)slot * g.slot_bytes + rb + pcol[sub * kJoinSub];
-            uint32_t w0[16], w1[16];
+            // all sixteen loads first, then each 8-term group's 16 words and its tensor-memory store
+            float2 v[kJoinSub];
 #pragma unroll
-            for (int t = 0; t < kJoinSub; t++) {
-                const float2 v = *reinterpret_cast<const float2*>(raw + pc[t]);
-                const float x0 = fmaf(v.x, a0, v.y * b0), x1 = fmaf(v.x, a1, v.y * b1);
-                uint32_t h0 = tf32_bits(x0), h1 = tf32_bits(x1);
-                const uint32_t l0 = tf32_bits(x0 - __uint_as_float(h0)), l1 = tf32_bits(x1 - __uint_as_float(h1));
-                h0 = lo ? l0 : h0;
-                h1 = lo ? l1 : h1;
-                if (t < 8) { w0[t] = h0; w0[8 + t] = h1; }
-                else { w1[t - 8] = h0; w1[t] = h1; }
-            }
+            for (int t = 0; t < kJoinSub; t++) v[t] = *reinterpret_cast<const float2*>(raw + pc[t]);
             const uint32_t ta = lane_base + S::kACol0 + (uint32_t)st * kJoinStageCols;
-            tmem_st16(ta, w0);
-            tmem_st16(ta + 16, w1);
+#pragma unroll
+            for (int h8 = 0; h8 < 2; h8++) {
+                uint32_t w[16];
+#pragma unroll
+                for (int t = 0; t < 8; t++) {
+                    const float2 x = v[8 * h8 + t];
+                    const float x0 = fmaf(x.x, a0, x.y * b0), x1 = fmaf(x.x, a1, x.y * b1);
+                    const uint32_t h0 = tf32_bits(x0), h1 = tf32_bits(x1);
+                    const uint32_t l0 = tf32_bits(x0 - __uint_as_float(h0)), l1 = tf32_bits(x1 - __uint_as_float(h1));
+                    w[t] = lo ? l0 : h0;
+                    w[8 + t] = lo ? l1 : h1;
+                }
+                tmem_st16(ta + 16 * h8, w);
+            }
             tmem_wait_st();
             fence_before();
             __syncwarp();
@@ -431,6 +461,7 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
             if (sub + kJoinPGroups >= kJoinSubs) {      // this group's last stage of the chunk
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&rempty[slot]);
+                if (++slot == R) { slot = 0; rph ^= 1u; }
             }
         }
         if (pg == 0) {
@@ -442,7 +473,8 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
             int emax = kExpUnset;
 #pragma unroll
             for (int j = 0; j < NQ; j++) {
-                double x = (double)ah[j] + (double)al[j];
+                const float2 a = accs[j * 32];
+                double x = (double)a.x + (double)a.y;
                 x += __shfl_xor_sync(0xffffffffu, x, 16);
                 const double im = __shfl_down_sync(0xffffffffu, x, 8);
                 if (lane < 8) {
@@ -465,32 +497,31 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
         }
     } else if (warp == 0 && lane == 0) {
         // MMA issuer
-        const int64_t fm = g.flush - 1;
+        const int64_t fm = fmask;
         for (int64_t u = 0; u < U; u++) {
-            const int64_t v = u / g.flush;
+            const int64_t v = u >> fsh;
             const uint32_t buf = (uint32_t)(v & 1);
-            const int st = (int)(u % kJoinStages);
+            const int st = (int)(u & (kJoinStages - 1));
             const bool first = (u & fm) == 0;
             if (first) {
                 if (!wait(&acce[buf], (uint32_t)((v >> 1) & 1) ^ 1u)) { give_up(14); break; }
                 fence_after();
             }
-            if (!wait(&fullA[st], (uint32_t)((u / kJoinStages) & 1)) ||
-                !wait(&qfull[u % kJoinQBufs], (uint32_t)((u / kJoinQBufs) & 1))) {
+            if (!wait(&fullA[st], (uint32_t)((u >> 2) & 1)) ||
+                !wait(&qfull[u & (kJoinQBufs - 1)], (uint32_t)((u >> 3) & 1))) {
                 give_up(15);
                 break;
             }
             fence_after();
             const uint32_t d = tmem + buf * S::kAccCols;
             const uint32_t ta = tmem + S::kACol0 + (uint32_t)st * kJoinStageCols;
-            const uint32_t qb = smem_u32(qst + (size_t)(u % kJoinQBufs) * S::kQStage);
+            const uint32_t qb = smem_u32(qst + (size_t)(u & (kJoinQBufs - 1)) * S::kQStage);
 #pragma unroll
             for (int ks = 0; ks < kJoinSub / 4; ks++) {
                 const uint64_t db = smem_desc(qb + (ks >> 1) * S::kQTile + (ks & 1) * 256);
                 mma_ts<true>(d, ta + ks * 8, db, g.idesc, (first && ks == 0) ? 0u : 1u);
             }
-            mma_commit(&empty[st]);
-            mma_commit(&qempty[u % kJoinQBufs]);
+            mma_commit(&sdone[u & (kJoinQBufs - 1)]);
             if ((u & fm) == fm || u + 1 == U) mma_commit(&accf[buf]);
         }
         // the MMAs must have finished before the tensor memory is freed
@@ -538,8 +569,9 @@ int join_ilog2(int64_t x) {
     return b;
 }
 
+// Ring, B stages, and the drained sums (128 lanes x NQ FP32 pairs).
 size_t join_smem_bytes(const TcJoinArgs& g) {
-    return (size_t)g.ring * g.slot_bytes + (size_t)kJoinQBufs * 2 * join_qtile_bytes(g.nq) + 128;
+    return (size_t)g.ring * g.slot_bytes + (size_t)kJoinQBufs * 2 * join_qtile_bytes(g.nq) + (size_t)128 * g.nq * 8 + 128;
 }
 
 // Slot layout for the copy mode: TMA boxes land densely, bulk segments with 16 bytes of padding
@@ -552,7 +584,7 @@ bool join_layout(TcJoinArgs& a, bool tma) {
     a.segQ_stride = (8 << a.sbQ) + pad;
     a.slotP_bytes = (a.nsegP * a.segP_stride + 127) / 128 * 128;
     a.slot_bytes = a.slotP_bytes + (a.nsegQ * a.segQ_stride + 127) / 128 * 128;
-    const size_t stages = (size_t)kJoinQBufs * 2 * join_qtile_bytes(a.nq);
+    const size_t stages = (size_t)kJoinQBufs * 2 * join_qtile_bytes(a.nq) + (size_t)128 * a.nq * 8;
     a.ring = 0;
     for (int r = kJoinMaxRing; r >= 2 && !a.ring; r--)
         if ((size_t)r * a.slot_bytes + stages <= kJoinSmemCap) a.ring = r;

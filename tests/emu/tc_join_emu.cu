@@ -101,13 +101,13 @@ static bool emulate_block(const TcJoinArgs& g, int64_t bi, int64_t si, std::vect
             memcpy(&v, &slot.at((size_t)byte), 8);
             return v;
         };
-        // the Q splitters: thread tq takes elements tq + 64 m, stores (re, im) words into the B tiles
+        // the Q splitters: thread tq takes elements tq + 128 m, stores (re, im) words into the B tiles
         std::fill(bwritten.begin(), bwritten.end(), 0);
-        for (int tq = 0; tq < 64; tq++)
-            for (int m = 0; m < g.nq; m++) {
-                const int64_t e = tq + 64 * m;
-                const int src = g.slotP_bytes + join_qsrc(g, tq) + join_qsrc(g, 64 * m);
-                const int dst = join_qdst(g, tq) + join_qdst(g, 64 * m);
+        for (int tq = 0; tq < kJoinQThreads; tq++)
+            for (int m = 0; m < g.nq * kJoinKR / kJoinQThreads; m++) {
+                const int64_t e = tq + (int64_t)kJoinQThreads * m;
+                const int src = g.slotP_bytes + join_qsrc(g, tq) + join_qsrc(g, (int64_t)kJoinQThreads * m);
+                const int dst = join_qdst(g, tq) + join_qdst(g, (int64_t)kJoinQThreads * m);
                 if (src != g.slotP_bytes + join_qsrc(g, e) || dst != join_qdst(g, e)) {
                     printf("Q tables do not add\n");
                     return false;
