@@ -66,7 +66,9 @@ constexpr int kJoinMaxRing = 4;                     // raw chunks in the ring
 constexpr int kJoinPGroups = 2;                     // P splitter groups (alternate stages)
 constexpr int kJoinQWarps = 4;                      // Q splitter warps (2, 3 and the last two)
 constexpr int kJoinQThreads = 32 * kJoinQWarps;
-constexpr int kJoinThreads = 32 * (2 + kJoinQWarps + 4 * kJoinPGroups);
+constexpr int kJoinIssuers = 2;                     // MMA issuing threads (alternate stages)
+constexpr int kJoinThreads = 32 * (2 + kJoinQWarps + 4 * kJoinPGroups + (kJoinIssuers - 1));
+static_assert(kJoinIssuers == 2 && kJoinPGroups == 2, "stage parity decides both the issuer and the P group");
 constexpr uint32_t kJoinSleepNs = 2000;             // suspend hint of a barrier poll
 constexpr int kJoinStageCols = 2 * kJoinSub;        // tensor-memory columns of one A stage (32)
 constexpr int kJoinFlushTerms = 128;                // summed terms per FP32 accumulator
@@ -137,7 +139,7 @@ struct JoinShape {
     static constexpr int kQStage = 2 * kQTile;                 // B operand of one MMA stage
     static constexpr int kQLo = (NQ / 8) * 512;                // lo rows NQ + j: NQ / 8 row groups on
     static constexpr uint32_t kAccCols = 2 * NQ;               // columns of one accumulator
-    static constexpr uint32_t kACol0 = 2 * kAccCols;           // first A stage column
+    static constexpr uint32_t kACol0 = 2 * kJoinIssuers * kAccCols;   // first A stage column
     static constexpr uint32_t kNeed = kACol0 + kJoinStages * kJoinStageCols;
     static constexpr uint32_t kCols = kNeed <= 128 ? 128 : (kNeed <= 256 ? 256 : 512);
 };
@@ -159,7 +161,7 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
     // rfull / rempty per ring slot, fullA per A stage, qfull per B stage, sdone per B stage (the
     // MMAs of stage u done: u's B stage and, four stages on, its A stage are free), accf / acce per
     // accumulator, drain
-    __shared__ uint64_t bars[2 * kJoinMaxRing + kJoinStages + 2 * kJoinQBufs + 5];
+    __shared__ uint64_t bars[2 * kJoinMaxRing + kJoinStages + 2 * kJoinQBufs + 4 * kJoinIssuers + 1];
     constexpr int kQPer = NQ * kJoinKR / kJoinQThreads;        // Q elements per splitter thread
     __shared__ int32_t prow[32], pcol[kJoinKR], qsrc_hi[kQPer], qdst_hi[kQPer];
     __shared__ int64_t psegoff[kJoinMaxSeg], qsegoff[kJoinMaxSeg];
@@ -174,9 +176,9 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
     uint64_t* fullA = bars + 2 * kJoinMaxRing;
     uint64_t* qfull = fullA + kJoinStages;
     uint64_t* sdone = qfull + kJoinQBufs;
-    uint64_t* accf = sdone + kJoinQBufs;
-    uint64_t* acce = accf + 2;
-    uint64_t* drain = acce + 2;
+    uint64_t* accf = sdone + kJoinQBufs;    // [issuer][buffer]
+    uint64_t* acce = accf + 2 * kJoinIssuers;
+    uint64_t* drain = acce + 2 * kJoinIssuers;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int* const errw = g.err;
     const uint32_t wl = g.wait_limit ? g.wait_limit : kWaitLimit;
@@ -202,8 +204,8 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
         }
         for (int s = 0; s < kJoinStages; s++) mbar_init(&fullA[s], 4u);
         for (int s = 0; s < kJoinQBufs; s++) { mbar_init(&qfull[s], (uint32_t)kJoinQWarps); mbar_init(&sdone[s], 1u); }
-        for (int j = 0; j < 2; j++) { mbar_init(&accf[j], 1u); mbar_init(&acce[j], 4u); }
-        mbar_init(drain, 1u);
+        for (int j = 0; j < 2 * kJoinIssuers; j++) { mbar_init(&accf[j], 1u); mbar_init(&acce[j], 4u); }
+        mbar_init(drain, (uint32_t)kJoinIssuers);
         abort_flag = 0;
         if (bad) atomicExch(errw, 10);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -287,7 +289,7 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
         if (lane == 0)
             for (int64_t q = issued - 1; q >= 0 && q >= issued - R; q--)
                 mbar_wait(&rfull[q % R], (uint32_t)((q / R) & 1));     // full limit: copies must land
-    } else if (warp == 2 || warp == 3 || warp >= 4 + 4 * kJoinPGroups) {
+    } else if (warp == 2 || warp == 3 || (warp >= 4 + 4 * kJoinPGroups && warp < 4 + 4 * kJoinPGroups + kJoinQWarps - 2)) {
         // Q splitters: a raw chunk at a time; thread tq takes the chunk's elements tq + 128 m (in
         // the slot's order) and stores their split words into the chunk's B stages 4 (c mod 2) ..
         const int tq = (warp < 4 ? warp - 2 : warp - 2 - 4 * kJoinPGroups) * 32 + lane;
@@ -376,43 +378,62 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
         int64_t drained = 0;
         auto drain_acc = [&](int64_t v) -> bool {
             const uint32_t buf = (uint32_t)(v & 1);
-            const bool ok = wait(&accf[buf], (uint32_t)((v >> 1) & 1));
+            bool ok = true;
+            for (int k = 0; k < kJoinIssuers && ok; k++) ok = wait(&accf[2 * k + buf], (uint32_t)((v >> 1) & 1));
             fence_after();
             if (!__all_sync(0xffffffffu, ok)) {
                 if (lane == 0) give_up(16);
                 return false;
             }
-            const uint32_t d0 = lane_base + buf * S::kAccCols;
+            // the issuers' accumulators of this interval (hi and lo rows of Q) summed in FP32
+            auto col = [&](int k, uint32_t c) { return lane_base + (uint32_t)(2 * k + buf) * S::kAccCols + c; };
             if constexpr (NQ >= 16) {
 #pragma unroll
                 for (int j0 = 0; j0 < NQ; j0 += 16) {
-                    uint32_t hi[16], lo16[16];
-                    tmem_ld16(d0 + j0, hi);
-                    tmem_ld16(d0 + NQ + j0, lo16);
-                    tmem_wait_ld();
+                    float x[16];
+#pragma unroll
+                    for (int j = 0; j < 16; j++) x[j] = 0.f;
+#pragma unroll
+                    for (int k = 0; k < kJoinIssuers; k++) {
+                        uint32_t hi[16], lo16[16];
+                        tmem_ld16(col(k, j0), hi);
+                        tmem_ld16(col(k, NQ + j0), lo16);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int j = 0; j < 16; j++) x[j] += __uint_as_float(hi[j]) + __uint_as_float(lo16[j]);
+                    }
 #pragma unroll
                     for (int j = 0; j < 16; j++)
                         if (j0 + j < NQ) {
                             float2 a = accs[(j0 + j) * 32];
-                            two_sum(a, __uint_as_float(hi[j]) + __uint_as_float(lo16[j]));
+                            two_sum(a, x[j]);
                             accs[(j0 + j) * 32] = a;
                         }
                 }
             } else {
-                uint32_t w[16];             // hi columns 0 .. NQ-1, lo columns NQ .. 2NQ-1
-                tmem_ld16(d0, w);
-                tmem_wait_ld();
+                float x[NQ];
+#pragma unroll
+                for (int j = 0; j < NQ; j++) x[j] = 0.f;
+#pragma unroll
+                for (int k = 0; k < kJoinIssuers; k++) {
+                    uint32_t w[16];         // hi columns 0 .. NQ-1, lo columns NQ .. 2NQ-1
+                    tmem_ld16(col(k, 0), w);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < NQ; j++) x[j] += __uint_as_float(w[j]) + __uint_as_float(w[NQ + j]);
+                }
 #pragma unroll
                 for (int j = 0; j < NQ; j++) {
                     float2 a = accs[j * 32];
-                    two_sum(a, __uint_as_float(w[j]) + __uint_as_float(w[NQ + j]));
+                    two_sum(a, x[j]);
                     accs[j * 32] = a;
                 }
             }
-            // the accumulator may be overwritten once all four warps' loads have completed
+            // the accumulators may be overwritten once all four warps' loads have completed
             fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&acce[buf]);
+            if (lane == 0)
+                for (int k = 0; k < kJoinIssuers; k++) mbar_arrive(&acce[2 * k + buf]);
             return true;
         };
         bool ok_all = true;
@@ -495,16 +516,17 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
                 if (lane == 0 && emax != kExpUnset) atomicMax(&exps[2 * g.expC + 1], emax);
             }
         }
-    } else if (warp == 0 && lane == 0) {
-        // MMA issuer
+    } else if (lane == 0 && (warp == 0 || warp >= kJoinThreads / 32 - (kJoinIssuers - 1))) {
+        // MMA issuer k takes the stages u = k mod kJoinIssuers into its own two accumulators
+        const int k = warp == 0 ? 0 : warp - (kJoinThreads / 32 - kJoinIssuers);
         const int64_t fm = fmask;
-        for (int64_t u = 0; u < U; u++) {
+        for (int64_t u = k; u < U; u += kJoinIssuers) {
             const int64_t v = u >> fsh;
             const uint32_t buf = (uint32_t)(v & 1);
             const int st = (int)(u & (kJoinStages - 1));
-            const bool first = (u & fm) == 0;
+            const bool first = (u & fm) == k;
             if (first) {
-                if (!wait(&acce[buf], (uint32_t)((v >> 1) & 1) ^ 1u)) { give_up(14); break; }
+                if (!wait(&acce[2 * k + buf], (uint32_t)((v >> 1) & 1) ^ 1u)) { give_up(14); break; }
                 fence_after();
             }
             if (!wait(&fullA[st], (uint32_t)((u >> 2) & 1)) ||
@@ -513,7 +535,7 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
                 break;
             }
             fence_after();
-            const uint32_t d = tmem + buf * S::kAccCols;
+            const uint32_t d = tmem + (uint32_t)(2 * k + buf) * S::kAccCols;
             const uint32_t ta = tmem + S::kACol0 + (uint32_t)st * kJoinStageCols;
             const uint32_t qb = smem_u32(qst + (size_t)(u & (kJoinQBufs - 1)) * S::kQStage);
 #pragma unroll
@@ -522,7 +544,7 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
                 mma_ts<true>(d, ta + ks * 8, db, g.idesc, (first && ks == 0) ? 0u : 1u);
             }
             mma_commit(&sdone[u & (kJoinQBufs - 1)]);
-            if ((u & fm) == fm || u + 1 == U) mma_commit(&accf[buf]);
+            if ((u & fm) == fm - (kJoinIssuers - 1) + k || u + kJoinIssuers >= U) mma_commit(&accf[2 * k + buf]);
         }
         // the MMAs must have finished before the tensor memory is freed
         mma_commit(drain);
