@@ -121,10 +121,11 @@ constexpr int kJoinMaxSeg = 256;    // contiguous segments per operand in a raw 
 
 // One operand's raw tile as a TMA tensor box: dimension 0 is contiguous with extent 2^H (H the
 // operand's lowest batch bit), so its coordinate carries the chunk's offset; the tile's other
-// runs of address bits follow (coordinate 0, box = extent); the batch bits are dimension tb (box 1,
-// coordinate = batch index).  The box lands in shared memory in the tile's address order.
+// runs of address bits follow (coordinate 0, box = extent); the batch bits, contiguous from bit H
+// in any order, are dimension tb (box 1, coordinate = the operand's batch offset >> H).  The box
+// lands in shared memory in the tile's address order.
 struct JoinBox {
-    int32_t td, tb;                 // dimensions used (<= 5); the batch dimension (-1: none)
+    int32_t td, tb, th;             // dimensions used (<= 5); the batch dimension (-1: none); H
     int64_t dim[5], stride[5];      // extents and strides, in elements (stride[0] = 1)
     int32_t box[5];
 };

@@ -75,6 +75,8 @@ constexpr int kJoinFlushTerms = 128;                // summed terms per FP32 acc
 constexpr int kJoinChunkBits = 48;                  // delta-table entries (chunk index bits)
 constexpr size_t kJoinSmemCap = 200 * 1024;         // ring + B stages (one CTA per SM)
 constexpr int kJoinPadBytes = 16;                   // padding after each bulk segment and each B tile
+constexpr int kJoinMaxBulkSegs = 96;                // bulk segments per chunk above which the join declines
+                                                    // (each cp.async.bulk costs ~70 cycles of the loader)
 
 // Byte of tile element e inside a slot: segment e >> sb, element e mod 2^sb.
 __host__ __device__ __forceinline__ int join_slot_byte(int64_t e, int sb, int stride) {
@@ -264,10 +266,10 @@ __global__ void __launch_bounds__(kJoinThreads, 1)
             if (g.tma) {
                 if (lane == 0) {
                     int co[5] = {(int)chP, 0, 0, 0, 0};
-                    if (g.boxP.tb >= 0) co[g.boxP.tb] = (int)bi;
+                    if (g.boxP.tb >= 0) co[g.boxP.tb] = (int)(bP0 >> g.boxP.th);
                     tma_load_5d(dst, &mapP, co, &rfull[slot]);
                     int cq[5] = {(int)chQ, 0, 0, 0, 0};
-                    if (g.boxQ.tb >= 0) cq[g.boxQ.tb] = (int)bi;
+                    if (g.boxQ.tb >= 0) cq[g.boxQ.tb] = (int)(bQ0 >> g.boxQ.th);
                     tma_load_5d(dst + g.slotP_bytes, &mapQ, cq, &rfull[slot]);
                 }
             } else {
@@ -614,14 +616,16 @@ bool join_layout(TcJoinArgs& a, bool tma) {
 }
 
 // One operand's tile (address positions `tile`, ascending, the lowest run starting at bit 0) as a
-// TMA box, when its batch bits (positions `batch`, in batch-index order) are contiguous above every
-// other bit of the operand (maxnb: the highest non-batch position) and five dimensions suffice.
-bool join_box(const std::vector<int>& tile, const std::vector<int>& batch, int maxnb, JoinBox* b) {
+// TMA box, when its batch bits (positions `batch`) are contiguous above every other bit of the
+// operand (maxnb: the highest non-batch position) and five dimensions suffice.
+bool join_box(const std::vector<int>& tile, std::vector<int> batch, int maxnb, JoinBox* b) {
     memset(b, 0, sizeof(*b));
+    std::sort(batch.begin(), batch.end());
     const int H = batch.empty() ? maxnb + 1 : batch[0];
     for (size_t i = 0; i < batch.size(); i++)
         if (batch[i] != H + (int)i) return false;
     if (maxnb >= H || H > 31) return false;
+    b->th = H;
     std::vector<std::pair<int, int>> runs;  // (position, length)
     for (int p : tile) {
         if (!runs.empty() && runs.back().first + runs.back().second == p) runs.back().second++;
@@ -791,6 +795,9 @@ bool tc_join_plan(const StepArgs& s, int sm_count, TcJoinArgs* out, int min_log2
             return join_box(tile, batch, maxnb, b);
         };
         const bool tma = box_of(cP, fP, posP, &a.boxP) && box_of(cQ, fQ, posQ, &a.boxQ);
+        // without boxes the loader issues one bulk copy per segment: many small ones are slower
+        // than the batched small GEMM
+        if (!tma && a.nsegP + a.nsegQ > kJoinMaxBulkSegs) return false;
         if (!join_layout(a, tma)) return false;
     }
     a.run_p = 1 << sbP;

@@ -65,7 +65,7 @@ static bool emulate_block(const TcJoinArgs& g, int64_t bi, int64_t si, std::vect
         };
         auto copy_box = [&](const float2* src, const JoinBox& bx, int64_t chunk_off, bool p) {
             int co[5] = {(int)chunk_off, 0, 0, 0, 0};
-            if (bx.tb >= 0) co[bx.tb] = (int)bi;
+            if (bx.tb >= 0) co[bx.tb] = (int)((p ? bP0 : bQ0) >> bx.th);
             if ((co[0] * 8) % 16 != 0) { printf("TMA x coordinate not 16-byte aligned\n"); return false; }
             int64_t n = 1;
             for (int d = 0; d < bx.td; d++) n *= bx.box[d];

@@ -215,15 +215,25 @@ def test_batched_join_gemm(q, gpu_lib, precision, nk, na, nb, ng):
 
 
 def join_programme(q, nk, na, nb, ng, seed, batch_on_top=True):
-    """One ncon of the final-join shape; the batch labels last in both operands (the highest
-    address bits, as the programme's layout rule places them in intermediates), the others in a
-    seeded random order.  Returns the programme and the einsum result."""
+    """One ncon of the final-join shape, laid out so a raw chunk of the tensor-core join is a TMA
+    box: in each operand six summed labels first (the same six in both, in each operand's own
+    seeded order), then the free labels in one or two blocks around three other summed labels,
+    then the remaining summed labels, and the batch labels last (the highest address bits, as the
+    programme's layout rule places them in intermediates).  With batch_on_top=False every label is
+    in a random place.  Returns the programme and the einsum result."""
     rng = np.random.default_rng(seed)
     kl = list(range(1, nk + 1))
     al, bl, gl = list(range(100, 100 + na)), list(range(200, 200 + nb)), list(range(300, 300 + ng))
     if batch_on_top:
-        la = [int(v) for v in rng.permutation(al + kl)] + [int(v) for v in rng.permutation(gl)]
-        lb = [int(v) for v in rng.permutation(bl + kl)] + [int(v) for v in rng.permutation(gl)]
+        perm = lambda xs: [int(v) for v in rng.permutation(xs)] if xs else []
+        ks = perm(kl)
+        first, rest = ks[:6], ks[6:]
+
+        def lay(free):
+            f, r = perm(free), perm(rest)
+            split = int(rng.integers(1, len(free) + 1))
+            return perm(first) + f[:split] + r[:3] + f[split:] + r[3:] + perm(gl)
+        la, lb = lay(al), lay(bl)
     else:
         la = [int(v) for v in rng.permutation(al + gl + kl)]
         lb = [int(v) for v in rng.permutation(bl + gl + kl)]
@@ -255,7 +265,7 @@ def test_tensor_core_join(q, gpu_lib, nk, na, nb, ng):
         got = ex.amplitudes([""])[0]
         got2 = ex.amplitudes([""])[0]
         desc = ex.explain(2)
-        assert "tensor-core join" in desc, desc
+        assert "tensor-core join" in desc and "copies=tma" in desc, desc
         assert ex.info()["num_steps_tensor_core"] == 1
     with q.Executor(prog, precision="split_tf32", cuda_core_joins=True) as ex:
         cc = ex.amplitudes([""])[0]
