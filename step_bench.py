@@ -13,6 +13,12 @@ highest row bits to shrink a case (for profiler captures).
 
 Prints one JSON line per case: milliseconds per call and the algorithmic bandwidth
 8 (|X| + |Y| + |C|) bytes / time.
+
+Final joins run only inside programmes (the tensor-core join is chosen by the programme compiler):
+`--programme` times the JOINS cases as one-ncon split-TF32 programmes through the executor (the
+step's own time from the executor's profile), `--cuda-core-joins` on the batched small GEMM.
+
+    python step_bench.py join7x7 --programme [--cuda-core-joins] [--reps 5]
 """
 from __future__ import annotations
 
@@ -40,6 +46,53 @@ CASES = {
     # 6x6, 14 cycles: 64 x 16 results per batch value, 2^16 summed (2^22 in a pass), 2^5 batch values
     "join_6x6": ("kbbbbbrkkkrrrkkrrkkkkkkkkkk", "kkkkknnnnrrrrrkkkkkkkkkkk", "bbbbbrrrrrrnnnn"),
 }
+
+
+# Final joins (programme mode): A's, B's and C's index bits from the lowest address bit, as named
+# in qxg_program_explain (k summed, m free in A, n free in B, b batch).
+_K = ["k%d" % i for i in range(17)]
+JOINS = {
+    # the 7x7 stand-in's final join (2^17 summed terms, 32 x 32 results per batch value) with 2^5
+    # of its 2^11 batch values: 1 GiB per operand
+    "join7x7": (_K[:14] + ["m0", "k14", "m1", "m2", "k15", "m3", "m4", "k16"] + ["b%d" % i for i in range(5)],
+                "k3,k4,k13,n0,n1,k2,k1,k11,n2,n3,k16,k0,n4,k12,k5,k6,k15,k8,k14,k7,k10,k9".split(",")
+                + ["b%d" % i for i in range(5)],
+                ["m%d" % i for i in range(5)] + ["n%d" % i for i in range(5)] + ["b%d" % i for i in range(5)]),
+}
+
+
+def run_join(name: str, reps: int, cuda_core_joins: bool):
+    """One JOINS case as a one-ncon split-TF32 programme: milliseconds per call of the step."""
+    from collections import OrderedDict
+    import __graft_entry__ as entry
+    q = entry.load()
+    a_bits, b_bits, c_bits = JOINS[name]
+    lab = {n: i + 1 for i, n in enumerate(sorted(set(a_bits) | set(b_bits)))}
+    rng = np.random.default_rng(1)
+
+    def rnd(n):
+        x = rng.standard_normal(2 ** n, dtype=np.float32) + 1j * rng.standard_normal(2 ** n, dtype=np.float32)
+        return x.astype(np.complex128).reshape((2,) * n)
+    A, B = rnd(len(a_bits)), rnd(len(b_bits))
+    cmds = [q.Load("a", "data_1", A.shape), q.Load("b", "data_2", B.shape),
+            q.Ncon("c", tuple(lab[x] for x in c_bits), "a", tuple(lab[x] for x in a_bits), "b",
+                   tuple(lab[x] for x in b_bits)), q.Save("output", "c")]
+    prog = q.Programme.from_commands(cmds, OrderedDict([("data_1", A), ("data_2", B)]), 0)
+    del A, B
+    nbytes = 8 * (2 ** len(a_bits) + 2 ** len(b_bits) + 2 ** len(c_bits))
+    with q.Executor(prog, precision="split_tf32", cuda_core_joins=cuda_core_joins) as ex:
+        ex.amplitudes([""])
+        form = ex.explain(2)
+        best = None
+        for _ in range(reps):
+            ex.profile(True)                # clears the records of the previous call
+            ex.amplitudes([""])
+            rows, _ = ex.profile_read()
+            ms = sum(r["ms"] for r in rows if r["instr"] == 2)
+            best = ms if best is None else min(best, ms)
+        ex.profile(False)
+    print(json.dumps({"case": name, "programme": True, "form": form.split(" c_bits=")[0], "ms": round(best, 4),
+                      "gb_s": round(nbytes / best / 1e6, 1)}), flush=True)
 
 
 def labels(x: str, y: str, c: str, drop: int):
@@ -91,7 +144,13 @@ def main():
     ap.add_argument("--drop", type=int, default=0)
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--lib", default=str(HERE / "qxtools.jl_gb300" / "_build" / "libqxgpu.so"))
+    ap.add_argument("--programme", action="store_true", help="JOINS cases through the executor")
+    ap.add_argument("--cuda-core-joins", action="store_true", help="programme mode: the batched small GEMM")
     args = ap.parse_args()
+    if args.programme:
+        for name in args.cases.split(","):
+            run_join(name, args.reps, args.cuda_core_joins)
+        return
     import torch
     lib = ct.CDLL(args.lib)
     P = ct.c_void_p
