@@ -829,6 +829,26 @@ __global__ void leaf_grad_kernel(const LeafGradArgs a, const int* exps) {
     }
 }
 
+// Every leaf's gradient in one launch: block b adds leaf tab[b]'s adjoint into grad + 2 goff.
+template <typename T>
+__global__ void leaf_grad_batch_kernel(const LeafGradArgs* __restrict__ tab, double* grad, const int* exps) {
+    const LeafGradArgs& a = tab[blockIdx.x];
+    const T* __restrict__ S = static_cast<const T*>(a.sbar);
+    const double scale = exps ? pow2d(exps[2 * a.exp_s]) : 1.0;
+    double* gp = grad + 2 * a.goff;
+    for (int64_t i = threadIdx.x; i < a.n; i += blockDim.x) {
+        int64_t rem = i, off = 0, st = 1;
+        for (int d = 0; d < a.rank; d++) {
+            off += (rem % a.dims[d]) * st;
+            rem /= a.dims[d];
+            st *= a.pdims[d];
+        }
+        const T v = S[off];
+        gp[2 * i] += (double)v.x * scale;
+        gp[2 * i + 1] += (double)v.y * scale;
+    }
+}
+
 __global__ void reset_exps_kernel(int* exps, int begin, int end) {
     for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
         exps[2 * i] = 0;
@@ -1283,6 +1303,14 @@ cudaError_t launch_leaf_grad(const LeafGradArgs& a, bool fp64, const int* exps, 
     const int g = grid_for(a.n, 256, 1024);
     if (fp64) leaf_grad_kernel<double2><<<g, 256, 0, s>>>(a, exps);
     else leaf_grad_kernel<float2><<<g, 256, 0, s>>>(a, exps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_grads(const LeafGradArgs* d_tab, int n, double* grad, bool fp64, const int* exps,
+                              cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (fp64) leaf_grad_batch_kernel<double2><<<n, 64, 0, s>>>(d_tab, grad, exps);
+    else leaf_grad_batch_kernel<float2><<<n, 64, 0, s>>>(d_tab, grad, exps);
     return cudaGetLastError();
 }
 

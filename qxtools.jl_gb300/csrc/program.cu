@@ -128,7 +128,12 @@ struct Plan {
     std::vector<Batch> batches[4];
     std::vector<std::pair<int, int>> order[4];
     BatchStep* d_batch = nullptr;       // device copies of the batched steps' arguments
-    ~Plan() { if (d_batch) cudaFree(d_batch); }
+    LeafGradArgs* d_leaf = nullptr;     // device copies of the leaf-gradient steps' arguments
+    int nleaf = 0;                      // (one launch adds every leaf's gradient)
+    ~Plan() {
+        if (d_batch) cudaFree(d_batch);
+        if (d_leaf) cudaFree(d_leaf);
+    }
 };
 
 }  // namespace
@@ -1427,7 +1432,10 @@ int plan_batches(qxg_program* P, Plan& pl) {
             top = std::max(top, level[j]);
         }
         std::vector<std::vector<int>> at(top + 1);
-        for (int j = 0; j < n; j++) at[level[j]].push_back(j);
+        // the leaf gradients are the list's last steps (their adjoints live to its end): one
+        // launch after every other step, not one per leaf
+        for (int j = 0; j < n; j++)
+            if (steps[j].bkind != kBwdLeaf) at[level[j]].push_back(j);
         for (auto& lv : at) {
             std::vector<int> small;
             for (int j : lv)
@@ -1465,6 +1473,20 @@ int plan_batches(qxg_program* P, Plan& pl) {
     if (!host.empty()) {
         QXG_CUDA(cudaMalloc(&pl.d_batch, sizeof(BatchStep) * host.size()));
         QXG_CUDA(cudaMemcpy(pl.d_batch, host.data(), sizeof(BatchStep) * host.size(), cudaMemcpyHostToDevice));
+    }
+    std::vector<LeafGradArgs> leaves;
+    for (const Step& st : pl.bsteps)
+        if (st.bkind == kBwdLeaf) {
+            LeafGradArgs la = st.largs;
+            la.goff = st.goff;
+            leaves.push_back(la);
+        }
+    if (pl.d_leaf) cudaFree(pl.d_leaf);
+    pl.d_leaf = nullptr;
+    pl.nleaf = (int)leaves.size();
+    if (!leaves.empty()) {
+        QXG_CUDA(cudaMalloc(&pl.d_leaf, sizeof(LeafGradArgs) * leaves.size()));
+        QXG_CUDA(cudaMemcpy(pl.d_leaf, leaves.data(), sizeof(LeafGradArgs) * leaves.size(), cudaMemcpyHostToDevice));
     }
     return 0;
 }
@@ -1676,6 +1698,18 @@ int run_grad_passes(qxg_program* P, int nbits, int64_t s0, int64_t s1, double* d
             w.push_back(std::move(x));
         }
         append_list_works(P, pl, 3, exps, w, [&bwd_step](Step& st, cudaStream_t s) { return bwd_step(st, s); });
+        if (pl.nleaf > 0) {
+            Work x;
+            x.launch = [&](cudaStream_t s) -> int {
+                size_t ev = 0;
+                if (int r = prof_begin(P, &ev)) return r;
+                QXG_CUDA(launch_leaf_grads(pl.d_leaf, pl.nleaf, d_grad, P->fp64, exps, s));
+                return prof_end(P, ev, -1, QXG_KERNEL_REDUCE, 0.0, 0.0);
+            };
+            for (const Step& st : pl.bsteps)
+                if (st.bkind == kBwdLeaf) add_step_spans(P, pl, st, x);
+            w.push_back(std::move(x));
+        }
         return launch_works(P, w);
     };
     // with use_graphs (outside profiling) the pass is captured on its second run with the same

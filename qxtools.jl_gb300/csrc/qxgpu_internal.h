@@ -115,6 +115,7 @@ struct LeafGradArgs {
     int32_t rank;
     int32_t dims[16], pdims[16];
     int32_t exp_s;
+    int64_t goff;              // batched launch: complex offset of this leaf in the gradient vector
 };
 
 // Materialise a view of a leaf/output tensor for a batch of slices.
@@ -197,6 +198,9 @@ cudaError_t launch_reset_exps(int* exps, int begin, int end, cudaStream_t s);
 cudaError_t launch_seed(const SeedArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_view_adjoint(const ViewAdjArgs& a, bool fp64, int* exps, cudaStream_t s);
 cudaError_t launch_leaf_grad(const LeafGradArgs& a, bool fp64, const int* exps, cudaStream_t s);
+// All n leaves of a device table in one launch (leaf b into grad + 2 tab[b].goff).
+cudaError_t launch_leaf_grads(const LeafGradArgs* d_tab, int n, double* grad, bool fp64, const int* exps,
+                              cudaStream_t s);
 
 // Exponent slots: exps[2*i] = e (true value = stored * 2^e), exps[2*i+1] = m (max stored
 // exponent, atomically raised by the producer).

@@ -417,6 +417,8 @@ class Executor:
 
     def leaf_slices(self) -> dict:
         """instruction index of each `load` -> (offset, shape) of its gradient in the flat vector."""
+        if getattr(self, "_leaf_layout", None) is not None:
+            return self._leaf_layout
         out, o = {}, 0
         for i, r in enumerate(self.programme.instrs):
             if int(r[0]) == QXG_OP["load"]:
@@ -424,12 +426,14 @@ class Executor:
                 out[i] = (o, shape)
                 o += int(np.prod(shape)) if shape else 1
         self._gsize = o
+        self._leaf_layout = out
         return out
 
-    def gradient(self, bitstrings, amp_bar=None, slices=None):
+    def gradient(self, bitstrings, amp_bar=None, slices=None, flat=False):
         """Reverse-mode gradient (qxg_gradient): returns (amplitudes (n, out_size), {instruction
         index of each load: dL/d conj(leaf) as an array of the leaf's shape}).  amp_bar = dL/d
-        conj(amplitude) per bitstring, shape (n, out_size); None -> L = sum |amplitude|^2."""
+        conj(amplitude) per bitstring, shape (n, out_size); None -> L = sum |amplitude|^2.
+        flat=True returns the gradients as the one complex vector that leaf_slices() indexes."""
         if isinstance(bitstrings, str):
             bitstrings = [bitstrings]
         bitstrings = list(bitstrings)
@@ -448,8 +452,11 @@ class Executor:
         _check(self.lib, self.lib.qxg_gradient(self._h, buf, n, s0, s1, ab.ctypes.data_as(D) if ab is not None else None,
                                                out.ctypes.data_as(D), grads.ctypes.data_as(D)))
         g = grads.view(np.complex128)
+        amps = out.view(np.complex128).reshape(n, info["output_size"])
+        if flat:
+            return amps, g
         leaf = {i: g[o:o + (int(np.prod(s)) if s else 1)].reshape(s, order="F") for i, (o, s) in lay.items()}
-        return out.view(np.complex128).reshape(n, info["output_size"]), leaf
+        return amps, leaf
 
     def amplitudes_device(self, d_bitstrings_ptr: int, n: int, d_out_ptr: int, slices=None):
         """Enqueue on the programme's stream with device-resident inputs/outputs (no sync)."""

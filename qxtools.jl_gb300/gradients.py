@@ -83,14 +83,27 @@ class ParametrisedCircuitLoss:
                 full = dm.reshape(shape, order="F")
                 self.terms.append((pid, instr, self.tnc.tn.reduced_data(name, full)))
         self.num_params = circ.num_params
+        # the chain rule as one gather over the flat gradient vector: element idx[e] of the leaf
+        # gradients times dT/dtheta (column-major, as the leaves are laid out), added into parameter
+        # pid[e]
+        lay = self.executor.leaf_slices()
+        idx, dtv, pid = [], [], []
+        for p, instr, dt in self.terms:
+            o, shape = lay[instr]
+            n = int(np.prod(shape)) if shape else 1
+            idx.append(np.arange(o, o + n))
+            dtv.append(np.asarray(dt, dtype=np.complex128).reshape(-1, order="F"))
+            pid.append(np.full(n, p))
+        self._gidx = np.concatenate(idx) if idx else np.zeros(0, dtype=np.int64)
+        self._gdt = np.concatenate(dtv) if dtv else np.zeros(0, dtype=np.complex128)
+        self._gpid = np.concatenate(pid) if pid else np.zeros(0, dtype=np.int64)
 
     def loss_and_grad(self, bitstrings, slices=None):
-        amps, leaf = self.executor.gradient(bitstrings, amp_bar=None if slices is None else None, slices=slices)
+        amps, gvec = self.executor.gradient(bitstrings, slices=slices, flat=True)
         loss = float(np.sum(np.abs(amps) ** 2))
         # L = sum |a|^2 with amp_bar = a; dL/dtheta = 2 Re sum conj(dL/d conj T) dT/dtheta
-        g = np.zeros(self.num_params)
-        for pid, instr, dt in self.terms:
-            g[pid] += 2.0 * float(np.real(np.sum(np.conj(leaf[instr]) * dt)))
+        w = 2.0 * np.real(np.conj(gvec[self._gidx]) * self._gdt)
+        g = np.bincount(self._gpid, weights=w, minlength=self.num_params)[: self.num_params]
         return loss, g, amps
 
     def loss(self, bitstrings) -> float:
