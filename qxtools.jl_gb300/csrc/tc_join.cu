@@ -18,7 +18,7 @@
 // tensor-memory lane 32 q + 8 r + (i mod 8) with q = i / 8, so the warp that owns lanes
 // 32 q .. 32 q + 31 holds all four roles of eight free values.
 //
-// One CTA (14 warps) per (batch value, K range):
+// One CTA (15 warps) per (batch value, K range):
 //   warp 1         loader: per raw chunk of 64 summed terms, the chunk's P tile (32 x 64) and Q
 //                  tile (NQ x 64) land in a ring slot in each operand's address order: one TMA
 //                  tensor copy per operand (the tile's runs of address bits as box dimensions),
@@ -28,19 +28,22 @@
 //   warps 4-11     P splitters, two groups on alternate MMA stages (16 summed terms each): warp
 //                  4 + 4 g + q reads the stage's terms for its eight free values from the slot,
 //                  splits them into the four roles and stores 32 columns of its lanes with
-//                  tcgen05.st.  Group 0 also drains: every `flush` stages (128 terms) the MMA
-//                  issuer commits one accumulator and switches to the other; group 0 adds each
-//                  committed accumulator (h = hi and lo summed in FP32) into FP32 register pairs
-//                  before the stage that reuses it, so the FP32 sums never run over more than 128
-//                  terms, and at the end combines the four roles with shuffles and writes C (or
-//                  its FP64 partial, added in K-range order by tc_join_reduce_kernel);
+//                  tcgen05.st.  Group 0 also drains: every `flush` stages (128 terms) each MMA
+//                  issuer commits one of its accumulators and switches to the other; group 0
+//                  adds the committed accumulators (h = hi and lo summed in FP32) into FP32 pairs
+//                  in shared memory (Knuth's TwoSum) before the stage that reuses them, so the
+//                  FP32 sums never run over more than 128 terms, and at the end combines the four
+//                  roles with shuffles and writes C (or its FP64 partial, added in K-range order
+//                  by tc_join_reduce_kernel);
 //   warps 2-3, 12-13  Q splitters: a whole raw chunk at a time, each thread reading elements in the
 //                  slot's order (consecutive threads, consecutive elements) and storing their
 //                  four split words into the chunk's eight B tiles (K-major core matrices, 64-byte
 //                  rows: real parts in core columns 0-1, imaginary in 2-3; the tiles 16 bytes
 //                  apart in bank position), two chunks of B stages in flight;
-//   warp 0 lane 0  MMA issuer: four tcgen05.mma (kind::tf32, A from tensor memory) per stage and
-//                  one commit, whose barrier frees the stage's B buffer and, four stages on, its A stage.
+//   warps 0, 14    MMA issuers, lane 0 of each on alternate stages into its own two accumulators
+//                  (a thread issues about one small MMA per 200 cycles): four tcgen05.mma
+//                  (kind::tf32, A from tensor memory) per stage and one commit, whose barrier frees
+//                  the stage's B buffer and, four stages on, its A stage.
 // Waiting warps sleep in their barrier polls (a suspend-time hint), so they leave the issue slots
 // to the splitters.
 // Every wait is bounded; a wait that gives up writes its code to the programme's error word, the
