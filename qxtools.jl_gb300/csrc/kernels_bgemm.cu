@@ -22,8 +22,8 @@
 //     complex multiply-add is two paired FMAs (fma.rn.f32x2) on one 16-byte read of each
 //     (two quadruple buffers, one barrier per chunk).  The ring keeps tens of KB per SM in flight
 //     without holding registers, which the step needs to reach HBM speed;
-//   * every thread sums at most kFlushK terms in FP32 before adding them into FP64
-//     accumulators, so the error does not grow with K (the long-sum kernel's rule);
+//   * every thread sums at most kFlushK terms in FP32 before adding them into FP32 TwoSum pairs
+//     (about 48 bits, no FP64 pipe), so the error does not grow with K (the long-sum kernel's rule);
 //   * with one K range per batch value the block writes C directly; otherwise it writes FP64
 //     partials and bgemm_reduce_kernel adds them in range order (deterministic).
 // Blocks are numbered batch value first, so blocks running side by side read neighbouring batch
@@ -163,14 +163,22 @@ __host__ __device__ __forceinline__ void bgemm_chunk(const float4* as, const flo
             for (int j = 0; j < S.tn; j++) fma2(acc[i][j], qa[i].y, qb[j].y);
     }
 }
+// Knuth's TwoSum: (h, l) accumulates the flushed FP32 sums as an unevaluated pair (about 48 bits)
+// without the FP64 pipe, which GB300 runs at a small fraction of FP32.
+__host__ __device__ __forceinline__ void bgemm_two_sum(float& h, float& l, float x) {
+    const float t = h + x, bp = t - h;
+    l += (h - (t - bp)) + (x - bp);
+    h = t;
+}
+// dacc = (re hi, re lo, im hi, im lo)
 template <int TM, int TN>
-__host__ __device__ __forceinline__ void bgemm_flush(unsigned long long (&acc)[TM][TN], double2 (&dacc)[TM][TN]) {
+__host__ __device__ __forceinline__ void bgemm_flush(unsigned long long (&acc)[TM][TN], float4 (&dacc)[TM][TN]) {
 #pragma unroll
     for (int i = 0; i < TM; i++)
 #pragma unroll
         for (int j = 0; j < TN; j++) {
-            dacc[i][j].x += (double)u2f((unsigned)acc[i][j]);
-            dacc[i][j].y += (double)u2f((unsigned)(acc[i][j] >> 32));
+            bgemm_two_sum(dacc[i][j].x, dacc[i][j].y, u2f((unsigned)acc[i][j]));
+            bgemm_two_sum(dacc[i][j].z, dacc[i][j].w, u2f((unsigned)(acc[i][j] >> 32)));
             acc[i][j] = 0ull;
         }
 }
@@ -261,13 +269,13 @@ __global__ void __launch_bounds__(bgemm_shape(M, N).nthr, bgemm_shape(M, N).nthr
         for (int j = 0; j < S.lb; j++) bs[slotB[j]] = bgemm_quad_b(r[(S.la + j) * NT], sb, sbi);
     };
     unsigned long long acc[S.tm][S.tn];
-    double2 dacc[S.tm][S.tn];
+    float4 dacc[S.tm][S.tn];
 #pragma unroll
     for (int i = 0; i < S.tm; i++)
 #pragma unroll
         for (int j = 0; j < S.tn; j++) {
             acc[i][j] = 0ull;
-            dacc[i][j] = make_double2(0.0, 0.0);
+            dacc[i][j] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
     for (int c = 0; c < R - 1; c++) issue(c);
@@ -286,7 +294,7 @@ __global__ void __launch_bounds__(bgemm_shape(M, N).nthr, bgemm_shape(M, N).nthr
         for (int i = 0; i < S.tm; i++)
 #pragma unroll
             for (int j = 0; j < S.tn; j++) {
-                const float2 v = make_float2((float)dacc[i][j].x, (float)dacc[i][j].y);
+                const float2 v = make_float2(dacc[i][j].x + dacc[i][j].y, dacc[i][j].z + dacc[i][j].w);
                 g.C[bgemm_c_offset(g, bi, tm * S.tm + i, tn * S.tn + j)] = v;
                 const float mx = fmaxf(fabsf(v.x), fabsf(v.y));
                 if (SCALED && mx > 0.f) emax = max(emax, exp_of(mx));
@@ -303,7 +311,9 @@ __global__ void __launch_bounds__(bgemm_shape(M, N).nthr, bgemm_shape(M, N).nthr
 #pragma unroll
         for (int i = 0; i < S.tm; i++)
 #pragma unroll
-            for (int j = 0; j < S.tn; j++) p[(tm * S.tm + i) * N + tn * S.tn + j] = dacc[i][j];
+            for (int j = 0; j < S.tn; j++)
+                p[(tm * S.tm + i) * N + tn * S.tn + j] =
+                    make_double2((double)dacc[i][j].x + (double)dacc[i][j].y, (double)dacc[i][j].z + (double)dacc[i][j].w);
     }
 }
 

@@ -283,9 +283,9 @@ void emulate_bgemm(const BGemmArgs& g, std::vector<double2>& partial) {
         const int64_t bi = blk % g.nbatch, si = blk / g.nbatch;
         std::vector<float4> As((size_t)2 * S.kc * S.ra), Bs((size_t)2 * S.kc * S.rb);
         std::vector<std::array<unsigned long long, TM * TN>> acc(nthr);
-        std::vector<std::array<double2, TM * TN>> dacc(nthr);
+        std::vector<std::array<float4, TM * TN>> dacc(nthr);
         for (int t = 0; t < nthr; t++)
-            for (int q = 0; q < TM * TN; q++) { acc[t][q] = 0ull; dacc[t][q] = make_double2(0, 0); }
+            for (int q = 0; q < TM * TN; q++) { acc[t][q] = 0ull; dacc[t][q] = make_float4(0, 0, 0, 0); }
         int64_t wa = bgemm_base_a(g, bi, si, 0), wb = bgemm_base_b(g, bi, si, 0);
         for (int64_t c = 0; c < g.nchunks; c++) {
             const int buf = (int)(c & 1);
@@ -320,7 +320,7 @@ void emulate_bgemm(const BGemmArgs& g, std::vector<double2>& partial) {
                 const size_t last_b = (size_t)buf * S.kc * S.rb + tn * (TN + 1) + (S.kc - 1) * S.rb + TN - 1;
                 if (last_a >= As.size() || last_b >= Bs.size()) { printf("chunk read out of range\n"); exit(1); }
                 unsigned long long a2[TM][TN];
-                double2 d2[TM][TN];
+                float4 d2[TM][TN];
                 for (int i = 0; i < TM; i++)
                     for (int j = 0; j < TN; j++) { a2[i][j] = acc[t][i * TN + j]; d2[i][j] = dacc[t][i * TN + j]; }
                 bgemm_chunk<M, N>(As.data() + (size_t)buf * S.kc * S.ra, Bs.data() + (size_t)buf * S.kc * S.rb, tm, tn, a2);
@@ -334,7 +334,8 @@ void emulate_bgemm(const BGemmArgs& g, std::vector<double2>& partial) {
             for (int i = 0; i < TM; i++)
                 for (int j = 0; j < TN; j++) {
                     const int m = tm * TM + i, n = tn * TN + j;
-                    const double2 v = dacc[t][i * TN + j];
+                    const float4 f = dacc[t][i * TN + j];
+                    const double2 v = make_double2((double)f.x + (double)f.y, (double)f.z + (double)f.w);
                     if (g.nsplit == 1) g.C[bgemm_c_offset(g, bi, m, n)] = make_float2((float)v.x, (float)v.y);
                     else partial.at((size_t)((si * g.nbatch + bi) * M + m) * N + n) = v;
                 }
