@@ -67,7 +67,7 @@ static_assert(kJoinSubs == 4 && kJoinStages == 4 && kJoinQBufs == 8,
               "the kernel's loops index stages with shifts by 2 (4 per chunk, 4 A stages) and 3 (8 B stages)");
 constexpr int kJoinMaxRing = 4;                     // raw chunks in the ring
 constexpr int kJoinPGroups = 2;                     // P splitter groups (alternate stages)
-constexpr int kJoinQWarps = 4;                      // Q splitter warps (2, 3 and the last two)
+constexpr int kJoinQWarps = 4;                      // Q splitter warps (2, 3 and the two after the P groups)
 constexpr int kJoinQThreads = 32 * kJoinQWarps;
 constexpr int kJoinIssuers = 2;                     // MMA issuing threads (alternate stages)
 constexpr int kJoinThreads = 32 * (2 + kJoinQWarps + 4 * kJoinPGroups + (kJoinIssuers - 1));
@@ -76,7 +76,7 @@ constexpr uint32_t kJoinSleepNs = 2000;             // suspend hint of a barrier
 constexpr int kJoinStageCols = 2 * kJoinSub;        // tensor-memory columns of one A stage (32)
 constexpr int kJoinFlushTerms = 128;                // summed terms per FP32 accumulator
 constexpr int kJoinChunkBits = 48;                  // delta-table entries (chunk index bits)
-constexpr size_t kJoinSmemCap = 200 * 1024;         // ring + B stages (one CTA per SM)
+constexpr size_t kJoinSmemCap = 200 * 1024;         // ring + B stages + drained sums (one CTA per SM)
 constexpr int kJoinPadBytes = 16;                   // padding after each bulk segment and each B tile
 constexpr int kJoinMaxBulkSegs = 96;                // bulk segments per chunk above which the join declines
                                                     // (each cp.async.bulk costs ~70 cycles of the loader)
