@@ -43,6 +43,32 @@ def gate_derivatives(gate) -> list:
     raise ValueError(f"no derivative for gate {name!r}")
 
 
+def chain_rule_tables(terms, layout):
+    """Index tables of the chain rule to the parameters: for terms (parameter id, load instruction,
+    dT/dtheta as an array of the leaf's shape) and the gradient vector's layout (instruction ->
+    (offset, shape), `Executor.leaf_slices`), element e of the concatenation is entry idx[e] of the
+    flat gradient vector times dt[e] (column-major, as the leaves are laid out), added into
+    parameter pid[e].  Returns (idx, dt, pid)."""
+    idx, dtv, pid = [], [], []
+    for p, instr, dt in terms:
+        o, shape = layout[instr]
+        n = int(np.prod(shape)) if shape else 1
+        idx.append(np.arange(o, o + n))
+        dtv.append(np.asarray(dt, dtype=np.complex128).reshape(-1, order="F"))
+        pid.append(np.full(n, p))
+    if not idx:
+        return np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.complex128), np.zeros(0, dtype=np.int64)
+    return np.concatenate(idx), np.concatenate(dtv), np.concatenate(pid)
+
+
+def apply_chain_rule(gvec, tables, num_params):
+    """dL/dtheta = 2 Re sum conj(dL/d conj T) dT/dtheta for every parameter, from the flat leaf
+    gradient vector and chain_rule_tables."""
+    idx, dt, pid = tables
+    w = 2.0 * np.real(np.conj(gvec[idx]) * dt)
+    return np.bincount(pid, weights=w, minlength=num_params)[:num_params]
+
+
 class ParametrisedCircuitLoss:
     """L(theta) = sum over bitstrings of |<x|C(theta)|0>|^2 and dL/dtheta on the GPU.
 
@@ -83,28 +109,14 @@ class ParametrisedCircuitLoss:
                 full = dm.reshape(shape, order="F")
                 self.terms.append((pid, instr, self.tnc.tn.reduced_data(name, full)))
         self.num_params = circ.num_params
-        # the chain rule as one gather over the flat gradient vector: element idx[e] of the leaf
-        # gradients times dT/dtheta (column-major, as the leaves are laid out), added into parameter
-        # pid[e]
-        lay = self.executor.leaf_slices()
-        idx, dtv, pid = [], [], []
-        for p, instr, dt in self.terms:
-            o, shape = lay[instr]
-            n = int(np.prod(shape)) if shape else 1
-            idx.append(np.arange(o, o + n))
-            dtv.append(np.asarray(dt, dtype=np.complex128).reshape(-1, order="F"))
-            pid.append(np.full(n, p))
-        self._gidx = np.concatenate(idx) if idx else np.zeros(0, dtype=np.int64)
-        self._gdt = np.concatenate(dtv) if dtv else np.zeros(0, dtype=np.complex128)
-        self._gpid = np.concatenate(pid) if pid else np.zeros(0, dtype=np.int64)
+        # the chain rule as one gather over the flat gradient vector
+        self._chain = chain_rule_tables(self.terms, self.executor.leaf_slices())
 
     def loss_and_grad(self, bitstrings, slices=None):
         amps, gvec = self.executor.gradient(bitstrings, slices=slices, flat=True)
         loss = float(np.sum(np.abs(amps) ** 2))
         # L = sum |a|^2 with amp_bar = a; dL/dtheta = 2 Re sum conj(dL/d conj T) dT/dtheta
-        w = 2.0 * np.real(np.conj(gvec[self._gidx]) * self._gdt)
-        g = np.bincount(self._gpid, weights=w, minlength=self.num_params)[: self.num_params]
-        return loss, g, amps
+        return loss, apply_chain_rule(gvec, self._chain, self.num_params), amps
 
     def loss(self, bitstrings) -> float:
         return float(np.sum(np.abs(self.executor.amplitudes(bitstrings)) ** 2))

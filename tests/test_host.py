@@ -208,3 +208,31 @@ def test_rqc_generator_family(q):
     for g in c.circ_ops:
         m = g.matrix
         assert np.allclose(m.conj().T @ m, np.eye(m.shape[0]))
+
+
+def test_chain_rule_to_the_parameters_matches_the_per_gate_sum(q):
+    """gradients.chain_rule_tables / apply_chain_rule (one gather + bincount over the flat leaf
+    gradient vector) equal the per-gate sum 2 Re sum conj(dL/d conj T) dT/dtheta, with leaves of
+    several shapes laid out column-major and parameters shared between gates."""
+    rng = np.random.default_rng(5)
+    shapes = [(2, 2), (4, 4), (2, 2, 2, 2), (), (2, 4)]
+    layout, o = {}, 0
+    for i in range(40):
+        s = shapes[i % len(shapes)]
+        layout[3 * i] = (o, s)
+        o += int(np.prod(s)) if s else 1
+    gvec = rng.standard_normal(o) + 1j * rng.standard_normal(o)
+    terms = []
+    for instr, (_, s) in layout.items():
+        for _ in range(int(rng.integers(1, 3))):
+            dt = rng.standard_normal(s) + 1j * rng.standard_normal(s)
+            terms.append((int(rng.integers(0, 25)), instr, dt))
+    want = np.zeros(25)
+    for pid, instr, dt in terms:
+        off, s = layout[instr]
+        n = int(np.prod(s)) if s else 1
+        leaf = gvec[off:off + n].reshape(s, order="F")
+        want[pid] += 2.0 * float(np.real(np.sum(np.conj(leaf) * dt)))
+    got = q.gradients.apply_chain_rule(gvec, q.gradients.chain_rule_tables(terms, layout), 25)
+    assert got.shape == (25,)
+    assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
